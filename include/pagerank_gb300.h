@@ -1,0 +1,215 @@
+/*
+ * pagerank_gb300.h -- C ABI of the GB300 PageRank library.
+ *
+ * Replaces the five solver templates of puzzlef/pagerank-cuda-dynamic
+ * (inc/pagerankCuda.hxx) and the host-side marshalling they perform
+ * (pagerankInvokeCuda, inc/pagerankCuda.hxx:713-849):
+ *
+ *   pagerankStaticCuda<PARTITION,FLAG>(x, xt, o)                 :864-875
+ *   pagerankNaiveDynamicCuda<PARTITION,FLAG>(x, xt, q, o)        :891-901
+ *   pagerankDynamicTraversalCuda<...>(x, xt, y, yt, del, ins, q, o)  :921-930
+ *   pagerankDynamicFrontierCuda<...>(x, xt, y, yt, del, ins, q, o)   :950-959
+ *   pagerankPruneDynamicFrontierCuda<...>(x, xt, y, yt, del, ins, q, o) :979-988
+ *
+ * all of which map onto prx_solve() with a prx_mode.  The C++ header
+ * pagerankCudaGb300.hxx re-exposes those templates on top of this ABI.
+ *
+ * Graphs are dense CSR: vertex ids 0..n-1 in the reference's vertexKeys()
+ * order (inc/properties.hxx:26-33), neighbours ascending per row (the order
+ * LazyBitset keeps, inc/_bitset.hxx).  Offsets are 32-bit, so m < 2^32, the
+ * same limit as the reference (O = uint32_t, inc/pagerankCuda.hxx:715).
+ *
+ * Every entry point returns a prx_status; none of them exits the process
+ * (the reference's TRY_CUDA exits, inc/_cuda.hxx:136-150).  Host buffers
+ * belong to the caller; device memory belongs to the context and the graph.
+ * A context and the graphs made from it must be used from one host thread
+ * at a time.
+ */
+#ifndef PAGERANK_GB300_H
+#define PAGERANK_GB300_H
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PRX_OK = 0,
+  PRX_EINVAL = 1,    /* bad argument or malformed graph / batch          */
+  PRX_ENOMEM = 2,    /* device or host allocation failed                 */
+  PRX_ECUDA = 3,     /* a CUDA call failed (see prx_last_error())         */
+  PRX_ETIMEOUT = 4,  /* a bounded device-side wait gave up               */
+  PRX_ERANGE = 5,    /* size beyond a documented limit                   */
+  PRX_ESTATE = 6     /* call not valid for this object (e.g. no out-CSR) */
+} prx_status;
+
+/* The reference's five solvers (inc/pagerankCuda.hxx:864-988). */
+typedef enum {
+  PRX_STATIC = 0,
+  PRX_NAIVE_DYNAMIC = 1,
+  PRX_DYNAMIC_TRAVERSAL = 2,
+  PRX_DYNAMIC_FRONTIER = 3,
+  PRX_PRUNE_DYNAMIC_FRONTIER = 4
+} prx_mode;
+
+typedef enum {
+  PRX_FP64 = 0,         /* the drop-in: ranks and contributions in FP64, the
+                           reference's summation order, bit-exact to the oracle */
+  PRX_FP32_REFINE = 1   /* FP32 storage / gathers / accumulation of a correction,
+                           FP64 base ranks, FP64 residual and convergence test */
+} prx_precision;
+
+typedef enum {
+  PRX_LOOP_AUTO = 0,    /* CUDA graph with a device-side while loop if possible */
+  PRX_LOOP_HOST = 1,    /* host-driven loop, convergence read back in batches   */
+  PRX_LOOP_GRAPH = 2    /* CUDA graph with a conditional while node             */
+} prx_loop;
+
+/* PagerankOptions<V> (inc/pagerank.hxx:24-55) plus the GB300 knobs. */
+typedef struct {
+  int    repeat;              /* times to repeat the timed solve [1]        */
+  double tolerance;           /* L-inf convergence tolerance [1e-10]        */
+  double frontier_tolerance;  /* DF / DF-P expansion tolerance [1e-6]       */
+  double prune_tolerance;     /* DF-P pruning tolerance [1e-6]              */
+  double damping;             /* damping factor [0.85]                      */
+  int    max_iterations;      /* iteration cap [500]                        */
+  int    precision;           /* prx_precision [PRX_FP64]                   */
+  int    loop;                /* prx_loop [PRX_LOOP_AUTO]                   */
+  int    partition;           /* the reference's PARTITION template flag;
+                                 accepted for drop-in use, results are the
+                                 same either way [0]                         */
+} prx_options;
+
+/* PagerankResult<V> (inc/pagerank.hxx:64-113) minus the rank vector, which
+ * goes to the caller's buffer.  Times are milliseconds averaged over repeat,
+ * measured with CUDA events on the context's stream. */
+typedef struct {
+  int      iterations;
+  float    time_ms;
+  float    initialization_time_ms;
+  float    marking_time_ms;
+  float    computation_time_ms;
+  uint64_t affected_initial;   /* vertices marked before the first iteration  */
+  uint64_t edges_processed;    /* in-edges gathered over all iterations         */
+  double   last_delta;         /* L-inf change of the last iteration            */
+  int      refinements;        /* FP32_REFINE: outer FP64 residual checks run   */
+} prx_result;
+
+typedef struct prx_context prx_context;
+typedef struct prx_graph prx_graph;
+
+void        prx_options_default(prx_options* o);
+const char* prx_status_string(int status);
+/* Text of the last failure on this host thread ("" if none). */
+const char* prx_last_error(void);
+
+/* A context owns one CUDA stream on `device` and a workspace that grows on
+ * demand.  cudaSetDeviceFlags(cudaDeviceMapHost) is not needed (the
+ * reference sets it, inc/pagerankCuda.hxx:777). */
+int prx_context_create(int device, prx_context** out);
+int prx_context_destroy(prx_context* ctx);
+/* The context's stream, as a cudaStream_t cast to void*. */
+void* prx_context_stream(prx_context* ctx);
+
+/* Upload a graph (the csrCreate*W / cudaMemcpy part of pagerankInvokeCuda,
+ * inc/pagerankCuda.hxx:756-805).  xoff/xedg: out-CSR of the graph, needed by
+ * the dynamic modes and prx_graph_apply_batch (may be NULL for Static / ND);
+ * xtoff/xtedg: in-CSR (transpose); xtdat: out-degree of each vertex.  All
+ * pointers are host pointers.  `validate` != 0 checks every offset and id. */
+int prx_graph_create(prx_context* ctx, uint32_t n, uint64_t m,
+                     const uint32_t* xoff, const uint32_t* xedg,
+                     const uint32_t* xtoff, const uint32_t* xtedg,
+                     const uint32_t* xtdat, int validate, prx_graph** out);
+int prx_graph_destroy(prx_graph* g);
+/* Current vertex / edge counts (m changes with prx_graph_apply_batch). */
+int prx_graph_size(const prx_graph* g, uint32_t* n, uint64_t* m);
+/* Copy the graph back to host buffers (any pointer may be NULL). */
+int prx_graph_download(prx_graph* g, uint32_t* xoff, uint32_t* xedg,
+                       uint32_t* xtoff, uint32_t* xtedg, uint32_t* xtdat);
+
+/* Apply a tidied batch on the device to both CSRs and the out-degrees:
+ * deletions must exist, insertions must not, each list sorted by (u, v)
+ * and free of duplicates -- the output of tidyBatchUpdateU
+ * (inc/batch.hxx:200-208).  Same effect as applyBatchUpdateOmpU
+ * (inc/batch.hxx:239-247) followed by transposeWithDegreeOmp
+ * (inc/transpose.hxx:128-134).  Host pointers. */
+int prx_graph_apply_batch(prx_graph* g,
+                          const uint32_t* delu, const uint32_t* delv, uint64_t nd,
+                          const uint32_t* insu, const uint32_t* insv, uint64_t ni);
+
+/* Solve with the ranks and batch in HOST memory.  The graph must already hold
+ * the updated graph y / yt (as the reference's callers pass it).  q: previous
+ * ranks (n doubles) or NULL for 1/n; Static ignores q.  deletions/insertions:
+ * the tidied batch that produced the graph (dynamic modes; insv may be NULL).
+ * ranks_out: n doubles.  res may be NULL. */
+int prx_solve(prx_context* ctx, prx_graph* g, int mode,
+              const uint32_t* delu, const uint32_t* delv, uint64_t nd,
+              const uint32_t* insu, const uint32_t* insv, uint64_t ni,
+              const double* q, const prx_options* o,
+              double* ranks_out, prx_result* res);
+
+/* Same, with q, ranks_out and the batch arrays in DEVICE memory (inputs
+ * already resident in HBM).  Runs on the context's stream and returns after
+ * the solve completed. */
+int prx_solve_device(prx_context* ctx, prx_graph* g, int mode,
+                     const uint32_t* delu, const uint32_t* delv, uint64_t nd,
+                     const uint32_t* insu, const uint32_t* insv, uint64_t ni,
+                     const double* q, const prx_options* o,
+                     double* ranks_out, prx_result* res);
+
+/* Run only the initial affected-vertex marking of a dynamic mode
+ * (pagerankAffectedFrontierCuW :405-412 for DF / DF-P,
+ * pagerankAffectedTraversalCuW :438-456 for DT) and copy the flags (n bytes,
+ * 0/1) to host memory. */
+int prx_mark_affected(prx_context* ctx, prx_graph* g, int mode,
+                      const uint32_t* delu, const uint32_t* delv, uint64_t nd,
+                      const uint32_t* insu, uint64_t ni, uint8_t* flags_out);
+
+/* ---- host-side graph utilities (C++ / OpenMP; no device work) ---------- */
+
+/* A CSR allocated by the library; free with prx_host_csr_free. */
+typedef struct {
+  uint32_t  n;
+  uint64_t  m;
+  uint32_t* off;   /* n+1 */
+  uint32_t* edg;   /* m   */
+} prx_host_csr;
+
+void prx_host_csr_free(prx_host_csr* g);
+
+/* R-MAT (a, b, c; d = 1-a-b-c) with n = 2^scale and edge_factor*n draws,
+ * duplicates removed, a self-loop on every vertex, rows ascending. */
+int prx_gen_rmat(int scale, int edge_factor, double a, double b, double c,
+                 uint64_t seed, prx_host_csr* out);
+/* Web-like graph: out-degree floor(dmin * U^(-1/(alpha-1))) capped at dmax,
+ * a fraction `local` of each row's targets within +/-window of the source,
+ * the rest uniform; duplicates removed; self-loops on all vertices. */
+int prx_gen_weblike(uint32_t n, double alpha, double dmin, uint32_t dmax,
+                    double local, uint32_t window, uint64_t seed, prx_host_csr* out);
+/* w x w grid, 4-neighbour edges both ways, a diagonal edge pair (both ways)
+ * from a fraction `diag` of the vertices, self-loops on all vertices. */
+int prx_gen_grid(uint32_t w, double diag, uint64_t seed, prx_host_csr* out);
+/* Random batch on x: ni_req insertions of uniform pairs and nd_req deletions
+ * of uniformly chosen existing non-self-loop edges, then tidied (filtered by
+ * existence, sorted, unique; inc/batch.hxx:152-208).  Arrays are allocated
+ * by the library; free with prx_host_free. */
+int prx_gen_batch(const prx_host_csr* x, uint64_t nd_req, uint64_t ni_req, uint64_t seed,
+                  uint32_t** delu, uint32_t** delv, uint64_t* nd,
+                  uint32_t** insu, uint32_t** insv, uint64_t* ni);
+/* tidyBatchUpdateU on caller arrays, in place; returns new lengths. */
+int prx_host_tidy_batch(const prx_host_csr* x, uint32_t* delu, uint32_t* delv, uint64_t* nd,
+                        uint32_t* insu, uint32_t* insv, uint64_t* ni);
+/* Out-CSR of x with a tidied batch applied (host). */
+int prx_host_apply_batch(const prx_host_csr* x,
+                         const uint32_t* delu, const uint32_t* delv, uint64_t nd,
+                         const uint32_t* insu, const uint32_t* insv, uint64_t ni,
+                         prx_host_csr* y);
+/* In-CSR (sources ascending) and out-degrees of x; xtdat has n entries. */
+int prx_host_transpose(const prx_host_csr* x, prx_host_csr* xt, uint32_t* xtdat);
+void prx_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

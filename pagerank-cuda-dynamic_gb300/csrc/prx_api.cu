@@ -1,0 +1,561 @@
+// prx_api.cu -- the C ABI (include/pagerank_gb300.h): contexts, device graphs
+// and the solve driver that replaces pagerankInvokeCuda + pagerankLoopCuU
+// (inc/pagerankCuda.hxx:675-849).
+//
+// Differences from the reference's driver, none of which changes a result:
+//  - the graph stays on the device across solves (the reference re-uploads
+//    and re-partitions it on every call, :777-813);
+//  - the loop keeps its state on the device (iteration count, L-inf delta,
+//    done flag) and the host reads it back once per batch of iterations
+//    instead of after each one (:685), or never (CUDA-graph loop);
+//  - errors come back as status codes instead of exit() (inc/_cuda.hxx:136).
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "prx_internal.h"
+
+using namespace prx;
+
+namespace prx {
+static thread_local std::string g_last_error;
+void set_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace prx
+
+struct prx_context {
+  int device = 0;
+  int sms = 152;
+  cudaStream_t stream = nullptr;
+  State* st = nullptr;        // device control block
+  State* st_host = nullptr;   // pinned: [0] after marking, [1] loop checks
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // workspace (grows on demand)
+  uint32_t ws_n = 0;
+  bool ws_dyn = false;
+  double* r[2] = {nullptr, nullptr};
+  double* c[2] = {nullptr, nullptr};
+  uint8_t* uflags = nullptr;
+  uint32_t* vaff = nullptr;
+  uint32_t* naff = nullptr;
+  uint32_t* lists[2][NCLS] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+  uint32_t* xl = nullptr;
+  uint32_t* fr[2] = {nullptr, nullptr};
+  uint32_t* batch = nullptr;  // device copy of a batch
+  size_t batch_cap = 0;       // in uint32 elements
+};
+
+struct prx_graph {
+  prx_context* ctx = nullptr;
+  GraphDev g;
+};
+
+#define TRY_CUDA_ST(x)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (x);                                                                \
+    if (e_ != cudaSuccess) {                                                             \
+      set_error(std::string(#x) + ": " + cudaGetErrorString(e_));                        \
+      return e_ == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;                   \
+    }                                                                                    \
+  } while (0)
+
+#define FAIL(code, msg)  \
+  do {                   \
+    set_error(msg);      \
+    return (code);       \
+  } while (0)
+
+extern "C" {
+
+void prx_options_default(prx_options* o) {
+  if (!o) return;
+  o->repeat = 1;
+  o->tolerance = 1e-10;
+  o->frontier_tolerance = 1e-6;
+  o->prune_tolerance = 1e-6;
+  o->damping = 0.85;
+  o->max_iterations = 500;
+  o->precision = PRX_FP64;
+  o->loop = PRX_LOOP_AUTO;
+  o->partition = 0;
+}
+
+const char* prx_status_string(int s) {
+  switch (s) {
+    case PRX_OK: return "ok";
+    case PRX_EINVAL: return "invalid argument";
+    case PRX_ENOMEM: return "out of memory";
+    case PRX_ECUDA: return "CUDA error";
+    case PRX_ETIMEOUT: return "device wait timed out";
+    case PRX_ERANGE: return "size out of range";
+    case PRX_ESTATE: return "invalid state";
+    default: return "unknown status";
+  }
+}
+
+const char* prx_last_error(void) { return g_last_error.c_str(); }
+
+int prx_context_create(int device, prx_context** out) {
+  if (!out) FAIL(PRX_EINVAL, "prx_context_create: out is NULL");
+  *out = nullptr;
+  int count = 0;
+  TRY_CUDA_ST(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count) FAIL(PRX_EINVAL, "prx_context_create: no such device");
+  TRY_CUDA_ST(cudaSetDevice(device));
+  prx_context* c = new prx_context();
+  c->device = device;
+  cudaError_t e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->st, sizeof(State));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->st_host, 2 * sizeof(State));
+  for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+  if (e != cudaSuccess) {
+    set_error(std::string("prx_context_create: ") + cudaGetErrorString(e));
+    prx_context_destroy(c);
+    return e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
+  }
+  *out = c;
+  return PRX_OK;
+}
+
+static void free_ws(prx_context* c) {
+  for (int p = 0; p < 2; ++p) {
+    cudaFree(c->r[p]); c->r[p] = nullptr;
+    cudaFree(c->c[p]); c->c[p] = nullptr;
+    cudaFree(c->fr[p]); c->fr[p] = nullptr;
+    for (int k = 0; k < NCLS; ++k) { cudaFree(c->lists[p][k]); c->lists[p][k] = nullptr; }
+  }
+  cudaFree(c->uflags); c->uflags = nullptr;
+  cudaFree(c->vaff); c->vaff = nullptr;
+  cudaFree(c->naff); c->naff = nullptr;
+  cudaFree(c->xl); c->xl = nullptr;
+  c->ws_n = 0;
+  c->ws_dyn = false;
+}
+
+int prx_context_destroy(prx_context* c) {
+  if (!c) return PRX_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_ws(c);
+  cudaFree(c->batch);
+  cudaFree(c->st);
+  cudaFreeHost(c->st_host);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return PRX_OK;
+}
+
+void* prx_context_stream(prx_context* c) { return c ? (void*)c->stream : nullptr; }
+
+}  // extern "C"
+
+// ---- workspace -------------------------------------------------------------------
+static int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
+  if (c->ws_n >= n && (c->ws_dyn || !dyn)) return PRX_OK;
+  const uint32_t cap = std::max(n, c->ws_n);
+  const bool want_dyn = dyn || c->ws_dyn;
+  free_ws(c);
+  const size_t words = ((size_t)cap + 31) / 32;
+  for (int p = 0; p < 2; ++p) {
+    TRY_CUDA_ST(cudaMalloc(&c->r[p], sizeof(double) * cap));
+    TRY_CUDA_ST(cudaMalloc(&c->c[p], sizeof(double) * cap));
+  }
+  if (want_dyn) {
+    TRY_CUDA_ST(cudaMalloc(&c->uflags, cap));
+    TRY_CUDA_ST(cudaMalloc(&c->vaff, sizeof(uint32_t) * words));
+    TRY_CUDA_ST(cudaMalloc(&c->naff, sizeof(uint32_t) * words));
+    TRY_CUDA_ST(cudaMalloc(&c->xl, sizeof(uint32_t) * cap));
+    for (int p = 0; p < 2; ++p) {
+      TRY_CUDA_ST(cudaMalloc(&c->fr[p], sizeof(uint32_t) * cap));
+      for (int k = 0; k < NCLS; ++k) TRY_CUDA_ST(cudaMalloc(&c->lists[p][k], sizeof(uint32_t) * cap));
+    }
+  }
+  c->ws_n = cap;
+  c->ws_dyn = want_dyn;
+  return PRX_OK;
+}
+
+static int ensure_batch(prx_context* c, size_t elems) {
+  if (c->batch_cap >= elems) return PRX_OK;
+  cudaFree(c->batch);
+  c->batch = nullptr;
+  c->batch_cap = 0;
+  TRY_CUDA_ST(cudaMalloc(&c->batch, sizeof(uint32_t) * std::max<size_t>(elems, 1024)));
+  c->batch_cap = std::max<size_t>(elems, 1024);
+  return PRX_OK;
+}
+
+static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options& o) {
+  SolveArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.xoff = g.xoff; a.xedg = g.xedg;
+  a.xtoff = g.xtoff; a.xtedg = g.xtedg; a.xtdat = g.xtdat;
+  a.cls_list = g.cls_list;
+  for (int p = 0; p < 2; ++p) {
+    a.r[p] = c->r[p];
+    a.c[p] = c->c[p];
+    a.fr[p] = c->fr[p];
+    for (int k = 0; k < NCLS; ++k) a.list[p][k] = c->lists[p][k];
+  }
+  a.uflags = c->uflags; a.vaff = c->vaff; a.naff = c->naff; a.xl = c->xl;
+  a.st = c->st;
+  a.n = g.n;
+  a.mid_max = g.mid_max;
+  a.P = o.damping;
+  a.C0 = (1 - o.damping) / (double)g.n;  // pagerankLoopCuU :679, N = order
+  a.D = o.frontier_tolerance;
+  a.C = o.prune_tolerance;
+  return a;
+}
+
+static bool valid_mode(int m) { return m >= PRX_STATIC && m <= PRX_PRUNE_DYNAMIC_FRONTIER; }
+
+// Initial marking of a dynamic mode on batch arrays already on the device.
+static int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint32_t* du, const uint32_t* dv,
+                       uint64_t nd, const uint32_t* iu, uint64_t ni) {
+  cudaStream_t s = c->stream;
+  const size_t words = ((size_t)a.n + 31) / 32;
+  TRY_CUDA_ST(cudaMemsetAsync(c->vaff, 0, words * 4, s));
+  TRY_CUDA_ST(cudaMemsetAsync(c->naff, 0, words * 4, s));
+  if (nd + ni == 0) return PRX_OK;  // :927,956,985 -- nothing marked
+  launch_mark_seed(a, du, dv, nd, iu, ni, c->sms, s);
+  launch_expand(a, EXPAND_XL, c->sms, s);
+  if (mode == PRX_DYNAMIC_TRAVERSAL) {
+    launch_frontier_from_lists(a, c->sms, s);
+    for (int cur = 0;; cur ^= 1) {
+      TRY_CUDA_ST(cudaMemsetAsync(&c->st->fcnt[cur ^ 1], 0, sizeof(uint32_t), s));
+      launch_expand(a, EXPAND_FRONTIER | (cur << 8), c->sms, s);
+      TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1].fcnt[cur ^ 1], &c->st->fcnt[cur ^ 1], sizeof(uint32_t),
+                                  cudaMemcpyDeviceToHost, s));
+      TRY_CUDA_ST(cudaStreamSynchronize(s));
+      if (c->st_host[1].fcnt[cur ^ 1] == 0) break;
+    }
+  }
+  TRY_CUDA_ST(cudaMemsetAsync(&c->st->xcnt, 0, sizeof(uint32_t), s));
+  return PRX_OK;
+}
+
+static void enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArgs& a, int mode) {
+  cudaStream_t s = c->stream;
+  if (mode < PRX_DYNAMIC_TRAVERSAL) {
+    launch_update_static(a, gr->g, c->sms, s);
+  } else {
+    launch_update_dynamic(a, mode, c->sms, s);
+    launch_commit(a, mode, c->sms, s);
+    if (mode >= PRX_DYNAMIC_FRONTIER) launch_expand(a, EXPAND_XL_INTO_NEXT, c->sms, s);
+  }
+  launch_finalize(a, mode, s);
+}
+
+// Core solve; q_dev/batch arrays are device pointers.  On success *final_ranks
+// points at the device buffer holding the ranks.
+static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* du, const uint32_t* dv, uint64_t nd,
+                      const uint32_t* iu, uint64_t ni, const double* q_dev, const prx_options& o,
+                      prx_result* res, const double** final_ranks) {
+  const GraphDev& g = gr->g;
+  const bool dyn = mode >= PRX_DYNAMIC_TRAVERSAL;
+  if (dyn && !g.xoff) FAIL(PRX_ESTATE, "prx_solve: dynamic modes need the out-CSR (xoff/xedg) of the graph");
+  if (o.precision != PRX_FP64) FAIL(PRX_EINVAL, "prx_solve: unsupported precision");
+  int st = ensure_ws(c, g.n, dyn);
+  if (st) return st;
+  cudaStream_t s = c->stream;
+  const SolveArgs a = make_args(c, g, o);
+  const int repeat = o.repeat > 0 ? o.repeat : 1;
+  float ti = 0, tm = 0, tc = 0, tt = 0;
+  for (int rep = 0; rep < repeat; ++rep) {
+    TRY_CUDA_ST(cudaEventRecord(c->ev[0], s));
+    launch_state_reset(c->st, o.max_iterations, o.tolerance, s);
+    launch_init_ranks(a, (mode == PRX_STATIC) ? nullptr : q_dev, dyn, s);
+    TRY_CUDA_ST(cudaEventRecord(c->ev[1], s));
+    if (dyn) {
+      st = run_marking(c, a, mode, du, dv, nd, iu, ni);
+      if (st) return st;
+      TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[0], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
+    }
+    TRY_CUDA_ST(cudaEventRecord(c->ev[2], s));
+    for (int k = 1;; k = std::min(2 * k, 16)) {
+      for (int i = 0; i < k; ++i) enqueue_iteration(c, gr, a, mode);
+      TRY_CUDA_ST(cudaGetLastError());
+      TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
+      TRY_CUDA_ST(cudaStreamSynchronize(s));
+      if (c->st_host[1].done) break;
+    }
+    TRY_CUDA_ST(cudaEventRecord(c->ev[3], s));
+    TRY_CUDA_ST(cudaEventSynchronize(c->ev[3]));
+    float x;
+    cudaEventElapsedTime(&x, c->ev[0], c->ev[1]); ti += x;
+    cudaEventElapsedTime(&x, c->ev[1], c->ev[2]); tm += x;
+    cudaEventElapsedTime(&x, c->ev[2], c->ev[3]); tc += x;
+    cudaEventElapsedTime(&x, c->ev[0], c->ev[3]); tt += x;
+  }
+  const State& h = c->st_host[1];
+  if (res) {
+    res->iterations = h.iter;
+    res->time_ms = tt / repeat;
+    res->initialization_time_ms = ti / repeat;
+    res->marking_time_ms = tm / repeat;
+    res->computation_time_ms = tc / repeat;
+    res->affected_initial = dyn ? (uint64_t)c->st_host[0].cnt[0][0] + c->st_host[0].cnt[0][1] + c->st_host[0].cnt[0][2] : g.n;
+    res->edges_processed = dyn ? h.edges : g.m * (uint64_t)h.iter;
+    res->last_delta = h.last_delta;
+    res->refinements = 0;
+  }
+  *final_ranks = dyn ? c->r[0] : c->r[h.iter & 1];
+  return PRX_OK;
+}
+
+static int check_batch_ids(uint32_t n, const uint32_t* du, const uint32_t* dv, uint64_t nd, const uint32_t* iu,
+                           const uint32_t* iv, uint64_t ni) {
+  if ((nd && (!du || !dv)) || (ni && !iu)) FAIL(PRX_EINVAL, "batch: NULL array with a non-zero length");
+  for (uint64_t i = 0; i < nd; ++i)
+    if (du[i] >= n || dv[i] >= n) FAIL(PRX_EINVAL, "batch: deletion vertex id out of range");
+  for (uint64_t i = 0; i < ni; ++i)
+    if (iu[i] >= n || (iv && iv[i] >= n)) FAIL(PRX_EINVAL, "batch: insertion vertex id out of range");
+  return PRX_OK;
+}
+
+extern "C" {
+
+int prx_graph_create(prx_context* c, uint32_t n, uint64_t m, const uint32_t* xoff, const uint32_t* xedg,
+                     const uint32_t* xtoff, const uint32_t* xtedg, const uint32_t* xtdat, int validate,
+                     prx_graph** out) {
+  if (!c || !out) FAIL(PRX_EINVAL, "prx_graph_create: NULL context or out");
+  *out = nullptr;
+  if (m > 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_create: m >= 2^32 does not fit 32-bit offsets");
+  if (!xtoff || (n && !xtdat) || (m && !xtedg))
+    FAIL(PRX_EINVAL, "prx_graph_create: xtoff, xtedg and xtdat are required");
+  if ((xedg && !xoff) || (xoff && m && !xedg)) FAIL(PRX_EINVAL, "prx_graph_create: give both xoff and xedg or neither");
+  if (xtoff[0] != 0 || xtoff[n] != m) FAIL(PRX_EINVAL, "prx_graph_create: xtoff must start at 0 and end at m");
+  if (xoff && (xoff[0] != 0 || xoff[n] != m)) FAIL(PRX_EINVAL, "prx_graph_create: xoff must start at 0 and end at m");
+  if (validate) {
+    for (uint32_t v = 0; v < n; ++v) {
+      if (xtoff[v + 1] < xtoff[v]) FAIL(PRX_EINVAL, "prx_graph_create: xtoff not monotone");
+      if (xoff && xoff[v + 1] < xoff[v]) FAIL(PRX_EINVAL, "prx_graph_create: xoff not monotone");
+      if (xoff && xtdat[v] != xoff[v + 1] - xoff[v]) FAIL(PRX_EINVAL, "prx_graph_create: xtdat != out-degree");
+    }
+    for (uint64_t i = 0; i < m; ++i) {
+      if (xtedg[i] >= n) FAIL(PRX_EINVAL, "prx_graph_create: xtedg id out of range");
+      if (xedg && xedg[i] >= n) FAIL(PRX_EINVAL, "prx_graph_create: xedg id out of range");
+    }
+  }
+  TRY_CUDA_ST(cudaSetDevice(c->device));
+  prx_graph* gr = new prx_graph();
+  gr->ctx = c;
+  GraphDev& g = gr->g;
+  g.n = n;
+  g.m = m;
+  g.m_cap = m;
+  cudaStream_t s = c->stream;
+  auto upload = [&](uint32_t** dst, const uint32_t* src, size_t cnt) -> cudaError_t {
+    cudaError_t e = cudaMalloc(dst, sizeof(uint32_t) * (cnt ? cnt : 1));
+    if (e == cudaSuccess && cnt) e = cudaMemcpyAsync(*dst, src, sizeof(uint32_t) * cnt, cudaMemcpyHostToDevice, s);
+    return e;
+  };
+  cudaError_t e = upload(&g.xtoff, xtoff, (size_t)n + 1);
+  if (e == cudaSuccess) e = upload(&g.xtedg, xtedg, m);
+  if (e == cudaSuccess) e = upload(&g.xtdat, xtdat, n);
+  if (e == cudaSuccess && xoff) e = upload(&g.xoff, xoff, (size_t)n + 1);
+  if (e == cudaSuccess && xoff) e = upload(&g.xedg, xedg, m);
+  if (e == cudaSuccess) e = build_classes(g, c->sms, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    set_error(std::string("prx_graph_create: ") + cudaGetErrorString(e));
+    prx_graph_destroy(gr);
+    return e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
+  }
+  *out = gr;
+  return PRX_OK;
+}
+
+int prx_graph_destroy(prx_graph* gr) {
+  if (!gr) return PRX_OK;
+  if (gr->ctx) {
+    cudaSetDevice(gr->ctx->device);
+    cudaStreamSynchronize(gr->ctx->stream);
+  }
+  GraphDev& g = gr->g;
+  cudaFree(g.xoff); cudaFree(g.xedg); cudaFree(g.xtoff); cudaFree(g.xtedg); cudaFree(g.xtdat); cudaFree(g.cls_list);
+  delete gr;
+  return PRX_OK;
+}
+
+int prx_graph_size(const prx_graph* gr, uint32_t* n, uint64_t* m) {
+  if (!gr) FAIL(PRX_EINVAL, "prx_graph_size: NULL graph");
+  if (n) *n = gr->g.n;
+  if (m) *m = gr->g.m;
+  return PRX_OK;
+}
+
+int prx_graph_download(prx_graph* gr, uint32_t* xoff, uint32_t* xedg, uint32_t* xtoff, uint32_t* xtedg,
+                       uint32_t* xtdat) {
+  if (!gr) FAIL(PRX_EINVAL, "prx_graph_download: NULL graph");
+  const GraphDev& g = gr->g;
+  cudaStream_t s = gr->ctx->stream;
+  TRY_CUDA_ST(cudaSetDevice(gr->ctx->device));
+  if ((xoff || xedg) && !g.xoff) FAIL(PRX_ESTATE, "prx_graph_download: graph has no out-CSR");
+  if (xoff) TRY_CUDA_ST(cudaMemcpyAsync(xoff, g.xoff, 4 * ((size_t)g.n + 1), cudaMemcpyDeviceToHost, s));
+  if (xedg && g.m) TRY_CUDA_ST(cudaMemcpyAsync(xedg, g.xedg, 4 * g.m, cudaMemcpyDeviceToHost, s));
+  if (xtoff) TRY_CUDA_ST(cudaMemcpyAsync(xtoff, g.xtoff, 4 * ((size_t)g.n + 1), cudaMemcpyDeviceToHost, s));
+  if (xtedg && g.m) TRY_CUDA_ST(cudaMemcpyAsync(xtedg, g.xtedg, 4 * g.m, cudaMemcpyDeviceToHost, s));
+  if (xtdat && g.n) TRY_CUDA_ST(cudaMemcpyAsync(xtdat, g.xtdat, 4 * (size_t)g.n, cudaMemcpyDeviceToHost, s));
+  TRY_CUDA_ST(cudaStreamSynchronize(s));
+  return PRX_OK;
+}
+
+int prx_graph_apply_batch(prx_graph* gr, const uint32_t* du, const uint32_t* dv, uint64_t nd, const uint32_t* iu,
+                          const uint32_t* iv, uint64_t ni) {
+  if (!gr) FAIL(PRX_EINVAL, "prx_graph_apply_batch: NULL graph");
+  GraphDev& g = gr->g;
+  prx_context* c = gr->ctx;
+  if (!g.xoff) FAIL(PRX_ESTATE, "prx_graph_apply_batch: graph has no out-CSR");
+  if (ni && !iv) FAIL(PRX_EINVAL, "prx_graph_apply_batch: insertions need targets");
+  int st = check_batch_ids(g.n, du, dv, nd, iu, iv, ni);
+  if (st) return st;
+  auto sorted_unique = [](const uint32_t* a, const uint32_t* b, uint64_t len) {
+    for (uint64_t i = 1; i < len; ++i)
+      if (a[i - 1] > a[i] || (a[i - 1] == a[i] && b[i - 1] >= b[i])) return false;
+    return true;
+  };
+  if (!sorted_unique(du, dv, nd) || !sorted_unique(iu, iv, ni))
+    FAIL(PRX_EINVAL, "prx_graph_apply_batch: batch must be sorted by (u, v) and unique (tidyBatchUpdateU)");
+  if (g.m - nd + ni > 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_apply_batch: edge count would reach 2^32");
+  // The in-CSR wants the batch ordered by (v, u): a stable sort by v of the
+  // (u, v)-sorted lists (LSD radix, two 16-bit digits).
+  std::vector<uint32_t> host(4 * (size_t)(nd + ni));
+  auto by_target = [](const uint32_t* u, const uint32_t* v, uint64_t len, uint32_t* ok, uint32_t* ov) {
+    std::vector<uint32_t> tu(u, u + len), tv(v, v + len), su(len), sv(len);
+    for (int shift = 0; shift < 32; shift += 16) {
+      std::vector<uint64_t> cnt(65537, 0);
+      for (uint64_t i = 0; i < len; ++i) cnt[((tv[i] >> shift) & 0xffff) + 1]++;
+      for (int d = 0; d < 65536; ++d) cnt[d + 1] += cnt[d];
+      for (uint64_t i = 0; i < len; ++i) {
+        const uint64_t p = cnt[(tv[i] >> shift) & 0xffff]++;
+        su[p] = tu[i];
+        sv[p] = tv[i];
+      }
+      tu.swap(su);
+      tv.swap(sv);
+    }
+    std::copy(tv.begin(), tv.end(), ok);
+    std::copy(tu.begin(), tu.end(), ov);
+  };
+  uint32_t* h = host.data();
+  std::copy(du, du + nd, h);
+  std::copy(dv, dv + nd, h + nd);
+  std::copy(iu, iu + ni, h + 2 * nd);
+  std::copy(iv, iv + ni, h + 2 * nd + ni);
+  by_target(du, dv, nd, h + 2 * (nd + ni), h + 2 * (nd + ni) + nd);
+  by_target(iu, iv, ni, h + 2 * (nd + ni) + 2 * nd, h + 2 * (nd + ni) + 2 * nd + ni);
+  TRY_CUDA_ST(cudaSetDevice(c->device));
+  st = ensure_batch(c, host.size());
+  if (st) return st;
+  if (!host.empty())
+    TRY_CUDA_ST(cudaMemcpyAsync(c->batch, h, 4 * host.size(), cudaMemcpyHostToDevice, c->stream));
+  const cudaError_t e = apply_batch_device(g, c->batch, nd, ni, c->sms, c->stream);
+  if (e == cudaErrorInvalidValue)
+    FAIL(PRX_EINVAL, "prx_graph_apply_batch: batch is not tidy (a deletion is missing or an insertion exists)");
+  TRY_CUDA_ST(e);
+  return PRX_OK;
+}
+
+static int solve_common(prx_context* c, prx_graph* gr, int mode, const uint32_t* du, const uint32_t* dv,
+                        uint64_t nd, const uint32_t* iu, const uint32_t* iv, uint64_t ni, const double* q,
+                        const prx_options* o, double* ranks_out, prx_result* res, bool host) {
+  if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_solve: bad context or graph");
+  if (!valid_mode(mode)) FAIL(PRX_EINVAL, "prx_solve: unknown mode");
+  prx_options opt;
+  prx_options_default(&opt);
+  if (o) opt = *o;
+  if (!(opt.damping > 0 && opt.damping < 1)) FAIL(PRX_EINVAL, "prx_solve: damping must be in (0, 1)");
+  if (!ranks_out && gr->g.n) FAIL(PRX_EINVAL, "prx_solve: ranks_out is NULL");
+  if (res) std::memset(res, 0, sizeof(*res));
+  const GraphDev& g = gr->g;
+  if (g.n == 0) return PRX_OK;  // empty graph: the reference returns {} (:869)
+  const bool dyn = mode >= PRX_DYNAMIC_TRAVERSAL;
+  if (!dyn) nd = ni = 0;
+  TRY_CUDA_ST(cudaSetDevice(c->device));
+  const uint32_t *ddu = du, *ddv = dv, *diu = iu;
+  const double* dq = q;
+  int st;
+  if (host) {
+    if (dyn) {
+      st = check_batch_ids(g.n, du, dv, nd, iu, iv, ni);
+      if (st) return st;
+      st = ensure_batch(c, 2 * nd + ni);
+      if (st) return st;
+      if (nd) {
+        TRY_CUDA_ST(cudaMemcpyAsync(c->batch, du, 4 * nd, cudaMemcpyHostToDevice, c->stream));
+        TRY_CUDA_ST(cudaMemcpyAsync(c->batch + nd, dv, 4 * nd, cudaMemcpyHostToDevice, c->stream));
+      }
+      if (ni) TRY_CUDA_ST(cudaMemcpyAsync(c->batch + 2 * nd, iu, 4 * ni, cudaMemcpyHostToDevice, c->stream));
+      ddu = c->batch; ddv = c->batch + nd; diu = c->batch + 2 * nd;
+    }
+    st = ensure_ws(c, g.n, dyn);
+    if (st) return st;
+    if (q && mode != PRX_STATIC) {
+      // stage q in r[1]: init reads it before anything writes r[1]
+      TRY_CUDA_ST(cudaMemcpyAsync(c->r[1], q, sizeof(double) * g.n, cudaMemcpyHostToDevice, c->stream));
+      dq = c->r[1];
+    } else {
+      dq = nullptr;
+    }
+  }
+  const double* fr = nullptr;
+  st = solve_core(c, gr, mode, ddu, ddv, nd, diu, ni, dq, opt, res, &fr);
+  if (st) return st;
+  TRY_CUDA_ST(cudaMemcpyAsync(ranks_out, fr, sizeof(double) * g.n,
+                              host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, c->stream));
+  TRY_CUDA_ST(cudaStreamSynchronize(c->stream));
+  return PRX_OK;
+}
+
+int prx_solve(prx_context* c, prx_graph* gr, int mode, const uint32_t* du, const uint32_t* dv, uint64_t nd,
+              const uint32_t* iu, const uint32_t* iv, uint64_t ni, const double* q, const prx_options* o,
+              double* ranks_out, prx_result* res) {
+  return solve_common(c, gr, mode, du, dv, nd, iu, iv, ni, q, o, ranks_out, res, true);
+}
+
+int prx_solve_device(prx_context* c, prx_graph* gr, int mode, const uint32_t* du, const uint32_t* dv, uint64_t nd,
+                     const uint32_t* iu, const uint32_t* iv, uint64_t ni, const double* q, const prx_options* o,
+                     double* ranks_out, prx_result* res) {
+  return solve_common(c, gr, mode, du, dv, nd, iu, iv, ni, q, o, ranks_out, res, false);
+}
+
+int prx_mark_affected(prx_context* c, prx_graph* gr, int mode, const uint32_t* du, const uint32_t* dv, uint64_t nd,
+                      const uint32_t* iu, uint64_t ni, uint8_t* flags_out) {
+  if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_mark_affected: bad context or graph");
+  if (mode < PRX_DYNAMIC_TRAVERSAL || mode > PRX_PRUNE_DYNAMIC_FRONTIER)
+    FAIL(PRX_EINVAL, "prx_mark_affected: mode must be DT, DF or DF-P");
+  const GraphDev& g = gr->g;
+  if (!g.xoff) FAIL(PRX_ESTATE, "prx_mark_affected: graph has no out-CSR");
+  if (g.n == 0) return PRX_OK;
+  if (!flags_out) FAIL(PRX_EINVAL, "prx_mark_affected: flags_out is NULL");
+  int st = check_batch_ids(g.n, du, dv, nd, iu, nullptr, ni);
+  if (st) return st;
+  TRY_CUDA_ST(cudaSetDevice(c->device));
+  st = ensure_ws(c, g.n, true);
+  if (st) return st;
+  st = ensure_batch(c, 2 * nd + ni);
+  if (st) return st;
+  cudaStream_t s = c->stream;
+  if (nd) {
+    TRY_CUDA_ST(cudaMemcpyAsync(c->batch, du, 4 * nd, cudaMemcpyHostToDevice, s));
+    TRY_CUDA_ST(cudaMemcpyAsync(c->batch + nd, dv, 4 * nd, cudaMemcpyHostToDevice, s));
+  }
+  if (ni) TRY_CUDA_ST(cudaMemcpyAsync(c->batch + 2 * nd, iu, 4 * ni, cudaMemcpyHostToDevice, s));
+  prx_options o;
+  prx_options_default(&o);
+  const SolveArgs a = make_args(c, g, o);
+  launch_state_reset(c->st, 0, 0.0, s);
+  st = run_marking(c, a, mode, c->batch, c->batch + nd, nd, c->batch + 2 * nd, ni);
+  if (st) return st;
+  launch_flags_from_bitmap(c->vaff, c->uflags, g.n, s);
+  TRY_CUDA_ST(cudaMemcpyAsync(flags_out, c->uflags, g.n, cudaMemcpyDeviceToHost, s));
+  TRY_CUDA_ST(cudaStreamSynchronize(s));
+  TRY_CUDA_ST(cudaGetLastError());
+  return PRX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,83 @@
+// prx_device.cuh -- device helpers shared by the kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "prx_internal.h"
+
+namespace prx {
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// In-degree class of v (see kLowMax).
+__device__ __forceinline__ int in_class(const uint32_t* __restrict__ xtoff, uint32_t v, uint32_t mid_max) {
+  const uint32_t d = xtoff[v + 1] - xtoff[v];
+  return d <= kLowMax ? LOW : (d <= mid_max ? MID : HIGH);
+}
+
+// Set bit v of a bitmap; true if this call changed it from 0 to 1.  Bits only
+// go 0 -> 1 while marking kernels run, so a set bit seen by the plain load is
+// final and the atomic can be skipped.
+__device__ __forceinline__ bool test_and_set(uint32_t* bm, uint32_t v) {
+  const uint32_t bit = 1u << (v & 31u);
+  if (bm[v >> 5] & bit) return false;
+  return !(atomicOr(&bm[v >> 5], bit) & bit);
+}
+
+__device__ __forceinline__ void clear_bit(uint32_t* bm, uint32_t v) {
+  atomicAnd(&bm[v >> 5], ~(1u << (v & 31u)));
+}
+
+// Append v to list/cnt.  Lanes of the active set that append to the same
+// counter share one atomicAdd (safe under divergence).
+__device__ __forceinline__ void push(uint32_t* list, uint32_t* cnt, uint32_t v) {
+  const unsigned active = __activemask();
+  const unsigned peers = __match_any_sync(active, (unsigned long long)(uintptr_t)cnt);
+  const int leader = __ffs(peers) - 1;
+  const unsigned lane = lane_id();
+  uint32_t base = 0;
+  if ((int)lane == leader) base = atomicAdd(cnt, (uint32_t)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  list[base + __popc(peers & ((1u << lane) - 1u))] = v;
+}
+
+// Block-wide max of a non-negative double given as its bit pattern (for
+// x >= 0 the IEEE-754 bit patterns order like the values), folded into *dst
+// with one atomicMax per block.  Every thread of the block must call it.
+__device__ __forceinline__ void block_max_bits(unsigned long long x, unsigned long long* dst) {
+  __shared__ unsigned long long smax[32];
+  for (int o = 16; o; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, x, o);
+    x = y > x ? y : x;
+  }
+  const int w = threadIdx.x >> 5;
+  if (lane_id() == 0) smax[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    x = lane_id() < (blockDim.x >> 5) ? smax[lane_id()] : 0ull;
+    for (int o = 16; o; o >>= 1) {
+      const unsigned long long y = __shfl_xor_sync(0xffffffffu, x, o);
+      x = y > x ? y : x;
+    }
+    if (lane_id() == 0 && x) atomicMax(dst, x);
+  }
+}
+
+__device__ __forceinline__ void block_sum_u64(unsigned long long x, unsigned long long* dst) {
+  __shared__ unsigned long long ssum[32];
+  for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  const int w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane_id() == 0) ssum[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    x = lane_id() < (blockDim.x >> 5) ? ssum[lane_id()] : 0ull;
+    for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane_id() == 0 && x) atomicAdd(dst, x);
+  }
+}
+
+__device__ __forceinline__ unsigned long long dbits(double x) {
+  return (unsigned long long)__double_as_longlong(x);
+}
+
+}  // namespace prx

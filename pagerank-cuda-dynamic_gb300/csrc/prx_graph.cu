@@ -1,0 +1,206 @@
+// prx_graph.cu -- device-side graph preparation.
+//
+// build_classes(): the reference splits vertices into in-degree <= 64 and
+// > 64 with two CUB scans, two scatters and a blocking copy of the split
+// point (pagerankPartitionVerticesCuW, inc/pagerankCuda.hxx:625-638), rebuilt
+// inside every timed solve (:812-813).  Here one stable 3-way partition
+// (LOW / MID / HIGH, ids ascending within each class) is built once per graph
+// version with three kernels of our own and reused by every solve on it.
+#include <vector>
+#include "prx_device.cuh"
+
+namespace prx {
+
+constexpr uint32_t kTileV = 2048;            // vertices per tile (256 threads x 8)
+constexpr int kFieldBits = 21;               // per-class count within a tile, packed into a u64
+constexpr unsigned long long kFieldMask = (1ull << kFieldBits) - 1;
+
+__device__ __forceinline__ unsigned long long cls_code(const uint32_t* __restrict__ xtoff, uint32_t v, uint32_t mid_max) {
+  return 1ull << (kFieldBits * in_class(xtoff, v, mid_max));
+}
+
+// Inclusive scan over a 256-thread block; *total receives the block sum.
+__device__ __forceinline__ unsigned long long block_scan_incl(unsigned long long x, unsigned long long* total) {
+  __shared__ unsigned long long wsum[8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  unsigned long long pre = 0, tot = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    if (i < w) pre += wsum[i];
+    tot += wsum[i];
+  }
+  *total = tot;
+  __syncthreads();
+  return x + pre;
+}
+
+// Per-tile class counts, class-major: cnt[c * ntiles + tile].
+__global__ void __launch_bounds__(256) k_cls_count(const uint32_t* __restrict__ xtoff, uint32_t n, uint32_t mid_max,
+                                                   uint32_t ntiles, uint32_t* __restrict__ cnt) {
+  const uint32_t v0 = blockIdx.x * kTileV + threadIdx.x * 8;
+  unsigned long long x = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    if (v0 + k < n) x += cls_code(xtoff, v0 + k, mid_max);
+  unsigned long long tot;
+  block_scan_incl(x, &tot);
+  if (threadIdx.x == 0)
+    for (int c = 0; c < NCLS; ++c) cnt[c * ntiles + blockIdx.x] = (uint32_t)((tot >> (kFieldBits * c)) & kFieldMask);
+}
+
+// One block of 1024 threads: exclusive scan of cnt[0 .. len) in place (the
+// class-major layout makes the result the global start of each (class, tile)),
+// plus the class boundaries bounds[0..3].
+__global__ void __launch_bounds__(1024) k_cls_scan(uint32_t* cnt, uint32_t ntiles, uint32_t* bounds) {
+  __shared__ uint32_t sh[1024];
+  const uint32_t len = NCLS * ntiles;
+  const uint32_t t = threadIdx.x;
+  const uint32_t per = (len + 1023) / 1024;
+  const uint32_t b = min(len, t * per), e = min(len, b + per);
+  uint32_t local = 0;
+  for (uint32_t i = b; i < e; ++i) local += cnt[i];
+  sh[t] = local;
+  __syncthreads();
+  for (uint32_t o = 1; o < 1024; o <<= 1) {
+    const uint32_t y = t >= o ? sh[t - o] : 0;
+    __syncthreads();
+    sh[t] += y;
+    __syncthreads();
+  }
+  uint32_t run = t ? sh[t - 1] : 0;
+  for (uint32_t i = b; i < e; ++i) {
+    const uint32_t x = cnt[i];
+    cnt[i] = run;
+    if (i % ntiles == 0) bounds[i / ntiles] = run;
+    run += x;
+  }
+  if (t == 1023) bounds[NCLS] = sh[1023];
+}
+
+__global__ void __launch_bounds__(256) k_cls_scatter(const uint32_t* __restrict__ xtoff, uint32_t n, uint32_t mid_max,
+                                                     uint32_t ntiles, const uint32_t* __restrict__ start,
+                                                     uint32_t* __restrict__ out) {
+  const uint32_t v0 = blockIdx.x * kTileV + threadIdx.x * 8;
+  int cls[8];
+  unsigned long long x = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    cls[k] = v0 + k < n ? in_class(xtoff, v0 + k, mid_max) : -1;
+    if (cls[k] >= 0) x += 1ull << (kFieldBits * cls[k]);
+  }
+  unsigned long long tot;
+  unsigned long long pos = block_scan_incl(x, &tot) - x;  // exclusive, packed per class
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (cls[k] < 0) continue;
+    const int c = cls[k];
+    const uint32_t local = (uint32_t)((pos >> (kFieldBits * c)) & kFieldMask);
+    out[start[c * ntiles + blockIdx.x] + local] = v0 + k;
+    pos += 1ull << (kFieldBits * c);
+  }
+}
+
+cudaError_t build_classes(GraphDev& g, int, cudaStream_t s) {
+  const uint32_t n = g.n;
+  if (n == 0) {
+    for (int c = 0; c <= NCLS; ++c) g.cls_begin[c] = 0;
+    return cudaSuccess;
+  }
+  const uint32_t ntiles = (n + kTileV - 1) / kTileV;
+  uint32_t* cnt = nullptr;
+  cudaError_t e = cudaMallocAsync(&cnt, sizeof(uint32_t) * ((size_t)NCLS * ntiles + NCLS + 1), s);
+  if (e != cudaSuccess) return e;
+  uint32_t* bounds = cnt + (size_t)NCLS * ntiles;
+  if (!g.cls_list) {
+    e = cudaMalloc(&g.cls_list, sizeof(uint32_t) * n);
+    if (e != cudaSuccess) { cudaFreeAsync(cnt, s); return e; }
+  }
+  k_cls_count<<<ntiles, 256, 0, s>>>(g.xtoff, n, g.mid_max, ntiles, cnt);
+  k_cls_scan<<<1, 1024, 0, s>>>(cnt, ntiles, bounds);
+  k_cls_scatter<<<ntiles, 256, 0, s>>>(g.xtoff, n, g.mid_max, ntiles, cnt, g.cls_list);
+  uint32_t hb[NCLS + 1];
+  e = cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFreeAsync(cnt, s);
+  if (e != cudaSuccess) return e;
+  for (int c = 0; c <= NCLS; ++c) g.cls_begin[c] = hb[c];
+  return cudaGetLastError();
+}
+
+}  // namespace prx
+
+namespace prx {
+
+// ---- exclusive scan of uint32 (in place), three passes ----------------------
+__global__ void __launch_bounds__(256) k_scan_tile_sums(const uint32_t* __restrict__ in, uint32_t len,
+                                                        uint32_t* __restrict__ sums) {
+  const uint32_t i0 = blockIdx.x * kTileV + threadIdx.x * 8;
+  unsigned long long x = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x += i0 + k < len ? in[i0 + k] : 0u;
+  unsigned long long tot;
+  block_scan_incl(x, &tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = (uint32_t)tot;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_single(uint32_t* a, uint32_t len) {
+  __shared__ uint32_t sh[1024];
+  const uint32_t t = threadIdx.x;
+  const uint32_t per = (len + 1023) / 1024;
+  const uint32_t b = min(len, t * per), e = min(len, b + per);
+  uint32_t local = 0;
+  for (uint32_t i = b; i < e; ++i) local += a[i];
+  sh[t] = local;
+  __syncthreads();
+  for (uint32_t o = 1; o < 1024; o <<= 1) {
+    const uint32_t y = t >= o ? sh[t - o] : 0;
+    __syncthreads();
+    sh[t] += y;
+    __syncthreads();
+  }
+  uint32_t run = t ? sh[t - 1] : 0;
+  for (uint32_t i = b; i < e; ++i) {
+    const uint32_t x = a[i];
+    a[i] = run;
+    run += x;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_scan_apply(uint32_t* __restrict__ data, uint32_t len,
+                                                    const uint32_t* __restrict__ tile_pre) {
+  const uint32_t i0 = blockIdx.x * kTileV + threadIdx.x * 8;
+  uint32_t v[8];
+  unsigned long long x = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) { v[k] = i0 + k < len ? data[i0 + k] : 0u; x += v[k]; }
+  unsigned long long tot;
+  uint32_t run = tile_pre[blockIdx.x] + (uint32_t)(block_scan_incl(x, &tot) - x);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    if (i0 + k < len) data[i0 + k] = run;
+    run += v[k];
+  }
+}
+
+cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t len, cudaStream_t s) {
+  if (len == 0) return cudaSuccess;
+  const uint32_t ntiles = (len + kTileV - 1) / kTileV;
+  uint32_t* sums = nullptr;
+  cudaError_t e = cudaMallocAsync(&sums, sizeof(uint32_t) * ntiles, s);
+  if (e != cudaSuccess) return e;
+  k_scan_tile_sums<<<ntiles, 256, 0, s>>>(data, len, sums);
+  k_scan_single<<<1, 1024, 0, s>>>(sums, ntiles);
+  k_scan_apply<<<ntiles, 256, 0, s>>>(data, len, sums);
+  e = cudaGetLastError();
+  cudaFreeAsync(sums, s);
+  return e;
+}
+
+}  // namespace prx

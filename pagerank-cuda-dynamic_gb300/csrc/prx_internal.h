@@ -1,0 +1,102 @@
+// prx_internal.h -- shared host/device declarations of the GB300 PageRank
+// library.  Not part of the public ABI (that is include/pagerank_gb300.h).
+#pragma once
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <cuda_runtime.h>
+#include "pagerank_gb300.h"
+
+namespace prx {
+
+// In-degree classes of the pull update.  The 64 boundary is semantic: the
+// reference adds the in-edges of a vertex with in-degree <= 64 front to back
+// in one thread and those of a vertex with in-degree > 64 in 256 strided
+// partial sums folded by a halving tree (inc/pagerankCuda.hxx:93,169,177;
+// inc/_cuda.hxx:541-551).  The MID/HIGH boundary only picks warp-per-vertex
+// or block-per-vertex execution of that same 256-way order.
+constexpr uint32_t kLowMax = 64;
+constexpr uint32_t kDefaultMidMax = 4096;
+enum Cls { LOW = 0, MID = 1, HIGH = 2, NCLS = 3 };
+
+constexpr int kThreads = 256;  // threads per block for all map-like kernels
+
+// Device-resident control block of one solve.
+struct State {
+  unsigned long long el_bits[2];  // L-inf delta of the iteration with parity p (bits of a double >= 0)
+  int iter;                       // iterations completed
+  int done;                       // set once el < tol or iter == max_iter
+  int max_iter;
+  int pad0;
+  double tol;
+  double last_delta;
+  uint32_t cnt[2][NCLS];          // dynamic: affected-list lengths [parity][class]
+  uint32_t xcnt;                  // vertices whose out-neighbours must be marked
+  uint32_t fcnt[2];               // DT closure frontier lengths
+  uint32_t err;                   // device-detected error code, 0 = none
+  unsigned long long edges;       // in-edges gathered (statistic)
+};
+
+struct GraphDev {
+  uint32_t n = 0;
+  uint64_t m = 0;
+  uint64_t m_cap = 0;             // capacity of the edge arrays
+  uint32_t* xoff = nullptr;       // out-CSR (nullable)
+  uint32_t* xedg = nullptr;
+  uint32_t* xtoff = nullptr;      // in-CSR
+  uint32_t* xtedg = nullptr;
+  uint32_t* xtdat = nullptr;      // out-degree
+  uint32_t* cls_list = nullptr;   // n ids: LOW ids, then MID, then HIGH (each ascending)
+  uint32_t cls_begin[NCLS + 1] = {0, 0, 0, 0};
+  uint32_t mid_max = kDefaultMidMax;
+};
+
+// Pointers a solve kernel needs.  Passed by value.
+struct SolveArgs {
+  const uint32_t* xoff;
+  const uint32_t* xedg;
+  const uint32_t* xtoff;
+  const uint32_t* xtedg;
+  const uint32_t* xtdat;
+  const uint32_t* cls_list;       // static classes (see GraphDev)
+  double* r[2];                   // FP64 ranks, ping-pong (dynamic: r[0] = ranks, r[1] = new values)
+  double* c[2];                   // FP64 contributions r/outdeg, ping-pong (dynamic: c[0])
+  uint8_t* uflags;                // dynamic: per-vertex update flags (bit0 pruned, bit1 expand)
+  uint32_t* vaff;                 // bitmap of affected vertices
+  uint32_t* naff;                 // bitmap of seeded sources
+  uint32_t* list[2][NCLS];        // dynamic affected lists
+  uint32_t* xl;                   // vertices to expand
+  uint32_t* fr[2];                // DT closure frontiers
+  State* st;
+  uint32_t n;
+  uint32_t mid_max;
+  double C0, P, D, C;
+};
+
+// ---- launchers (prx_update.cu) ------------------------------------------
+void launch_init_ranks(const SolveArgs& a, const double* q, bool dynamic, cudaStream_t s);
+void launch_update_static(const SolveArgs& a, const GraphDev& g, int sms, cudaStream_t s);
+void launch_update_dynamic(const SolveArgs& a, int mode, int sms, cudaStream_t s);
+void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s);
+
+// ---- launchers (prx_mark.cu) --------------------------------------------
+void launch_mark_seed(const SolveArgs& a, const uint32_t* delu, const uint32_t* delv, uint64_t nd,
+                      const uint32_t* insu, uint64_t ni, int sms, cudaStream_t s);
+void launch_expand(const SolveArgs& a, int which, int sms, cudaStream_t s);
+void launch_frontier_from_lists(const SolveArgs& a, int sms, cudaStream_t s);
+void launch_commit(const SolveArgs& a, int mode, int sms, cudaStream_t s);
+void launch_flags_from_bitmap(const uint32_t* bm, uint8_t* out, uint32_t n, cudaStream_t s);
+void launch_state_reset(State* st, int max_iter, double tol, cudaStream_t s);
+
+// ---- graph construction (prx_graph.cu) ----------------------------------
+cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s);
+// b: device array [du | dv | iu | iv | tdk | tdv | tik | tiv]; t* = batch sorted by (v, u)
+cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd, uint64_t ni, int sms, cudaStream_t s);
+cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t len, cudaStream_t s);
+
+// which list launch_expand reads
+enum ExpandSrc { EXPAND_XL = 0, EXPAND_XL_INTO_NEXT = 1, EXPAND_FRONTIER = 2 };
+
+void set_error(const std::string& msg);
+
+}  // namespace prx

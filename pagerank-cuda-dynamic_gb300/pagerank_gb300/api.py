@@ -1,0 +1,183 @@
+"""Python face of the C ABI: contexts, device graphs, solves.
+
+Mirrors the reference's solver surface (inc/pagerankCuda.hxx:864-988):
+
+    pagerank_static(ctx, g, options)                          pagerankStaticCuda
+    pagerank_naive_dynamic(ctx, g, q, options)                pagerankNaiveDynamicCuda
+    pagerank_dynamic_traversal(ctx, g, dels, ins, q, options) pagerankDynamicTraversalCuda
+    pagerank_dynamic_frontier(ctx, g, dels, ins, q, options)  pagerankDynamicFrontierCuda
+    pagerank_prune_dynamic_frontier(...)                      pagerankPruneDynamicFrontierCuda
+
+each returning (ranks, PagerankResult-like dict).  The graph passed is the
+updated graph y (with its transpose), as the reference's callers pass it.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import Options, Result, check, load
+
+
+def options(**kw):
+    o = Options()
+    load().prx_options_default(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError(f"unknown option {k}")
+        setattr(o, k, v)
+    return o
+
+
+def _u32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def _p(a):
+    return None if a is None or len(a) == 0 else a.ctypes.data
+
+
+class Context:
+    """prx_context: one CUDA device + stream + workspace."""
+
+    def __init__(self, device=0):
+        self._h = C.c_void_p()
+        check(load().prx_context_create(device, C.byref(self._h)), "prx_context_create")
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self):
+        return load().prx_context_stream(self._h)
+
+    def close(self):
+        if self._h:
+            load().prx_context_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Graph:
+    """prx_graph: device CSR of a graph and its transpose (+ out-degrees)."""
+
+    def __init__(self, ctx, xtoff, xtedg, xtdat, xoff=None, xedg=None, validate=False):
+        xtoff, xtedg, xtdat, xoff, xedg = (_u32(a) for a in (xtoff, xtedg, xtdat, xoff, xedg))
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        n, m = len(xtoff) - 1, len(xtedg)
+        check(load().prx_graph_create(ctx.handle, n, m, _p(xoff), _p(xedg) if xoff is not None else None,
+                                      xtoff.ctypes.data, _p(xtedg), _p(xtdat), int(validate), C.byref(self._h)),
+              "prx_graph_create")
+
+    @classmethod
+    def from_out_csr(cls, ctx, off, edg, dynamic=True, validate=False):
+        from .graphs import transpose
+        xtoff, xtedg, xtdat = transpose(off, edg)
+        return cls(ctx, xtoff, xtedg, xtdat, off if dynamic else None, edg if dynamic else None, validate)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def size(self):
+        n, m = C.c_uint32(), C.c_uint64()
+        check(load().prx_graph_size(self._h, C.byref(n), C.byref(m)), "prx_graph_size")
+        return n.value, m.value
+
+    def apply_batch(self, del_u, del_v, ins_u, ins_v):
+        du, dv, iu, iv = (_u32(a) for a in (del_u, del_v, ins_u, ins_v))
+        check(load().prx_graph_apply_batch(self._h, _p(du), _p(dv), len(du), _p(iu), _p(iv), len(iu)),
+              "prx_graph_apply_batch")
+
+    def download(self):
+        n, m = self.size()
+        xoff, xtoff = np.zeros(n + 1, np.uint32), np.zeros(n + 1, np.uint32)
+        xedg, xtedg = np.zeros(max(m, 1), np.uint32), np.zeros(max(m, 1), np.uint32)
+        xtdat = np.zeros(max(n, 1), np.uint32)
+        check(load().prx_graph_download(self._h, xoff.ctypes.data, xedg.ctypes.data, xtoff.ctypes.data,
+                                        xtedg.ctypes.data, xtdat.ctypes.data), "prx_graph_download")
+        return xoff, xedg[:m], xtoff, xtedg[:m], xtdat[:n]
+
+    def close(self):
+        if self._h:
+            load().prx_graph_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve(ctx, g, mode, deletions=None, insertions=None, q=None, opts=None):
+    """prx_solve with host buffers -> (ranks float64[n], result dict)."""
+    n, _ = g.size()
+    du = dv = iu = iv = None
+    if deletions is not None:
+        du, dv = _u32(deletions[0]), _u32(deletions[1])
+    if insertions is not None:
+        iu, iv = _u32(insertions[0]), _u32(insertions[1])
+    qq = None if q is None else np.ascontiguousarray(q, dtype=np.float64)
+    if qq is not None and len(qq) != n:
+        raise ValueError("q must have one entry per vertex")
+    ranks = np.zeros(max(n, 1), np.float64)
+    res = Result()
+    check(load().prx_solve(ctx.handle, g.handle, int(mode), _p(du), _p(dv), 0 if du is None else len(du),
+                           _p(iu), _p(iv), 0 if iu is None else len(iu), _p(qq), C.byref(opts or options()),
+                           ranks.ctypes.data, C.byref(res)), "prx_solve")
+    return ranks[:n], res.as_dict()
+
+
+def solve_device(ctx, g, mode, q_ptr, ranks_ptr, batch_ptrs=(None, None, 0, None, None, 0), opts=None):
+    """prx_solve_device with device pointers (ints) -> result dict."""
+    du, dv, nd, iu, iv, ni = batch_ptrs
+    res = Result()
+    check(load().prx_solve_device(ctx.handle, g.handle, int(mode), du, dv, nd, iu, iv, ni, q_ptr,
+                                  C.byref(opts or options()), ranks_ptr, C.byref(res)), "prx_solve_device")
+    return res.as_dict()
+
+
+def mark_affected(ctx, g, mode, deletions, insertions):
+    """Initial affected flags of a dynamic mode -> uint8[n]."""
+    n, _ = g.size()
+    du, dv = _u32(deletions[0]), _u32(deletions[1])
+    iu = _u32(insertions[0])
+    flags = np.zeros(max(n, 1), np.uint8)
+    check(load().prx_mark_affected(ctx.handle, g.handle, int(mode), _p(du), _p(dv), len(du), _p(iu), len(iu),
+                                   flags.ctypes.data), "prx_mark_affected")
+    return flags[:n]
+
+
+# ---- the reference's five entry points ------------------------------------
+def pagerank_static(ctx, g, opts=None):
+    return solve(ctx, g, _lib.STATIC, opts=opts)
+
+
+def pagerank_naive_dynamic(ctx, g, q, opts=None):
+    return solve(ctx, g, _lib.NAIVE_DYNAMIC, q=q, opts=opts)
+
+
+def pagerank_dynamic_traversal(ctx, g, deletions, insertions, q, opts=None):
+    return solve(ctx, g, _lib.DYNAMIC_TRAVERSAL, deletions, insertions, q, opts)
+
+
+def pagerank_dynamic_frontier(ctx, g, deletions, insertions, q, opts=None):
+    return solve(ctx, g, _lib.DYNAMIC_FRONTIER, deletions, insertions, q, opts)
+
+
+def pagerank_prune_dynamic_frontier(ctx, g, deletions, insertions, q, opts=None):
+    return solve(ctx, g, _lib.PRUNE_DYNAMIC_FRONTIER, deletions, insertions, q, opts)

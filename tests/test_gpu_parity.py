@@ -1,0 +1,170 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle.
+
+The FP64 path adds every in-edge contribution in the reference's order, so
+ranks must be bit-identical to the oracle's GPU-semantics restatement and the
+iteration counts equal; integer work (marking, batch apply) must be
+bit-exact against the golden fixtures made by the reference's own code."""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+MODES = ("static", "naive_dynamic", "dynamic_traversal", "dynamic_frontier", "prune_dynamic_frontier")
+
+
+def _graph(pg, ctx, off, edg, xt=None):
+    xtoff, xtedg, xtdat = xt if xt is not None else O.transpose(off, edg)
+    return pg.Graph(ctx, xtoff, xtedg, xtdat, off, edg, validate=True), (xtoff, xtedg, xtdat)
+
+
+def _oracle(mode, off, edg, xt, batch, q, opts=None):
+    du, dv, iu, iv = batch
+    return O.solve(mode, off, edg, *xt, du, dv, iu, iv, q=q, opts=opts)
+
+
+def _gpu(pg, ctx, g, mode, batch, q, opts=None):
+    du, dv, iu, iv = batch
+    return pg.solve(ctx, g, pg.MODES[mode], (du, dv), (iu, iv), q, opts)
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import pagerank_gb300
+    return pagerank_gb300
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_golden_all_modes_bit_exact(pg, ctx, case):
+    z = load_golden(case)
+    batch = (z["del_u"], z["del_v"], z["ins_u"], z["ins_v"])
+    xt = (z["yt_off"], z["yt_edg"], z["yt_dat"])
+    g, _ = _graph(pg, ctx, z["y_off"], z["y_edg"], xt)
+    q = z["static_x_ranks"]
+    for mode in MODES:
+        want, it_w = _oracle(mode, z["y_off"], z["y_edg"], xt, batch, q)
+        got, res = _gpu(pg, ctx, g, mode, batch, q)
+        assert res["iterations"] == it_w, mode
+        np.testing.assert_array_equal(got, want, err_msg=mode)
+    if int(z["n"]) > 1:
+        assert np.abs(pg.pagerank_static(ctx, g)[0] - z["static_y_ranks"]).max() <= 1e-15
+    g.close()
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_golden_marking_bit_exact(pg, ctx, case):
+    z = load_golden(case)
+    g, _ = _graph(pg, ctx, z["y_off"], z["y_edg"], (z["yt_off"], z["yt_edg"], z["yt_dat"]))
+    n = int(z["n"])
+    dels, ins = (z["del_u"], z["del_v"]), (z["ins_u"], z["ins_v"])
+    np.testing.assert_array_equal(pg.mark_affected(ctx, g, pg.DYNAMIC_FRONTIER, dels, ins), z["df_flags"][:n])
+    np.testing.assert_array_equal(pg.mark_affected(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, dels, ins), z["df_flags"][:n])
+    np.testing.assert_array_equal(pg.mark_affected(ctx, g, pg.DYNAMIC_TRAVERSAL, dels, ins), z["dt_flags"][:n])
+    g.close()
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_golden_device_batch_apply_bit_exact(pg, ctx, case):
+    z = load_golden(case)
+    g, _ = _graph(pg, ctx, z["x_off"], z["x_edg"], (z["xt_off"], z["xt_edg"], z["xt_dat"]))
+    g.apply_batch(z["del_u"], z["del_v"], z["ins_u"], z["ins_v"])
+    xoff, xedg, xtoff, xtedg, xtdat = g.download()
+    for got, k in ((xoff, "y_off"), (xedg, "y_edg"), (xtoff, "yt_off"), (xtedg, "yt_edg"), (xtdat, "yt_dat")):
+        np.testing.assert_array_equal(got, z[k], err_msg=k)
+    # solving on the device-updated graph equals solving on the uploaded one
+    q = z["static_x_ranks"]
+    batch = (z["del_u"], z["del_v"], z["ins_u"], z["ins_v"])
+    want, it = _oracle("prune_dynamic_frontier", z["y_off"], z["y_edg"], (z["yt_off"], z["yt_edg"], z["yt_dat"]),
+                       batch, q)
+    got, res = _gpu(pg, ctx, g, "prune_dynamic_frontier", batch, q)
+    assert res["iterations"] == it
+    np.testing.assert_array_equal(got, want)
+    g.close()
+
+
+def _synthetic(pg, kind):
+    if kind == "rmat16":   # R-MAT scale 16 (65,536 vertices, 16 edges/vertex)
+        return pg.graphs.rmat(16, 16, seed=42)
+    if kind == "web200k":  # web-like, scaled down
+        return pg.graphs.weblike(200000, dmax=20000, window=4096, seed=42)
+    if kind == "grid256":  # road-like grid
+        return pg.graphs.grid(256, 0.05, seed=42)
+    if kind == "hubs":     # R-MAT with heavy hubs to exercise the HIGH class
+        return pg.graphs.rmat(14, 48, a=0.7, b=0.1, c=0.1, seed=3)
+    raise KeyError(kind)
+
+
+@pytest.mark.parametrize("kind", ["rmat16", "web200k", "grid256", "hubs"])
+def test_synthetic_all_modes_bit_exact(pg, ctx, kind):
+    xoff, xedg = _synthetic(pg, kind)
+    m = len(xedg)
+    batch = pg.graphs.random_batch(xoff, xedg, max(1, int(2e-5 * m)), max(1, int(8e-5 * m)), seed=11)
+    xt = O.transpose(xoff, xedg)
+    q, _ = O.solve("static", None, None, *xt)
+    yoff, yedg = pg.graphs.apply_batch(xoff, xedg, *batch)
+    yt = O.transpose(yoff, yedg)
+    g, _ = _graph(pg, ctx, xoff, xedg, xt)
+    g.apply_batch(*batch)       # the device applies the batch to both CSRs
+    for mode in MODES:
+        want, it_w = _oracle(mode, yoff, yedg, yt, batch, q)
+        got, res = _gpu(pg, ctx, g, mode, batch, q)
+        assert res["iterations"] == it_w, (kind, mode)
+        np.testing.assert_array_equal(got, want, err_msg=f"{kind} {mode}")
+    g.close()
+
+
+def test_options_edge_cases(pg, ctx):
+    xoff, xedg = pg.graphs.rmat(10, 16, seed=1)
+    xt = O.transpose(xoff, xedg)
+    g, _ = _graph(pg, ctx, xoff, xedg, xt)
+    for kw in ({"max_iterations": 0}, {"max_iterations": 1}, {"max_iterations": 7}, {"tolerance": 1.0},
+               {"tolerance": 1e-14}, {"damping": 0.5}, {"repeat": 3}):
+        opts = pg.options(**kw)
+        oo = O.options(**{k: v for k, v in kw.items() if k != "repeat"})
+        want, it = O.solve("static", None, None, *xt, opts=oo)
+        got, res = pg.solve(ctx, g, pg.STATIC, opts=opts)
+        assert res["iterations"] == it, kw
+        np.testing.assert_array_equal(got, want, err_msg=str(kw))
+    g.close()
+
+
+def test_empty_batch_and_empty_graph(pg, ctx):
+    xoff, xedg = pg.graphs.rmat(9, 8, seed=1)
+    xt = O.transpose(xoff, xedg)
+    g, _ = _graph(pg, ctx, xoff, xedg, xt)
+    q = np.full(len(xoff) - 1, 1.0 / (len(xoff) - 1))
+    e = np.zeros(0, np.uint32)
+    for mode in MODES[2:]:
+        got, res = pg.solve(ctx, g, pg.MODES[mode], (e, e), (e, e), q)
+        assert res["iterations"] == 1 and res["affected_initial"] == 0
+        np.testing.assert_array_equal(got, q)
+    g.close()
+    z = np.zeros(1, np.uint32)
+    g0 = pg.Graph(ctx, z, np.zeros(0, np.uint32), np.zeros(0, np.uint32))
+    r, res = pg.solve(ctx, g0, pg.STATIC)
+    assert len(r) == 0 and res["iterations"] == 0
+    g0.close()
+
+
+def test_errors_are_status_codes(pg, ctx):
+    xoff, xedg = pg.graphs.rmat(8, 8, seed=1)
+    xtoff, xtedg, xtdat = O.transpose(xoff, xedg)
+    g = pg.Graph(ctx, xtoff, xtedg, xtdat)       # no out-CSR
+    with pytest.raises(pg.PrxError) as e:
+        pg.solve(ctx, g, pg.DYNAMIC_FRONTIER, (np.zeros(0), np.zeros(0)), ([1], [2]), None)
+    assert e.value.status == 6
+    g.close()
+    g = pg.Graph(ctx, xtoff, xtedg, xtdat, xoff, xedg)
+    with pytest.raises(pg.PrxError) as e:             # vertex id out of range
+        pg.solve(ctx, g, pg.DYNAMIC_FRONTIER, ([0], [10 ** 6]), ([0], [1]), None)
+    assert e.value.status == 1
+    with pytest.raises(pg.PrxError) as e:             # insertion of an existing edge: not tidy
+        g.apply_batch([], [], [0], [0])
+    assert e.value.status == 1
+    bad = xtedg.copy()
+    bad[0] = 10 ** 6
+    with pytest.raises(pg.PrxError):
+        pg.Graph(ctx, xtoff, bad, xtdat, validate=True)
+    g.close()
