@@ -1,0 +1,337 @@
+#!/usr/bin/env python3
+"""PageRank benchmark on one GB300 (or N replicas, one per GPU).
+
+Workload: the web-like power-law graph -- 50M vertices, ~1.9B edges, Zipf
+out-degree (exponent 2.1, max 100k), 70% of targets within +/-4096 ids, 30%
+uniform, self-loops on all vertices -- generated from a fixed seed on the
+host (synthetic stand-in for the reference's web graphs).
+
+A step is one Static FP64 PageRank solve (alpha 0.85, tol 1e-10 L-inf, at
+most 500 iterations) over that graph.  `value` is GE/s = edges x iterations /
+solve time with the graph and ranks resident in HBM; `e2e` is the same metric
+through the C ABI from pinned host buffers (graph upload, solve, ranks back).
+The line also carries the roofline of the dominant update kernel, a DF-P run
+after one 1e-4|E| batch (80% insertions / 20% deletions) applied on the
+device, and the reference's CPU Static (OpenMP port) timed on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "pagerank-cuda-dynamic_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "PageRank GE/s (Static FP64, edges x iterations / solve time)"
+WORKLOAD = "weblike-50M: 50M vertices, ~1.9B edges, Zipf(2.1, max 100k) out-degree, 70% within +/-4096, self-loops"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--vertices", type=int, default=50_000_000)
+    p.add_argument("--dmin", type=float, default=5.9)
+    p.add_argument("--seed", type=int, default=42)
+    p.add_argument("--cpu-sweeps", type=int, default=3, help="sweeps in the bounded CPU baseline sample")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-dfp", action="store_true")
+    p.add_argument("--e2e-steps", type=int, default=2)
+    return p.parse_args()
+
+
+def make_graph(args, pg):
+    t = time.perf_counter()
+    xoff, xedg = pg.graphs.weblike(args.vertices, alpha=2.1, dmin=args.dmin, dmax=100000, local=0.7,
+                                   window=4096, seed=args.seed)
+    t1 = time.perf_counter()
+    xt = pg.graphs.transpose(xoff, xedg)
+    log(f"graph: n={len(xoff) - 1} m={len(xedg)} generated in {t1 - t:.1f}s, transposed in "
+        f"{time.perf_counter() - t1:.1f}s")
+    return xoff, xedg, xt
+
+
+def dist_setup(args):
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", init_method="env://")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p:
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=10)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out, _ = self.p.communicate()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in (self.out or "").strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel, workload):
+    """DRAM bytes per launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    try:
+        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def cpu_baseline(args, xt, m):
+    from oracle import pyoracle as O
+    threads = os.cpu_count() or 1
+    _, sweeps, ms = O.cpu_static(*xt, threads=threads, sweeps_cap=args.cpu_sweeps, with_time=True)
+    return {"value": m * sweeps / (ms / 1e3) / 1e9, "unit": "GE/s", "cores": threads, "kind": "port",
+            "sample": f"{sweeps} synchronous sweeps of pagerankStaticOmp (OpenMP port, {threads} threads) on the "
+                      f"same graph, {ms / 1e3:.1f}s"}
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU Static PageRank (OpenMP port of
+    pagerankStaticOmp; the reference's own binary cannot be built on this
+    aarch64 host) on the same graph, bounded sweeps per step."""
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import pagerank_gb300 as pg
+    from oracle import pyoracle as O
+    xoff, xedg, xt = make_graph(args, pg)
+    m = len(xedg)
+    threads = os.cpu_count() or 1
+    per_step = 1
+    for _ in range(args.warmup):
+        O.cpu_static(*xt, threads=threads, sweeps_cap=per_step)
+    tot_ms, tot_sweeps = 0.0, 0
+    for _ in range(args.steps):
+        _, sweeps, ms = O.cpu_static(*xt, threads=threads, sweeps_cap=per_step, with_time=True)
+        tot_ms += ms
+        tot_sweeps += sweeps
+    v = m * tot_sweeps / (tot_ms / 1e3) / 1e9
+    out = {"metric": METRIC, "value": v, "unit": "GE/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": tot_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic (seeded generator)", "impl": "reference",
+           "config": {"workload": WORKLOAD, "vertices": len(xoff) - 1, "edges": m, "alpha": 0.85},
+           "cpu_baseline": {"value": v, "unit": "GE/s", "cores": threads, "kind": "port",
+                            "sample": f"{per_step} synchronous sweep of pagerankStaticOmp per step, "
+                                      f"{threads} OpenMP threads"},
+           "e2e": {"value": v, "unit": "GE/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import pagerank_gb300 as pg
+    ws, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    xoff, xedg, xt = make_graph(args, pg)
+    n, m = len(xoff) - 1, len(xedg)
+    ctx = pg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    g = pg.Graph(ctx, *xt, xoff, xedg)
+    cls_v, cls_e = g.class_stats()
+    ranks = torch.empty(n, dtype=torch.float64, device=f"cuda:{local}")
+    opts = pg.options(timing=1)
+    log(f"classes: vertices {cls_v} edges {cls_e}")
+    for _ in range(args.warmup):
+        pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr(), opts=opts)
+    results = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(ws)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            results.append(pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr(), opts=opts))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(ws)
+    ms = max_over_ranks(ws, e0.elapsed_time(e1))
+    iters = [r["iterations"] for r in results]
+    value = ws * m * sum(iters) / (ms / 1e3) / 1e9
+    launches = int(sum(r["kernel_launches"] for r in results))
+    # roofline of the dominant update kernel (FP64 algorithmic bytes: offsets 4,
+    # previous + new rank 16 per vertex; index 4 + gathered contribution 8 per edge)
+    upd_ms = [sum(r["update_ms"][c] for r in results) for c in range(3)]
+    upd_n = [sum(r["update_launches"][c] for r in results) for c in range(3)]
+    dom = max(range(3), key=lambda c: upd_ms[c])
+    names = ("k_update_low", "k_update_mid", "k_update_high")
+    bytes_per_launch = 20 * cls_v[dom] + 12 * cls_e[dom]
+    per_launch_ms = upd_ms[dom] / max(upd_n[dom], 1)
+    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": ncu_traffic(names[dom], "weblike50m"), "alg_bytes_per_launch": bytes_per_launch,
+                "launch_ms": per_launch_ms, "share_of_step": upd_ms[dom] / ms}
+    # all three update kernels together, same byte model
+    all_bytes = sum((20 * cls_v[c] + 12 * cls_e[c]) * upd_n[c] for c in range(3))
+    roofline["all_update_kernels_gbs"] = all_bytes / (sum(upd_ms) / 1e3) / 1e9 if sum(upd_ms) else None
+    log(f"static: {iters} iterations, {ms / args.steps:.1f} ms/step, {value:.2f} GE/s, update ms {upd_ms}")
+
+    # ---- end to end through the C ABI from pinned host buffers ----------------
+    pin = [torch.from_numpy(np.asarray(a)).pin_memory() for a in xt]
+    host_ranks = torch.empty(n, dtype=torch.float64).pin_memory()
+    h2d = sum(p.numel() * 4 for p in pin)
+    d2h = n * 8
+    e2e_ms, e2e_it = [], []
+    for _ in range(args.e2e_steps):
+        t = time.perf_counter()
+        ge = pg.Graph(ctx, *(p.numpy() for p in pin))
+        r_e2e = pg.api.solve_into(ctx, ge, pg.STATIC, host_ranks.data_ptr())
+        ge.close()
+        e2e_ms.append((time.perf_counter() - t) * 1e3)
+        e2e_it.append(r_e2e["iterations"])
+    e2e_ms_max = max_over_ranks(ws, statistics.median(e2e_ms))
+    e2e_value = ws * m * statistics.median(e2e_it) / (e2e_ms_max / 1e3) / 1e9
+    log(f"e2e: {e2e_ms} ms")
+
+    # ---- DF-P after one 1e-4|E| batch applied on the device ------------------
+    dfp = None
+    if not args.no_dfp:
+        q = ranks.clone()
+        size = int(1e-4 * m)
+        du, dv, iu, iv = pg.graphs.random_batch(xoff, xedg, size // 5, size - size // 5, seed=args.seed + 1)
+        t = time.perf_counter()
+        g.apply_batch(du, dv, iu, iv)
+        apply_ms = (time.perf_counter() - t) * 1e3
+        bt = [torch.from_numpy(np.asarray(a, dtype=np.uint32).view(np.int32)).to(f"cuda:{local}")
+              for a in (du, dv, iu, iv)]
+        out = torch.empty_like(q)
+        bp = (bt[0].data_ptr(), bt[1].data_ptr(), len(du), bt[2].data_ptr(), bt[3].data_ptr(), len(iu))
+        r_dfp = pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=pg.options())
+        r_df = pg.solve_device(ctx, g, pg.DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=pg.options())
+        r_st = pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr(), opts=pg.options())
+        r_dfp2 = pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp,
+                                 opts=pg.options())
+        err = float((out - ranks).abs().max())
+        dfp = {"batch": {"deletions": len(du), "insertions": len(iu)}, "apply_ms": apply_ms,
+               "dfp_ms": r_dfp2["time_ms"], "dfp_iterations": r_dfp2["iterations"],
+               "dfp_affected_initial": r_dfp2["affected_initial"], "dfp_edges": r_dfp2["edges_processed"],
+               "df_ms": r_df["time_ms"], "df_iterations": r_df["iterations"],
+               "static_ms": r_st["time_ms"], "static_iterations": r_st["iterations"],
+               "dfp_speedup_vs_static": r_st["time_ms"] / max(r_dfp2["time_ms"], 1e-9),
+               "df_speedup_vs_static": r_st["time_ms"] / max(r_df["time_ms"], 1e-9),
+               "dfp_linf_vs_static": err}
+        log(f"dfp: {dfp}")
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(args, xt, m)
+        log(f"cpu: {cpu}")
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "GE/s", "n_gpus": ws, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, host)",
+               "config": {"workload": WORKLOAD, "vertices": n, "edges": m, "alpha": 0.85, "tolerance": 1e-10,
+                          "max_iterations": 500, "parallelism": f"replicas{ws}",
+                          "l2": "inputs larger than L2 (7.6 GB in-CSR per sweep)"},
+               "iterations": iters, "gpu_launches": launches,
+               "e2e": {"value": e2e_value, "unit": "GE/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "ms_per_step": e2e_ms_max},
+               "roofline": roofline, "clocks": clk.summary(), "dfp": dfp, "cpu_baseline": cpu}
+        print(json.dumps(out), flush=True)
+    g.close()
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    import __graft_entry__
+    __graft_entry__.build()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -79,6 +79,8 @@ typedef struct {
   int    partition;           /* the reference's PARTITION template flag;
                                  accepted for drop-in use, results are the
                                  same either way [0]                         */
+  int    timing;              /* 1: time every rank-update launch with CUDA
+                                 events (prx_result.update_*) [0]            */
 } prx_options;
 
 /* PagerankResult<V> (inc/pagerank.hxx:64-113) minus the rank vector, which
@@ -94,6 +96,11 @@ typedef struct {
   uint64_t edges_processed;    /* in-edges gathered over all iterations         */
   double   last_delta;         /* L-inf change of the last iteration            */
   int      refinements;        /* FP32_REFINE: outer FP64 residual checks run   */
+  uint64_t kernel_launches;    /* kernels this library launched for the solve  */
+  /* With prx_options.timing: per in-degree class (<= 64, warp, block) the
+   * summed device time and count of rank-update launches (last repeat). */
+  double   update_ms[3];
+  uint32_t update_launches[3];
 } prx_result;
 
 typedef struct prx_context prx_context;
@@ -124,6 +131,10 @@ int prx_graph_create(prx_context* ctx, uint32_t n, uint64_t m,
 int prx_graph_destroy(prx_graph* g);
 /* Current vertex / edge counts (m changes with prx_graph_apply_batch). */
 int prx_graph_size(const prx_graph* g, uint32_t* n, uint64_t* m);
+/* Vertices and in-edges in each in-degree class of the rank update:
+ * [0] in-degree <= 64 (thread per vertex), [1] up to the warp limit (warp per
+ * vertex), [2] above it (block per vertex).  Either pointer may be NULL. */
+int prx_graph_class_stats(const prx_graph* g, uint32_t vertices[3], uint64_t edges[3]);
 /* Copy the graph back to host buffers (any pointer may be NULL). */
 int prx_graph_download(prx_graph* g, uint32_t* xoff, uint32_t* xedg,
                        uint32_t* xtoff, uint32_t* xtedg, uint32_t* xtdat);

@@ -194,10 +194,13 @@ int orc_solve(int mode, uint32_t n, uint64_t m,
 
 int orc_cpu_static(uint32_t n, const uint32_t* xtoff, const uint32_t* xtedg,
                    const uint32_t* xtdat, const orc_options* o, double* ranks,
-                   int threads, int sweeps_cap) {
+                   int threads, int sweeps_cap, double* time_ms) {
   /* pagerankStaticOmp<ASYNC=false> (inc/pagerank.hxx:474-482): init 1/N
    * (:303-313), then sync sweeps (pagerankUpdateRanksSyncOmp :217-227,
-   * pagerankUpdateRank :131-141) and liNormDeltaOmp (inc/_vector.hxx:1266). */
+   * pagerankUpdateRank :131-141) and liNormDeltaOmp (inc/_vector.hxx:1266).
+   * *time_ms (optional) covers what the reference's `time` covers
+   * (:423-438): initialisation and sweeps, not the allocations. */
+  if (time_ms) *time_ms = 0;
   if (n == 0) return 0;
 #ifdef _OPENMP
   if (threads > 0) omp_set_num_threads(threads);
@@ -210,6 +213,9 @@ int orc_cpu_static(uint32_t n, const uint32_t* xtoff, const uint32_t* xtedg,
   double* a = (double*)malloc(sizeof(double) * n);
   double* r = (double*)malloc(sizeof(double) * n);
   const int64_t N = n;
+#ifdef _OPENMP
+  const double t0 = omp_get_wtime();
+#endif
   #pragma omp parallel for schedule(static)
   for (int64_t v = 0; v < N; ++v) { r[v] = 1.0 / (double)n; a[v] = r[v]; }
   const double C0 = (1 - P) / (double)n;
@@ -231,6 +237,9 @@ int orc_cpu_static(uint32_t n, const uint32_t* xtoff, const uint32_t* xtedg,
     double* t = a; a = r; r = t;
     if (el < E) break;
   }
+#ifdef _OPENMP
+  if (time_ms) *time_ms = (omp_get_wtime() - t0) * 1e3;
+#endif
   memcpy(ranks, r, sizeof(double) * n);
   free(a); free(r);
   return l;

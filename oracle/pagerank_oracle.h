@@ -70,10 +70,12 @@ void orc_mark_traversal(uint32_t n, const uint32_t* xoff, const uint32_t* xedg,
                         const uint32_t* insu, uint64_t ni, uint8_t* vaff);
 
 /* Reference CPU Static PageRank, synchronous, OpenMP
- * (inc/pagerank.hxx:217-227, 413-440, 474-482).  Returns iterations. */
+ * (inc/pagerank.hxx:217-227, 413-440, 474-482).  Returns iterations; at
+ * most sweeps_cap sweeps when sweeps_cap > 0; *time_ms (may be NULL) gets
+ * the time of initialisation + sweeps, as the reference's `time`. */
 int orc_cpu_static(uint32_t n, const uint32_t* xtoff, const uint32_t* xtedg,
                    const uint32_t* xtdat, const orc_options* o, double* ranks,
-                   int threads, int sweeps_cap);
+                   int threads, int sweeps_cap, double* time_ms);
 
 /* Reference CPU DF-P, asynchronous, OpenMP (inc/pagerankPrune.hxx:141-158,
  * 227-263, 306-311), initial marking per inc/pagerank.hxx:663-676.  The

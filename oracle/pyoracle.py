@@ -51,7 +51,8 @@ def lib():
             f.restype = None
             f.argtypes = [C.c_uint32, u32p, u32p, C.c_void_p, C.c_void_p, u64, C.c_void_p, u64, u8p]
         L.orc_cpu_static.restype = C.c_int
-        L.orc_cpu_static.argtypes = [C.c_uint32, u32p, u32p, u32p, C.POINTER(Options), f64p, C.c_int, C.c_int]
+        L.orc_cpu_static.argtypes = [C.c_uint32, u32p, u32p, u32p, C.POINTER(Options), f64p, C.c_int, C.c_int,
+                                     C.POINTER(C.c_double)]
         L.orc_cpu_prune_dynamic_frontier.restype = C.c_int
         L.orc_cpu_prune_dynamic_frontier.argtypes = [C.c_uint32, u32p, u32p, u32p, u32p, u32p, u32p, u32p,
                                                      C.c_void_p, u64, C.c_void_p, u64, f64p,
@@ -110,12 +111,15 @@ def mark(kind, xoff, xedg, delu, delv, insu):
     return flags[:n]
 
 
-def cpu_static(xtoff, xtedg, xtdat, opts=None, threads=0, sweeps_cap=0):
+def cpu_static(xtoff, xtedg, xtdat, opts=None, threads=0, sweeps_cap=0, with_time=False):
+    """Reference CPU Static (sync, OpenMP) -> (ranks, iterations[, time_ms])."""
     xtoff, xtedg, xtdat = _u32(xtoff), _u32(xtedg), _u32(xtdat)
     n = len(xtoff) - 1
     ranks = np.zeros(n, np.float64)
-    it = lib().orc_cpu_static(n, xtoff, xtedg, xtdat, C.byref(opts or options()), ranks, threads, sweeps_cap)
-    return ranks, it
+    t = C.c_double()
+    it = lib().orc_cpu_static(n, xtoff, xtedg, xtdat, C.byref(opts or options()), ranks, threads, sweeps_cap,
+                              C.byref(t))
+    return (ranks, it, t.value) if with_time else (ranks, it)
 
 
 def cpu_prune_dynamic_frontier(xoff_old, xedg_old, yoff, yedg, ytoff, ytedg, ytdat, delu, insu, q,

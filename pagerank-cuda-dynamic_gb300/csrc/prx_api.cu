@@ -42,6 +42,13 @@ struct prx_context {
   uint32_t* fr[2] = {nullptr, nullptr};
   uint32_t* batch = nullptr;  // device copy of a batch
   size_t batch_cap = 0;       // in uint32 elements
+  // launch accounting and optional per-launch timing of the rank update
+  uint64_t launches = 0;
+  std::vector<cudaEvent_t> tev;   // pairs: start, end
+  std::vector<int> tev_cls;       // class of each recorded pair
+  size_t tev_used = 0;            // pairs recorded since the last drain
+  double upd_ms[NCLS] = {0, 0, 0};
+  uint32_t upd_n[NCLS] = {0, 0, 0};
 };
 
 struct prx_graph {
@@ -77,6 +84,7 @@ void prx_options_default(prx_options* o) {
   o->precision = PRX_FP64;
   o->loop = PRX_LOOP_AUTO;
   o->partition = 0;
+  o->timing = 0;
 }
 
 const char* prx_status_string(int s) {
@@ -142,6 +150,7 @@ int prx_context_destroy(prx_context* c) {
   cudaFreeHost(c->st_host);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : c->tev) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return PRX_OK;
@@ -222,11 +231,14 @@ static int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint3
   if (nd + ni == 0) return PRX_OK;  // :927,956,985 -- nothing marked
   launch_mark_seed(a, du, dv, nd, iu, ni, c->sms, s);
   launch_expand(a, EXPAND_XL, c->sms, s);
+  c->launches += 2;
   if (mode == PRX_DYNAMIC_TRAVERSAL) {
     launch_frontier_from_lists(a, c->sms, s);
+    c->launches += 1;
     for (int cur = 0;; cur ^= 1) {
       TRY_CUDA_ST(cudaMemsetAsync(&c->st->fcnt[cur ^ 1], 0, sizeof(uint32_t), s));
       launch_expand(a, EXPAND_FRONTIER | (cur << 8), c->sms, s);
+      c->launches += 1;
       TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1].fcnt[cur ^ 1], &c->st->fcnt[cur ^ 1], sizeof(uint32_t),
                                   cudaMemcpyDeviceToHost, s));
       TRY_CUDA_ST(cudaStreamSynchronize(s));
@@ -237,16 +249,50 @@ static int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint3
   return PRX_OK;
 }
 
-static void enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArgs& a, int mode) {
+// Fold the recorded update-launch timings into the context's totals.
+static int drain_timing(prx_context* c) {
+  for (size_t i = 0; i < c->tev_used; ++i) {
+    float ms = 0;
+    TRY_CUDA_ST(cudaEventElapsedTime(&ms, c->tev[2 * i], c->tev[2 * i + 1]));
+    c->upd_ms[c->tev_cls[i]] += ms;
+    c->upd_n[c->tev_cls[i]] += 1;
+  }
+  c->tev_used = 0;
+  return PRX_OK;
+}
+
+static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArgs& a, int mode, bool timing) {
   cudaStream_t s = c->stream;
-  if (mode < PRX_DYNAMIC_TRAVERSAL) {
-    launch_update_static(a, gr->g, c->sms, s);
-  } else {
-    launch_update_dynamic(a, mode, c->sms, s);
+  for (int cls = 0; cls < NCLS; ++cls) {
+    if (timing) {
+      if (c->tev.size() < 2 * (c->tev_used + 1)) {
+        cudaEvent_t e0, e1;
+        TRY_CUDA_ST(cudaEventCreate(&e0));
+        TRY_CUDA_ST(cudaEventCreate(&e1));
+        c->tev.push_back(e0);
+        c->tev.push_back(e1);
+        c->tev_cls.push_back(0);
+      }
+      TRY_CUDA_ST(cudaEventRecord(c->tev[2 * c->tev_used], s));
+    }
+    const bool launched = launch_update_class(a, gr->g, mode, cls, c->sms, s);
+    c->launches += launched;
+    if (timing && launched) {
+      TRY_CUDA_ST(cudaEventRecord(c->tev[2 * c->tev_used + 1], s));
+      c->tev_cls[c->tev_used++] = cls;
+    }
+  }
+  if (mode >= PRX_DYNAMIC_TRAVERSAL) {
     launch_commit(a, mode, c->sms, s);
-    if (mode >= PRX_DYNAMIC_FRONTIER) launch_expand(a, EXPAND_XL_INTO_NEXT, c->sms, s);
+    c->launches += 1;
+    if (mode >= PRX_DYNAMIC_FRONTIER) {
+      launch_expand(a, EXPAND_XL_INTO_NEXT, c->sms, s);
+      c->launches += 1;
+    }
   }
   launch_finalize(a, mode, s);
+  c->launches += 1;
+  return PRX_OK;
 }
 
 // Core solve; q_dev/batch arrays are device pointers.  On success *final_ranks
@@ -264,10 +310,15 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   const SolveArgs a = make_args(c, g, o);
   const int repeat = o.repeat > 0 ? o.repeat : 1;
   float ti = 0, tm = 0, tc = 0, tt = 0;
+  const bool timing = o.timing != 0;
   for (int rep = 0; rep < repeat; ++rep) {
+    c->launches = 0;
+    c->tev_used = 0;
+    for (int k = 0; k < NCLS; ++k) { c->upd_ms[k] = 0; c->upd_n[k] = 0; }
     TRY_CUDA_ST(cudaEventRecord(c->ev[0], s));
     launch_state_reset(c->st, o.max_iterations, o.tolerance, s);
     launch_init_ranks(a, (mode == PRX_STATIC) ? nullptr : q_dev, dyn, s);
+    c->launches += 2;
     TRY_CUDA_ST(cudaEventRecord(c->ev[1], s));
     if (dyn) {
       st = run_marking(c, a, mode, du, dv, nd, iu, ni);
@@ -276,10 +327,14 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
     }
     TRY_CUDA_ST(cudaEventRecord(c->ev[2], s));
     for (int k = 1;; k = std::min(2 * k, 16)) {
-      for (int i = 0; i < k; ++i) enqueue_iteration(c, gr, a, mode);
+      for (int i = 0; i < k; ++i) {
+        st = enqueue_iteration(c, gr, a, mode, timing);
+        if (st) return st;
+      }
       TRY_CUDA_ST(cudaGetLastError());
       TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
       TRY_CUDA_ST(cudaStreamSynchronize(s));
+      if (timing && (st = drain_timing(c))) return st;
       if (c->st_host[1].done) break;
     }
     TRY_CUDA_ST(cudaEventRecord(c->ev[3], s));
@@ -301,6 +356,11 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
     res->edges_processed = dyn ? h.edges : g.m * (uint64_t)h.iter;
     res->last_delta = h.last_delta;
     res->refinements = 0;
+    res->kernel_launches = c->launches;
+    for (int k = 0; k < NCLS; ++k) {
+      res->update_ms[k] = c->upd_ms[k];
+      res->update_launches[k] = c->upd_n[k];
+    }
   }
   *final_ranks = dyn ? c->r[0] : c->r[h.iter & 1];
   return PRX_OK;
@@ -385,6 +445,15 @@ int prx_graph_size(const prx_graph* gr, uint32_t* n, uint64_t* m) {
   if (!gr) FAIL(PRX_EINVAL, "prx_graph_size: NULL graph");
   if (n) *n = gr->g.n;
   if (m) *m = gr->g.m;
+  return PRX_OK;
+}
+
+int prx_graph_class_stats(const prx_graph* gr, uint32_t vertices[3], uint64_t edges[3]) {
+  if (!gr) FAIL(PRX_EINVAL, "prx_graph_class_stats: NULL graph");
+  for (int k = 0; k < NCLS; ++k) {
+    if (vertices) vertices[k] = gr->g.cls_begin[k + 1] - gr->g.cls_begin[k];
+    if (edges) edges[k] = gr->g.cls_edges[k];
+  }
   return PRX_OK;
 }
 

@@ -107,30 +107,56 @@ __global__ void __launch_bounds__(256) k_cls_scatter(const uint32_t* __restrict_
   }
 }
 
-cudaError_t build_classes(GraphDev& g, int, cudaStream_t s) {
+// In-edges per class (statistics for the roofline): one u64 atomic per block
+// and class.
+__global__ void __launch_bounds__(256) k_cls_edges(const uint32_t* __restrict__ xtoff, uint32_t n, uint32_t mid_max,
+                                                   unsigned long long* __restrict__ out) {
+  __shared__ unsigned long long acc[NCLS];
+  if (threadIdx.x < NCLS) acc[threadIdx.x] = 0;
+  __syncthreads();
+  unsigned long long mine[NCLS] = {0, 0, 0};
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    mine[in_class(xtoff, v, mid_max)] += xtoff[v + 1] - xtoff[v];
+  for (int c = 0; c < NCLS; ++c)
+    if (mine[c]) atomicAdd(&acc[c], mine[c]);
+  __syncthreads();
+  if (threadIdx.x < NCLS && acc[threadIdx.x]) atomicAdd(&out[threadIdx.x], acc[threadIdx.x]);
+}
+
+cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
   const uint32_t n = g.n;
   if (n == 0) {
     for (int c = 0; c <= NCLS; ++c) g.cls_begin[c] = 0;
+    for (int c = 0; c < NCLS; ++c) g.cls_edges[c] = 0;
     return cudaSuccess;
   }
   const uint32_t ntiles = (n + kTileV - 1) / kTileV;
   uint32_t* cnt = nullptr;
-  cudaError_t e = cudaMallocAsync(&cnt, sizeof(uint32_t) * ((size_t)NCLS * ntiles + NCLS + 1), s);
+  // [class-major tile counts | 4 bounds | pad | 3 u64 edge sums]
+  const size_t words = (size_t)NCLS * ntiles + NCLS + 1;
+  const size_t bytes = ((words * sizeof(uint32_t) + 7) & ~(size_t)7) + NCLS * sizeof(unsigned long long);
+  cudaError_t e = cudaMallocAsync(&cnt, bytes, s);
   if (e != cudaSuccess) return e;
   uint32_t* bounds = cnt + (size_t)NCLS * ntiles;
+  unsigned long long* edges = (unsigned long long*)((char*)cnt + ((words * sizeof(uint32_t) + 7) & ~(size_t)7));
   if (!g.cls_list) {
     e = cudaMalloc(&g.cls_list, sizeof(uint32_t) * n);
     if (e != cudaSuccess) { cudaFreeAsync(cnt, s); return e; }
   }
+  e = cudaMemsetAsync(edges, 0, NCLS * sizeof(unsigned long long), s);
   k_cls_count<<<ntiles, 256, 0, s>>>(g.xtoff, n, g.mid_max, ntiles, cnt);
   k_cls_scan<<<1, 1024, 0, s>>>(cnt, ntiles, bounds);
   k_cls_scatter<<<ntiles, 256, 0, s>>>(g.xtoff, n, g.mid_max, ntiles, cnt, g.cls_list);
+  k_cls_edges<<<sms * 4, 256, 0, s>>>(g.xtoff, n, g.mid_max, edges);
   uint32_t hb[NCLS + 1];
-  e = cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s);
+  unsigned long long he[NCLS];
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(he, edges, sizeof(he), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   cudaFreeAsync(cnt, s);
   if (e != cudaSuccess) return e;
   for (int c = 0; c <= NCLS; ++c) g.cls_begin[c] = hb[c];
+  for (int c = 0; c < NCLS; ++c) g.cls_edges[c] = he[c];
   return cudaGetLastError();
 }
 

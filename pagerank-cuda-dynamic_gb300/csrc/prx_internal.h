@@ -48,6 +48,7 @@ struct GraphDev {
   uint32_t* xtdat = nullptr;      // out-degree
   uint32_t* cls_list = nullptr;   // n ids: LOW ids, then MID, then HIGH (each ascending)
   uint32_t cls_begin[NCLS + 1] = {0, 0, 0, 0};
+  uint64_t cls_edges[NCLS] = {0, 0, 0};  // in-edges per class
   uint32_t mid_max = kDefaultMidMax;
 };
 
@@ -75,8 +76,8 @@ struct SolveArgs {
 
 // ---- launchers (prx_update.cu) ------------------------------------------
 void launch_init_ranks(const SolveArgs& a, const double* q, bool dynamic, cudaStream_t s);
-void launch_update_static(const SolveArgs& a, const GraphDev& g, int sms, cudaStream_t s);
-void launch_update_dynamic(const SolveArgs& a, int mode, int sms, cudaStream_t s);
+// Rank update of one in-degree class; false if nothing was launched.
+bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cls, int sms, cudaStream_t s);
 void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s);
 
 // ---- launchers (prx_mark.cu) --------------------------------------------

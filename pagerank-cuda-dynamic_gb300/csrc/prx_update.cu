@@ -243,31 +243,29 @@ void launch_init_ranks(const SolveArgs& a, const double* q, bool, cudaStream_t s
 }
 
 template <int MODE>
-static void update_static_t(const SolveArgs& a, const GraphDev& g, int sms, cudaStream_t s) {
-  const uint32_t nl = g.cls_begin[1] - g.cls_begin[0];
-  const uint32_t nm = g.cls_begin[2] - g.cls_begin[1];
-  const uint32_t nh = g.cls_begin[3] - g.cls_begin[2];
-  if (nl) k_update_low<MODE><<<cap_grid((nl + kThreads - 1) / kThreads, sms * 8), kThreads, 0, s>>>(a, g.cls_begin[0], nl);
-  if (nm) k_update_mid<MODE><<<cap_grid((nm + 7) / 8, sms * 8), kThreads, 0, s>>>(a, g.cls_begin[1], nm);
-  if (nh) k_update_high<MODE><<<cap_grid(nh, sms * 4), 256, 0, s>>>(a, g.cls_begin[2], nh);
+static bool update_class_t(const SolveArgs& a, const GraphDev& g, int cls, int sms, cudaStream_t s) {
+  if (ModeTraits<MODE>::DYN) {
+    // list lengths live on the device: fixed grids that stride over them
+    if (cls == LOW) k_update_low<MODE><<<sms * 8, kThreads, 0, s>>>(a, 0, 0);
+    else if (cls == MID) k_update_mid<MODE><<<sms * 4, kThreads, 0, s>>>(a, 0, 0);
+    else k_update_high<MODE><<<sms * 2, 256, 0, s>>>(a, 0, 0);
+    return true;
+  }
+  const uint32_t b = g.cls_begin[cls], cnt = g.cls_begin[cls + 1] - b;
+  if (!cnt) return false;
+  if (cls == LOW) k_update_low<MODE><<<cap_grid((cnt + kThreads - 1) / kThreads, sms * 8), kThreads, 0, s>>>(a, b, cnt);
+  else if (cls == MID) k_update_mid<MODE><<<cap_grid((cnt + 7) / 8, sms * 8), kThreads, 0, s>>>(a, b, cnt);
+  else k_update_high<MODE><<<cap_grid(cnt, sms * 4), 256, 0, s>>>(a, b, cnt);
+  return true;
 }
 
-void launch_update_static(const SolveArgs& a, const GraphDev& g, int sms, cudaStream_t s) {
-  update_static_t<PRX_STATIC>(a, g, sms, s);
-}
-
-template <int MODE>
-static void update_dynamic_t(const SolveArgs& a, int sms, cudaStream_t s) {
-  k_update_low<MODE><<<sms * 8, kThreads, 0, s>>>(a, 0, 0);
-  k_update_mid<MODE><<<sms * 4, kThreads, 0, s>>>(a, 0, 0);
-  k_update_high<MODE><<<sms * 2, 256, 0, s>>>(a, 0, 0);
-}
-
-void launch_update_dynamic(const SolveArgs& a, int mode, int sms, cudaStream_t s) {
+bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cls, int sms, cudaStream_t s) {
   switch (mode) {
-    case PRX_DYNAMIC_TRAVERSAL: update_dynamic_t<PRX_DYNAMIC_TRAVERSAL>(a, sms, s); break;
-    case PRX_DYNAMIC_FRONTIER: update_dynamic_t<PRX_DYNAMIC_FRONTIER>(a, sms, s); break;
-    default: update_dynamic_t<PRX_PRUNE_DYNAMIC_FRONTIER>(a, sms, s); break;
+    case PRX_STATIC:
+    case PRX_NAIVE_DYNAMIC: return update_class_t<PRX_STATIC>(a, g, cls, sms, s);
+    case PRX_DYNAMIC_TRAVERSAL: return update_class_t<PRX_DYNAMIC_TRAVERSAL>(a, g, cls, sms, s);
+    case PRX_DYNAMIC_FRONTIER: return update_class_t<PRX_DYNAMIC_FRONTIER>(a, g, cls, sms, s);
+    default: return update_class_t<PRX_PRUNE_DYNAMIC_FRONTIER>(a, g, cls, sms, s);
   }
 }
 

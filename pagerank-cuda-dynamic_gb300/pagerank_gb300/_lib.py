@@ -21,7 +21,7 @@ class Options(C.Structure):
     """prx_options (PagerankOptions<V>, inc/pagerank.hxx:24-55, plus GB300 knobs)."""
     _fields_ = [("repeat", C.c_int), ("tolerance", C.c_double), ("frontier_tolerance", C.c_double),
                 ("prune_tolerance", C.c_double), ("damping", C.c_double), ("max_iterations", C.c_int),
-                ("precision", C.c_int), ("loop", C.c_int), ("partition", C.c_int)]
+                ("precision", C.c_int), ("loop", C.c_int), ("partition", C.c_int), ("timing", C.c_int)]
 
 
 class Result(C.Structure):
@@ -29,10 +29,15 @@ class Result(C.Structure):
     _fields_ = [("iterations", C.c_int), ("time_ms", C.c_float), ("initialization_time_ms", C.c_float),
                 ("marking_time_ms", C.c_float), ("computation_time_ms", C.c_float),
                 ("affected_initial", C.c_uint64), ("edges_processed", C.c_uint64),
-                ("last_delta", C.c_double), ("refinements", C.c_int)]
+                ("last_delta", C.c_double), ("refinements", C.c_int), ("kernel_launches", C.c_uint64),
+                ("update_ms", C.c_double * 3), ("update_launches", C.c_uint32 * 3)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {}
+        for k, _ in self._fields_:
+            v = getattr(self, k)
+            d[k] = list(v) if hasattr(v, "__len__") else v
+        return d
 
 
 class HostCsr(C.Structure):
@@ -49,7 +54,8 @@ class PrxError(RuntimeError):
 _lib = None
 EXPORTS = (
     "prx_options_default", "prx_status_string", "prx_last_error", "prx_context_create", "prx_context_destroy",
-    "prx_context_stream", "prx_graph_create", "prx_graph_destroy", "prx_graph_size", "prx_graph_download",
+    "prx_context_stream", "prx_graph_create", "prx_graph_destroy", "prx_graph_size", "prx_graph_class_stats",
+    "prx_graph_download",
     "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_host_csr_free",
     "prx_gen_rmat", "prx_gen_weblike", "prx_gen_grid", "prx_gen_batch", "prx_host_tidy_batch",
     "prx_host_apply_batch", "prx_host_transpose", "prx_host_free",
@@ -82,6 +88,7 @@ def load(build_if_missing=True):
         "prx_graph_create": (i32, [vp, C.c_uint32, u64, vp, vp, vp, vp, vp, i32, C.POINTER(vp)]),
         "prx_graph_destroy": (i32, [vp]),
         "prx_graph_size": (i32, [vp, C.POINTER(C.c_uint32), C.POINTER(u64)]),
+        "prx_graph_class_stats": (i32, [vp, C.POINTER(C.c_uint32), C.POINTER(u64)]),
         "prx_graph_download": (i32, [vp, vp, vp, vp, vp, vp]),
         "prx_graph_apply_batch": (i32, [vp, vp, vp, u64, vp, vp, u64]),
         "prx_solve": (i32, [vp, vp, i32, vp, vp, u64, vp, vp, u64, vp, C.POINTER(Options), vp, C.POINTER(Result)]),

@@ -97,6 +97,12 @@ class Graph:
         check(load().prx_graph_size(self._h, C.byref(n), C.byref(m)), "prx_graph_size")
         return n.value, m.value
 
+    def class_stats(self):
+        """(vertices[3], in-edges[3]) per in-degree class of the rank update."""
+        nv, ne = (C.c_uint32 * 3)(), (C.c_uint64 * 3)()
+        check(load().prx_graph_class_stats(self._h, nv, ne), "prx_graph_class_stats")
+        return list(nv), list(ne)
+
     def apply_batch(self, del_u, del_v, ins_u, ins_v):
         du, dv, iu, iv = (_u32(a) for a in (del_u, del_v, ins_u, ins_v))
         check(load().prx_graph_apply_batch(self._h, _p(du), _p(dv), len(du), _p(iu), _p(iv), len(iu)),
@@ -140,6 +146,14 @@ def solve(ctx, g, mode, deletions=None, insertions=None, q=None, opts=None):
                            _p(iu), _p(iv), 0 if iu is None else len(iu), _p(qq), C.byref(opts or options()),
                            ranks.ctypes.data, C.byref(res)), "prx_solve")
     return ranks[:n], res.as_dict()
+
+
+def solve_into(ctx, g, mode, ranks_host_ptr, q_host_ptr=None, opts=None):
+    """prx_solve into a caller-owned host buffer (e.g. pinned memory) -> result dict."""
+    res = Result()
+    check(load().prx_solve(ctx.handle, g.handle, int(mode), None, None, 0, None, None, 0, q_host_ptr,
+                           C.byref(opts or options()), ranks_host_ptr, C.byref(res)), "prx_solve")
+    return res.as_dict()
 
 
 def solve_device(ctx, g, mode, q_ptr, ranks_ptr, batch_ptrs=(None, None, 0, None, None, 0), opts=None):
