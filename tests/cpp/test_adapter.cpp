@@ -117,8 +117,9 @@ int main() {
     const int it = orc_solve(mode, NV, on_y ? ye.size() : xe.size(), on_y ? yo.data() : xo.data(), on_y ? ye.data() : xe.data(),
                              on_y ? yto.data() : xto.data(), on_y ? yte.data() : xte.data(), on_y ? ytd.data() : xtd.data(),
                              du.data(), dv.data(), du.size(), iu.data(), iv.data(), iu.size(), qq, &o, want.data(), nullptr);
-    bool ok = got.iterations == it && got.ranks.size() == 3 * NV;
-    for (K i = 0; ok && i < 3 * NV; ++i) ok = (i % 3) ? got.ranks[i] == 0 : got.ranks[i] == want[i / 3];
+    const size_t S = x.span();  // ranks are indexed by original id, span = 3*(NV-1)+1
+    bool ok = got.iterations == it && got.ranks.size() == S;
+    for (K i = 0; ok && i < S; ++i) ok = (i % 3) ? got.ranks[i] == 0 : got.ranks[i] == want[i / 3];
     printf("%-28s iterations %3d (oracle %3d) %s\n", name, got.iterations, it, ok ? "bit-exact" : "MISMATCH");
     fails += !ok;
   };
@@ -128,8 +129,10 @@ int main() {
   cmp("pagerankDynamicTraversalCuda", 2, dt, q.data(), true);
   cmp("pagerankDynamicFrontierCuda", 3, df, q.data(), true);
   cmp("pagerankPruneDynamicFrontier", 4, dp, q.data(), true);
-  bool fok = sf.iterations == s0.iterations;
-  for (K i = 0; fok && i < 3 * NV; ++i) fok = sf.ranks[i] == (float)s0.ranks[i];
+  // PagerankOptions<float> carries float-rounded parameters (damping
+  // 0.85f = 0.8500000238...), so the solve differs slightly from the FP64 one.
+  bool fok = sf.ranks.size() == s0.ranks.size();
+  for (K i = 0; fok && i < s0.ranks.size(); ++i) fok = std::fabs(sf.ranks[i] - s0.ranks[i]) <= 1e-5 * s0.ranks[i] + 1e-12;
   printf("%-28s %s\n", "V=float", fok ? "ok" : "MISMATCH");
   fails += !fok;
   MiniGraph<> e0;
