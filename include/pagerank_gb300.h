@@ -177,6 +177,25 @@ int prx_mark_affected(prx_context* ctx, prx_graph* g, int mode,
                       const uint32_t* delu, const uint32_t* delv, uint64_t nd,
                       const uint32_t* insu, uint64_t ni, uint8_t* flags_out);
 
+/* Static FP64 PageRank that allocates no memory.  No counterpart in the
+ * reference: it serves callers that may not allocate device memory behind
+ * their own allocator (a serving process that reserves its HBM up front, a
+ * plugin host that owns all device memory).  The caller passes the in-CSR,
+ * the out-degrees and the ranks buffer (n doubles), all in device memory;
+ * stream is a cudaStream_t or NULL.  Results and iteration count equal
+ * prx_solve(PRX_STATIC) bit for bit.  Scratch is one static device array
+ * sized for PRX_NOALLOC_MAX_VERTICES vertices (24 MiB per GPU that uses the
+ * call, held until the process exits); larger n returns PRX_ERANGE.  All
+ * calls share that array, so calls that overlap on the GPU race and must be
+ * ordered by the caller.  The first call on a device looks up the array's
+ * device address with that device current.  Returns after the solve
+ * finished. */
+#define PRX_NOALLOC_MAX_VERTICES 1048576u
+int prx_static_solve_noalloc(uint32_t n, uint64_t m,
+                             const uint32_t* xtoff, const uint32_t* xtedg, const uint32_t* xtdat,
+                             double damping, double tolerance, int max_iterations,
+                             double* ranks, int* iterations, void* stream);
+
 /* ---- host-side graph utilities (C++ / OpenMP; no device work) ---------- */
 
 /* A CSR allocated by the library; free with prx_host_csr_free. */
