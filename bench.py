@@ -52,7 +52,11 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-dfp", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=2)
-    return p.parse_args()
+    p.add_argument("--static-only", action="store_true", help="upload only the in-CSR; skip DF-P and the CPU leg")
+    a = p.parse_args()
+    if a.static_only:
+        a.no_dfp = a.no_cpu = True
+    return a
 
 
 def make_graph(args, pg):
@@ -213,7 +217,7 @@ def run_ours(args):
     n, m = len(xoff) - 1, len(xedg)
     ctx = pg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    g = pg.Graph(ctx, *xt, xoff, xedg)
+    g = pg.Graph(ctx, *xt) if args.static_only else pg.Graph(ctx, *xt, xoff, xedg)
     cls_v, cls_e = g.class_stats()
     ranks = torch.empty(n, dtype=torch.float64, device=f"cuda:{local}")
     opts = pg.options(timing=1)
