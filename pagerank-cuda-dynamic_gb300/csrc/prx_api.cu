@@ -34,8 +34,8 @@ struct prx_context {
   bool ws_dyn = false;
   double* r[2] = {nullptr, nullptr};
   double* c[2] = {nullptr, nullptr};
-  uint8_t* uflags = nullptr;
-  uint32_t* vaff = nullptr;
+  uint8_t* flags = nullptr;   // byte flags for prx_mark_affected
+  uint32_t* bm[3] = {nullptr, nullptr, nullptr};
   uint32_t* naff = nullptr;
   uint32_t* lists[2][NCLS] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   uint32_t* xl = nullptr;
@@ -132,8 +132,8 @@ static void free_ws(prx_context* c) {
     cudaFree(c->fr[p]); c->fr[p] = nullptr;
     for (int k = 0; k < NCLS; ++k) { cudaFree(c->lists[p][k]); c->lists[p][k] = nullptr; }
   }
-  cudaFree(c->uflags); c->uflags = nullptr;
-  cudaFree(c->vaff); c->vaff = nullptr;
+  cudaFree(c->flags); c->flags = nullptr;
+  for (auto& b : c->bm) { cudaFree(b); b = nullptr; }
   cudaFree(c->naff); c->naff = nullptr;
   cudaFree(c->xl); c->xl = nullptr;
   c->ws_n = 0;
@@ -172,14 +172,12 @@ static int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
     TRY_CUDA_ST(cudaMalloc(&c->c[p], sizeof(double) * cap));
   }
   if (want_dyn) {
-    TRY_CUDA_ST(cudaMalloc(&c->uflags, cap));
-    TRY_CUDA_ST(cudaMalloc(&c->vaff, sizeof(uint32_t) * words));
+    TRY_CUDA_ST(cudaMalloc(&c->flags, cap));
+    for (auto& b : c->bm) TRY_CUDA_ST(cudaMalloc(&b, sizeof(uint32_t) * words));
     TRY_CUDA_ST(cudaMalloc(&c->naff, sizeof(uint32_t) * words));
     TRY_CUDA_ST(cudaMalloc(&c->xl, sizeof(uint32_t) * cap));
-    for (int p = 0; p < 2; ++p) {
-      TRY_CUDA_ST(cudaMalloc(&c->fr[p], sizeof(uint32_t) * cap));
-      for (int k = 0; k < NCLS; ++k) TRY_CUDA_ST(cudaMalloc(&c->lists[p][k], sizeof(uint32_t) * cap));
-    }
+    for (int p = 0; p < 2; ++p) TRY_CUDA_ST(cudaMalloc(&c->fr[p], sizeof(uint32_t) * cap));
+    for (int k = MID; k < NCLS; ++k) TRY_CUDA_ST(cudaMalloc(&c->lists[0][k], sizeof(uint32_t) * cap));
   }
   c->ws_n = cap;
   c->ws_dyn = want_dyn;
@@ -208,7 +206,8 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
     a.fr[p] = c->fr[p];
     for (int k = 0; k < NCLS; ++k) a.list[p][k] = c->lists[p][k];
   }
-  a.uflags = c->uflags; a.vaff = c->vaff; a.naff = c->naff; a.xl = c->xl;
+  for (int k = 0; k < 3; ++k) a.bm[k] = c->bm[k];
+  a.naff = c->naff; a.xl = c->xl;
   a.st = c->st;
   a.n = g.n;
   a.mid_max = g.mid_max;
@@ -226,18 +225,18 @@ static int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint3
                        uint64_t nd, const uint32_t* iu, uint64_t ni) {
   cudaStream_t s = c->stream;
   const size_t words = ((size_t)a.n + 31) / 32;
-  TRY_CUDA_ST(cudaMemsetAsync(c->vaff, 0, words * 4, s));
+  for (auto b : c->bm) TRY_CUDA_ST(cudaMemsetAsync(b, 0, words * 4, s));
   TRY_CUDA_ST(cudaMemsetAsync(c->naff, 0, words * 4, s));
   if (nd + ni == 0) return PRX_OK;  // :927,956,985 -- nothing marked
   launch_mark_seed(a, du, dv, nd, iu, ni, c->sms, s);
-  launch_expand(a, EXPAND_XL, c->sms, s);
+  launch_expand_seeds(a, c->sms, s);
   c->launches += 2;
   if (mode == PRX_DYNAMIC_TRAVERSAL) {
-    launch_frontier_from_lists(a, c->sms, s);
+    launch_frontier_from_bitmap(a, c->sms, s);
     c->launches += 1;
     for (int cur = 0;; cur ^= 1) {
       TRY_CUDA_ST(cudaMemsetAsync(&c->st->fcnt[cur ^ 1], 0, sizeof(uint32_t), s));
-      launch_expand(a, EXPAND_FRONTIER | (cur << 8), c->sms, s);
+      launch_expand_frontier(a, cur, c->sms, s);
       c->launches += 1;
       TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1].fcnt[cur ^ 1], &c->st->fcnt[cur ^ 1], sizeof(uint32_t),
                                   cudaMemcpyDeviceToHost, s));
@@ -246,6 +245,8 @@ static int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint3
     }
   }
   TRY_CUDA_ST(cudaMemsetAsync(&c->st->xcnt, 0, sizeof(uint32_t), s));
+  launch_popcount(c->bm[0], a.n, &c->st->affected, c->sms, s);
+  c->launches += 1;
   return PRX_OK;
 }
 
@@ -282,13 +283,9 @@ static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArg
       c->tev_cls[c->tev_used++] = cls;
     }
   }
-  if (mode >= PRX_DYNAMIC_TRAVERSAL) {
-    launch_commit(a, mode, c->sms, s);
+  if (mode >= PRX_DYNAMIC_FRONTIER) {
+    launch_expand_queued(a, c->sms, s);  // high out-degree vertices whose change exceeded D
     c->launches += 1;
-    if (mode >= PRX_DYNAMIC_FRONTIER) {
-      launch_expand(a, EXPAND_XL_INTO_NEXT, c->sms, s);
-      c->launches += 1;
-    }
   }
   launch_finalize(a, mode, s);
   c->launches += 1;
@@ -352,7 +349,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
     res->initialization_time_ms = ti / repeat;
     res->marking_time_ms = tm / repeat;
     res->computation_time_ms = tc / repeat;
-    res->affected_initial = dyn ? (uint64_t)c->st_host[0].cnt[0][0] + c->st_host[0].cnt[0][1] + c->st_host[0].cnt[0][2] : g.n;
+    res->affected_initial = dyn ? c->st_host[0].affected : g.n;
     res->edges_processed = dyn ? h.edges : g.m * (uint64_t)h.iter;
     res->last_delta = h.last_delta;
     res->refinements = 0;
@@ -362,7 +359,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
       res->update_launches[k] = c->upd_n[k];
     }
   }
-  *final_ranks = dyn ? c->r[0] : c->r[h.iter & 1];
+  *final_ranks = c->r[h.iter & 1];
   return PRX_OK;
 }
 
@@ -620,8 +617,8 @@ int prx_mark_affected(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   launch_state_reset(c->st, 0, 0.0, s);
   st = run_marking(c, a, mode, c->batch, c->batch + nd, nd, c->batch + 2 * nd, ni);
   if (st) return st;
-  launch_flags_from_bitmap(c->vaff, c->uflags, g.n, s);
-  TRY_CUDA_ST(cudaMemcpyAsync(flags_out, c->uflags, g.n, cudaMemcpyDeviceToHost, s));
+  launch_flags_from_bitmap(c->bm[0], c->flags, g.n, s);
+  TRY_CUDA_ST(cudaMemcpyAsync(flags_out, c->flags, g.n, cudaMemcpyDeviceToHost, s));
   TRY_CUDA_ST(cudaStreamSynchronize(s));
   TRY_CUDA_ST(cudaGetLastError());
   return PRX_OK;

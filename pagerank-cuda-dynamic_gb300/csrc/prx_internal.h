@@ -30,11 +30,12 @@ struct State {
   int pad0;
   double tol;
   double last_delta;
-  uint32_t cnt[2][NCLS];          // dynamic: affected-list lengths [parity][class]
+  uint32_t cnt[2][NCLS];          // dynamic: queued MID / HIGH vertices (cnt[0][MID], cnt[0][HIGH])
   uint32_t xcnt;                  // vertices whose out-neighbours must be marked
   uint32_t fcnt[2];               // DT closure frontier lengths
   uint32_t err;                   // device-detected error code, 0 = none
   unsigned long long edges;       // in-edges gathered (statistic)
+  unsigned long long affected;    // vertices marked before the first iteration
 };
 
 struct GraphDev {
@@ -60,13 +61,12 @@ struct SolveArgs {
   const uint32_t* xtedg;
   const uint32_t* xtdat;
   const uint32_t* cls_list;       // static classes (see GraphDev)
-  double* r[2];                   // FP64 ranks, ping-pong (dynamic: r[0] = ranks, r[1] = new values)
-  double* c[2];                   // FP64 contributions r/outdeg, ping-pong (dynamic: c[0])
-  uint8_t* uflags;                // dynamic: per-vertex update flags (bit0 pruned, bit1 expand)
-  uint32_t* vaff;                 // bitmap of affected vertices
-  uint32_t* naff;                 // bitmap of seeded sources
-  uint32_t* list[2][NCLS];        // dynamic affected lists
-  uint32_t* xl;                   // vertices to expand
+  double* r[2];                   // FP64 ranks, ping-pong by iteration parity
+  double* c[2];                   // FP64 contributions r/outdeg, ping-pong
+  uint32_t* bm[3];                // affected bitmaps: iteration k uses bm[k%3] (cur), bm[(k+1)%3] (next)
+  uint32_t* naff;                 // bitmap of seeded sources (marking)
+  uint32_t* list[2][NCLS];        // dynamic: affected MID / HIGH vertices queued per iteration (list[0])
+  uint32_t* xl;                   // vertices whose out-neighbours must be marked
   uint32_t* fr[2];                // DT closure frontiers
   State* st;
   uint32_t n;
@@ -80,12 +80,15 @@ void launch_init_ranks(const SolveArgs& a, const double* q, bool dynamic, cudaSt
 bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cls, int sms, cudaStream_t s);
 void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s);
 
+void launch_expand_queued(const SolveArgs& a, int sms, cudaStream_t s);
+
 // ---- launchers (prx_mark.cu) --------------------------------------------
 void launch_mark_seed(const SolveArgs& a, const uint32_t* delu, const uint32_t* delv, uint64_t nd,
                       const uint32_t* insu, uint64_t ni, int sms, cudaStream_t s);
-void launch_expand(const SolveArgs& a, int which, int sms, cudaStream_t s);
-void launch_frontier_from_lists(const SolveArgs& a, int sms, cudaStream_t s);
-void launch_commit(const SolveArgs& a, int mode, int sms, cudaStream_t s);
+void launch_expand_seeds(const SolveArgs& a, int sms, cudaStream_t s);
+void launch_frontier_from_bitmap(const SolveArgs& a, int sms, cudaStream_t s);
+void launch_expand_frontier(const SolveArgs& a, int cur, int sms, cudaStream_t s);
+void launch_popcount(const uint32_t* bm, uint32_t n, unsigned long long* out, int sms, cudaStream_t s);
 void launch_flags_from_bitmap(const uint32_t* bm, uint8_t* out, uint32_t n, cudaStream_t s);
 void launch_state_reset(State* st, int max_iter, double tol, cudaStream_t s);
 
@@ -94,9 +97,6 @@ cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s);
 // b: device array [du | dv | iu | iv | tdk | tdv | tik | tiv]; t* = batch sorted by (v, u)
 cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd, uint64_t ni, int sms, cudaStream_t s);
 cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t len, cudaStream_t s);
-
-// which list launch_expand reads
-enum ExpandSrc { EXPAND_XL = 0, EXPAND_XL_INTO_NEXT = 1, EXPAND_FRONTIER = 2 };
 
 void set_error(const std::string& msg);
 

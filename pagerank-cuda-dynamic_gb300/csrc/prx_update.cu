@@ -22,6 +22,17 @@
 // reduction pass (liNormDeltaInplaceCuW, inc/_cuda.hxx:926-934) is needed.
 // C0 + P*x is written as fma(): nvcc contracts the reference's expression
 // into one DFMA.
+//
+// Vertex order.  The LOW kernel walks vertex ids in order, one warp per 32
+// consecutive ids, so neighbouring rows and their local gathers stay close.
+// The dynamic modes (DT, DF, DF-P) keep the affected set as bitmaps and the
+// ranks / contributions as a ping-pong pair, like Static: iteration k reads
+// parity p and writes parity p^1 for the vertices it updates.  A vertex that
+// was updated in k-1 but is not updated in k has a stale copy in parity p^1
+// and is copied across (the only copies needed -- the reference copies every
+// unaffected vertex, :94-96).  Three bitmaps rotate: cur (k), nxt (k+1),
+// prev (k-1); the LOW kernel clears prev after reading it, which makes it the
+// empty nxt of iteration k+1.
 #include "prx_device.cuh"
 
 namespace prx {
@@ -30,79 +41,139 @@ template <int MODE> struct ModeTraits {
   static constexpr bool DYN = MODE >= PRX_DYNAMIC_TRAVERSAL;
   static constexpr bool FRONTIER = MODE >= PRX_DYNAMIC_FRONTIER;
   static constexpr bool PRUNE = MODE == PRX_PRUNE_DYNAMIC_FRONTIER;
-  static constexpr bool FIXED_LISTS = MODE == PRX_DYNAMIC_TRAVERSAL;
 };
 
-// Finish vertex v given its contribution sum; returns |a_v - r_v| as bits.
+__device__ __forceinline__ uint32_t* bm_at(const SolveArgs& a, int k) { return a.bm[k]; }
+
+// Mark the out-neighbours of u in bitmap nxt (u's rank changed by more than
+// the frontier tolerance; pagerankAffectedExtend*CukU :313-366, 686-687).
+__device__ __forceinline__ void expand_inline(const SolveArgs& a, uint32_t u, uint32_t* nxt) {
+  const uint32_t e = a.xoff[u + 1];
+  for (uint32_t j = a.xoff[u]; j < e; ++j) {
+    const uint32_t w = a.xedg[j];
+    const uint32_t bit = 1u << (w & 31u);
+    if (!(nxt[w >> 5] & bit)) atomicOr(&nxt[w >> 5], bit);
+  }
+}
+
+// Finish vertex v given its contribution sum.  Returns |a_v - r_v| as bits.
+// *survive (dynamic) tells whether v stays affected next iteration.
 template <int MODE>
-__device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, uint32_t v, double cv, int p) {
+__device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, uint32_t v, double cv, int p,
+                                                            bool& survive) {
   using T = ModeTraits<MODE>;
   const uint32_t d = a.xtdat[v];
-  const double rv = T::DYN ? a.r[0][v] : a.r[p][v];
+  const double rv = a.r[p][v];
   double av;
   if (T::PRUNE) av = fma(a.P, cv - rv / (double)d, a.C0) * (1 / (1 - (a.P / (double)d)));
   else          av = fma(a.P, cv, a.C0);
   const double ev = fabs(av - rv);
-  if (T::DYN) {
-    a.r[1][v] = av;
-    if (T::FRONTIER) {
-      const double rel = ev / fmax(rv, av);
-      uint8_t f = 0;
-      if (T::PRUNE && rel <= a.C) { f |= 1; clear_bit(a.vaff, v); }
-      if (rel > a.D) f |= 2;
-      a.uflags[v] = f;
+  a.r[p ^ 1][v] = av;
+  a.c[p ^ 1][v] = av / (double)d;
+  survive = true;
+  if (T::FRONTIER) {
+    const double rel = ev / fmax(rv, av);
+    if (T::PRUNE && rel <= a.C) survive = false;  // :106
+    if (rel > a.D) {                              // :107, expanded after the sweep
+      uint32_t* nxt = a.bm[(a.st->iter + 1) % 3];
+      if (a.xoff[v + 1] - a.xoff[v] <= kLowMax) expand_inline(a, v, nxt);
+      else push(a.xl, &a.st->xcnt, v);
     }
-  } else {
-    a.r[p ^ 1][v] = av;
-    a.c[p ^ 1][v] = av / (double)d;
   }
   return dbits(ev);
 }
 
+// ---- LOW: one warp per 32 consecutive vertex ids ------------------------------
 template <int MODE>
-__device__ __forceinline__ void list_of(const SolveArgs& a, int cls, uint32_t begin, uint32_t count_static, int p,
-                                        const uint32_t*& list, uint32_t& count) {
+__global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a) {
   using T = ModeTraits<MODE>;
+  State* st = a.st;
+  if (st->done) return;
+  const int iter = st->iter, p = iter & 1;
+  const double* __restrict__ c = a.c[p];
+  const uint32_t* __restrict__ xtedg = a.xtedg;
+  uint32_t *cur = nullptr, *nxt = nullptr, *prev = nullptr;
   if (T::DYN) {
-    const int q = T::FIXED_LISTS ? 0 : p;
-    list = a.list[q][cls];
-    count = a.st->cnt[q][cls];
+    cur = a.bm[iter % 3];
+    nxt = a.bm[(iter + 1) % 3];
+    prev = a.bm[(iter + 2) % 3];
+  }
+  const uint32_t lane = lane_id();
+  const uint32_t words = (a.n + 31) >> 5;
+  unsigned long long emax = 0, edges = 0;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t v = (w << 5) | lane;
+    bool mine = v < a.n;
+    if (T::DYN) {
+      const uint32_t cw = cur[w], pw = prev[w];
+      if (((pw & ~cw) >> lane) & 1u) {  // updated last iteration, not this one: refresh parity p^1
+        a.r[p ^ 1][v] = a.r[p][v];
+        a.c[p ^ 1][v] = a.c[p][v];
+      }
+      if (lane == 0 && pw) prev[w] = 0;  // becomes the empty nxt of iteration k+1
+      mine = mine && ((cw >> lane) & 1u);
+      if (!__any_sync(0xffffffffu, mine)) continue;
+    }
+    uint32_t s = 0, e = 0;
+    if (mine) {
+      s = a.xtoff[v];
+      e = a.xtoff[v + 1];
+      if (e - s > kLowMax) {
+        if (T::DYN) {
+          const int cls = e - s <= a.mid_max ? MID : HIGH;
+          push(a.list[0][cls], &st->cnt[0][cls], v);
+        }
+        mine = false;
+      }
+    }
+    bool survive = false;
+    if (mine) {
+      double acc = 0.0;
+      uint32_t j = s;
+      for (; j + 4 <= e; j += 4) {
+        const uint32_t u0 = __ldg(xtedg + j), u1 = __ldg(xtedg + j + 1);
+        const uint32_t u2 = __ldg(xtedg + j + 2), u3 = __ldg(xtedg + j + 3);
+        const double c0 = __ldg(c + u0), c1 = __ldg(c + u1), c2 = __ldg(c + u2), c3 = __ldg(c + u3);
+        acc += c0; acc += c1; acc += c2; acc += c3;
+      }
+      for (; j < e; ++j) acc += __ldg(c + __ldg(xtedg + j));
+      const unsigned long long ev = finish_vertex<MODE>(a, v, acc, p, survive);
+      emax = ev > emax ? ev : emax;
+      edges += e - s;
+    }
+    if (T::DYN) {
+      const unsigned keep = __ballot_sync(0xffffffffu, mine && survive);
+      if (lane == 0 && keep) atomicOr(&nxt[w], keep);
+    }
+  }
+  block_max_bits(emax, &st->el_bits[p]);
+  if (T::DYN) block_sum_u64(edges, &st->edges);
+}
+
+// MID / HIGH lists: Static and ND use the graph's class lists; the dynamic
+// modes use the affected MID / HIGH vertices the LOW kernel queued.
+template <int MODE>
+__device__ __forceinline__ void list_of(const SolveArgs& a, int cls, uint32_t begin, uint32_t count_static,
+                                        const uint32_t*& list, uint32_t& count) {
+  if (ModeTraits<MODE>::DYN) {
+    list = a.list[0][cls];
+    count = a.st->cnt[0][cls];
   } else {
     list = a.cls_list + begin;
     count = count_static;
   }
 }
 
-// ---- LOW: thread per vertex -------------------------------------------------
 template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, uint32_t begin, uint32_t count_static) {
-  using T = ModeTraits<MODE>;
-  if (a.st->done) return;
-  const int p = a.st->iter & 1;
-  const uint32_t* list;
-  uint32_t count;
-  list_of<MODE>(a, LOW, begin, count_static, p, list, count);
-  const double* __restrict__ c = T::DYN ? a.c[0] : a.c[p];
-  const uint32_t* __restrict__ xtedg = a.xtedg;
-  unsigned long long emax = 0, edges = 0;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-    const uint32_t v = list[i];
-    const uint32_t s = a.xtoff[v], e = a.xtoff[v + 1];
-    double acc = 0.0;
-    uint32_t j = s;
-    for (; j + 4 <= e; j += 4) {
-      const uint32_t u0 = __ldg(xtedg + j), u1 = __ldg(xtedg + j + 1);
-      const uint32_t u2 = __ldg(xtedg + j + 2), u3 = __ldg(xtedg + j + 3);
-      const double c0 = __ldg(c + u0), c1 = __ldg(c + u1), c2 = __ldg(c + u2), c3 = __ldg(c + u3);
-      acc += c0; acc += c1; acc += c2; acc += c3;
-    }
-    for (; j < e; ++j) acc += __ldg(c + __ldg(xtedg + j));
-    const unsigned long long ev = finish_vertex<MODE>(a, v, acc, p);
-    emax = ev > emax ? ev : emax;
-    edges += e - s;
+__device__ __forceinline__ void finish_listed(const SolveArgs& a, uint32_t v, double x, int p,
+                                              unsigned long long& emax) {
+  bool survive;
+  const unsigned long long ev = finish_vertex<MODE>(a, v, x, p, survive);
+  emax = ev > emax ? ev : emax;
+  if (ModeTraits<MODE>::DYN && survive) {
+    uint32_t* nxt = a.bm[(a.st->iter + 1) % 3];
+    atomicOr(&nxt[v >> 5], 1u << (v & 31u));
   }
-  block_max_bits(emax, &a.st->el_bits[p]);
-  if (T::DYN) block_sum_u64(edges, &a.st->edges);
 }
 
 // ---- MID: warp per vertex, 256 virtual threads --------------------------------
@@ -113,8 +184,8 @@ __global__ void __launch_bounds__(kThreads) k_update_mid(SolveArgs a, uint32_t b
   const int p = a.st->iter & 1;
   const uint32_t* list;
   uint32_t count;
-  list_of<MODE>(a, MID, begin, count_static, p, list, count);
-  const double* __restrict__ c = T::DYN ? a.c[0] : a.c[p];
+  list_of<MODE>(a, MID, begin, count_static, list, count);
+  const double* __restrict__ c = a.c[p];
   const uint32_t lane = lane_id();
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -147,8 +218,7 @@ __global__ void __launch_bounds__(kThreads) k_update_mid(SolveArgs a, uint32_t b
 #pragma unroll
     for (int o = 16; o; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if (lane == 0) {
-      const unsigned long long ev = finish_vertex<MODE>(a, v, x, p);
-      emax = ev > emax ? ev : emax;
+      finish_listed<MODE>(a, v, x, p, emax);
       edges += d;
     }
   }
@@ -165,8 +235,8 @@ __global__ void __launch_bounds__(256) k_update_high(SolveArgs a, uint32_t begin
   const int p = a.st->iter & 1;
   const uint32_t* list;
   uint32_t count;
-  list_of<MODE>(a, HIGH, begin, count_static, p, list, count);
-  const double* __restrict__ c = T::DYN ? a.c[0] : a.c[p];
+  list_of<MODE>(a, HIGH, begin, count_static, list, count);
+  const double* __restrict__ c = a.c[p];
   const uint32_t t = threadIdx.x;
   unsigned long long emax = 0, edges = 0;
   for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
@@ -197,8 +267,7 @@ __global__ void __launch_bounds__(256) k_update_high(SolveArgs a, uint32_t begin
 #pragma unroll
       for (int o = 16; o; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
       if (t == 0) {
-        const unsigned long long ev = finish_vertex<MODE>(a, v, x, p);
-        emax = ev > emax ? ev : emax;
+        finish_listed<MODE>(a, v, x, p, emax);
         edges += d;
       }
     }
@@ -208,19 +277,43 @@ __global__ void __launch_bounds__(256) k_update_high(SolveArgs a, uint32_t begin
   if (T::DYN) block_sum_u64(edges, &a.st->edges);
 }
 
-// ---- init / finalize ----------------------------------------------------------
-__global__ void k_init_ranks(SolveArgs a, const double* __restrict__ q) {
-  // pagerankInitializeRanksCukW (inc/pagerankCuda.hxx:232-239) or the copy of
-  // the previous ranks (:810,817), plus the contributions r/outdeg.
-  const double r0 = 1.0 / (double)a.n;
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
-    const double r = q ? q[v] : r0;
-    a.r[0][v] = r;
-    a.c[0][v] = r / (double)a.xtdat[v];
+// ---- expansion of high out-degree vertices (warp per vertex) ----------------
+__global__ void __launch_bounds__(kThreads) k_expand_queued(SolveArgs a) {
+  State* st = a.st;
+  if (st->done) return;
+  uint32_t* nxt = a.bm[(st->iter + 1) % 3];
+  const uint32_t count = st->xcnt;
+  const uint32_t lane = lane_id();
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t u = a.xl[i];
+    const uint32_t e = a.xoff[u + 1];
+    for (uint32_t j = a.xoff[u] + lane; j < e; j += 32) {
+      const uint32_t w = a.xedg[j];
+      const uint32_t bit = 1u << (w & 31u);
+      if (!(nxt[w >> 5] & bit)) atomicOr(&nxt[w >> 5], bit);
+    }
   }
 }
 
-template <bool DYN, bool FIXED>
+// ---- init / finalize ----------------------------------------------------------
+__global__ void k_init_ranks(SolveArgs a, const double* __restrict__ q, int both) {
+  // pagerankInitializeRanksCukW (inc/pagerankCuda.hxx:232-239) or the copy of
+  // the previous ranks (:810,817), plus the contributions r/outdeg.  The
+  // dynamic modes fill both parities (a vertex never updated reads either).
+  const double r0 = 1.0 / (double)a.n;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
+    const double r = q ? q[v] : r0;
+    const double c = r / (double)a.xtdat[v];
+    a.r[0][v] = r;
+    a.c[0][v] = c;
+    if (both) {
+      a.r[1][v] = r;
+      a.c[1][v] = c;
+    }
+  }
+}
+
+template <bool DYN>
 __global__ void k_finalize(State* st) {
   if (st->done) return;
   const int p = st->iter & 1;
@@ -229,8 +322,8 @@ __global__ void k_finalize(State* st) {
   st->iter += 1;
   if (el < st->tol || st->iter >= st->max_iter) st->done = 1;  // pagerankLoopCuU :680,689
   st->el_bits[p ^ 1] = 0;
-  if (DYN && !FIXED) {
-    st->cnt[p][0] = st->cnt[p][1] = st->cnt[p][2] = 0;
+  if (DYN) {
+    st->cnt[0][MID] = st->cnt[0][HIGH] = 0;
     st->xcnt = 0;
   }
 }
@@ -238,23 +331,29 @@ __global__ void k_finalize(State* st) {
 // ---- launchers ------------------------------------------------------------------
 static inline int cap_grid(uint64_t want, int cap) { return (int)(want < (uint64_t)cap ? (want ? want : 1) : cap); }
 
-void launch_init_ranks(const SolveArgs& a, const double* q, bool, cudaStream_t s) {
-  k_init_ranks<<<cap_grid((a.n + kThreads - 1) / kThreads, 152 * 16), kThreads, 0, s>>>(a, q);
+void launch_init_ranks(const SolveArgs& a, const double* q, bool dynamic, cudaStream_t s) {
+  k_init_ranks<<<cap_grid((a.n + kThreads - 1) / kThreads, 152 * 16), kThreads, 0, s>>>(a, q, dynamic ? 1 : 0);
 }
 
 template <int MODE>
 static bool update_class_t(const SolveArgs& a, const GraphDev& g, int cls, int sms, cudaStream_t s) {
-  if (ModeTraits<MODE>::DYN) {
-    // list lengths live on the device: fixed grids that stride over them
-    if (cls == LOW) k_update_low<MODE><<<sms * 8, kThreads, 0, s>>>(a, 0, 0);
-    else if (cls == MID) k_update_mid<MODE><<<sms * 4, kThreads, 0, s>>>(a, 0, 0);
+  constexpr bool DYN = ModeTraits<MODE>::DYN;
+  if (cls == LOW) {
+    // static: skip when the graph has no LOW vertex; dynamic: always (it also
+    // maintains the bitmaps)
+    if (!DYN && g.cls_begin[1] == g.cls_begin[0]) return false;
+    const uint64_t words = ((uint64_t)g.n + 31) / 32;
+    k_update_low<MODE><<<cap_grid((words + 7) / 8, sms * 8), kThreads, 0, s>>>(a);
+    return true;
+  }
+  if (DYN) {
+    if (cls == MID) k_update_mid<MODE><<<sms * 4, kThreads, 0, s>>>(a, 0, 0);
     else k_update_high<MODE><<<sms * 2, 256, 0, s>>>(a, 0, 0);
     return true;
   }
   const uint32_t b = g.cls_begin[cls], cnt = g.cls_begin[cls + 1] - b;
   if (!cnt) return false;
-  if (cls == LOW) k_update_low<MODE><<<cap_grid((cnt + kThreads - 1) / kThreads, sms * 8), kThreads, 0, s>>>(a, b, cnt);
-  else if (cls == MID) k_update_mid<MODE><<<cap_grid((cnt + 7) / 8, sms * 8), kThreads, 0, s>>>(a, b, cnt);
+  if (cls == MID) k_update_mid<MODE><<<cap_grid((cnt + 7) / 8, sms * 8), kThreads, 0, s>>>(a, b, cnt);
   else k_update_high<MODE><<<cap_grid(cnt, sms * 4), 256, 0, s>>>(a, b, cnt);
   return true;
 }
@@ -269,11 +368,13 @@ bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cl
   }
 }
 
+void launch_expand_queued(const SolveArgs& a, int sms, cudaStream_t s) {
+  k_expand_queued<<<sms * 4, kThreads, 0, s>>>(a);
+}
+
 void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s) {
-  // DT keeps its affected lists for the whole loop; DF / DF-P rebuild them.
-  if (mode < PRX_DYNAMIC_TRAVERSAL) k_finalize<false, false><<<1, 1, 0, s>>>(a.st);
-  else if (mode == PRX_DYNAMIC_TRAVERSAL) k_finalize<true, true><<<1, 1, 0, s>>>(a.st);
-  else k_finalize<true, false><<<1, 1, 0, s>>>(a.st);
+  if (mode < PRX_DYNAMIC_TRAVERSAL) k_finalize<false><<<1, 1, 0, s>>>(a.st);
+  else k_finalize<true><<<1, 1, 0, s>>>(a.st);
 }
 
 }  // namespace prx
