@@ -296,6 +296,7 @@ def run_ours(args):
         err = float((out - ranks).abs().max())
         dfp = {"batch": {"deletions": len(du), "insertions": len(iu)}, "apply_ms": apply_ms,
                "dfp_ms": r_dfp2["time_ms"], "dfp_iterations": r_dfp2["iterations"],
+               "dfp_marking_ms": r_dfp2["marking_time_ms"], "dfp_computation_ms": r_dfp2["computation_time_ms"],
                "dfp_affected_initial": r_dfp2["affected_initial"], "dfp_edges": r_dfp2["edges_processed"],
                "df_ms": r_df["time_ms"], "df_iterations": r_df["iterations"],
                "static_ms": r_st["time_ms"], "static_iterations": r_st["iterations"],

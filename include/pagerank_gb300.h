@@ -81,6 +81,10 @@ typedef struct {
                                  same either way [0]                         */
   int    timing;              /* 1: time every rank-update launch with CUDA
                                  events (prx_result.update_*) [0]            */
+  int    expansion;           /* DF / DF-P marking after each sweep: 0 picks
+                                 push or pull per iteration, 1 always pushes
+                                 from changed vertices, 2 always pulls into
+                                 unmarked ones; the marked set is the same [0] */
 } prx_options;
 
 /* PagerankResult<V> (inc/pagerank.hxx:64-113) minus the rank vector, which

@@ -36,6 +36,8 @@ struct prx_context {
   double* c[2] = {nullptr, nullptr};
   uint8_t* flags = nullptr;   // byte flags for prx_mark_affected
   uint32_t* bm[3] = {nullptr, nullptr, nullptr};
+  uint32_t* nf[2] = {nullptr, nullptr};
+  uint32_t* xb = nullptr;
   uint32_t* naff = nullptr;
   uint32_t* lists[2][NCLS] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   uint32_t* xl = nullptr;
@@ -85,6 +87,7 @@ void prx_options_default(prx_options* o) {
   o->loop = PRX_LOOP_AUTO;
   o->partition = 0;
   o->timing = 0;
+  o->expansion = 0;
 }
 
 const char* prx_status_string(int s) {
@@ -134,6 +137,8 @@ static void free_ws(prx_context* c) {
   }
   cudaFree(c->flags); c->flags = nullptr;
   for (auto& b : c->bm) { cudaFree(b); b = nullptr; }
+  for (auto& b : c->nf) { cudaFree(b); b = nullptr; }
+  cudaFree(c->xb); c->xb = nullptr;
   cudaFree(c->naff); c->naff = nullptr;
   cudaFree(c->xl); c->xl = nullptr;
   c->ws_n = 0;
@@ -174,6 +179,8 @@ static int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
   if (want_dyn) {
     TRY_CUDA_ST(cudaMalloc(&c->flags, cap));
     for (auto& b : c->bm) TRY_CUDA_ST(cudaMalloc(&b, sizeof(uint32_t) * words));
+    for (auto& b : c->nf) TRY_CUDA_ST(cudaMalloc(&b, sizeof(uint32_t) * words));
+    TRY_CUDA_ST(cudaMalloc(&c->xb, sizeof(uint32_t) * cap));
     TRY_CUDA_ST(cudaMalloc(&c->naff, sizeof(uint32_t) * words));
     TRY_CUDA_ST(cudaMalloc(&c->xl, sizeof(uint32_t) * cap));
     for (int p = 0; p < 2; ++p) TRY_CUDA_ST(cudaMalloc(&c->fr[p], sizeof(uint32_t) * cap));
@@ -207,7 +214,10 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
     for (int k = 0; k < NCLS; ++k) a.list[p][k] = c->lists[p][k];
   }
   for (int k = 0; k < 3; ++k) a.bm[k] = c->bm[k];
-  a.naff = c->naff; a.xl = c->xl;
+  a.nf[0] = c->nf[0]; a.nf[1] = c->nf[1];
+  a.naff = c->naff; a.xl = c->xl; a.xb = c->xb;
+  // expand by pulling once more than 1/16 of the vertices changed by > D
+  a.pull_threshold = o.expansion == 1 ? 0xffffffffu : (o.expansion == 2 ? 0u : g.n / 16);
   a.st = c->st;
   a.n = g.n;
   a.mid_max = g.mid_max;
@@ -226,11 +236,14 @@ static int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint3
   cudaStream_t s = c->stream;
   const size_t words = ((size_t)a.n + 31) / 32;
   for (auto b : c->bm) TRY_CUDA_ST(cudaMemsetAsync(b, 0, words * 4, s));
+  for (auto b : c->nf) TRY_CUDA_ST(cudaMemsetAsync(b, 0, words * 4, s));
   TRY_CUDA_ST(cudaMemsetAsync(c->naff, 0, words * 4, s));
   if (nd + ni == 0) return PRX_OK;  // :927,956,985 -- nothing marked
   launch_mark_seed(a, du, dv, nd, iu, ni, c->sms, s);
   launch_expand_seeds(a, c->sms, s);
-  c->launches += 2;
+  launch_expand_big(a, 0, c->sms, s);
+  c->launches += 3;
+  TRY_CUDA_ST(cudaMemsetAsync(&c->st->xbcnt, 0, sizeof(uint32_t), s));
   if (mode == PRX_DYNAMIC_TRAVERSAL) {
     launch_frontier_from_bitmap(a, c->sms, s);
     c->launches += 1;
@@ -284,8 +297,8 @@ static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArg
     }
   }
   if (mode >= PRX_DYNAMIC_FRONTIER) {
-    launch_expand_queued(a, c->sms, s);  // high out-degree vertices whose change exceeded D
-    c->launches += 1;
+    launch_expand_iteration(a, c->sms, s);  // push or pull, chosen on the device
+    c->launches += 3;
   }
   launch_finalize(a, mode, s);
   c->launches += 1;

@@ -36,6 +36,8 @@ struct State {
   uint32_t err;                   // device-detected error code, 0 = none
   unsigned long long edges;       // in-edges gathered (statistic)
   unsigned long long affected;    // vertices marked before the first iteration
+  uint32_t nfcnt;                 // DF / DF-P: vertices whose change exceeded D this iteration
+  uint32_t xbcnt;                 // high out-degree vertices queued for block-wide expansion
 };
 
 struct GraphDev {
@@ -66,11 +68,14 @@ struct SolveArgs {
   uint32_t* bm[3];                // affected bitmaps: iteration k uses bm[k%3] (cur), bm[(k+1)%3] (next)
   uint32_t* naff;                 // bitmap of seeded sources (marking)
   uint32_t* list[2][NCLS];        // dynamic: affected MID / HIGH vertices queued per iteration (list[0])
-  uint32_t* xl;                   // vertices whose out-neighbours must be marked
+  uint32_t* xl;                   // marking: queued sources
+  uint32_t* xb;                   // high out-degree vertices to expand block-wide
+  uint32_t* nf[2];                // DF / DF-P: bitmap of vertices whose change exceeded D, by parity
   uint32_t* fr[2];                // DT closure frontiers
   State* st;
   uint32_t n;
   uint32_t mid_max;
+  uint32_t pull_threshold;        // expand by pulling when more than this many vertices changed by > D
   double C0, P, D, C;
 };
 
@@ -80,7 +85,12 @@ void launch_init_ranks(const SolveArgs& a, const double* q, bool dynamic, cudaSt
 bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cls, int sms, cudaStream_t s);
 void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s);
 
-void launch_expand_queued(const SolveArgs& a, int sms, cudaStream_t s);
+// DF / DF-P expansion after an iteration's updates: push from the changed
+// vertices or pull into the unmarked ones, chosen on the device.
+void launch_expand_iteration(const SolveArgs& a, int sms, cudaStream_t s);
+// Block-per-vertex expansion of the queued high out-degree vertices into
+// bitmap `target` (0..2), or into the next-iteration bitmap when target < 0.
+void launch_expand_big(const SolveArgs& a, int target, int sms, cudaStream_t s);
 
 // ---- launchers (prx_mark.cu) --------------------------------------------
 void launch_mark_seed(const SolveArgs& a, const uint32_t* delu, const uint32_t* delv, uint64_t nd,

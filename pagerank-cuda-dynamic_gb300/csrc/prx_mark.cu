@@ -35,15 +35,20 @@ __global__ void k_mark_seed(SolveArgs a, const uint32_t* __restrict__ delu, cons
   }
 }
 
-// Mark the out-neighbours of every queued source in bitmap 0, one warp per source.
+// Mark the out-neighbours of every queued source in bitmap 0, one warp per
+// source; sources with more than 1024 out-edges go to the block-wide queue.
 __global__ void __launch_bounds__(kThreads) k_expand_seeds(SolveArgs a) {
   const uint32_t count = a.st->xcnt;
   uint32_t* b0 = a.bm[0];
   const uint32_t lane = lane_id();
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t u = a.xl[i];
-    const uint32_t e = a.xoff[u + 1];
-    for (uint32_t j = a.xoff[u] + lane; j < e; j += 32) set_bit(b0, a.xedg[j]);
+    const uint32_t b = a.xoff[u], e = a.xoff[u + 1];
+    if (e - b > 1024) {
+      if (lane == 0) push(a.xb, &a.st->xbcnt, u);
+      continue;
+    }
+    for (uint32_t j = b + lane; j < e; j += 32) set_bit(b0, a.xedg[j]);
   }
 }
 
@@ -98,6 +103,8 @@ __global__ void k_state_reset(State* st, int max_iter, double tol) {
   st->err = 0;
   st->edges = 0;
   st->affected = 0;
+  st->nfcnt = 0;
+  st->xbcnt = 0;
 }
 
 // ---- launchers ------------------------------------------------------------------

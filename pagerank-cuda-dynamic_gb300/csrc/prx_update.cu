@@ -43,24 +43,18 @@ template <int MODE> struct ModeTraits {
   static constexpr bool PRUNE = MODE == PRX_PRUNE_DYNAMIC_FRONTIER;
 };
 
-__device__ __forceinline__ uint32_t* bm_at(const SolveArgs& a, int k) { return a.bm[k]; }
-
-// Mark the out-neighbours of u in bitmap nxt (u's rank changed by more than
-// the frontier tolerance; pagerankAffectedExtend*CukU :313-366, 686-687).
-__device__ __forceinline__ void expand_inline(const SolveArgs& a, uint32_t u, uint32_t* nxt) {
-  const uint32_t e = a.xoff[u + 1];
-  for (uint32_t j = a.xoff[u]; j < e; ++j) {
-    const uint32_t w = a.xedg[j];
-    const uint32_t bit = 1u << (w & 31u);
-    if (!(nxt[w >> 5] & bit)) atomicOr(&nxt[w >> 5], bit);
-  }
+__device__ __forceinline__ void set_bit(uint32_t* bm, uint32_t w) {
+  const uint32_t bit = 1u << (w & 31u);
+  if (!(bm[w >> 5] & bit)) atomicOr(&bm[w >> 5], bit);
 }
 
 // Finish vertex v given its contribution sum.  Returns |a_v - r_v| as bits.
-// *survive (dynamic) tells whether v stays affected next iteration.
+// survive (dynamic): v stays affected next iteration; changed (DF / DF-P):
+// its relative change exceeded the frontier tolerance, so its out-neighbours
+// become affected (:106-107, expanded after the sweep as at :686-687).
 template <int MODE>
 __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, uint32_t v, double cv, int p,
-                                                            bool& survive) {
+                                                            bool& survive, bool& changed) {
   using T = ModeTraits<MODE>;
   const uint32_t d = a.xtdat[v];
   const double rv = a.r[p][v];
@@ -71,14 +65,11 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
   a.r[p ^ 1][v] = av;
   a.c[p ^ 1][v] = av / (double)d;
   survive = true;
+  changed = false;
   if (T::FRONTIER) {
     const double rel = ev / fmax(rv, av);
     if (T::PRUNE && rel <= a.C) survive = false;  // :106
-    if (rel > a.D) {                              // :107, expanded after the sweep
-      uint32_t* nxt = a.bm[(a.st->iter + 1) % 3];
-      if (a.xoff[v + 1] - a.xoff[v] <= kLowMax) expand_inline(a, v, nxt);
-      else push(a.xl, &a.st->xcnt, v);
-    }
+    changed = rel > a.D;                          // :107
   }
   return dbits(ev);
 }
@@ -110,7 +101,11 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a) {
         a.r[p ^ 1][v] = a.r[p][v];
         a.c[p ^ 1][v] = a.c[p][v];
       }
-      if (lane == 0 && pw) prev[w] = 0;  // becomes the empty nxt of iteration k+1
+      if (lane == 0) {
+        if (pw) prev[w] = 0;  // becomes the empty nxt of iteration k+1
+        // nf[p^1] was filled and expanded by iteration k-1; clear it for k+1
+        if (T::FRONTIER && a.nf[p ^ 1][w]) a.nf[p ^ 1][w] = 0;
+      }
       mine = mine && ((cw >> lane) & 1u);
       if (!__any_sync(0xffffffffu, mine)) continue;
     }
@@ -126,7 +121,7 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a) {
         mine = false;
       }
     }
-    bool survive = false;
+    bool survive = false, changed = false;
     if (mine) {
       double acc = 0.0;
       uint32_t j = s;
@@ -137,13 +132,20 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a) {
         acc += c0; acc += c1; acc += c2; acc += c3;
       }
       for (; j < e; ++j) acc += __ldg(c + __ldg(xtedg + j));
-      const unsigned long long ev = finish_vertex<MODE>(a, v, acc, p, survive);
+      const unsigned long long ev = finish_vertex<MODE>(a, v, acc, p, survive, changed);
       emax = ev > emax ? ev : emax;
       edges += e - s;
     }
     if (T::DYN) {
       const unsigned keep = __ballot_sync(0xffffffffu, mine && survive);
       if (lane == 0 && keep) atomicOr(&nxt[w], keep);
+    }
+    if (T::FRONTIER) {
+      const unsigned ch = __ballot_sync(0xffffffffu, mine && changed);
+      if (lane == 0 && ch) {
+        atomicOr(&a.nf[p][w], ch);
+        atomicAdd(&st->nfcnt, (uint32_t)__popc(ch));
+      }
     }
   }
   block_max_bits(emax, &st->el_bits[p]);
@@ -167,12 +169,13 @@ __device__ __forceinline__ void list_of(const SolveArgs& a, int cls, uint32_t be
 template <int MODE>
 __device__ __forceinline__ void finish_listed(const SolveArgs& a, uint32_t v, double x, int p,
                                               unsigned long long& emax) {
-  bool survive;
-  const unsigned long long ev = finish_vertex<MODE>(a, v, x, p, survive);
+  bool survive, changed;
+  const unsigned long long ev = finish_vertex<MODE>(a, v, x, p, survive, changed);
   emax = ev > emax ? ev : emax;
-  if (ModeTraits<MODE>::DYN && survive) {
-    uint32_t* nxt = a.bm[(a.st->iter + 1) % 3];
-    atomicOr(&nxt[v >> 5], 1u << (v & 31u));
+  if (ModeTraits<MODE>::DYN && survive) atomicOr(&a.bm[(a.st->iter + 1) % 3][v >> 5], 1u << (v & 31u));
+  if (ModeTraits<MODE>::FRONTIER && changed) {
+    atomicOr(&a.nf[p][v >> 5], 1u << (v & 31u));
+    atomicAdd(&a.st->nfcnt, 1u);
   }
 }
 
@@ -277,21 +280,71 @@ __global__ void __launch_bounds__(256) k_update_high(SolveArgs a, uint32_t begin
   if (T::DYN) block_sum_u64(edges, &a.st->edges);
 }
 
-// ---- expansion of high out-degree vertices (warp per vertex) ----------------
-__global__ void __launch_bounds__(kThreads) k_expand_queued(SolveArgs a) {
+// ---- DF / DF-P expansion after the sweep (:686-687) ---------------------------
+// Nothing to expand once the iteration has converged: the loop ends here.
+__device__ __forceinline__ bool expansion_needed(const State* st) {
+  return !st->done && !(__longlong_as_double((long long)st->el_bits[st->iter & 1]) < st->tol);
+}
+
+// Push: every changed vertex marks its out-neighbours; out-degree <= 64 in
+// the thread, larger ones are queued for k_expand_big.
+__global__ void __launch_bounds__(kThreads) k_expand_push(SolveArgs a) {
   State* st = a.st;
-  if (st->done) return;
+  if (!expansion_needed(st) || st->nfcnt > a.pull_threshold) return;
+  const int p = st->iter & 1;
   uint32_t* nxt = a.bm[(st->iter + 1) % 3];
-  const uint32_t count = st->xcnt;
+  const uint32_t* nf = a.nf[p];
+  const uint32_t words = (a.n + 31) >> 5;
   const uint32_t lane = lane_id();
-  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += (gridDim.x * blockDim.x) >> 5) {
-    const uint32_t u = a.xl[i];
-    const uint32_t e = a.xoff[u + 1];
-    for (uint32_t j = a.xoff[u] + lane; j < e; j += 32) {
-      const uint32_t w = a.xedg[j];
-      const uint32_t bit = 1u << (w & 31u);
-      if (!(nxt[w >> 5] & bit)) atomicOr(&nxt[w >> 5], bit);
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
+    if (!((nf[w] >> lane) & 1u)) continue;
+    const uint32_t u = (w << 5) | lane;
+    const uint32_t b = a.xoff[u], e = a.xoff[u + 1];
+    if (e - b > kLowMax) {
+      push(a.xb, &st->xbcnt, u);
+      continue;
     }
+    for (uint32_t j = b; j < e; ++j) set_bit(nxt, a.xedg[j]);
+  }
+}
+
+// Pull: a vertex not yet marked becomes affected when any in-neighbour
+// changed (the same set as the push; cheaper when most vertices changed).
+__global__ void __launch_bounds__(kThreads) k_expand_pull(SolveArgs a) {
+  State* st = a.st;
+  if (!expansion_needed(st) || st->nfcnt <= a.pull_threshold) return;
+  const int p = st->iter & 1;
+  uint32_t* nxt = a.bm[(st->iter + 1) % 3];
+  const uint32_t* nf = a.nf[p];
+  const uint32_t words = (a.n + 31) >> 5;
+  const uint32_t lane = lane_id();
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t word = nxt[w];
+    const uint32_t v = (w << 5) | lane;
+    bool hit = false;
+    if (v < a.n && !((word >> lane) & 1u)) {
+      const uint32_t e = a.xtoff[v + 1];
+      for (uint32_t j = a.xtoff[v]; j < e && !hit; ++j) {
+        const uint32_t u = a.xtedg[j];
+        hit = (nf[u >> 5] >> (u & 31u)) & 1u;
+      }
+    }
+    const unsigned add = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0 && add) nxt[w] = word | add;  // this warp is the only writer of word w here
+  }
+}
+
+// Block-wide expansion of queued high out-degree vertices into bitmap `target`
+// (initial marking) or, with target < 0, into the next iteration's bitmap.
+__global__ void __launch_bounds__(256) k_expand_big(SolveArgs a, int target) {
+  State* st = a.st;
+  if (target < 0 && !expansion_needed(st)) return;
+  uint32_t* bm = target < 0 ? a.bm[(st->iter + 1) % 3] : a.bm[target];
+  const uint32_t count = st->xbcnt;
+  for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
+    const uint32_t u = a.xb[i];
+    const uint32_t e = a.xoff[u + 1];
+    for (uint32_t j = a.xoff[u] + threadIdx.x; j < e; j += blockDim.x) set_bit(bm, a.xedg[j]);
   }
 }
 
@@ -325,6 +378,8 @@ __global__ void k_finalize(State* st) {
   if (DYN) {
     st->cnt[0][MID] = st->cnt[0][HIGH] = 0;
     st->xcnt = 0;
+    st->nfcnt = 0;
+    st->xbcnt = 0;
   }
 }
 
@@ -368,8 +423,16 @@ bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cl
   }
 }
 
-void launch_expand_queued(const SolveArgs& a, int sms, cudaStream_t s) {
-  k_expand_queued<<<sms * 4, kThreads, 0, s>>>(a);
+void launch_expand_iteration(const SolveArgs& a, int sms, cudaStream_t s) {
+  const uint64_t words = ((uint64_t)a.n + 31) / 32;
+  const int grid = cap_grid((words + 7) / 8, sms * 8);
+  k_expand_push<<<grid, kThreads, 0, s>>>(a);
+  k_expand_pull<<<grid, kThreads, 0, s>>>(a);
+  k_expand_big<<<sms * 4, 256, 0, s>>>(a, -1);
+}
+
+void launch_expand_big(const SolveArgs& a, int target, int sms, cudaStream_t s) {
+  k_expand_big<<<sms * 4, 256, 0, s>>>(a, target);
 }
 
 void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s) {

@@ -115,6 +115,29 @@ def test_synthetic_all_modes_bit_exact(pg, ctx, kind):
     g.close()
 
 
+@pytest.mark.parametrize("kind", ["rmat16", "web200k"])
+def test_frontier_expansion_push_and_pull_agree(pg, ctx, kind):
+    # DF / DF-P mark the out-neighbours of every vertex whose change exceeded
+    # D; pushing from those vertices and pulling into the unmarked ones must
+    # give the oracle's ranks bit for bit, on a batch large enough that many
+    # vertices change in the first iterations.
+    xoff, xedg = _synthetic(pg, kind)
+    m = len(xedg)
+    batch = pg.graphs.random_batch(xoff, xedg, int(5e-4 * m), int(2e-3 * m), seed=5)
+    xt = O.transpose(xoff, xedg)
+    q, _ = O.solve("static", None, None, *xt)
+    yoff, yedg = pg.graphs.apply_batch(xoff, xedg, *batch)
+    yt = O.transpose(yoff, yedg)
+    g, _ = _graph(pg, ctx, yoff, yedg, yt)
+    for mode in ("dynamic_frontier", "prune_dynamic_frontier"):
+        want, it_w = _oracle(mode, yoff, yedg, yt, batch, q)
+        for expansion in (0, 1, 2):
+            got, res = _gpu(pg, ctx, g, mode, batch, q, pg.options(expansion=expansion))
+            assert res["iterations"] == it_w, (kind, mode, expansion)
+            np.testing.assert_array_equal(got, want, err_msg=f"{kind} {mode} expansion={expansion}")
+    g.close()
+
+
 def test_options_edge_cases(pg, ctx):
     xoff, xedg = pg.graphs.rmat(10, 16, seed=1)
     xt = O.transpose(xoff, xedg)
