@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--cpu-sweeps", type=int, default=3, help="sweeps in the bounded CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-dfp", action="store_true")
+    p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--static-only", action="store_true", help="upload only the in-CSR; skip DF-P and the CPU leg")
     a = p.parse_args()
@@ -258,6 +259,33 @@ def run_ours(args):
     roofline["all_update_kernels_gbs"] = all_bytes / (sum(upd_ms) / 1e3) / 1e9 if sum(upd_ms) else None
     log(f"static: {iters} iterations, {ms / args.steps:.1f} ms/step, {value:.2f} GE/s, update ms {upd_ms}")
 
+    # ---- FP32 storage + FP64 refinement, same graph, same tolerance --------------
+    fp32 = None
+    if not args.no_fp32:
+        ranks64 = ranks.clone()
+        r32 = torch.empty_like(ranks)
+        o32 = pg.options(precision=pg.FP32_REFINE, timing=1)
+        for _ in range(2):
+            pg.solve_device(ctx, g, pg.STATIC, None, r32.data_ptr(), opts=o32)
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        res32 = [pg.solve_device(ctx, g, pg.STATIC, None, r32.data_ptr(), opts=o32) for _ in range(args.steps)]
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ms32 = f0.elapsed_time(f1) / args.steps
+        it32 = [r["iterations"] for r in res32]
+        u64 = [sum(r["update_ms"][c] for r in res32) / args.steps for c in range(3)]
+        u32 = [sum(r["update32_ms"][c] for r in res32) / args.steps for c in range(3)]
+        n32 = [sum(r["update32_launches"][c] for r in res32) / args.steps for c in range(3)]
+        fp32 = {"ms_per_solve": ms32, "iterations": it32, "refinements": res32[-1]["refinements"],
+                "speedup_vs_fp64": (ms / args.steps) / ms32,
+                "linf_vs_fp64": float((r32 - ranks64).abs().max()),
+                "ge_s_fp64_equivalent": m * iters[0] / (ms32 / 1e3) / 1e9,
+                "fp64_sweep_ms": sum(u64), "fp32_sweep_ms_each": sum(u32) / max(n32[0], 1),
+                "fp32_low_gbs": (12 * cls_v[0] + 8 * cls_e[0]) * n32[0] / (u32[0] / 1e3) / 1e9 if u32[0] else None}
+        log(f"fp32-refine: {fp32}")
+
     # ---- end to end through the C ABI from pinned host buffers ----------------
     pin = [torch.from_numpy(np.asarray(a)).pin_memory() for a in xt]
     host_ranks = torch.empty(n, dtype=torch.float64).pin_memory()
@@ -319,7 +347,8 @@ def run_ours(args):
                "iterations": iters, "gpu_launches": launches,
                "e2e": {"value": e2e_value, "unit": "GE/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "ms_per_step": e2e_ms_max},
-               "roofline": roofline, "clocks": clk.summary(), "dfp": dfp, "cpu_baseline": cpu}
+               "roofline": roofline, "clocks": clk.summary(), "fp32_refine": fp32, "dfp": dfp,
+               "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     g.close()
     ctx.close()

@@ -105,6 +105,9 @@ typedef struct {
    * summed device time and count of rank-update launches (last repeat). */
   double   update_ms[3];
   uint32_t update_launches[3];
+  /* the same for the FP32 correction sweeps of PRX_FP32_REFINE */
+  double   update32_ms[3];
+  uint32_t update32_launches[3];
 } prx_result;
 
 typedef struct prx_context prx_context;
@@ -132,6 +135,8 @@ int prx_graph_create(prx_context* ctx, uint32_t n, uint64_t m,
                      const uint32_t* xoff, const uint32_t* xedg,
                      const uint32_t* xtoff, const uint32_t* xtedg,
                      const uint32_t* xtdat, int validate, prx_graph** out);
+/* A graph may be destroyed before or after its context; every other call on
+ * a graph needs its context alive. */
 int prx_graph_destroy(prx_graph* g);
 /* Current vertex / edge counts (m changes with prx_graph_apply_batch). */
 int prx_graph_size(const prx_graph* g, uint32_t* n, uint64_t* m);

@@ -42,6 +42,11 @@ struct prx_context {
   uint32_t* lists[2][NCLS] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   uint32_t* xl = nullptr;
   uint32_t* fr[2] = {nullptr, nullptr};
+  // FP32 refinement (grown on first use)
+  uint32_t ws32_n = 0;
+  float* rho = nullptr;
+  float* e32[2] = {nullptr, nullptr};
+  float* ce32[2] = {nullptr, nullptr};
   uint32_t* batch = nullptr;  // device copy of a batch
   size_t batch_cap = 0;       // in uint32 elements
   // launch accounting and optional per-launch timing of the rank update
@@ -49,8 +54,8 @@ struct prx_context {
   std::vector<cudaEvent_t> tev;   // pairs: start, end
   std::vector<int> tev_cls;       // class of each recorded pair
   size_t tev_used = 0;            // pairs recorded since the last drain
-  double upd_ms[NCLS] = {0, 0, 0};
-  uint32_t upd_n[NCLS] = {0, 0, 0};
+  double upd_ms[2 * NCLS] = {0, 0, 0, 0, 0, 0};     // [FP64 classes | FP32 classes]
+  uint32_t upd_n[2 * NCLS] = {0, 0, 0, 0, 0, 0};
 };
 
 struct prx_graph {
@@ -150,6 +155,8 @@ int prx_context_destroy(prx_context* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_ws(c);
+  cudaFree(c->rho);
+  for (int p = 0; p < 2; ++p) { cudaFree(c->e32[p]); cudaFree(c->ce32[p]); }
   cudaFree(c->batch);
   cudaFree(c->st);
   cudaFreeHost(c->st_host);
@@ -191,6 +198,24 @@ static int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
   return PRX_OK;
 }
 
+static int ensure_ws32(prx_context* c, uint32_t n) {
+  if (c->ws32_n >= n) return PRX_OK;
+  cudaFree(c->rho);
+  c->rho = nullptr;
+  for (int p = 0; p < 2; ++p) {
+    cudaFree(c->e32[p]); c->e32[p] = nullptr;
+    cudaFree(c->ce32[p]); c->ce32[p] = nullptr;
+  }
+  c->ws32_n = 0;
+  TRY_CUDA_ST(cudaMalloc(&c->rho, sizeof(float) * n));
+  for (int p = 0; p < 2; ++p) {
+    TRY_CUDA_ST(cudaMalloc(&c->e32[p], sizeof(float) * n));
+    TRY_CUDA_ST(cudaMalloc(&c->ce32[p], sizeof(float) * n));
+  }
+  c->ws32_n = n;
+  return PRX_OK;
+}
+
 static int ensure_batch(prx_context* c, size_t elems) {
   if (c->batch_cap >= elems) return PRX_OK;
   cudaFree(c->batch);
@@ -216,6 +241,8 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
   for (int k = 0; k < 3; ++k) a.bm[k] = c->bm[k];
   a.nf[0] = c->nf[0]; a.nf[1] = c->nf[1];
   a.naff = c->naff; a.xl = c->xl; a.xb = c->xb;
+  a.rho = c->rho;
+  for (int p = 0; p < 2; ++p) { a.e[p] = c->e32[p]; a.ce[p] = c->ce32[p]; }
   // expand by pulling once more than 1/16 of the vertices changed by > D
   a.pull_threshold = o.expansion == 1 ? 0xffffffffu : (o.expansion == 2 ? 0u : g.n / 16);
   a.st = c->st;
@@ -275,26 +302,37 @@ static int drain_timing(prx_context* c) {
   return PRX_OK;
 }
 
+// Launch one rank-update kernel through `fn` (returns whether it launched),
+// bracketed by CUDA events when timing; `slot` is its row in upd_ms.
+template <class F>
+static int launch_update_timed(prx_context* c, bool timing, int slot, F fn) {
+  cudaStream_t s = c->stream;
+  if (timing) {
+    if (c->tev.size() < 2 * (c->tev_used + 1)) {
+      cudaEvent_t e0, e1;
+      TRY_CUDA_ST(cudaEventCreate(&e0));
+      TRY_CUDA_ST(cudaEventCreate(&e1));
+      c->tev.push_back(e0);
+      c->tev.push_back(e1);
+      c->tev_cls.push_back(0);
+    }
+    TRY_CUDA_ST(cudaEventRecord(c->tev[2 * c->tev_used], s));
+  }
+  const bool launched = fn();
+  c->launches += launched;
+  if (timing && launched) {
+    TRY_CUDA_ST(cudaEventRecord(c->tev[2 * c->tev_used + 1], s));
+    c->tev_cls[c->tev_used++] = slot;
+  }
+  return PRX_OK;
+}
+
 static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArgs& a, int mode, bool timing) {
   cudaStream_t s = c->stream;
   for (int cls = 0; cls < NCLS; ++cls) {
-    if (timing) {
-      if (c->tev.size() < 2 * (c->tev_used + 1)) {
-        cudaEvent_t e0, e1;
-        TRY_CUDA_ST(cudaEventCreate(&e0));
-        TRY_CUDA_ST(cudaEventCreate(&e1));
-        c->tev.push_back(e0);
-        c->tev.push_back(e1);
-        c->tev_cls.push_back(0);
-      }
-      TRY_CUDA_ST(cudaEventRecord(c->tev[2 * c->tev_used], s));
-    }
-    const bool launched = launch_update_class(a, gr->g, mode, cls, c->sms, s);
-    c->launches += launched;
-    if (timing && launched) {
-      TRY_CUDA_ST(cudaEventRecord(c->tev[2 * c->tev_used + 1], s));
-      c->tev_cls[c->tev_used++] = cls;
-    }
+    const int st = launch_update_timed(c, timing, cls,
+                                       [&] { return launch_update_class(a, gr->g, mode, cls, c->sms, s); });
+    if (st) return st;
   }
   if (mode >= PRX_DYNAMIC_FRONTIER) {
     launch_expand_iteration(a, c->sms, s);  // push or pull, chosen on the device
@@ -305,6 +343,53 @@ static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArg
   return PRX_OK;
 }
 
+// FP32 refinement loop (prx_refine.cu).  *final_parity: 1 when the last FP64
+// sweep converged (its output in r[1]), 0 when the cap stopped an FP32 round
+// (the committed ranks in r[0]).
+static int run_refine_loop(prx_context* c, const prx_graph* gr, const SolveArgs& a, bool timing, int max_iter,
+                           int* final_parity) {
+  cudaStream_t s = c->stream;
+  int st;
+  for (;;) {
+    for (int cls = 0; cls < NCLS; ++cls) {
+      st = launch_update_timed(c, timing, cls, [&] { return launch_refine_sweep64(a, gr->g, cls, c->sms, s); });
+      if (st) return st;
+    }
+    launch_refine_finalize64(a, s);
+    c->launches += 1;
+    TRY_CUDA_ST(cudaGetLastError());
+    TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
+    TRY_CUDA_ST(cudaStreamSynchronize(s));
+    if (timing && (st = drain_timing(c))) return st;
+    if (c->st_host[1].done) {
+      *final_parity = 1;
+      return PRX_OK;
+    }
+    for (int k = 1;; k = std::min(2 * k, 16)) {
+      for (int i = 0; i < k; ++i) {
+        for (int cls = 0; cls < NCLS; ++cls) {
+          st = launch_update_timed(c, timing, NCLS + cls, [&] { return launch_sweep32(a, gr->g, cls, c->sms, s); });
+          if (st) return st;
+        }
+        launch_finalize32(a, s);
+        c->launches += 1;
+      }
+      TRY_CUDA_ST(cudaGetLastError());
+      TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
+      TRY_CUDA_ST(cudaStreamSynchronize(s));
+      if (timing && (st = drain_timing(c))) return st;
+      if (c->st_host[1].inner_done) break;
+    }
+    launch_refine_commit(a, c->sms, s);
+    c->launches += 1;
+    if (c->st_host[1].iter >= max_iter) {
+      TRY_CUDA_ST(cudaStreamSynchronize(s));
+      *final_parity = 0;
+      return PRX_OK;
+    }
+  }
+}
+
 // Core solve; q_dev/batch arrays are device pointers.  On success *final_ranks
 // points at the device buffer holding the ranks.
 static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* du, const uint32_t* dv, uint64_t nd,
@@ -313,9 +398,13 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   const GraphDev& g = gr->g;
   const bool dyn = mode >= PRX_DYNAMIC_TRAVERSAL;
   if (dyn && !g.xoff) FAIL(PRX_ESTATE, "prx_solve: dynamic modes need the out-CSR (xoff/xedg) of the graph");
-  if (o.precision != PRX_FP64) FAIL(PRX_EINVAL, "prx_solve: unsupported precision");
+  if (o.precision != PRX_FP64 && o.precision != PRX_FP32_REFINE) FAIL(PRX_EINVAL, "prx_solve: unknown precision");
+  const bool refine = o.precision == PRX_FP32_REFINE;
+  if (refine && dyn) FAIL(PRX_EINVAL, "prx_solve: PRX_FP32_REFINE is available for Static and ND");
   int st = ensure_ws(c, g.n, dyn);
   if (st) return st;
+  if (refine && (st = ensure_ws32(c, g.n))) return st;
+  int final_parity = -1;
   cudaStream_t s = c->stream;
   const SolveArgs a = make_args(c, g, o);
   const int repeat = o.repeat > 0 ? o.repeat : 1;
@@ -324,7 +413,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   for (int rep = 0; rep < repeat; ++rep) {
     c->launches = 0;
     c->tev_used = 0;
-    for (int k = 0; k < NCLS; ++k) { c->upd_ms[k] = 0; c->upd_n[k] = 0; }
+    for (int k = 0; k < 2 * NCLS; ++k) { c->upd_ms[k] = 0; c->upd_n[k] = 0; }
     TRY_CUDA_ST(cudaEventRecord(c->ev[0], s));
     launch_state_reset(c->st, o.max_iterations, o.tolerance, s);
     launch_init_ranks(a, (mode == PRX_STATIC) ? nullptr : q_dev, dyn, s);
@@ -336,16 +425,20 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
       TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[0], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
     }
     TRY_CUDA_ST(cudaEventRecord(c->ev[2], s));
-    for (int k = 1;; k = std::min(2 * k, 16)) {
-      for (int i = 0; i < k; ++i) {
-        st = enqueue_iteration(c, gr, a, mode, timing);
-        if (st) return st;
+    if (refine) {
+      if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, &final_parity))) return st;
+    } else {
+      for (int k = 1;; k = std::min(2 * k, 16)) {
+        for (int i = 0; i < k; ++i) {
+          st = enqueue_iteration(c, gr, a, mode, timing);
+          if (st) return st;
+        }
+        TRY_CUDA_ST(cudaGetLastError());
+        TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
+        TRY_CUDA_ST(cudaStreamSynchronize(s));
+        if (timing && (st = drain_timing(c))) return st;
+        if (c->st_host[1].done) break;
       }
-      TRY_CUDA_ST(cudaGetLastError());
-      TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
-      TRY_CUDA_ST(cudaStreamSynchronize(s));
-      if (timing && (st = drain_timing(c))) return st;
-      if (c->st_host[1].done) break;
     }
     TRY_CUDA_ST(cudaEventRecord(c->ev[3], s));
     TRY_CUDA_ST(cudaEventSynchronize(c->ev[3]));
@@ -365,14 +458,16 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
     res->affected_initial = dyn ? c->st_host[0].affected : g.n;
     res->edges_processed = dyn ? h.edges : g.m * (uint64_t)h.iter;
     res->last_delta = h.last_delta;
-    res->refinements = 0;
+    res->refinements = refine ? h.rounds : 0;
     res->kernel_launches = c->launches;
     for (int k = 0; k < NCLS; ++k) {
       res->update_ms[k] = c->upd_ms[k];
       res->update_launches[k] = c->upd_n[k];
+      res->update32_ms[k] = c->upd_ms[NCLS + k];
+      res->update32_launches[k] = c->upd_n[NCLS + k];
     }
   }
-  *final_ranks = c->r[h.iter & 1];
+  *final_ranks = refine ? c->r[final_parity] : c->r[h.iter & 1];
   return PRX_OK;
 }
 
@@ -414,6 +509,7 @@ int prx_graph_create(prx_context* c, uint32_t n, uint64_t m, const uint32_t* xof
   prx_graph* gr = new prx_graph();
   gr->ctx = c;
   GraphDev& g = gr->g;
+  g.device = c->device;
   g.n = n;
   g.m = m;
   g.m_cap = m;
@@ -440,11 +536,10 @@ int prx_graph_create(prx_context* c, uint32_t n, uint64_t m, const uint32_t* xof
 }
 
 int prx_graph_destroy(prx_graph* gr) {
+  // Does not touch the context, which may already be destroyed: cudaFree
+  // waits for the device's outstanding work on these arrays.
   if (!gr) return PRX_OK;
-  if (gr->ctx) {
-    cudaSetDevice(gr->ctx->device);
-    cudaStreamSynchronize(gr->ctx->stream);
-  }
+  cudaSetDevice(gr->g.device);
   GraphDev& g = gr->g;
   cudaFree(g.xoff); cudaFree(g.xedg); cudaFree(g.xtoff); cudaFree(g.xtedg); cudaFree(g.xtdat); cudaFree(g.cls_list);
   delete gr;

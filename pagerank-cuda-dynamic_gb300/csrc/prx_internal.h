@@ -38,9 +38,20 @@ struct State {
   unsigned long long affected;    // vertices marked before the first iteration
   uint32_t nfcnt;                 // DF / DF-P: vertices whose change exceeded D this iteration
   uint32_t xbcnt;                 // high out-degree vertices queued for block-wide expansion
+  // FP32 refinement
+  int k32;                        // FP32 sweeps in the current round (parity of e / ce)
+  int inner_done;                 // the current round's FP32 sweeps have converged / hit the cap
+  int rounds;                     // FP64 residual sweeps run
+  unsigned int el32_bits[2];      // L-inf change of the FP32 sweep with parity k32 & 1 (bits of a float >= 0)
 };
 
+// Internal mode of the update kernels: the FP64 residual sweep of the FP32
+// refinement (reads the base ranks r[0] / c[0], writes the next iterate to
+// r[1] and the residual, as FP32, to rho and e[0] / ce[0]).
+constexpr int MODE_REFINE64 = 10;
+
 struct GraphDev {
+  int device = 0;                 // device holding the arrays
   uint32_t n = 0;
   uint64_t m = 0;
   uint64_t m_cap = 0;             // capacity of the edge arrays
@@ -72,6 +83,9 @@ struct SolveArgs {
   uint32_t* xb;                   // high out-degree vertices to expand block-wide
   uint32_t* nf[2];                // DF / DF-P: bitmap of vertices whose change exceeded D, by parity
   uint32_t* fr[2];                // DT closure frontiers
+  float* rho;                     // FP32 refinement: residual of the base ranks
+  float* e[2];                    // FP32 refinement: correction, ping-pong
+  float* ce[2];                   // FP32 refinement: correction / outdeg, ping-pong
   State* st;
   uint32_t n;
   uint32_t mid_max;
@@ -84,6 +98,16 @@ void launch_init_ranks(const SolveArgs& a, const double* q, bool dynamic, cudaSt
 // Rank update of one in-degree class; false if nothing was launched.
 bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cls, int sms, cudaStream_t s);
 void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s);
+
+// ---- FP32 refinement (prx_refine.cu) --------------------------------------
+// FP64 residual sweep of one in-degree class (update kernels in MODE_REFINE64).
+bool launch_refine_sweep64(const SolveArgs& a, const GraphDev& g, int cls, int sms, cudaStream_t s);
+void launch_refine_finalize64(const SolveArgs& a, cudaStream_t s);
+// One FP32 correction sweep of one class, and its finalize.
+bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, int sms, cudaStream_t s);
+void launch_finalize32(const SolveArgs& a, cudaStream_t s);
+// x_b += e; c_b = x_b / outdeg.
+void launch_refine_commit(const SolveArgs& a, int sms, cudaStream_t s);
 
 // DF / DF-P expansion after an iteration's updates: push from the changed
 // vertices or pull into the unmarked ones, chosen on the device.

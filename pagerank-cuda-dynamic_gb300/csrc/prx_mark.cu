@@ -105,6 +105,10 @@ __global__ void k_state_reset(State* st, int max_iter, double tol) {
   st->affected = 0;
   st->nfcnt = 0;
   st->xbcnt = 0;
+  st->k32 = 0;
+  st->inner_done = 0;
+  st->rounds = 0;
+  st->el32_bits[0] = st->el32_bits[1] = 0;
 }
 
 // ---- launchers ------------------------------------------------------------------

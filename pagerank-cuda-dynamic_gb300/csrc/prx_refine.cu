@@ -1,0 +1,185 @@
+// prx_refine.cu -- FP32 storage with FP64 refinement (Static, ND).
+//
+// Defect correction around the reference's Jacobi iteration
+// (pagerankLoopCuU, inc/pagerankCuda.hxx:675-692):
+//   1. FP64 sweep from the base ranks x_b (the reference's update, its order
+//      and fma; update kernels in MODE_REFINE64): a = C0 + P*A*(x_b/d), and
+//      rho = a - x_b.  Its L-inf is the reference's convergence test; when
+//      it is below tol, a is the answer.
+//   2. FP32 sweeps of the correction: e_1 = rho, e_{k+1} = rho + P*A*(e_k/d).
+//      x_b + e_k is the k-th Jacobi iterate from x_b, so the FP32 loop stops on
+//      the same criterion, |e_{k+1} - e_k|_inf < tol.  Contributions e/d are
+//      stored and gathered in FP32 (4 bytes per edge instead of 8) and
+//      accumulated in FP32.
+//   3. x_b += e in FP64, back to 1.
+// Every FP64 and FP32 sweep counts as one iteration against max_iterations.
+#include "prx_device.cuh"
+
+namespace prx {
+
+__device__ __forceinline__ unsigned int fbits(float x) { return __float_as_uint(x); }
+
+__device__ __forceinline__ void block_max_u32(unsigned int x, unsigned int* dst) {
+  __shared__ unsigned int smax[32];
+  for (int o = 16; o; o >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, o));
+  const int w = threadIdx.x >> 5;
+  if (lane_id() == 0) smax[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    x = lane_id() < (blockDim.x >> 5) ? smax[lane_id()] : 0u;
+    for (int o = 16; o; o >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if (lane_id() == 0 && x) atomicMax(dst, x);
+  }
+}
+
+__device__ __forceinline__ unsigned int finish32(const SolveArgs& a, uint32_t v, float sum, int q) {
+  const float en = fmaf((float)a.P, sum, a.rho[v]);
+  const float dl = fabsf(en - a.e[q][v]);
+  a.e[q ^ 1][v] = en;
+  a.ce[q ^ 1][v] = en / (float)a.xtdat[v];
+  return fbits(dl);
+}
+
+// LOW: one warp per 32 consecutive ids, one lane per vertex.
+__global__ void __launch_bounds__(kThreads) k32_low(SolveArgs a) {
+  State* st = a.st;
+  if (st->done || st->inner_done) return;
+  const int q = st->k32 & 1;
+  const float* __restrict__ ce = a.ce[q];
+  const uint32_t* __restrict__ xtedg = a.xtedg;
+  const uint32_t words = (a.n + 31) >> 5;
+  unsigned int emax = 0;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t v = (w << 5) | lane_id();
+    if (v >= a.n) continue;
+    const uint32_t s = a.xtoff[v], e = a.xtoff[v + 1];
+    if (e - s > kLowMax) continue;
+    float acc = 0.f;
+    uint32_t j = s;
+    for (; j + 4 <= e; j += 4) {
+      const uint32_t u0 = __ldg(xtedg + j), u1 = __ldg(xtedg + j + 1);
+      const uint32_t u2 = __ldg(xtedg + j + 2), u3 = __ldg(xtedg + j + 3);
+      const float c0 = __ldg(ce + u0), c1 = __ldg(ce + u1), c2 = __ldg(ce + u2), c3 = __ldg(ce + u3);
+      acc += c0; acc += c1; acc += c2; acc += c3;
+    }
+    for (; j < e; ++j) acc += __ldg(ce + __ldg(xtedg + j));
+    emax = max(emax, finish32(a, v, acc, q));
+  }
+  block_max_u32(emax, &st->el32_bits[st->k32 & 1]);
+}
+
+// MID: warp per vertex, lane-strided sums folded by shuffles.
+__global__ void __launch_bounds__(kThreads) k32_mid(SolveArgs a, uint32_t begin, uint32_t count) {
+  State* st = a.st;
+  if (st->done || st->inner_done) return;
+  const int q = st->k32 & 1;
+  const float* __restrict__ ce = a.ce[q];
+  const uint32_t lane = lane_id();
+  unsigned int emax = 0;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t v = a.cls_list[begin + i];
+    const uint32_t s = a.xtoff[v], d = a.xtoff[v + 1] - s;
+    const uint32_t* __restrict__ ed = a.xtedg + s;
+    float acc = 0.f;
+    for (uint32_t t = lane; t < d; t += 32) acc += __ldg(ce + __ldg(ed + t));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) emax = max(emax, finish32(a, v, acc, q));
+  }
+  block_max_u32(emax, &st->el32_bits[st->k32 & 1]);
+}
+
+// HIGH: block per vertex.
+__global__ void __launch_bounds__(256) k32_high(SolveArgs a, uint32_t begin, uint32_t count) {
+  __shared__ float part[8];
+  State* st = a.st;
+  if (st->done || st->inner_done) return;
+  const int q = st->k32 & 1;
+  const float* __restrict__ ce = a.ce[q];
+  unsigned int emax = 0;
+  for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
+    const uint32_t v = a.cls_list[begin + i];
+    const uint32_t s = a.xtoff[v], d = a.xtoff[v + 1] - s;
+    const uint32_t* __restrict__ ed = a.xtedg + s;
+    float acc = 0.f;
+    for (uint32_t t = threadIdx.x; t < d; t += 256) acc += __ldg(ce + __ldg(ed + t));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane_id() == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      float x = threadIdx.x < 8 ? part[threadIdx.x] : 0.f;
+#pragma unroll
+      for (int o = 4; o; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (threadIdx.x == 0) emax = max(emax, finish32(a, v, x, q));
+    }
+    __syncthreads();
+  }
+  block_max_u32(emax, &st->el32_bits[st->k32 & 1]);
+}
+
+// After the FP64 sweep: its L-inf decides (:689); otherwise start a round of
+// FP32 sweeps.
+__global__ void k_refine_finalize64(State* st) {
+  if (st->done) return;
+  const int p = st->iter & 1;
+  const double el = __longlong_as_double((long long)st->el_bits[p]);
+  st->last_delta = el;
+  st->iter += 1;
+  st->rounds += 1;
+  st->el_bits[p ^ 1] = 0;
+  st->el_bits[p] = 0;
+  if (el < st->tol || st->iter >= st->max_iter) {
+    st->done = 1;  // the answer is the FP64 sweep's output
+    return;
+  }
+  st->k32 = 0;
+  st->inner_done = 0;
+  st->el32_bits[0] = st->el32_bits[1] = 0;
+}
+
+__global__ void k_finalize32(State* st) {
+  if (st->done || st->inner_done) return;
+  const int q = st->k32 & 1;
+  const float dl = __uint_as_float(st->el32_bits[q]);
+  st->iter += 1;
+  st->k32 += 1;
+  st->el32_bits[q ^ 1] = 0;
+  if (dl < (float)st->tol || st->iter >= st->max_iter) st->inner_done = 1;
+}
+
+// x_b += e (FP64), c_b = x_b / outdeg.
+__global__ void k_refine_commit(SolveArgs a) {
+  const float* __restrict__ e = a.e[a.st->k32 & 1];
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
+    const double x = a.r[0][v] + (double)e[v];
+    a.r[0][v] = x;
+    a.c[0][v] = x / (double)a.xtdat[v];
+  }
+}
+
+static inline int cap_grid32(uint64_t want, int cap) { return (int)(want < (uint64_t)cap ? (want ? want : 1) : cap); }
+
+bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, int sms, cudaStream_t s) {
+  const uint32_t b = g.cls_begin[cls], cnt = g.cls_begin[cls + 1] - b;
+  if (!cnt) return false;
+  if (cls == LOW) {
+    const uint64_t words = ((uint64_t)g.n + 31) / 32;
+    k32_low<<<cap_grid32((words + 7) / 8, sms * 8), kThreads, 0, s>>>(a);
+  } else if (cls == MID) {
+    k32_mid<<<cap_grid32((cnt + 7) / 8, sms * 8), kThreads, 0, s>>>(a, b, cnt);
+  } else {
+    k32_high<<<cap_grid32(cnt, sms * 4), 256, 0, s>>>(a, b, cnt);
+  }
+  return true;
+}
+
+void launch_refine_finalize64(const SolveArgs& a, cudaStream_t s) { k_refine_finalize64<<<1, 1, 0, s>>>(a.st); }
+
+void launch_finalize32(const SolveArgs& a, cudaStream_t s) { k_finalize32<<<1, 1, 0, s>>>(a.st); }
+
+void launch_refine_commit(const SolveArgs& a, int sms, cudaStream_t s) {
+  k_refine_commit<<<cap_grid32((a.n + kThreads - 1) / kThreads, sms * 16), kThreads, 0, s>>>(a);
+}
+
+}  // namespace prx

@@ -38,10 +38,18 @@
 namespace prx {
 
 template <int MODE> struct ModeTraits {
-  static constexpr bool DYN = MODE >= PRX_DYNAMIC_TRAVERSAL;
-  static constexpr bool FRONTIER = MODE >= PRX_DYNAMIC_FRONTIER;
+  static constexpr bool REFINE = MODE == MODE_REFINE64;
+  static constexpr bool DYN = !REFINE && MODE >= PRX_DYNAMIC_TRAVERSAL;
+  static constexpr bool FRONTIER = DYN && MODE >= PRX_DYNAMIC_FRONTIER;
   static constexpr bool PRUNE = MODE == PRX_PRUNE_DYNAMIC_FRONTIER;
 };
+
+// Data parity read by an iteration: the refinement's FP64 sweep always reads
+// the base ranks (parity 0) and writes parity 1.
+template <int MODE>
+__device__ __forceinline__ int data_parity(const State* st) {
+  return ModeTraits<MODE>::REFINE ? 0 : (st->iter & 1);
+}
 
 __device__ __forceinline__ void set_bit(uint32_t* bm, uint32_t w) {
   const uint32_t bit = 1u << (w & 31u);
@@ -63,7 +71,15 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
   else          av = fma(a.P, cv, a.C0);
   const double ev = fabs(av - rv);
   a.r[p ^ 1][v] = av;
-  a.c[p ^ 1][v] = av / (double)d;
+  if (T::REFINE) {
+    // residual of the base ranks, the first FP32 correction and its contribution
+    const float rho = (float)(av - rv);
+    a.rho[v] = rho;
+    a.e[0][v] = rho;
+    a.ce[0][v] = rho / (float)d;
+  } else {
+    a.c[p ^ 1][v] = av / (double)d;
+  }
   survive = true;
   changed = false;
   if (T::FRONTIER) {
@@ -80,7 +96,7 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a) {
   using T = ModeTraits<MODE>;
   State* st = a.st;
   if (st->done) return;
-  const int iter = st->iter, p = iter & 1;
+  const int iter = st->iter, p = data_parity<MODE>(st);
   const double* __restrict__ c = a.c[p];
   const uint32_t* __restrict__ xtedg = a.xtedg;
   uint32_t *cur = nullptr, *nxt = nullptr, *prev = nullptr;
@@ -148,7 +164,7 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a) {
       }
     }
   }
-  block_max_bits(emax, &st->el_bits[p]);
+  block_max_bits(emax, &st->el_bits[iter & 1]);
   if (T::DYN) block_sum_u64(edges, &st->edges);
 }
 
@@ -184,7 +200,7 @@ template <int MODE>
 __global__ void __launch_bounds__(kThreads) k_update_mid(SolveArgs a, uint32_t begin, uint32_t count_static) {
   using T = ModeTraits<MODE>;
   if (a.st->done) return;
-  const int p = a.st->iter & 1;
+  const int p = data_parity<MODE>(a.st);
   const uint32_t* list;
   uint32_t count;
   list_of<MODE>(a, MID, begin, count_static, list, count);
@@ -225,7 +241,7 @@ __global__ void __launch_bounds__(kThreads) k_update_mid(SolveArgs a, uint32_t b
       edges += d;
     }
   }
-  block_max_bits(emax, &a.st->el_bits[p]);
+  block_max_bits(emax, &a.st->el_bits[a.st->iter & 1]);
   if (T::DYN) block_sum_u64(edges, &a.st->edges);
 }
 
@@ -235,7 +251,7 @@ __global__ void __launch_bounds__(256) k_update_high(SolveArgs a, uint32_t begin
   using T = ModeTraits<MODE>;
   __shared__ double part[256];
   if (a.st->done) return;
-  const int p = a.st->iter & 1;
+  const int p = data_parity<MODE>(a.st);
   const uint32_t* list;
   uint32_t count;
   list_of<MODE>(a, HIGH, begin, count_static, list, count);
@@ -276,7 +292,7 @@ __global__ void __launch_bounds__(256) k_update_high(SolveArgs a, uint32_t begin
     }
     __syncthreads();
   }
-  block_max_bits(emax, &a.st->el_bits[p]);
+  block_max_bits(emax, &a.st->el_bits[a.st->iter & 1]);
   if (T::DYN) block_sum_u64(edges, &a.st->edges);
 }
 
@@ -421,6 +437,10 @@ bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cl
     case PRX_DYNAMIC_FRONTIER: return update_class_t<PRX_DYNAMIC_FRONTIER>(a, g, cls, sms, s);
     default: return update_class_t<PRX_PRUNE_DYNAMIC_FRONTIER>(a, g, cls, sms, s);
   }
+}
+
+bool launch_refine_sweep64(const SolveArgs& a, const GraphDev& g, int cls, int sms, cudaStream_t s) {
+  return update_class_t<MODE_REFINE64>(a, g, cls, sms, s);
 }
 
 void launch_expand_iteration(const SolveArgs& a, int sms, cudaStream_t s) {

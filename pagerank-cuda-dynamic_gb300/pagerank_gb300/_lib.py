@@ -31,7 +31,8 @@ class Result(C.Structure):
                 ("marking_time_ms", C.c_float), ("computation_time_ms", C.c_float),
                 ("affected_initial", C.c_uint64), ("edges_processed", C.c_uint64),
                 ("last_delta", C.c_double), ("refinements", C.c_int), ("kernel_launches", C.c_uint64),
-                ("update_ms", C.c_double * 3), ("update_launches", C.c_uint32 * 3)]
+                ("update_ms", C.c_double * 3), ("update_launches", C.c_uint32 * 3),
+                ("update32_ms", C.c_double * 3), ("update32_launches", C.c_uint32 * 3)]
 
     def as_dict(self):
         d = {}
