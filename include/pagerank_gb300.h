@@ -85,6 +85,13 @@ typedef struct {
                                  push or pull per iteration, 1 always pushes
                                  from changed vertices, 2 always pulls into
                                  unmarked ones; the marked set is the same [0] */
+  uint32_t chunk_vertices;    /* source-chunk width of the gathers of the
+                                 in-degree <= 64 class: each sweep reads the
+                                 contributions one chunk of this many source
+                                 vertices at a time; 0 sizes chunks to 200 MB
+                                 of FP64 / 48 MB of FP32 contributions, >= n
+                                 disables chunking.  Results do not depend
+                                 on it [0]                                  */
 } prx_options;
 
 /* PagerankResult<V> (inc/pagerank.hxx:64-113) minus the rank vector, which

@@ -34,6 +34,8 @@ struct prx_context {
   bool ws_dyn = false;
   double* r[2] = {nullptr, nullptr};
   double* c[2] = {nullptr, nullptr};
+  double* acc64 = nullptr;    // partial sums between chunk passes
+  float* acc32 = nullptr;
   uint8_t* flags = nullptr;   // byte flags for prx_mark_affected
   uint32_t* bm[3] = {nullptr, nullptr, nullptr};
   uint32_t* nf[2] = {nullptr, nullptr};
@@ -93,6 +95,7 @@ void prx_options_default(prx_options* o) {
   o->partition = 0;
   o->timing = 0;
   o->expansion = 0;
+  o->chunk_vertices = 0;
 }
 
 const char* prx_status_string(int s) {
@@ -140,6 +143,8 @@ static void free_ws(prx_context* c) {
     cudaFree(c->fr[p]); c->fr[p] = nullptr;
     for (int k = 0; k < NCLS; ++k) { cudaFree(c->lists[p][k]); c->lists[p][k] = nullptr; }
   }
+  cudaFree(c->acc64); c->acc64 = nullptr;
+  cudaFree(c->acc32); c->acc32 = nullptr;
   cudaFree(c->flags); c->flags = nullptr;
   for (auto& b : c->bm) { cudaFree(b); b = nullptr; }
   for (auto& b : c->nf) { cudaFree(b); b = nullptr; }
@@ -183,6 +188,8 @@ static int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
     TRY_CUDA_ST(cudaMalloc(&c->r[p], sizeof(double) * cap));
     TRY_CUDA_ST(cudaMalloc(&c->c[p], sizeof(double) * cap));
   }
+  TRY_CUDA_ST(cudaMalloc(&c->acc64, sizeof(double) * cap));
+  TRY_CUDA_ST(cudaMalloc(&c->acc32, sizeof(float) * cap));
   if (want_dyn) {
     TRY_CUDA_ST(cudaMalloc(&c->flags, cap));
     for (auto& b : c->bm) TRY_CUDA_ST(cudaMalloc(&b, sizeof(uint32_t) * words));
@@ -243,6 +250,9 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
   a.naff = c->naff; a.xl = c->xl; a.xb = c->xb;
   a.rho = c->rho;
   for (int p = 0; p < 2; ++p) { a.e[p] = c->e32[p]; a.ce[p] = c->ce32[p]; }
+  a.low_bm = g.low_bm;
+  a.acc64 = c->acc64;
+  a.acc32 = c->acc32;
   // expand by pulling once more than 1/16 of the vertices changed by > D
   a.pull_threshold = o.expansion == 1 ? 0xffffffffu : (o.expansion == 2 ? 0u : g.n / 16);
   a.st = c->st;
@@ -327,11 +337,12 @@ static int launch_update_timed(prx_context* c, bool timing, int slot, F fn) {
   return PRX_OK;
 }
 
-static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArgs& a, int mode, bool timing) {
+static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArgs& a, int mode, bool timing,
+                             const ChunkLayout* lay) {
   cudaStream_t s = c->stream;
   for (int cls = 0; cls < NCLS; ++cls) {
     const int st = launch_update_timed(c, timing, cls,
-                                       [&] { return launch_update_class(a, gr->g, mode, cls, c->sms, s); });
+                                       [&] { return launch_update_class(a, gr->g, mode, cls, lay, c->sms, s); });
     if (st) return st;
   }
   if (mode >= PRX_DYNAMIC_FRONTIER) {
@@ -347,12 +358,13 @@ static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArg
 // sweep converged (its output in r[1]), 0 when the cap stopped an FP32 round
 // (the committed ranks in r[0]).
 static int run_refine_loop(prx_context* c, const prx_graph* gr, const SolveArgs& a, bool timing, int max_iter,
-                           int* final_parity) {
+                           const ChunkLayout* lay64, const ChunkLayout* lay32, int* final_parity) {
   cudaStream_t s = c->stream;
   int st;
   for (;;) {
     for (int cls = 0; cls < NCLS; ++cls) {
-      st = launch_update_timed(c, timing, cls, [&] { return launch_refine_sweep64(a, gr->g, cls, c->sms, s); });
+      st = launch_update_timed(c, timing, cls,
+                               [&] { return launch_refine_sweep64(a, gr->g, cls, lay64, c->sms, s); });
       if (st) return st;
     }
     launch_refine_finalize64(a, s);
@@ -362,13 +374,16 @@ static int run_refine_loop(prx_context* c, const prx_graph* gr, const SolveArgs&
     TRY_CUDA_ST(cudaStreamSynchronize(s));
     if (timing && (st = drain_timing(c))) return st;
     if (c->st_host[1].done) {
-      *final_parity = 1;
+      // converged (or capped) at this FP64 sweep; with max_iterations <= 0
+      // no sweep ran and the initial ranks in r[0] are the answer
+      *final_parity = c->st_host[1].iter > 0 ? 1 : 0;
       return PRX_OK;
     }
     for (int k = 1;; k = std::min(2 * k, 16)) {
       for (int i = 0; i < k; ++i) {
         for (int cls = 0; cls < NCLS; ++cls) {
-          st = launch_update_timed(c, timing, NCLS + cls, [&] { return launch_sweep32(a, gr->g, cls, c->sms, s); });
+          st = launch_update_timed(c, timing, NCLS + cls,
+                                   [&] { return launch_sweep32(a, gr->g, cls, lay32, c->sms, s); });
           if (st) return st;
         }
         launch_finalize32(a, s);
@@ -405,6 +420,16 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   if (st) return st;
   if (refine && (st = ensure_ws32(c, g.n))) return st;
   int final_parity = -1;
+  // source-chunk layouts of the LOW gathers, built once per graph version and
+  // width.  Defaults from a width sweep on the 50M-vertex web-like graph: the
+  // FP64 sweep (bound by GB300's FP64 add rate as much as by HBM) gains from
+  // two chunks only (200 MB of contributions each), the FP32 sweep from
+  // 48 MB chunks.
+  const uint32_t w64 = o.chunk_vertices ? o.chunk_vertices : (200u << 20) / sizeof(double);
+  const uint32_t w32 = o.chunk_vertices ? o.chunk_vertices : (48u << 20) / sizeof(float);
+  const ChunkLayout *lay64 = nullptr, *lay32 = nullptr;
+  TRY_CUDA_ST(ensure_chunks(gr->g, w64, refine ? w32 : w64, c->sms, c->stream, &lay64));
+  if (refine) TRY_CUDA_ST(ensure_chunks(gr->g, w32, w64, c->sms, c->stream, &lay32));
   cudaStream_t s = c->stream;
   const SolveArgs a = make_args(c, g, o);
   const int repeat = o.repeat > 0 ? o.repeat : 1;
@@ -426,11 +451,11 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
     }
     TRY_CUDA_ST(cudaEventRecord(c->ev[2], s));
     if (refine) {
-      if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, &final_parity))) return st;
+      if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity))) return st;
     } else {
       for (int k = 1;; k = std::min(2 * k, 16)) {
         for (int i = 0; i < k; ++i) {
-          st = enqueue_iteration(c, gr, a, mode, timing);
+          st = enqueue_iteration(c, gr, a, mode, timing, lay64);
           if (st) return st;
         }
         TRY_CUDA_ST(cudaGetLastError());
@@ -542,6 +567,8 @@ int prx_graph_destroy(prx_graph* gr) {
   cudaSetDevice(gr->g.device);
   GraphDev& g = gr->g;
   cudaFree(g.xoff); cudaFree(g.xedg); cudaFree(g.xtoff); cudaFree(g.xtedg); cudaFree(g.xtdat); cudaFree(g.cls_list);
+  cudaFree(g.low_bm);
+  free_chunks(g);
   delete gr;
   return PRX_OK;
 }

@@ -80,4 +80,19 @@ __device__ __forceinline__ unsigned long long dbits(double x) {
   return (unsigned long long)__double_as_longlong(x);
 }
 
+// Sum of c[edg[j]] for j in [s, e) added front to back onto acc, four
+// gathers in flight.
+template <class T>
+__device__ __forceinline__ T lane_row_sum(const T* __restrict__ c, const uint32_t* __restrict__ edg, uint32_t s,
+                                          uint32_t e, T acc) {
+  uint32_t j = s;
+  for (; j + 4 <= e; j += 4) {
+    const uint32_t u0 = __ldg(edg + j), u1 = __ldg(edg + j + 1), u2 = __ldg(edg + j + 2), u3 = __ldg(edg + j + 3);
+    const T c0 = __ldg(c + u0), c1 = __ldg(c + u1), c2 = __ldg(c + u2), c3 = __ldg(c + u3);
+    acc += c0; acc += c1; acc += c2; acc += c3;
+  }
+  for (; j < e; ++j) acc += __ldg(c + __ldg(edg + j));
+  return acc;
+}
+
 }  // namespace prx

@@ -123,8 +123,109 @@ __global__ void __launch_bounds__(256) k_cls_edges(const uint32_t* __restrict__ 
   if (threadIdx.x < NCLS && acc[threadIdx.x]) atomicAdd(&out[threadIdx.x], acc[threadIdx.x]);
 }
 
+// Bitmap of the LOW class (warp per 32 ids).
+__global__ void __launch_bounds__(256) k_low_bitmap(const uint32_t* __restrict__ xtoff, uint32_t n,
+                                                    uint32_t* __restrict__ bm) {
+  const uint32_t words = (n + 31) >> 5;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t v = (w << 5) | (threadIdx.x & 31u);
+    const bool low = v < n && xtoff[v + 1] - xtoff[v] <= kLowMax;
+    const unsigned b = __ballot_sync(0xffffffffu, low);
+    if ((threadIdx.x & 31u) == 0) bm[w] = b;
+  }
+}
+
+// Per (chunk, vertex) in-edge counts of the LOW class, chunk-major, with a
+// zero at the end of every chunk row (so one exclusive scan gives offsets).
+__global__ void k_chunk_count(const uint32_t* __restrict__ xtoff, const uint32_t* __restrict__ xtedg,
+                              const uint32_t* __restrict__ low_bm, uint32_t n, uint32_t width, int K,
+                              uint32_t* __restrict__ cnt) {
+  const size_t row = (size_t)n + 1;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += gridDim.x * blockDim.x) {
+    const bool low = v < n && ((low_bm[v >> 5] >> (v & 31u)) & 1u);
+    uint32_t j = low ? xtoff[v] : 0, e = low ? xtoff[v + 1] : 0;
+    for (int k = 0; k < K; ++k) {
+      const uint64_t hi = (uint64_t)(k + 1) * width;
+      const uint32_t b = j;
+      while (j < e && xtedg[j] < hi) ++j;
+      cnt[k * row + v] = j - b;
+    }
+  }
+}
+
+__global__ void k_chunk_scatter(const uint32_t* __restrict__ xtoff, const uint32_t* __restrict__ xtedg,
+                                const uint32_t* __restrict__ low_bm, uint32_t n, uint32_t width, int K,
+                                const uint32_t* __restrict__ off, uint32_t* __restrict__ edg) {
+  const size_t row = (size_t)n + 1;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    if (!((low_bm[v >> 5] >> (v & 31u)) & 1u)) continue;
+    uint32_t j = xtoff[v];
+    const uint32_t e = xtoff[v + 1];
+    for (int k = 0; k < K; ++k) {
+      const uint64_t hi = (uint64_t)(k + 1) * width;
+      uint32_t pos = off[k * row + v];
+      while (j < e && xtedg[j] < hi) edg[pos++] = xtedg[j++];
+    }
+  }
+}
+
+void free_chunks(GraphDev& g) {
+  for (auto& l : g.lay) {
+    cudaFree(l.off);
+    cudaFree(l.edg);
+    l = ChunkLayout();
+  }
+}
+
+cudaError_t ensure_chunks(GraphDev& g, uint32_t width, uint32_t keep, int sms, cudaStream_t s,
+                          const ChunkLayout** out) {
+  *out = nullptr;
+  if (width == 0 || width >= g.n) return cudaSuccess;  // one chunk: the row-major CSR is the layout
+  for (auto& l : g.lay)
+    if (l.width == width) { *out = &l; return cudaSuccess; }
+  // an empty slot, else the one not holding `keep` (still in use by the caller)
+  ChunkLayout& l = g.lay[0].width == 0 ? g.lay[0]
+                   : g.lay[1].width == 0 ? g.lay[1]
+                   : (g.lay[0].width == keep ? g.lay[1] : g.lay[0]);
+  cudaFree(l.off);
+  cudaFree(l.edg);
+  l = ChunkLayout();
+  const int K = (int)((g.n + (uint64_t)width - 1) / width);
+  const size_t len = (size_t)K * ((size_t)g.n + 1);
+  if (len > 0xffffffffull) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMalloc(&l.off, sizeof(uint32_t) * len);
+  if (e == cudaSuccess) e = cudaMalloc(&l.edg, sizeof(uint32_t) * (g.cls_edges[LOW] ? g.cls_edges[LOW] : 1));
+  if (e != cudaSuccess) {
+    cudaFree(l.off); cudaFree(l.edg);
+    l = ChunkLayout();
+    return e;
+  }
+  const int grid = sms * 8;
+  k_chunk_count<<<grid, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, g.n, width, K, l.off);
+  e = exclusive_scan_u32(l.off, (uint32_t)len, s);
+  if (e == cudaSuccess) {
+    k_chunk_scatter<<<grid, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, g.n, width, K, l.off, l.edg);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) {
+    cudaFree(l.off); cudaFree(l.edg);
+    l = ChunkLayout();
+    return e;
+  }
+  l.width = width;
+  l.K = K;
+  *out = &l;
+  return cudaSuccess;
+}
+
 cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
   const uint32_t n = g.n;
+  free_chunks(g);
+  if (!g.low_bm) {
+    cudaError_t e = cudaMalloc(&g.low_bm, sizeof(uint32_t) * (((size_t)n + 31) / 32 + 1));
+    if (e != cudaSuccess) return e;
+  }
+  if (n) k_low_bitmap<<<sms * 4, 256, 0, s>>>(g.xtoff, n, g.low_bm);
   if (n == 0) {
     for (int c = 0; c <= NCLS; ++c) g.cls_begin[c] = 0;
     for (int c = 0; c < NCLS; ++c) g.cls_edges[c] = 0;

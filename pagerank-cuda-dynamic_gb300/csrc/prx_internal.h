@@ -50,6 +50,19 @@ struct State {
 // r[1] and the residual, as FP32, to rho and e[0] / ce[0]).
 constexpr int MODE_REFINE64 = 10;
 
+// In-edges of the LOW class regrouped by source chunk: chunk k holds, for
+// every vertex v, the in-edges whose source lies in [k*width, (k+1)*width),
+// in the row's (ascending) order.  Offsets are chunk-major: the segment
+// (k, v) is edg[off[k*(n+1) + v] .. off[k*(n+1) + v + 1]).  A sweep gathers
+// one chunk at a time, so the contributions it reads fit in L2; the row's
+// sum is carried across chunks in source order -- the reference's order.
+struct ChunkLayout {
+  uint32_t width = 0;             // vertices per source chunk, 0 = slot unused
+  int K = 0;                      // number of chunks
+  uint32_t* off = nullptr;
+  uint32_t* edg = nullptr;
+};
+
 struct GraphDev {
   int device = 0;                 // device holding the arrays
   uint32_t n = 0;
@@ -64,7 +77,16 @@ struct GraphDev {
   uint32_t cls_begin[NCLS + 1] = {0, 0, 0, 0};
   uint64_t cls_edges[NCLS] = {0, 0, 0};  // in-edges per class
   uint32_t mid_max = kDefaultMidMax;
+  uint32_t* low_bm = nullptr;     // bitmap of the LOW class
+  ChunkLayout lay[2];             // cached chunk layouts (rebuilt after a batch)
 };
+
+// Chunk layout of `width` vertices per chunk (built on first use, cached in
+// two slots; the layout of width `keep` is not evicted); width >= n means no
+// chunking (K = 1, *out = nullptr).
+cudaError_t ensure_chunks(GraphDev& g, uint32_t width, uint32_t keep, int sms, cudaStream_t s,
+                          const ChunkLayout** out);
+void free_chunks(GraphDev& g);
 
 // Pointers a solve kernel needs.  Passed by value.
 struct SolveArgs {
@@ -86,6 +108,9 @@ struct SolveArgs {
   float* rho;                     // FP32 refinement: residual of the base ranks
   float* e[2];                    // FP32 refinement: correction, ping-pong
   float* ce[2];                   // FP32 refinement: correction / outdeg, ping-pong
+  const uint32_t* low_bm;         // LOW-class bitmap
+  double* acc64;                  // partial row sums carried between chunk passes (FP64)
+  float* acc32;                   // the same for the FP32 sweeps
   State* st;
   uint32_t n;
   uint32_t mid_max;
@@ -95,16 +120,20 @@ struct SolveArgs {
 
 // ---- launchers (prx_update.cu) ------------------------------------------
 void launch_init_ranks(const SolveArgs& a, const double* q, bool dynamic, cudaStream_t s);
-// Rank update of one in-degree class; false if nothing was launched.
-bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cls, int sms, cudaStream_t s);
+// Rank update of one in-degree class; false if nothing was launched.  For
+// LOW, `lay` (may be null: no chunking) selects the chunk layout and one
+// launch per chunk is made.
+bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cls, const ChunkLayout* lay, int sms,
+                         cudaStream_t s);
 void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s);
 
 // ---- FP32 refinement (prx_refine.cu) --------------------------------------
 // FP64 residual sweep of one in-degree class (update kernels in MODE_REFINE64).
-bool launch_refine_sweep64(const SolveArgs& a, const GraphDev& g, int cls, int sms, cudaStream_t s);
+bool launch_refine_sweep64(const SolveArgs& a, const GraphDev& g, int cls, const ChunkLayout* lay, int sms,
+                           cudaStream_t s);
 void launch_refine_finalize64(const SolveArgs& a, cudaStream_t s);
 // One FP32 correction sweep of one class, and its finalize.
-bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, int sms, cudaStream_t s);
+bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, const ChunkLayout* lay, int sms, cudaStream_t s);
 void launch_finalize32(const SolveArgs& a, cudaStream_t s);
 // x_b += e; c_b = x_b / outdeg.
 void launch_refine_commit(const SolveArgs& a, int sms, cudaStream_t s);

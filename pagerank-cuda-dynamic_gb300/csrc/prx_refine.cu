@@ -40,32 +40,27 @@ __device__ __forceinline__ unsigned int finish32(const SolveArgs& a, uint32_t v,
   return fbits(dl);
 }
 
-// LOW: one warp per 32 consecutive ids, one lane per vertex.
-__global__ void __launch_bounds__(kThreads) k32_low(SolveArgs a) {
+// LOW: one warp per 32 consecutive ids, one lane per vertex, one launch per
+// source chunk (partial sums carried in acc32), as the FP64 kernel.
+template <bool FIRST, bool LAST>
+__global__ void __launch_bounds__(kThreads) k32_low(SolveArgs a, const uint32_t* __restrict__ off,
+                                                    const uint32_t* __restrict__ edg) {
   State* st = a.st;
   if (st->done || st->inner_done) return;
   const int q = st->k32 & 1;
   const float* __restrict__ ce = a.ce[q];
-  const uint32_t* __restrict__ xtedg = a.xtedg;
   const uint32_t words = (a.n + 31) >> 5;
   unsigned int emax = 0;
   for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t v = (w << 5) | lane_id();
-    if (v >= a.n) continue;
-    const uint32_t s = a.xtoff[v], e = a.xtoff[v + 1];
-    if (e - s > kLowMax) continue;
-    float acc = 0.f;
-    uint32_t j = s;
-    for (; j + 4 <= e; j += 4) {
-      const uint32_t u0 = __ldg(xtedg + j), u1 = __ldg(xtedg + j + 1);
-      const uint32_t u2 = __ldg(xtedg + j + 2), u3 = __ldg(xtedg + j + 3);
-      const float c0 = __ldg(ce + u0), c1 = __ldg(ce + u1), c2 = __ldg(ce + u2), c3 = __ldg(ce + u3);
-      acc += c0; acc += c1; acc += c2; acc += c3;
-    }
-    for (; j < e; ++j) acc += __ldg(ce + __ldg(xtedg + j));
-    emax = max(emax, finish32(a, v, acc, q));
+    if (v >= a.n || !((a.low_bm[w] >> lane_id()) & 1u)) continue;
+    const uint32_t s = off[v], e = off[v + 1];
+    if (!FIRST && !LAST && s == e) continue;
+    const float acc = lane_row_sum(ce, edg, s, e, FIRST ? 0.f : a.acc32[v]);
+    if (LAST) emax = max(emax, finish32(a, v, acc, q));
+    else a.acc32[v] = acc;
   }
-  block_max_u32(emax, &st->el32_bits[st->k32 & 1]);
+  if (LAST) block_max_u32(emax, &st->el32_bits[st->k32 & 1]);
 }
 
 // MID: warp per vertex, lane-strided sums folded by shuffles.
@@ -160,12 +155,23 @@ __global__ void k_refine_commit(SolveArgs a) {
 
 static inline int cap_grid32(uint64_t want, int cap) { return (int)(want < (uint64_t)cap ? (want ? want : 1) : cap); }
 
-bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, int sms, cudaStream_t s) {
+bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, const ChunkLayout* lay, int sms, cudaStream_t s) {
   const uint32_t b = g.cls_begin[cls], cnt = g.cls_begin[cls + 1] - b;
   if (!cnt) return false;
   if (cls == LOW) {
     const uint64_t words = ((uint64_t)g.n + 31) / 32;
-    k32_low<<<cap_grid32((words + 7) / 8, sms * 8), kThreads, 0, s>>>(a);
+    const int grid = cap_grid32((words + 7) / 8, sms * 8);
+    if (!lay || lay->K <= 1) {
+      k32_low<true, true><<<grid, kThreads, 0, s>>>(a, g.xtoff, g.xtedg);
+      return true;
+    }
+    const size_t row = (size_t)g.n + 1;
+    for (int k = 0; k < lay->K; ++k) {
+      const uint32_t* off = lay->off + k * row;
+      if (k == 0) k32_low<true, false><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
+      else if (k == lay->K - 1) k32_low<false, true><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
+      else k32_low<false, false><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
+    }
   } else if (cls == MID) {
     k32_mid<<<cap_grid32((cnt + 7) / 8, sms * 8), kThreads, 0, s>>>(a, b, cnt);
   } else {

@@ -91,14 +91,23 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
 }
 
 // ---- LOW: one warp per 32 consecutive vertex ids ------------------------------
-template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a) {
+// One launch per source chunk (PASS_ONLY when the row-major CSR is used
+// whole).  Pass k adds the row's chunk-k segment to the partial sum carried in
+// acc64 (sources ascending, so the chunks come in the row's own order); the
+// first pass also does the dynamic modes' per-iteration bookkeeping, the last
+// one finishes the vertex.
+enum Pass { PASS_ONLY = 0, PASS_FIRST = 1, PASS_INNER = 2, PASS_LAST = 3 };
+
+template <int MODE, int PASS>
+__global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const uint32_t* __restrict__ off,
+                                                         const uint32_t* __restrict__ edg) {
   using T = ModeTraits<MODE>;
+  constexpr bool FIRST = PASS == PASS_ONLY || PASS == PASS_FIRST;
+  constexpr bool LAST = PASS == PASS_ONLY || PASS == PASS_LAST;
   State* st = a.st;
   if (st->done) return;
   const int iter = st->iter, p = data_parity<MODE>(st);
   const double* __restrict__ c = a.c[p];
-  const uint32_t* __restrict__ xtedg = a.xtedg;
   uint32_t *cur = nullptr, *nxt = nullptr, *prev = nullptr;
   if (T::DYN) {
     cur = a.bm[iter % 3];
@@ -112,51 +121,50 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a) {
     const uint32_t v = (w << 5) | lane;
     bool mine = v < a.n;
     if (T::DYN) {
-      const uint32_t cw = cur[w], pw = prev[w];
-      if (((pw & ~cw) >> lane) & 1u) {  // updated last iteration, not this one: refresh parity p^1
-        a.r[p ^ 1][v] = a.r[p][v];
-        a.c[p ^ 1][v] = a.c[p][v];
-      }
-      if (lane == 0) {
-        if (pw) prev[w] = 0;  // becomes the empty nxt of iteration k+1
-        // nf[p^1] was filled and expanded by iteration k-1; clear it for k+1
-        if (T::FRONTIER && a.nf[p ^ 1][w]) a.nf[p ^ 1][w] = 0;
+      const uint32_t cw = cur[w];
+      if (FIRST) {
+        const uint32_t pw = prev[w];
+        if (((pw & ~cw) >> lane) & 1u) {  // updated last iteration, not this one: refresh parity p^1
+          a.r[p ^ 1][v] = a.r[p][v];
+          a.c[p ^ 1][v] = a.c[p][v];
+        }
+        if (lane == 0) {
+          if (pw) prev[w] = 0;  // becomes the empty nxt of iteration k+1
+          // nf[p^1] was filled and expanded by iteration k-1; clear it for k+1
+          if (T::FRONTIER && a.nf[p ^ 1][w]) a.nf[p ^ 1][w] = 0;
+        }
       }
       mine = mine && ((cw >> lane) & 1u);
       if (!__any_sync(0xffffffffu, mine)) continue;
     }
-    uint32_t s = 0, e = 0;
-    if (mine) {
-      s = a.xtoff[v];
-      e = a.xtoff[v + 1];
-      if (e - s > kLowMax) {
-        if (T::DYN) {
-          const int cls = e - s <= a.mid_max ? MID : HIGH;
-          push(a.list[0][cls], &st->cnt[0][cls], v);
-        }
-        mine = false;
-      }
+    const bool low = mine && ((a.low_bm[w] >> lane) & 1u);
+    if (T::DYN && FIRST && mine && !low) {  // affected MID / HIGH vertex: its own kernel updates it
+      const uint32_t d = a.xtoff[v + 1] - a.xtoff[v];
+      const int cls = d <= a.mid_max ? MID : HIGH;
+      push(a.list[0][cls], &st->cnt[0][cls], v);
     }
+    // One thread per row: a row's terms must be added front to back (the
+    // reference's order), and a whole row per lane keeps the warp's FP64 adds
+    // for different rows running side by side.
+    const uint32_t s = mine ? off[v] : 0, e = mine ? off[v + 1] : 0;
+    mine = low && (FIRST || LAST || s < e);
     bool survive = false, changed = false;
+    double acc = 0.0;
+    if (mine) acc = lane_row_sum(c, edg, s, e, FIRST ? 0.0 : a.acc64[v]);
     if (mine) {
-      double acc = 0.0;
-      uint32_t j = s;
-      for (; j + 4 <= e; j += 4) {
-        const uint32_t u0 = __ldg(xtedg + j), u1 = __ldg(xtedg + j + 1);
-        const uint32_t u2 = __ldg(xtedg + j + 2), u3 = __ldg(xtedg + j + 3);
-        const double c0 = __ldg(c + u0), c1 = __ldg(c + u1), c2 = __ldg(c + u2), c3 = __ldg(c + u3);
-        acc += c0; acc += c1; acc += c2; acc += c3;
-      }
-      for (; j < e; ++j) acc += __ldg(c + __ldg(xtedg + j));
-      const unsigned long long ev = finish_vertex<MODE>(a, v, acc, p, survive, changed);
-      emax = ev > emax ? ev : emax;
       edges += e - s;
+      if (LAST) {
+        const unsigned long long ev = finish_vertex<MODE>(a, v, acc, p, survive, changed);
+        emax = ev > emax ? ev : emax;
+      } else {
+        a.acc64[v] = acc;
+      }
     }
-    if (T::DYN) {
+    if (LAST && T::DYN) {
       const unsigned keep = __ballot_sync(0xffffffffu, mine && survive);
       if (lane == 0 && keep) atomicOr(&nxt[w], keep);
     }
-    if (T::FRONTIER) {
+    if (LAST && T::FRONTIER) {
       const unsigned ch = __ballot_sync(0xffffffffu, mine && changed);
       if (lane == 0 && ch) {
         atomicOr(&a.nf[p][w], ch);
@@ -164,7 +172,7 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a) {
       }
     }
   }
-  block_max_bits(emax, &st->el_bits[iter & 1]);
+  if (LAST) block_max_bits(emax, &st->el_bits[iter & 1]);
   if (T::DYN) block_sum_u64(edges, &st->edges);
 }
 
@@ -407,14 +415,26 @@ void launch_init_ranks(const SolveArgs& a, const double* q, bool dynamic, cudaSt
 }
 
 template <int MODE>
-static bool update_class_t(const SolveArgs& a, const GraphDev& g, int cls, int sms, cudaStream_t s) {
+static bool update_class_t(const SolveArgs& a, const GraphDev& g, int cls, const ChunkLayout* lay, int sms,
+                           cudaStream_t s) {
   constexpr bool DYN = ModeTraits<MODE>::DYN;
   if (cls == LOW) {
-    // static: skip when the graph has no LOW vertex; dynamic: always (it also
-    // maintains the bitmaps)
+    // static: skip when the graph has no LOW vertex; dynamic: always (the
+    // first pass also maintains the bitmaps)
     if (!DYN && g.cls_begin[1] == g.cls_begin[0]) return false;
     const uint64_t words = ((uint64_t)g.n + 31) / 32;
-    k_update_low<MODE><<<cap_grid((words + 7) / 8, sms * 8), kThreads, 0, s>>>(a);
+    const int grid = cap_grid((words + 7) / 8, sms * 8);
+    if (!lay || lay->K <= 1) {
+      k_update_low<MODE, PASS_ONLY><<<grid, kThreads, 0, s>>>(a, g.xtoff, g.xtedg);
+      return true;
+    }
+    const size_t row = (size_t)g.n + 1;
+    for (int k = 0; k < lay->K; ++k) {
+      const uint32_t* off = lay->off + k * row;
+      if (k == 0) k_update_low<MODE, PASS_FIRST><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
+      else if (k == lay->K - 1) k_update_low<MODE, PASS_LAST><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
+      else k_update_low<MODE, PASS_INNER><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
+    }
     return true;
   }
   if (DYN) {
@@ -429,18 +449,20 @@ static bool update_class_t(const SolveArgs& a, const GraphDev& g, int cls, int s
   return true;
 }
 
-bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cls, int sms, cudaStream_t s) {
+bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cls, const ChunkLayout* lay, int sms,
+                         cudaStream_t s) {
   switch (mode) {
     case PRX_STATIC:
-    case PRX_NAIVE_DYNAMIC: return update_class_t<PRX_STATIC>(a, g, cls, sms, s);
-    case PRX_DYNAMIC_TRAVERSAL: return update_class_t<PRX_DYNAMIC_TRAVERSAL>(a, g, cls, sms, s);
-    case PRX_DYNAMIC_FRONTIER: return update_class_t<PRX_DYNAMIC_FRONTIER>(a, g, cls, sms, s);
-    default: return update_class_t<PRX_PRUNE_DYNAMIC_FRONTIER>(a, g, cls, sms, s);
+    case PRX_NAIVE_DYNAMIC: return update_class_t<PRX_STATIC>(a, g, cls, lay, sms, s);
+    case PRX_DYNAMIC_TRAVERSAL: return update_class_t<PRX_DYNAMIC_TRAVERSAL>(a, g, cls, lay, sms, s);
+    case PRX_DYNAMIC_FRONTIER: return update_class_t<PRX_DYNAMIC_FRONTIER>(a, g, cls, lay, sms, s);
+    default: return update_class_t<PRX_PRUNE_DYNAMIC_FRONTIER>(a, g, cls, lay, sms, s);
   }
 }
 
-bool launch_refine_sweep64(const SolveArgs& a, const GraphDev& g, int cls, int sms, cudaStream_t s) {
-  return update_class_t<MODE_REFINE64>(a, g, cls, sms, s);
+bool launch_refine_sweep64(const SolveArgs& a, const GraphDev& g, int cls, const ChunkLayout* lay, int sms,
+                           cudaStream_t s) {
+  return update_class_t<MODE_REFINE64>(a, g, cls, lay, sms, s);
 }
 
 void launch_expand_iteration(const SolveArgs& a, int sms, cudaStream_t s) {

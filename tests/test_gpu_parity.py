@@ -138,6 +138,41 @@ def test_frontier_expansion_push_and_pull_agree(pg, ctx, kind):
     g.close()
 
 
+@pytest.mark.parametrize("kind,width", [("rmat16", 1000), ("rmat16", 20000), ("web200k", 7777),
+                                        ("hubs", 3000), ("grid256", 5000)])
+def test_chunked_gathers_bit_exact(pg, ctx, kind, width):
+    # The in-degree <= 64 class gathers its contributions one source chunk at a
+    # time, carrying the row sum between chunks; rows are sorted by source, so
+    # every chunk width must reproduce the reference's sequential order.
+    xoff, xedg = _synthetic(pg, kind)
+    m = len(xedg)
+    batch = pg.graphs.random_batch(xoff, xedg, max(1, int(2e-4 * m)), max(1, int(8e-4 * m)), seed=13)
+    xt = O.transpose(xoff, xedg)
+    q, _ = O.solve("static", None, None, *xt)
+    yoff, yedg = pg.graphs.apply_batch(xoff, xedg, *batch)
+    yt = O.transpose(yoff, yedg)
+    g, _ = _graph(pg, ctx, yoff, yedg, yt)
+    opts = pg.options(chunk_vertices=width)
+    for mode in MODES:
+        want, it_w = _oracle(mode, yoff, yedg, yt, batch, q)
+        got, res = _gpu(pg, ctx, g, mode, batch, q, opts)
+        assert res["iterations"] == it_w, (kind, width, mode)
+        np.testing.assert_array_equal(got, want, err_msg=f"{kind} width={width} {mode}")
+    want, _ = O.solve("static", None, None, *yt)
+    got, _ = pg.solve(ctx, g, pg.STATIC, opts=pg.options(chunk_vertices=width, precision=pg.FP32_REFINE))
+    assert np.abs(got - want).max() <= 1e-9
+    g.close()
+
+
+def test_graph_outlives_context(pg):
+    # destroying a context first must leave its graphs destroyable
+    c = pg.Context(0)
+    xoff, xedg = pg.graphs.rmat(8, 8, seed=2)
+    g = pg.Graph(c, *O.transpose(xoff, xedg))
+    c.close()
+    g.close()
+
+
 def test_options_edge_cases(pg, ctx):
     xoff, xedg = pg.graphs.rmat(10, 16, seed=1)
     xt = O.transpose(xoff, xedg)
