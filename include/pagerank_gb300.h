@@ -193,6 +193,13 @@ int prx_mark_affected(prx_context* ctx, prx_graph* g, int mode,
                       const uint32_t* delu, const uint32_t* delv, uint64_t nd,
                       const uint32_t* insu, uint64_t ni, uint8_t* flags_out);
 
+/* Diagnostic with no counterpart in the reference: counts, on the context's
+ * device, the dividends a and out-degrees d (d = 1 .. dmax, `per` values of a
+ * per d, spread over 2^-40 .. 2^2) for which the library's three-operation
+ * division by a precomputed reciprocal differs from the IEEE division a / d.
+ * The solvers divide ranks by out-degrees that way. */
+int prx_selftest_division(prx_context* ctx, uint32_t dmax, uint32_t per, unsigned long long* mismatches);
+
 /* Static FP64 PageRank that allocates no memory.  No counterpart in the
  * reference: it serves callers that may not allocate device memory behind
  * their own allocator (a serving process that reserves its HBM up front, a

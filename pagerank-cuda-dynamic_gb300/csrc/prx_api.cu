@@ -251,6 +251,7 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
   a.rho = c->rho;
   for (int p = 0; p < 2; ++p) { a.e[p] = c->e32[p]; a.ce[p] = c->ce32[p]; }
   a.low_bm = g.low_bm;
+  a.rcp = g.rcp;
   a.acc64 = c->acc64;
   a.acc32 = c->acc32;
   // expand by pulling once more than 1/16 of the vertices changed by > D
@@ -568,6 +569,7 @@ int prx_graph_destroy(prx_graph* gr) {
   GraphDev& g = gr->g;
   cudaFree(g.xoff); cudaFree(g.xedg); cudaFree(g.xtoff); cudaFree(g.xtedg); cudaFree(g.xtdat); cudaFree(g.cls_list);
   cudaFree(g.low_bm);
+  cudaFree(g.rcp);
   free_chunks(g);
   delete gr;
   return PRX_OK;
@@ -722,6 +724,14 @@ int prx_solve_device(prx_context* c, prx_graph* gr, int mode, const uint32_t* du
                      const uint32_t* iu, const uint32_t* iv, uint64_t ni, const double* q, const prx_options* o,
                      double* ranks_out, prx_result* res) {
   return solve_common(c, gr, mode, du, dv, nd, iu, iv, ni, q, o, ranks_out, res, false);
+}
+
+int prx_selftest_division(prx_context* c, uint32_t dmax, uint32_t per, unsigned long long* mismatches) {
+  if (!c || !mismatches) FAIL(PRX_EINVAL, "prx_selftest_division: bad context or NULL output");
+  if (dmax == 0 || per == 0) FAIL(PRX_EINVAL, "prx_selftest_division: dmax and per must be positive");
+  TRY_CUDA_ST(cudaSetDevice(c->device));
+  TRY_CUDA_ST(selftest_division(dmax, per, mismatches, c->sms, c->stream));
+  return PRX_OK;
 }
 
 int prx_mark_affected(prx_context* c, prx_graph* gr, int mode, const uint32_t* du, const uint32_t* dv, uint64_t nd,

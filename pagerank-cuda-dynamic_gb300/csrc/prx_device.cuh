@@ -80,6 +80,19 @@ __device__ __forceinline__ unsigned long long dbits(double x) {
   return (unsigned long long)__double_as_longlong(x);
 }
 
+// a / d correctly rounded, for an integer d >= 1 and y = RN(1/d), by
+// Markstein's method (P. Markstein, "IA-64 and Elementary Functions", 2000):
+// q = RN(a*y) is within one ulp of a/d, so r = a - q*d is exact in one fma,
+// and RN(q + r*y) is the correctly rounded quotient.  Three FP64 operations
+// instead of a full division; valid while nothing over- or underflows (ranks
+// and contributions here are far from both).  Checked bit for bit against
+// the IEEE division by prx_selftest.
+__device__ __forceinline__ double div_count(double a, uint32_t d, double y) {
+  const double q = a * y;
+  const double r = fma(-q, (double)d, a);
+  return fma(r, y, q);
+}
+
 // Sum of c[edg[j]] for j in [s, e) added front to back onto acc, four
 // gathers in flight.
 template <class T>

@@ -123,6 +123,43 @@ __global__ void __launch_bounds__(256) k_cls_edges(const uint32_t* __restrict__ 
   if (threadIdx.x < NCLS && acc[threadIdx.x]) atomicAdd(&out[threadIdx.x], acc[threadIdx.x]);
 }
 
+__global__ void k_reciprocals(const uint32_t* __restrict__ deg, uint32_t n, double* __restrict__ rcp) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    rcp[v] = 1.0 / (double)deg[v];
+}
+
+// Self-test of div_count against the IEEE division: d in [1, dmax] and
+// `per` dividends per d spread over 2^-40 .. 2^2 (mantissas from a hash).
+__global__ void k_selftest_div(uint32_t dmax, uint32_t per, unsigned long long* bad) {
+  unsigned long long mine = 0;
+  const uint64_t total = (uint64_t)dmax * per;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t d = (uint32_t)(i / per) + 1;
+    uint64_t z = i * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const int ex = 1023 - 40 + (int)((z >> 52) % 43);
+    const double a = __longlong_as_double((long long)(((uint64_t)ex << 52) | (z & 0xFFFFFFFFFFFFFull)));
+    const double y = 1.0 / (double)d;
+    if (dbits(div_count(a, d, y)) != dbits(a / (double)d)) ++mine;
+  }
+  if (mine) atomicAdd(bad, mine);
+}
+
+cudaError_t selftest_division(uint32_t dmax, uint32_t per, unsigned long long* bad_host, int sms, cudaStream_t s) {
+  unsigned long long* bad = nullptr;
+  cudaError_t e = cudaMalloc(&bad, sizeof(*bad));
+  if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(*bad), s);
+  if (e == cudaSuccess) {
+    k_selftest_div<<<sms * 8, 256, 0, s>>>(dmax, per, bad);
+    e = cudaMemcpyAsync(bad_host, bad, sizeof(*bad), cudaMemcpyDeviceToHost, s);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(bad);
+  return e;
+}
+
 // Bitmap of the LOW class (warp per 32 ids).
 __global__ void __launch_bounds__(256) k_low_bitmap(const uint32_t* __restrict__ xtoff, uint32_t n,
                                                     uint32_t* __restrict__ bm) {
@@ -225,7 +262,12 @@ cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
     cudaError_t e = cudaMalloc(&g.low_bm, sizeof(uint32_t) * (((size_t)n + 31) / 32 + 1));
     if (e != cudaSuccess) return e;
   }
+  if (!g.rcp) {
+    cudaError_t e = cudaMalloc(&g.rcp, sizeof(double) * (n ? n : 1));
+    if (e != cudaSuccess) return e;
+  }
   if (n) k_low_bitmap<<<sms * 4, 256, 0, s>>>(g.xtoff, n, g.low_bm);
+  if (n) k_reciprocals<<<sms * 4, 256, 0, s>>>(g.xtdat, n, g.rcp);
   if (n == 0) {
     for (int c = 0; c <= NCLS; ++c) g.cls_begin[c] = 0;
     for (int c = 0; c < NCLS; ++c) g.cls_edges[c] = 0;

@@ -78,6 +78,7 @@ struct GraphDev {
   uint64_t cls_edges[NCLS] = {0, 0, 0};  // in-edges per class
   uint32_t mid_max = kDefaultMidMax;
   uint32_t* low_bm = nullptr;     // bitmap of the LOW class
+  double* rcp = nullptr;          // RN(1 / outdeg) per vertex, for div_count
   ChunkLayout lay[2];             // cached chunk layouts (rebuilt after a batch)
 };
 
@@ -109,6 +110,7 @@ struct SolveArgs {
   float* e[2];                    // FP32 refinement: correction, ping-pong
   float* ce[2];                   // FP32 refinement: correction / outdeg, ping-pong
   const uint32_t* low_bm;         // LOW-class bitmap
+  const double* rcp;              // RN(1 / outdeg)
   double* acc64;                  // partial row sums carried between chunk passes (FP64)
   float* acc32;                   // the same for the FP32 sweeps
   State* st;
@@ -160,6 +162,8 @@ cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s);
 // b: device array [du | dv | iu | iv | tdk | tdv | tik | tiv]; t* = batch sorted by (v, u)
 cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd, uint64_t ni, int sms, cudaStream_t s);
 cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t len, cudaStream_t s);
+// Mismatches of div_count against the IEEE division (prx_selftest_division).
+cudaError_t selftest_division(uint32_t dmax, uint32_t per, unsigned long long* bad_host, int sms, cudaStream_t s);
 
 void set_error(const std::string& msg);
 

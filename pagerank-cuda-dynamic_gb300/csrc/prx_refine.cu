@@ -36,7 +36,7 @@ __device__ __forceinline__ unsigned int finish32(const SolveArgs& a, uint32_t v,
   const float en = fmaf((float)a.P, sum, a.rho[v]);
   const float dl = fabsf(en - a.e[q][v]);
   a.e[q ^ 1][v] = en;
-  a.ce[q ^ 1][v] = en / (float)a.xtdat[v];
+  a.ce[q ^ 1][v] = __fdividef(en, (float)a.xtdat[v]);
   return fbits(dl);
 }
 
@@ -149,7 +149,7 @@ __global__ void k_refine_commit(SolveArgs a) {
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
     const double x = a.r[0][v] + (double)e[v];
     a.r[0][v] = x;
-    a.c[0][v] = x / (double)a.xtdat[v];
+    a.c[0][v] = div_count(x, a.xtdat[v], a.rcp[v]);
   }
 }
 

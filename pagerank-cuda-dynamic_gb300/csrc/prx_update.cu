@@ -65,9 +65,10 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
                                                             bool& survive, bool& changed) {
   using T = ModeTraits<MODE>;
   const uint32_t d = a.xtdat[v];
+  const double y = a.rcp[v];
   const double rv = a.r[p][v];
   double av;
-  if (T::PRUNE) av = fma(a.P, cv - rv / (double)d, a.C0) * (1 / (1 - (a.P / (double)d)));
+  if (T::PRUNE) av = fma(a.P, cv - div_count(rv, d, y), a.C0) * (1 / (1 - div_count(a.P, d, y)));
   else          av = fma(a.P, cv, a.C0);
   const double ev = fabs(av - rv);
   a.r[p ^ 1][v] = av;
@@ -76,9 +77,9 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
     const float rho = (float)(av - rv);
     a.rho[v] = rho;
     a.e[0][v] = rho;
-    a.ce[0][v] = rho / (float)d;
+    a.ce[0][v] = __fdividef(rho, (float)d);
   } else {
-    a.c[p ^ 1][v] = av / (double)d;
+    a.c[p ^ 1][v] = div_count(av, d, y);
   }
   survive = true;
   changed = false;
@@ -380,7 +381,7 @@ __global__ void k_init_ranks(SolveArgs a, const double* __restrict__ q, int both
   const double r0 = 1.0 / (double)a.n;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
     const double r = q ? q[v] : r0;
-    const double c = r / (double)a.xtdat[v];
+    const double c = div_count(r, a.xtdat[v], a.rcp[v]);
     a.r[0][v] = r;
     a.c[0][v] = c;
     if (both) {

@@ -6,7 +6,8 @@ host C++); this package only builds and binds it.
 from ._lib import (DYNAMIC_FRONTIER, DYNAMIC_TRAVERSAL, FP32_REFINE, FP64, LOOP_AUTO, LOOP_GRAPH, LOOP_HOST,
                    NAIVE_DYNAMIC, PRUNE_DYNAMIC_FRONTIER, STATIC, PrxError, library_path, load)
 from .api import (Context, Graph, mark_affected, options, pagerank_dynamic_frontier, pagerank_dynamic_traversal,
-                  pagerank_naive_dynamic, pagerank_prune_dynamic_frontier, pagerank_static, solve, solve_device)
+                  pagerank_naive_dynamic, pagerank_prune_dynamic_frontier, pagerank_static, selftest_division, solve,
+                  solve_device)
 from . import graphs
 
 MODES = {"static": STATIC, "naive_dynamic": NAIVE_DYNAMIC, "dynamic_traversal": DYNAMIC_TRAVERSAL,

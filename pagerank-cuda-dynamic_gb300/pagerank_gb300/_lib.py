@@ -58,7 +58,8 @@ EXPORTS = (
     "prx_options_default", "prx_status_string", "prx_last_error", "prx_context_create", "prx_context_destroy",
     "prx_context_stream", "prx_graph_create", "prx_graph_destroy", "prx_graph_size", "prx_graph_class_stats",
     "prx_graph_download",
-    "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_host_csr_free",
+    "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_selftest_division",
+    "prx_host_csr_free",
     "prx_gen_rmat", "prx_gen_weblike", "prx_gen_grid", "prx_gen_batch", "prx_host_tidy_batch",
     "prx_host_apply_batch", "prx_host_transpose", "prx_host_free",
 )
@@ -97,6 +98,7 @@ def load(build_if_missing=True):
         "prx_solve_device": (i32, [vp, vp, i32, vp, vp, u64, vp, vp, u64, vp, C.POINTER(Options), vp,
                                    C.POINTER(Result)]),
         "prx_mark_affected": (i32, [vp, vp, i32, vp, vp, u64, vp, u64, vp]),
+        "prx_selftest_division": (i32, [vp, C.c_uint32, C.c_uint32, C.POINTER(u64)]),
         "prx_host_csr_free": (None, [C.POINTER(HostCsr)]),
         "prx_gen_rmat": (i32, [i32, i32, dbl, dbl, dbl, u64, C.POINTER(HostCsr)]),
         "prx_gen_weblike": (i32, [C.c_uint32, dbl, dbl, C.c_uint32, dbl, C.c_uint32, u64, C.POINTER(HostCsr)]),

@@ -176,6 +176,13 @@ def mark_affected(ctx, g, mode, deletions, insertions):
     return flags[:n]
 
 
+def selftest_division(ctx, dmax, per):
+    """Mismatches of the solvers' reciprocal division against IEEE a / d."""
+    bad = C.c_uint64(0)
+    check(load().prx_selftest_division(ctx.handle, int(dmax), int(per), C.byref(bad)), "prx_selftest_division")
+    return bad.value
+
+
 # ---- the reference's five entry points ------------------------------------
 def pagerank_static(ctx, g, opts=None):
     return solve(ctx, g, _lib.STATIC, opts=opts)

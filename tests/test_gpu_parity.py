@@ -226,3 +226,12 @@ def test_errors_are_status_codes(pg, ctx):
     with pytest.raises(pg.PrxError):
         pg.Graph(ctx, xtoff, bad, xtdat, validate=True)
     g.close()
+
+
+def test_reciprocal_division_matches_ieee(pg, ctx):
+    # The solvers form contributions r / outdeg as q = r*y, r' = fma(-q, d, r),
+    # fma(r', y, q) with y = 1/d precomputed; it must equal the IEEE quotient
+    # bit for bit: every out-degree 1 .. 2^17 with 256 dividends each, and a
+    # sparser sweep of large out-degrees.
+    assert pg.selftest_division(ctx, 1 << 17, 256) == 0
+    assert pg.selftest_division(ctx, 1 << 24, 4) == 0
