@@ -540,13 +540,13 @@ int prx_graph_create(prx_context* c, uint32_t n, uint64_t m, const uint32_t* xof
   g.m = m;
   g.m_cap = m;
   cudaStream_t s = c->stream;
-  auto upload = [&](uint32_t** dst, const uint32_t* src, size_t cnt) -> cudaError_t {
-    cudaError_t e = cudaMalloc(dst, sizeof(uint32_t) * (cnt ? cnt : 1));
+  auto upload = [&](uint32_t** dst, const uint32_t* src, size_t cnt, size_t slots = 0) -> cudaError_t {
+    cudaError_t e = cudaMalloc(dst, sizeof(uint32_t) * (slots > cnt ? slots : (cnt ? cnt : 1)));
     if (e == cudaSuccess && cnt) e = cudaMemcpyAsync(*dst, src, sizeof(uint32_t) * cnt, cudaMemcpyHostToDevice, s);
     return e;
   };
   cudaError_t e = upload(&g.xtoff, xtoff, (size_t)n + 1);
-  if (e == cudaSuccess) e = upload(&g.xtedg, xtedg, m);
+  if (e == cudaSuccess) e = upload(&g.xtedg, xtedg, m, edge_slots(m));
   if (e == cudaSuccess) e = upload(&g.xtdat, xtdat, n);
   if (e == cudaSuccess && xoff) e = upload(&g.xoff, xoff, (size_t)n + 1);
   if (e == cudaSuccess && xoff) e = upload(&g.xedg, xedg, m);

@@ -136,7 +136,7 @@ cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd64, ui
   PRX_CU(cudaMalloc(&noff, sizeof(uint32_t) * ((size_t)n + 1)));
   PRX_CU(cudaMalloc(&ntoff, sizeof(uint32_t) * ((size_t)n + 1)));
   PRX_CU(cudaMalloc(&nedg, sizeof(uint32_t) * (m2 ? m2 : 1)));
-  PRX_CU(cudaMalloc(&ntedg, sizeof(uint32_t) * (m2 ? m2 : 1)));
+  PRX_CU(cudaMalloc(&ntedg, sizeof(uint32_t) * edge_slots(m2)));
   PRX_CU(cudaMalloc(&ndat, sizeof(uint32_t) * (n ? n : 1)));
   k_new_degree<<<grid, kThreads, 0, s>>>(g.xoff, dout, n, noff);
   k_new_degree<<<grid, kThreads, 0, s>>>(g.xtoff, din, n, ntoff);

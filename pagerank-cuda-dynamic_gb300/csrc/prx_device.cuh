@@ -93,18 +93,38 @@ __device__ __forceinline__ double div_count(double a, uint32_t d, double y) {
   return fma(r, y, q);
 }
 
-// Sum of c[edg[j]] for j in [s, e) added front to back onto acc, four
-// gathers in flight.
+// Sum of c[edg[j]] for j in [s, e) added front to back onto acc.  The edge
+// ids are read as aligned 16-byte groups of four (edg must be 16-byte
+// aligned and allocated per edge_slots); ids outside [s, e) in the first and
+// last group are loaded but neither gathered nor added.  Four gathers are in
+// flight per group.
 template <class T>
 __device__ __forceinline__ T lane_row_sum(const T* __restrict__ c, const uint32_t* __restrict__ edg, uint32_t s,
                                           uint32_t e, T acc) {
-  uint32_t j = s;
+  if (s >= e) return acc;
+  uint32_t j = s & ~3u;
+  if (j < s) {  // head group: ids j+1 .. j+3 from s on
+    const uint4 u = __ldg(reinterpret_cast<const uint4*>(edg + j));
+    const bool b1 = s <= j + 1 && j + 1 < e, b2 = s <= j + 2 && j + 2 < e, b3 = j + 3 < e;
+    const T c1 = b1 ? __ldg(c + u.y) : T(0), c2 = b2 ? __ldg(c + u.z) : T(0), c3 = b3 ? __ldg(c + u.w) : T(0);
+    if (b1) acc += c1;
+    if (b2) acc += c2;
+    if (b3) acc += c3;
+    j += 4;
+  }
   for (; j + 4 <= e; j += 4) {
-    const uint32_t u0 = __ldg(edg + j), u1 = __ldg(edg + j + 1), u2 = __ldg(edg + j + 2), u3 = __ldg(edg + j + 3);
-    const T c0 = __ldg(c + u0), c1 = __ldg(c + u1), c2 = __ldg(c + u2), c3 = __ldg(c + u3);
+    const uint4 u = __ldg(reinterpret_cast<const uint4*>(edg + j));
+    const T c0 = __ldg(c + u.x), c1 = __ldg(c + u.y), c2 = __ldg(c + u.z), c3 = __ldg(c + u.w);
     acc += c0; acc += c1; acc += c2; acc += c3;
   }
-  for (; j < e; ++j) acc += __ldg(c + __ldg(edg + j));
+  if (j < e) {  // tail group: ids j .. e-1 (at most 3)
+    const uint4 u = __ldg(reinterpret_cast<const uint4*>(edg + j));
+    const bool b1 = j + 1 < e, b2 = j + 2 < e;
+    const T c0 = __ldg(c + u.x), c1 = b1 ? __ldg(c + u.y) : T(0), c2 = b2 ? __ldg(c + u.z) : T(0);
+    acc += c0;
+    if (b1) acc += c1;
+    if (b2) acc += c2;
+  }
   return acc;
 }
 

@@ -231,7 +231,7 @@ cudaError_t ensure_chunks(GraphDev& g, uint32_t width, uint32_t keep, int sms, c
   const size_t len = (size_t)K * ((size_t)g.n + 1);
   if (len > 0xffffffffull) return cudaErrorInvalidValue;
   cudaError_t e = cudaMalloc(&l.off, sizeof(uint32_t) * len);
-  if (e == cudaSuccess) e = cudaMalloc(&l.edg, sizeof(uint32_t) * (g.cls_edges[LOW] ? g.cls_edges[LOW] : 1));
+  if (e == cudaSuccess) e = cudaMalloc(&l.edg, sizeof(uint32_t) * edge_slots(g.cls_edges[LOW]));
   if (e != cudaSuccess) {
     cudaFree(l.off); cudaFree(l.edg);
     l = ChunkLayout();

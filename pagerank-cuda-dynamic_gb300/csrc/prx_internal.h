@@ -21,6 +21,11 @@ enum Cls { LOW = 0, MID = 1, HIGH = 2, NCLS = 3 };
 
 constexpr int kThreads = 256;  // threads per block for all map-like kernels
 
+// Elements allocated for an in-edge array of m edges: the LOW-class gathers
+// read a row's edge ids as aligned 16-byte groups, and the group holding a
+// row's last edge may reach 3 ids past the array's end.
+inline size_t edge_slots(uint64_t m) { return (size_t)((m + 3) & ~3ull) + 4; }
+
 // Device-resident control block of one solve.
 struct State {
   unsigned long long el_bits[2];  // L-inf delta of the iteration with parity p (bits of a double >= 0)
