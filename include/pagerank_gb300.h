@@ -193,6 +193,39 @@ int prx_mark_affected(prx_context* ctx, prx_graph* g, int mode,
                       const uint32_t* delu, const uint32_t* delv, uint64_t nd,
                       const uint32_t* insu, uint64_t ni, uint8_t* flags_out);
 
+/* ---- batched personalized PageRank (no counterpart in the reference) ---- */
+
+/* Statistics of one batched personalized PageRank solve. */
+typedef struct {
+  int      iterations;        /* sweeps of the slowest column block        */
+  int      fp64_sweeps;       /* FP64 sweeps, summed over column blocks     */
+  int      fp32_sweeps;       /* FP32 correction sweeps (FP32_REFINE)       */
+  int      refinements;       /* FP64 residual sweeps (FP32_REFINE)         */
+  float    time_ms;           /* device time of the solve (CUDA events)     */
+  double   last_delta;        /* largest final L-inf change of a block      */
+  uint64_t kernel_launches;
+} prx_ppr_result;
+
+/* Personalized PageRank of nvec teleport vectors on graph g.  Vector k
+ * teleports uniformly to the seeds seeds[seed_off[k] .. seed_off[k+1])
+ * (host arrays; non-empty sets of ids < n, a repeated id counts twice):
+ *   r_k = (1 - damping) t_k + damping * A^T D^-1 r_k,
+ * iterated by Jacobi sweeps from r_k = t_k until the largest change of one
+ * sweep over the vertices and the vectors of a block of 64 vectors is below
+ * o->tolerance, or o->max_iterations sweeps.  o->precision PRX_FP64 stores
+ * and sums in FP64; PRX_FP32_REFINE runs the correction sweeps in FP32 with
+ * FP64 residuals (the FP64 residual decides convergence).  Vectors are
+ * solved 64 at a time.  ranks_out: n * nvec doubles in host memory,
+ * vertex-major (ranks_out[v * nvec + k]).  Other options are ignored. */
+int prx_solve_ppr_batched(prx_context* ctx, prx_graph* g, uint32_t nvec,
+                          const uint32_t* seed_off, const uint32_t* seeds,
+                          const prx_options* o, double* ranks_out, prx_ppr_result* res);
+
+/* The same with ranks_out in device memory (seeds stay host arrays). */
+int prx_solve_ppr_batched_device(prx_context* ctx, prx_graph* g, uint32_t nvec,
+                                 const uint32_t* seed_off, const uint32_t* seeds,
+                                 const prx_options* o, double* ranks_out, prx_ppr_result* res);
+
 /* Diagnostic with no counterpart in the reference: counts, on the context's
  * device, the dividends a and out-degrees d (d = 1 .. dmax, `per` values of a
  * per d, spread over 2^-40 .. 2^2) for which the library's three-operation

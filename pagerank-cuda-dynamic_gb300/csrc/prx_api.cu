@@ -13,7 +13,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
-#include "prx_internal.h"
+#include "prx_ctx.h"
 
 using namespace prx;
 
@@ -21,64 +21,6 @@ namespace prx {
 static thread_local std::string g_last_error;
 void set_error(const std::string& msg) { g_last_error = msg; }
 }  // namespace prx
-
-struct prx_context {
-  int device = 0;
-  int sms = 152;
-  cudaStream_t stream = nullptr;
-  State* st = nullptr;        // device control block
-  State* st_host = nullptr;   // pinned: [0] after marking, [1] loop checks
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  // workspace (grows on demand)
-  uint32_t ws_n = 0;
-  bool ws_dyn = false;
-  double* r[2] = {nullptr, nullptr};
-  double* c[2] = {nullptr, nullptr};
-  double* acc64 = nullptr;    // partial sums between chunk passes
-  float* acc32 = nullptr;
-  uint8_t* flags = nullptr;   // byte flags for prx_mark_affected
-  uint32_t* bm[3] = {nullptr, nullptr, nullptr};
-  uint32_t* nf[2] = {nullptr, nullptr};
-  uint32_t* xb = nullptr;
-  uint32_t* naff = nullptr;
-  uint32_t* lists[2][NCLS] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
-  uint32_t* xl = nullptr;
-  uint32_t* fr[2] = {nullptr, nullptr};
-  // FP32 refinement (grown on first use)
-  uint32_t ws32_n = 0;
-  float* rho = nullptr;
-  float* e32[2] = {nullptr, nullptr};
-  float* ce32[2] = {nullptr, nullptr};
-  uint32_t* batch = nullptr;  // device copy of a batch
-  size_t batch_cap = 0;       // in uint32 elements
-  // launch accounting and optional per-launch timing of the rank update
-  uint64_t launches = 0;
-  std::vector<cudaEvent_t> tev;   // pairs: start, end
-  std::vector<int> tev_cls;       // class of each recorded pair
-  size_t tev_used = 0;            // pairs recorded since the last drain
-  double upd_ms[2 * NCLS] = {0, 0, 0, 0, 0, 0};     // [FP64 classes | FP32 classes]
-  uint32_t upd_n[2 * NCLS] = {0, 0, 0, 0, 0, 0};
-};
-
-struct prx_graph {
-  prx_context* ctx = nullptr;
-  GraphDev g;
-};
-
-#define TRY_CUDA_ST(x)                                                                   \
-  do {                                                                                   \
-    cudaError_t e_ = (x);                                                                \
-    if (e_ != cudaSuccess) {                                                             \
-      set_error(std::string(#x) + ": " + cudaGetErrorString(e_));                        \
-      return e_ == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;                   \
-    }                                                                                    \
-  } while (0)
-
-#define FAIL(code, msg)  \
-  do {                   \
-    set_error(msg);      \
-    return (code);       \
-  } while (0)
 
 extern "C" {
 
@@ -160,6 +102,8 @@ int prx_context_destroy(prx_context* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_ws(c);
+  ppr_free(c->ppr);
+  c->ppr = nullptr;
   cudaFree(c->rho);
   for (int p = 0; p < 2; ++p) { cudaFree(c->e32[p]); cudaFree(c->ce32[p]); }
   cudaFree(c->batch);
@@ -570,6 +514,7 @@ int prx_graph_destroy(prx_graph* gr) {
   cudaFree(g.xoff); cudaFree(g.xedg); cudaFree(g.xtoff); cudaFree(g.xtedg); cudaFree(g.xtdat); cudaFree(g.cls_list);
   cudaFree(g.low_bm);
   cudaFree(g.rcp);
+  cudaFree(g.rcp32);
   free_chunks(g);
   delete gr;
   return PRX_OK;

@@ -1,0 +1,73 @@
+// prx_ctx.h -- the opaque handles of the C ABI (contexts and device graphs)
+// and the status macros shared by the host drivers.  Internal.
+#pragma once
+#include <string>
+#include <vector>
+#include "prx_internal.h"
+
+namespace prx {
+struct PprWs;
+void ppr_free(PprWs* w);  // prx_ppr.cu
+}  // namespace prx
+
+using namespace prx;
+
+struct prx_context {
+  int device = 0;
+  int sms = 152;
+  cudaStream_t stream = nullptr;
+  State* st = nullptr;        // device control block
+  State* st_host = nullptr;   // pinned: [0] after marking, [1] loop checks
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // workspace (grows on demand)
+  uint32_t ws_n = 0;
+  bool ws_dyn = false;
+  double* r[2] = {nullptr, nullptr};
+  double* c[2] = {nullptr, nullptr};
+  double* acc64 = nullptr;    // partial sums between chunk passes
+  float* acc32 = nullptr;
+  uint8_t* flags = nullptr;   // byte flags for prx_mark_affected
+  uint32_t* bm[3] = {nullptr, nullptr, nullptr};
+  uint32_t* nf[2] = {nullptr, nullptr};
+  uint32_t* xb = nullptr;
+  uint32_t* naff = nullptr;
+  uint32_t* lists[2][NCLS] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+  uint32_t* xl = nullptr;
+  uint32_t* fr[2] = {nullptr, nullptr};
+  // FP32 refinement (grown on first use)
+  uint32_t ws32_n = 0;
+  float* rho = nullptr;
+  float* e32[2] = {nullptr, nullptr};
+  float* ce32[2] = {nullptr, nullptr};
+  uint32_t* batch = nullptr;  // device copy of a batch
+  size_t batch_cap = 0;       // in uint32 elements
+  // launch accounting and optional per-launch timing of the rank update
+  uint64_t launches = 0;
+  std::vector<cudaEvent_t> tev;   // pairs: start, end
+  std::vector<int> tev_cls;       // class of each recorded pair
+  size_t tev_used = 0;            // pairs recorded since the last drain
+  double upd_ms[2 * NCLS] = {0, 0, 0, 0, 0, 0};     // [FP64 classes | FP32 classes]
+  uint32_t upd_n[2 * NCLS] = {0, 0, 0, 0, 0, 0};
+  prx::PprWs* ppr = nullptr;  // batched personalized PageRank workspace (prx_ppr.cu)
+};
+
+struct prx_graph {
+  prx_context* ctx = nullptr;
+  GraphDev g;
+};
+
+#define TRY_CUDA_ST(x)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (x);                                                                \
+    if (e_ != cudaSuccess) {                                                             \
+      set_error(std::string(#x) + ": " + cudaGetErrorString(e_));                        \
+      return e_ == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;                   \
+    }                                                                                    \
+  } while (0)
+
+#define FAIL(code, msg)  \
+  do {                   \
+    set_error(msg);      \
+    return (code);       \
+  } while (0)
+

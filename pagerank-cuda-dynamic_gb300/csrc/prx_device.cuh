@@ -62,6 +62,20 @@ __device__ __forceinline__ void block_max_bits(unsigned long long x, unsigned lo
   }
 }
 
+// The same for a non-negative float given as its bit pattern.
+__device__ __forceinline__ void block_max_u32(unsigned int x, unsigned int* dst) {
+  __shared__ unsigned int smax[32];
+  for (int o = 16; o; o >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, o));
+  const int w = threadIdx.x >> 5;
+  if (lane_id() == 0) smax[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    x = lane_id() < (blockDim.x >> 5) ? smax[lane_id()] : 0u;
+    for (int o = 16; o; o >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if (lane_id() == 0 && x) atomicMax(dst, x);
+  }
+}
+
 __device__ __forceinline__ void block_sum_u64(unsigned long long x, unsigned long long* dst) {
   __shared__ unsigned long long ssum[32];
   for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);

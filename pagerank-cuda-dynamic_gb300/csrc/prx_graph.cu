@@ -123,9 +123,12 @@ __global__ void __launch_bounds__(256) k_cls_edges(const uint32_t* __restrict__ 
   if (threadIdx.x < NCLS && acc[threadIdx.x]) atomicAdd(&out[threadIdx.x], acc[threadIdx.x]);
 }
 
-__global__ void k_reciprocals(const uint32_t* __restrict__ deg, uint32_t n, double* __restrict__ rcp) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+__global__ void k_reciprocals(const uint32_t* __restrict__ deg, uint32_t n, double* __restrict__ rcp,
+                              float* __restrict__ rcp32) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     rcp[v] = 1.0 / (double)deg[v];
+    rcp32[v] = 1.0f / (float)deg[v];
+  }
 }
 
 // Self-test of div_count against the IEEE division: d in [1, dmax] and
@@ -266,8 +269,12 @@ cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
     cudaError_t e = cudaMalloc(&g.rcp, sizeof(double) * (n ? n : 1));
     if (e != cudaSuccess) return e;
   }
+  if (!g.rcp32) {
+    cudaError_t e = cudaMalloc(&g.rcp32, sizeof(float) * (n ? n : 1));
+    if (e != cudaSuccess) return e;
+  }
   if (n) k_low_bitmap<<<sms * 4, 256, 0, s>>>(g.xtoff, n, g.low_bm);
-  if (n) k_reciprocals<<<sms * 4, 256, 0, s>>>(g.xtdat, n, g.rcp);
+  if (n) k_reciprocals<<<sms * 4, 256, 0, s>>>(g.xtdat, n, g.rcp, g.rcp32);
   if (n == 0) {
     for (int c = 0; c <= NCLS; ++c) g.cls_begin[c] = 0;
     for (int c = 0; c < NCLS; ++c) g.cls_edges[c] = 0;

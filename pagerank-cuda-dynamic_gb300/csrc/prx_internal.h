@@ -48,6 +48,7 @@ struct State {
   int inner_done;                 // the current round's FP32 sweeps have converged / hit the cap
   int rounds;                     // FP64 residual sweeps run
   unsigned int el32_bits[2];      // L-inf change of the FP32 sweep with parity k32 & 1 (bits of a float >= 0)
+  unsigned int e32max_bits[2];    // L-inf of the correction it produced (personalized PageRank)
 };
 
 // Internal mode of the update kernels: the FP64 residual sweep of the FP32
@@ -84,6 +85,7 @@ struct GraphDev {
   uint32_t mid_max = kDefaultMidMax;
   uint32_t* low_bm = nullptr;     // bitmap of the LOW class
   double* rcp = nullptr;          // RN(1 / outdeg) per vertex, for div_count
+  float* rcp32 = nullptr;         // the same in FP32 (personalized PageRank sweeps)
   ChunkLayout lay[2];             // cached chunk layouts (rebuilt after a batch)
 };
 

@@ -19,19 +19,6 @@ namespace prx {
 
 __device__ __forceinline__ unsigned int fbits(float x) { return __float_as_uint(x); }
 
-__device__ __forceinline__ void block_max_u32(unsigned int x, unsigned int* dst) {
-  __shared__ unsigned int smax[32];
-  for (int o = 16; o; o >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, o));
-  const int w = threadIdx.x >> 5;
-  if (lane_id() == 0) smax[w] = x;
-  __syncthreads();
-  if (w == 0) {
-    x = lane_id() < (blockDim.x >> 5) ? smax[lane_id()] : 0u;
-    for (int o = 16; o; o >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, o));
-    if (lane_id() == 0 && x) atomicMax(dst, x);
-  }
-}
-
 __device__ __forceinline__ unsigned int finish32(const SolveArgs& a, uint32_t v, float sum, int q) {
   const float en = fmaf((float)a.P, sum, a.rho[v]);
   const float dl = fabsf(en - a.e[q][v]);

@@ -42,6 +42,15 @@ class Result(C.Structure):
         return d
 
 
+class PprResult(C.Structure):
+    """prx_ppr_result (batched personalized PageRank; no counterpart in the reference)."""
+    _fields_ = [("iterations", C.c_int), ("fp64_sweeps", C.c_int), ("fp32_sweeps", C.c_int),
+                ("refinements", C.c_int), ("time_ms", C.c_float), ("last_delta", C.c_double),
+                ("kernel_launches", C.c_uint64)]
+
+    as_dict = Result.as_dict
+
+
 class HostCsr(C.Structure):
     _fields_ = [("n", C.c_uint32), ("m", C.c_uint64), ("off", C.POINTER(C.c_uint32)),
                 ("edg", C.POINTER(C.c_uint32))]
@@ -59,6 +68,7 @@ EXPORTS = (
     "prx_context_stream", "prx_graph_create", "prx_graph_destroy", "prx_graph_size", "prx_graph_class_stats",
     "prx_graph_download",
     "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_selftest_division",
+    "prx_solve_ppr_batched", "prx_solve_ppr_batched_device",
     "prx_host_csr_free",
     "prx_gen_rmat", "prx_gen_weblike", "prx_gen_grid", "prx_gen_batch", "prx_host_tidy_batch",
     "prx_host_apply_batch", "prx_host_transpose", "prx_host_free",
@@ -99,6 +109,9 @@ def load(build_if_missing=True):
                                    C.POINTER(Result)]),
         "prx_mark_affected": (i32, [vp, vp, i32, vp, vp, u64, vp, u64, vp]),
         "prx_selftest_division": (i32, [vp, C.c_uint32, C.c_uint32, C.POINTER(u64)]),
+        "prx_solve_ppr_batched": (i32, [vp, vp, C.c_uint32, vp, vp, C.POINTER(Options), vp, C.POINTER(PprResult)]),
+        "prx_solve_ppr_batched_device": (i32, [vp, vp, C.c_uint32, vp, vp, C.POINTER(Options), vp,
+                                               C.POINTER(PprResult)]),
         "prx_host_csr_free": (None, [C.POINTER(HostCsr)]),
         "prx_gen_rmat": (i32, [i32, i32, dbl, dbl, dbl, u64, C.POINTER(HostCsr)]),
         "prx_gen_weblike": (i32, [C.c_uint32, dbl, dbl, C.c_uint32, dbl, C.c_uint32, u64, C.POINTER(HostCsr)]),

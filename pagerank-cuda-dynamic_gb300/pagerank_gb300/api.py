@@ -16,7 +16,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import Options, Result, check, load
+from ._lib import Options, PprResult, Result, check, load
 
 
 def options(**kw):
@@ -174,6 +174,38 @@ def mark_affected(ctx, g, mode, deletions, insertions):
     check(load().prx_mark_affected(ctx.handle, g.handle, int(mode), _p(du), _p(dv), len(du), _p(iu), len(iu),
                                    flags.ctypes.data), "prx_mark_affected")
     return flags[:n]
+
+
+def _seed_csr(seed_sets):
+    sets = [np.ascontiguousarray(x, dtype=np.uint32).ravel() for x in seed_sets]
+    off = np.zeros(len(sets) + 1, np.uint32)
+    off[1:] = np.cumsum([len(x) for x in sets])
+    seeds = np.concatenate(sets) if sets else np.zeros(0, np.uint32)
+    return off, np.ascontiguousarray(seeds, dtype=np.uint32)
+
+
+def solve_ppr_batched(ctx, g, seed_sets, opts=None):
+    """Personalized PageRank of len(seed_sets) teleport vectors (vector k
+    teleports uniformly to seed_sets[k]) -> (ranks float64[n, nvec], result dict)."""
+    n, _ = g.size()
+    off, seeds = _seed_csr(seed_sets)
+    nvec = len(off) - 1
+    ranks = np.zeros((max(n, 1), max(nvec, 1)), np.float64)
+    res = PprResult()
+    check(load().prx_solve_ppr_batched(ctx.handle, g.handle, nvec, off.ctypes.data, _p(seeds),
+                                       C.byref(opts or options()), ranks.ctypes.data, C.byref(res)),
+          "prx_solve_ppr_batched")
+    return ranks[:n, :nvec], res.as_dict()
+
+
+def solve_ppr_batched_device(ctx, g, seed_sets, ranks_ptr, opts=None):
+    """The same into device memory at ranks_ptr (n * nvec doubles) -> result dict."""
+    off, seeds = _seed_csr(seed_sets)
+    res = PprResult()
+    check(load().prx_solve_ppr_batched_device(ctx.handle, g.handle, len(off) - 1, off.ctypes.data, _p(seeds),
+                                              C.byref(opts or options()), ranks_ptr, C.byref(res)),
+          "prx_solve_ppr_batched_device")
+    return res.as_dict()
 
 
 def selftest_division(ctx, dmax, per):
