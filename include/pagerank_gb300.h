@@ -226,6 +226,39 @@ int prx_solve_ppr_batched_device(prx_context* ctx, prx_graph* g, uint32_t nvec,
                                  const uint32_t* seed_off, const uint32_t* seeds,
                                  const prx_options* o, double* ranks_out, prx_ppr_result* res);
 
+/* ---- weighted PageRank and its adjoint (no counterpart in the reference) --
+ * Edge u -> v carries a weight w_uv > 0, rows are normalised
+ * (P_uv = w_uv / W_u, W_u = sum_v w_uv) and
+ *   r = (1 - damping) t + damping P^T r.
+ * The adjoint of a loss L(r) with g = dL/dr solves
+ *   lambda = damping P lambda + g
+ * by the same pull kernels on the out-CSR (the reversed graph) and gives
+ *   dL/dw_uv = (r_u / W_u)(damping lambda_v - lambda_u + g_u),
+ *   dL/dt = (1 - damping) lambda,  dL/ddamping = lambda . (P^T r - t).
+ * Both solves are Jacobi iterations stopped by the reference's L-inf test
+ * (o->tolerance, o->max_iterations); they run in FP64.  Pointers are device
+ * pointers unless stated; the calls return after their work finished. */
+
+/* Attach weights w (m floats, device, in out-CSR order: the weight of edge
+ * xedg[j] at w[j]) to a graph created with its out-CSR.  A batch applied to
+ * the graph drops the weights. */
+int prx_graph_set_weights(prx_context* ctx, prx_graph* g, const float* w);
+
+/* Weighted PageRank: t (n, NULL = uniform 1/n) is the teleport vector, r0
+ * (n, NULL = t) the starting ranks; the converged ranks go to r (n).
+ * res->iterations, last_delta, time_ms and kernel_launches are set. */
+int prx_solve_weighted(prx_context* ctx, prx_graph* g, const double* t, const double* r0,
+                       const prx_options* o, double* r, prx_result* res);
+
+/* Adjoint of the weighted solve at converged ranks r (n) for teleport t (n,
+ * NULL = uniform) and loss gradient gl = dL/dr (n).  Outputs, each
+ * optional: lambda (n), grad_w (m, out-CSR order), grad_t (n) and
+ * grad_alpha (one double in HOST memory).  res->iterations counts the
+ * adjoint sweeps. */
+int prx_adjoint(prx_context* ctx, prx_graph* g, const double* t, const double* r, const double* gl,
+                const prx_options* o, double* lambda, double* grad_w, double* grad_t, double* grad_alpha,
+                prx_result* res);
+
 /* Diagnostic with no counterpart in the reference: counts, on the context's
  * device, the dividends a and out-degrees d (d = 1 .. dmax, `per` values of a
  * per d, spread over 2^-40 .. 2^2) for which the library's three-operation

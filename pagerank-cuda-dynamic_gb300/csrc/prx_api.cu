@@ -104,6 +104,7 @@ int prx_context_destroy(prx_context* c) {
   free_ws(c);
   ppr_free(c->ppr);
   c->ppr = nullptr;
+  cudaFree(c->wk);
   cudaFree(c->rho);
   for (int p = 0; p < 2; ++p) { cudaFree(c->e32[p]); cudaFree(c->ce32[p]); }
   cudaFree(c->batch);
@@ -515,6 +516,8 @@ int prx_graph_destroy(prx_graph* gr) {
   cudaFree(g.low_bm);
   cudaFree(g.rcp);
   cudaFree(g.rcp32);
+  drop_weights(g);
+  cudaFree(g.ocls_list);
   free_chunks(g);
   delete gr;
   return PRX_OK;
@@ -605,6 +608,7 @@ int prx_graph_apply_batch(prx_graph* gr, const uint32_t* du, const uint32_t* dv,
   if (e == cudaErrorInvalidValue)
     FAIL(PRX_EINVAL, "prx_graph_apply_batch: batch is not tidy (a deletion is missing or an insertion exists)");
   TRY_CUDA_ST(e);
+  drop_weights(g);  // the edges changed: weights must be set again
   return PRX_OK;
 }
 

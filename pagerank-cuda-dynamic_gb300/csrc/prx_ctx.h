@@ -49,6 +49,8 @@ struct prx_context {
   double upd_ms[2 * NCLS] = {0, 0, 0, 0, 0, 0};     // [FP64 classes | FP32 classes]
   uint32_t upd_n[2 * NCLS] = {0, 0, 0, 0, 0, 0};
   prx::PprWs* ppr = nullptr;  // batched personalized PageRank workspace (prx_ppr.cu)
+  double* wk = nullptr;       // weighted solves and the adjoint: 3 n-vectors + partial sums (prx_weighted.cu)
+  size_t wk_cap = 0;          // in doubles
 };
 
 struct prx_graph {

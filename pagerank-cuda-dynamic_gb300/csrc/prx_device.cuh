@@ -42,7 +42,9 @@ __device__ __forceinline__ void push(uint32_t* list, uint32_t* cnt, uint32_t v) 
 
 // Block-wide max of a non-negative double given as its bit pattern (for
 // x >= 0 the IEEE-754 bit patterns order like the values), folded into *dst
-// with one atomicMax per block.  Every thread of the block must call it.
+// with one atomicMax per block.  Every thread of the block must call it; the
+// leading barrier lets calls follow one another (warp 0 may still be reading
+// the shared slots of the previous call).
 __device__ __forceinline__ void block_max_bits(unsigned long long x, unsigned long long* dst) {
   __shared__ unsigned long long smax[32];
   for (int o = 16; o; o >>= 1) {
@@ -50,6 +52,7 @@ __device__ __forceinline__ void block_max_bits(unsigned long long x, unsigned lo
     x = y > x ? y : x;
   }
   const int w = threadIdx.x >> 5;
+  __syncthreads();
   if (lane_id() == 0) smax[w] = x;
   __syncthreads();
   if (w == 0) {
@@ -67,6 +70,7 @@ __device__ __forceinline__ void block_max_u32(unsigned int x, unsigned int* dst)
   __shared__ unsigned int smax[32];
   for (int o = 16; o; o >>= 1) x = max(x, __shfl_xor_sync(0xffffffffu, x, o));
   const int w = threadIdx.x >> 5;
+  __syncthreads();
   if (lane_id() == 0) smax[w] = x;
   __syncthreads();
   if (w == 0) {

@@ -275,9 +275,18 @@ cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
   }
   if (n) k_low_bitmap<<<sms * 4, 256, 0, s>>>(g.xtoff, n, g.low_bm);
   if (n) k_reciprocals<<<sms * 4, 256, 0, s>>>(g.xtdat, n, g.rcp, g.rcp32);
+  if (!g.cls_list) {
+    cudaError_t e = cudaMalloc(&g.cls_list, sizeof(uint32_t) * (n ? n : 1));
+    if (e != cudaSuccess) return e;
+  }
+  return build_class_lists(g.xtoff, n, g.mid_max, g.cls_list, g.cls_begin, g.cls_edges, sms, s);
+}
+
+cudaError_t build_class_lists(const uint32_t* off, uint32_t n, uint32_t mid_max, uint32_t* list,
+                              uint32_t begin[NCLS + 1], uint64_t edges_out[NCLS], int sms, cudaStream_t s) {
   if (n == 0) {
-    for (int c = 0; c <= NCLS; ++c) g.cls_begin[c] = 0;
-    for (int c = 0; c < NCLS; ++c) g.cls_edges[c] = 0;
+    for (int c = 0; c <= NCLS; ++c) begin[c] = 0;
+    for (int c = 0; c < NCLS; ++c) edges_out[c] = 0;
     return cudaSuccess;
   }
   const uint32_t ntiles = (n + kTileV - 1) / kTileV;
@@ -289,15 +298,11 @@ cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   uint32_t* bounds = cnt + (size_t)NCLS * ntiles;
   unsigned long long* edges = (unsigned long long*)((char*)cnt + ((words * sizeof(uint32_t) + 7) & ~(size_t)7));
-  if (!g.cls_list) {
-    e = cudaMalloc(&g.cls_list, sizeof(uint32_t) * n);
-    if (e != cudaSuccess) { cudaFreeAsync(cnt, s); return e; }
-  }
   e = cudaMemsetAsync(edges, 0, NCLS * sizeof(unsigned long long), s);
-  k_cls_count<<<ntiles, 256, 0, s>>>(g.xtoff, n, g.mid_max, ntiles, cnt);
+  k_cls_count<<<ntiles, 256, 0, s>>>(off, n, mid_max, ntiles, cnt);
   k_cls_scan<<<1, 1024, 0, s>>>(cnt, ntiles, bounds);
-  k_cls_scatter<<<ntiles, 256, 0, s>>>(g.xtoff, n, g.mid_max, ntiles, cnt, g.cls_list);
-  k_cls_edges<<<sms * 4, 256, 0, s>>>(g.xtoff, n, g.mid_max, edges);
+  k_cls_scatter<<<ntiles, 256, 0, s>>>(off, n, mid_max, ntiles, cnt, list);
+  k_cls_edges<<<sms * 4, 256, 0, s>>>(off, n, mid_max, edges);
   uint32_t hb[NCLS + 1];
   unsigned long long he[NCLS];
   if (e == cudaSuccess) e = cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s);
@@ -305,8 +310,8 @@ cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   cudaFreeAsync(cnt, s);
   if (e != cudaSuccess) return e;
-  for (int c = 0; c <= NCLS; ++c) g.cls_begin[c] = hb[c];
-  for (int c = 0; c < NCLS; ++c) g.cls_edges[c] = he[c];
+  for (int c = 0; c <= NCLS; ++c) begin[c] = hb[c];
+  for (int c = 0; c < NCLS; ++c) edges_out[c] = he[c];
   return cudaGetLastError();
 }
 

@@ -87,7 +87,17 @@ struct GraphDev {
   double* rcp = nullptr;          // RN(1 / outdeg) per vertex, for div_count
   float* rcp32 = nullptr;         // the same in FP32 (personalized PageRank sweeps)
   ChunkLayout lay[2];             // cached chunk layouts (rebuilt after a batch)
+  // edge weights (prx_graph_set_weights; dropped when a batch changes the edges)
+  double* px = nullptr;           // P_uv = w_uv / W_u in out-CSR (xedg) order
+  double* pt = nullptr;           // the same in in-CSR (xtedg) order
+  double* wsum = nullptr;         // W_u = sum of u's out-edge weights
+  uint32_t* ocls_list = nullptr;  // ids by out-degree class (rows of the out-CSR)
+  uint32_t ocls_begin[NCLS + 1] = {0, 0, 0, 0};
+  uint64_t ocls_edges[NCLS] = {0, 0, 0};
 };
+
+// Frees the edge weights of g (after a batch, or with the graph).
+void drop_weights(GraphDev& g);
 
 // Chunk layout of `width` vertices per chunk (built on first use, cached in
 // two slots; the layout of width `keep` is not evicted); width >= n means no
@@ -166,6 +176,10 @@ void launch_state_reset(State* st, int max_iter, double tol, cudaStream_t s);
 
 // ---- graph construction (prx_graph.cu) ----------------------------------
 cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s);
+// Ids of the rows of `off` by length class (LOW, MID, HIGH; each ascending)
+// into list (n), their bounds and the edges of each class.
+cudaError_t build_class_lists(const uint32_t* off, uint32_t n, uint32_t mid_max, uint32_t* list,
+                              uint32_t begin[NCLS + 1], uint64_t edges[NCLS], int sms, cudaStream_t s);
 // b: device array [du | dv | iu | iv | tdk | tdv | tik | tiv]; t* = batch sorted by (v, u)
 cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd, uint64_t ni, int sms, cudaStream_t s);
 cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t len, cudaStream_t s);

@@ -68,7 +68,8 @@ EXPORTS = (
     "prx_context_stream", "prx_graph_create", "prx_graph_destroy", "prx_graph_size", "prx_graph_class_stats",
     "prx_graph_download",
     "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_selftest_division",
-    "prx_solve_ppr_batched", "prx_solve_ppr_batched_device",
+    "prx_solve_ppr_batched", "prx_solve_ppr_batched_device", "prx_graph_set_weights", "prx_solve_weighted",
+    "prx_adjoint",
     "prx_host_csr_free",
     "prx_gen_rmat", "prx_gen_weblike", "prx_gen_grid", "prx_gen_batch", "prx_host_tidy_batch",
     "prx_host_apply_batch", "prx_host_transpose", "prx_host_free",
@@ -112,6 +113,10 @@ def load(build_if_missing=True):
         "prx_solve_ppr_batched": (i32, [vp, vp, C.c_uint32, vp, vp, C.POINTER(Options), vp, C.POINTER(PprResult)]),
         "prx_solve_ppr_batched_device": (i32, [vp, vp, C.c_uint32, vp, vp, C.POINTER(Options), vp,
                                                C.POINTER(PprResult)]),
+        "prx_graph_set_weights": (i32, [vp, vp, vp]),
+        "prx_solve_weighted": (i32, [vp, vp, vp, vp, C.POINTER(Options), vp, C.POINTER(Result)]),
+        "prx_adjoint": (i32, [vp, vp, vp, vp, vp, C.POINTER(Options), vp, vp, vp, C.POINTER(dbl),
+                              C.POINTER(Result)]),
         "prx_host_csr_free": (None, [C.POINTER(HostCsr)]),
         "prx_gen_rmat": (i32, [i32, i32, dbl, dbl, dbl, u64, C.POINTER(HostCsr)]),
         "prx_gen_weblike": (i32, [C.c_uint32, dbl, dbl, C.c_uint32, dbl, C.c_uint32, u64, C.POINTER(HostCsr)]),
