@@ -55,6 +55,12 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--static-only", action="store_true", help="upload only the in-CSR; skip DF-P and the CPU leg")
     p.add_argument("--chunk", type=int, default=0, help="source-chunk width of the gathers (0: library default)")
+    p.add_argument("--no-ppr", action="store_true", help="skip the batched personalized PageRank workload")
+    p.add_argument("--ppr-scale", type=int, default=22)
+    p.add_argument("--no-adjoint", action="store_true", help="skip the weighted PageRank adjoint workload")
+    p.add_argument("--adjoint-scale", type=int, default=20)
+    p.add_argument("--adjoint-fd-edges", type=int, default=200, help="edges checked by finite differences")
+    p.add_argument("--adjoint-batches", type=int, default=2, help="dynamic batches of 1e-4|E| after the first solve")
     a = p.parse_args()
     if a.static_only:
         a.no_dfp = a.no_cpu = True
@@ -209,6 +215,105 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_ppr(args, pg, ctx, local):
+    """Batched personalized PageRank: R-MAT (scale, 16 edges/vertex), 64
+    teleport vectors with seed sets log-uniform in [1, 1000], tolerance 1e-9;
+    FP64 and FP32 with FP64 residuals."""
+    import numpy as np
+    import torch
+    t = time.perf_counter()
+    xoff, xedg = pg.graphs.rmat(args.ppr_scale, 16, seed=args.seed)
+    xt = pg.graphs.transpose(xoff, xedg)
+    n, m = len(xoff) - 1, len(xedg)
+    g = pg.Graph(ctx, *xt)
+    log(f"ppr graph: rmat{args.ppr_scale} n={n} m={m} in {time.perf_counter() - t:.1f}s")
+    rng = np.random.default_rng(args.seed)
+    sizes = np.clip(np.exp(rng.uniform(0, np.log(1000), 64)).astype(np.int64), 1, 1000)
+    seeds = [rng.integers(0, n, s) for s in sizes]
+    outs, runs = {}, {}
+    for name, prec in (("fp64", pg.FP64), ("fp32_refine", pg.FP32_REFINE)):
+        o = pg.options(tolerance=1e-9, precision=prec)
+        out = torch.empty(n * 64, dtype=torch.float64, device=f"cuda:{local}")
+        pg.solve_ppr_batched_device(ctx, g, seeds, out.data_ptr(), o)
+        res = [pg.solve_ppr_batched_device(ctx, g, seeds, out.data_ptr(), o) for _ in range(2)]
+        outs[name], runs[name] = out, res[-1]
+    f64, f32 = runs["fp64"], runs["fp32_refine"]
+    sweep64 = f64["time_ms"] / max(f64["fp64_sweeps"], 1)
+    est32 = (f32["time_ms"] - f32["fp64_sweeps"] * sweep64) / max(f32["fp32_sweeps"], 1)
+    # FP32 correction sweep bytes: per edge index 4 + 256-byte row + rcp 4; per
+    # vertex offsets 4 + rho, old and new correction rows 3 * 256
+    b32 = m * (4 + 256 + 4) + n * (4 + 3 * 256)
+    peak, peak_kind = measured_peak()
+    res = {"workload": f"rmat{args.ppr_scale}: {n} vertices, {m} edges, 64 teleport vectors, seed sets "
+                       "log-uniform in [1, 1000], tolerance 1e-9",
+           "fp64": f64, "fp32_refine": f32, "speedup_fp32_refine_vs_fp64": f64["time_ms"] / f32["time_ms"],
+           "linf_fp32_refine_vs_fp64": float((outs["fp64"] - outs["fp32_refine"]).abs().max()),
+           "vector_ge_s_fp64": 64 * m * f64["fp64_sweeps"] / (f64["time_ms"] / 1e3) / 1e9,
+           "fp64_sweep_ms": sweep64, "fp32_sweep_ms_est": est32,
+           "fp32_sweep_gbs_est": b32 / (est32 / 1e3) / 1e9 if est32 > 0 else None,
+           "fp32_sweep_frac_est": (b32 / (est32 / 1e3) / 1e9) / peak if est32 > 0 else None,
+           "peak_gbs": peak, "peak_source": peak_kind}
+    g.close()
+    return res
+
+
+def run_adjoint(args, pg, ctx, local):
+    """Weighted PageRank and its adjoint: R-MAT (scale, 16 edges/vertex), FP32
+    weights U[0.5, 2] row-normalised, alpha 0.85, loss g . r with g ~ N(0, 1);
+    dL/dw checked by central differences (h = 1e-6) of forward solves on
+    random edges (differences formed without cancellation, see
+    fd_weight_gradients); then again after dynamic batches of 1e-4|E|."""
+    import numpy as np
+    import torch
+    from pagerank_gb300 import autograd as A
+    dev = f"cuda:{local}"
+    xoff, xedg = pg.graphs.rmat(args.adjoint_scale, 16, seed=args.seed + 7)
+    rng = np.random.default_rng(args.seed + 7)
+    n = len(xoff) - 1
+    gl = torch.from_numpy(rng.standard_normal(n)).to(dev)
+    tight = pg.options(tolerance=1e-19, max_iterations=2000)
+    solve_o = pg.options(tolerance=1e-12, max_iterations=1000)
+    rounds = []
+    r_prev = None
+    g = None
+    for b in range(args.adjoint_batches + 1):
+        if b:
+            size = int(1e-4 * len(xedg))
+            du, dv, iu, iv = pg.graphs.random_batch(xoff, xedg, size // 5, size - size // 5, seed=args.seed + b)
+            g.apply_batch(du, dv, iu, iv)
+            xoff, xedg = pg.graphs.apply_batch(xoff, xedg, du, dv, iu, iv)
+        else:
+            xt = pg.graphs.transpose(xoff, xedg)
+            g = pg.Graph(ctx, *xt, xoff, xedg)
+        m = len(xedg)
+        w = rng.uniform(0.5, 2.0, m).astype(np.float32)
+        wd = torch.from_numpy(w).to(dev)
+        A.set_weights(ctx, g, wd)
+        r, rf = A.solve_weighted(ctx, g, None, r0=r_prev, opts=solve_o)
+        out = A.adjoint(ctx, g, r, gl, None, opts=solve_o)
+        ra = out["result"]
+        # finite differences against tightly converged forward solves
+        r_t, _ = A.solve_weighted(ctx, g, None, r0=r, opts=tight)
+        adj_t = A.adjoint(ctx, g, r_t, gl, None, opts=tight)["grad_w"].cpu().numpy()
+        k = args.adjoint_fd_edges if b == 0 else max(1, args.adjoint_fd_edges // 10)
+        edges = rng.choice(m, k, replace=False)
+        t0 = time.perf_counter()
+        fd = A.fd_weight_gradients(ctx, g, xoff, xedg, w, r_t, gl, edges)
+        ref = adj_t[edges]
+        rel = float(np.abs(fd - ref).max() / np.abs(ref).max())
+        rounds.append({"batch": b, "edges": m, "forward_ms": rf["time_ms"], "forward_iterations": rf["iterations"],
+                       "adjoint_ms": ra["time_ms"], "adjoint_iterations": ra["iterations"],
+                       "grad_alpha": out["grad_alpha"], "fd_edges": int(k), "fd_max_rel_err": rel,
+                       "fd_seconds": time.perf_counter() - t0})
+        log(f"adjoint round {b}: {rounds[-1]}")
+        r_prev = r
+    g.close()
+    return {"workload": f"rmat{args.adjoint_scale}: {n} vertices, FP32 weights U[0.5, 2] row-normalised, "
+                        "alpha 0.85, loss g . r with g ~ N(0, 1), tolerance 1e-12 (gradient reference 1e-19, FD differences 1e-24), "
+                        f"then {args.adjoint_batches} batches of 1e-4|E|",
+            "rounds": rounds, "fd_max_rel_err": max(x["fd_max_rel_err"] for x in rounds)}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -340,6 +445,12 @@ def run_ours(args):
                "dfp_linf_vs_static": err}
         log(f"dfp: {dfp}")
 
+    ppr = adj = None
+    if rank == 0 and not args.no_ppr and not args.static_only:
+        ppr = run_ppr(args, pg, ctx, local)
+        log(f"ppr: {ppr}")
+    if rank == 0 and not args.no_adjoint and not args.static_only:
+        adj = run_adjoint(args, pg, ctx, local)
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(args, xt, m)
@@ -355,7 +466,7 @@ def run_ours(args):
                "e2e": {"value": e2e_value, "unit": "GE/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "ms_per_step": e2e_ms_max},
                "roofline": roofline, "clocks": clk.summary(), "fp32_refine": fp32, "dfp": dfp,
-               "cpu_baseline": cpu}
+               "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     g.close()
     ctx.close()

@@ -65,6 +65,52 @@ def adjoint(ctx, g, r, grad_r, teleport=None, opts=None, want_lambda=False):
     return out
 
 
+def fd_weight_gradients(ctx, g, xoff, xedg, weights, r, grad_r, edges, h=1e-6, teleport=None, alpha=0.85,
+                        tolerance=1e-24, max_iterations=3000):
+    """Central finite differences of L = grad_r . r with respect to the weights
+    of the given out-CSR edges: (L(w + h e_j) - L(w - h e_j)) / (w+_j - w-_j),
+    with w+-_j rounded to FP32 as the library stores them.
+
+    The two differences L(w +- h e_j) - L(w) are formed without cancellation:
+    r+- - r solves (I - alpha P+-^T) d = alpha (P+- - P)^T r exactly, a system
+    whose right-hand side is non-zero only on the out-neighbours of the edge's
+    source, solved by the library's weighted solver with that right-hand side
+    as (1 - alpha) times its teleport vector.  r must be the converged ranks
+    for `weights` (tightly converged: its residual enters both differences).
+    Leaves `weights` attached to g.  Returns a float64 numpy array."""
+    import numpy as np
+    xoff = np.asarray(xoff, np.int64)
+    w = np.asarray(weights.detach().cpu().numpy() if isinstance(weights, torch.Tensor) else weights, np.float32)
+    dev = r.device
+    gl = _f64(grad_r)
+    n = len(xoff) - 1
+    o = options(damping=alpha, tolerance=tolerance, max_iterations=max_iterations)
+    out = []
+    for j in edges:
+        u = int(np.searchsorted(xoff, j, side="right") - 1)
+        s, e = xoff[u], xoff[u + 1]
+        nb = torch.from_numpy(np.asarray(xedg[s:e], np.int64)).to(dev)
+        row = w[s:e].astype(np.float64)
+        ru = float(r[u])
+        diffs = []
+        wj = []
+        for sign in (1.0, -1.0):
+            wq = w.copy()
+            wq[j] = np.float32(w[j] + np.float32(sign * h))
+            wj.append(float(wq[j]))
+            rq = row.copy()
+            rq[j - s] = float(wq[j])
+            b = alpha * ru * (rq / rq.sum() - row / row.sum())     # alpha (Pq - P)^T r, rows of u only
+            t = torch.zeros(n, dtype=torch.float64, device=dev)
+            t.index_add_(0, nb, torch.from_numpy(b / (1 - alpha)).to(dev))
+            set_weights(ctx, g, torch.from_numpy(wq).to(dev))
+            d, _ = solve_weighted(ctx, g, t, opts=o)
+            diffs.append(float((gl * d).sum()))
+        out.append((diffs[0] - diffs[1]) / (wj[0] - wj[1]))
+    set_weights(ctx, g, torch.from_numpy(w).to(dev))
+    return np.array(out)
+
+
 class WeightedPageRank(torch.autograd.Function):
     """r = WeightedPageRank.apply(weights, teleport, alpha, ctx, graph, tolerance, max_iterations).
 
@@ -102,4 +148,5 @@ def weighted_pagerank(pctx, graph, weights, teleport=None, alpha=0.85, tolerance
     return WeightedPageRank.apply(weights, teleport, alpha, pctx, graph, tolerance, max_iterations)
 
 
-__all__ = ["set_weights", "solve_weighted", "adjoint", "WeightedPageRank", "weighted_pagerank"]
+__all__ = ["set_weights", "solve_weighted", "adjoint", "fd_weight_gradients", "WeightedPageRank",
+           "weighted_pagerank"]
