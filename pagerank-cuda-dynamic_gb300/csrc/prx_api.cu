@@ -307,24 +307,8 @@ static int run_refine_loop(prx_context* c, const prx_graph* gr, const SolveArgs&
                            const ChunkLayout* lay64, const ChunkLayout* lay32, int* final_parity) {
   cudaStream_t s = c->stream;
   int st;
-  for (;;) {
-    for (int cls = 0; cls < NCLS; ++cls) {
-      st = launch_update_timed(c, timing, cls,
-                               [&] { return launch_refine_sweep64(a, gr->g, cls, lay64, c->sms, s); });
-      if (st) return st;
-    }
-    launch_refine_finalize64(a, s);
-    c->launches += 1;
-    TRY_CUDA_ST(cudaGetLastError());
-    TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
-    TRY_CUDA_ST(cudaStreamSynchronize(s));
-    if (timing && (st = drain_timing(c))) return st;
-    if (c->st_host[1].done) {
-      // converged (or capped) at this FP64 sweep; with max_iterations <= 0
-      // no sweep ran and the initial ranks in r[0] are the answer
-      *final_parity = c->st_host[1].iter > 0 ? 1 : 0;
-      return PRX_OK;
-    }
+  // one round of FP32 correction sweeps until they stop, then x_b += e
+  auto fp32_round = [&]() -> int {
     for (int k = 1;; k = std::min(2 * k, 16)) {
       for (int i = 0; i < k; ++i) {
         for (int cls = 0; cls < NCLS; ++cls) {
@@ -343,6 +327,40 @@ static int run_refine_loop(prx_context* c, const prx_graph* gr, const SolveArgs&
     }
     launch_refine_commit(a, c->sms, s);
     c->launches += 1;
+    return PRX_OK;
+  };
+  if (max_iter <= 0) {
+    TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
+    TRY_CUDA_ST(cudaStreamSynchronize(s));
+    *final_parity = 0;  // no sweep: the initial ranks
+    return PRX_OK;
+  }
+  // round 0: FP32 sweeps of the ranks themselves from the initial ranks
+  launch_refine_round0(a, c->sms, s);
+  c->launches += 1;
+  if ((st = fp32_round())) return st;
+  if (c->st_host[1].iter >= max_iter) {
+    TRY_CUDA_ST(cudaStreamSynchronize(s));
+    *final_parity = 0;
+    return PRX_OK;
+  }
+  for (;;) {
+    for (int cls = 0; cls < NCLS; ++cls) {
+      st = launch_update_timed(c, timing, cls,
+                               [&] { return launch_refine_sweep64(a, gr->g, cls, lay64, c->sms, s); });
+      if (st) return st;
+    }
+    launch_refine_finalize64(a, s);
+    c->launches += 1;
+    TRY_CUDA_ST(cudaGetLastError());
+    TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
+    TRY_CUDA_ST(cudaStreamSynchronize(s));
+    if (timing && (st = drain_timing(c))) return st;
+    if (c->st_host[1].done) {  // converged (or capped) at this FP64 sweep: its output
+      *final_parity = 1;
+      return PRX_OK;
+    }
+    if ((st = fp32_round())) return st;
     if (c->st_host[1].iter >= max_iter) {
       TRY_CUDA_ST(cudaStreamSynchronize(s));
       *final_parity = 0;

@@ -156,6 +156,8 @@ bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, const ChunkL
 void launch_finalize32(const SolveArgs& a, cudaStream_t s);
 // x_b += e; c_b = x_b / outdeg.
 void launch_refine_commit(const SolveArgs& a, int sms, cudaStream_t s);
+// Round 0 of FP32 sweeps on the initial ranks in r[0] (x_b = 0, rho = C0).
+void launch_refine_round0(const SolveArgs& a, int sms, cudaStream_t s);
 
 // DF / DF-P expansion after an iteration's updates: push from the changed
 // vertices or pull into the unmarked ones, chosen on the device.

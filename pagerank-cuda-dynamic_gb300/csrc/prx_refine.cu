@@ -2,13 +2,18 @@
 //
 // Defect correction around the reference's Jacobi iteration
 // (pagerankLoopCuU, inc/pagerankCuda.hxx:675-692):
+//   0. FP32 sweeps of the ranks themselves from the initial ranks (a round
+//      with x_b = 0, rho = C0 and e_0 = the initial ranks), committed as the
+//      first base x_b; no FP64 sweep is spent on the far-from-converged start.
 //   1. FP64 sweep from the base ranks x_b (the reference's update, its order
 //      and fma; update kernels in MODE_REFINE64): a = C0 + P*A*(x_b/d), and
 //      rho = a - x_b.  Its L-inf is the reference's convergence test; when
 //      it is below tol, a is the answer.
 //   2. FP32 sweeps of the correction: e_1 = rho, e_{k+1} = rho + P*A*(e_k/d).
 //      x_b + e_k is the k-th Jacobi iterate from x_b, so the FP32 loop stops on
-//      the same criterion, |e_{k+1} - e_k|_inf < tol.  Contributions e/d are
+//      the same criterion, |e_{k+1} - e_k|_inf < tol, or once the change is
+//      below 2^-18 of |e|_inf (row sums of up to 64 FP32 terms cannot resolve
+//      more; the next FP64 residual takes over).  Contributions e/d are
 //      stored and gathered in FP32 (4 bytes per edge instead of 8) and
 //      accumulated in FP32.
 //   3. x_b += e in FP64, back to 1.
@@ -19,12 +24,21 @@ namespace prx {
 
 __device__ __forceinline__ unsigned int fbits(float x) { return __float_as_uint(x); }
 
-__device__ __forceinline__ unsigned int finish32(const SolveArgs& a, uint32_t v, float sum, int q) {
+// New correction of v; returns |change| and raises *mag to |e| (bits).
+__device__ __forceinline__ unsigned int finish32(const SolveArgs& a, uint32_t v, float sum, int q, unsigned int* mag) {
   const float en = fmaf((float)a.P, sum, a.rho[v]);
   const float dl = fabsf(en - a.e[q][v]);
   a.e[q ^ 1][v] = en;
   a.ce[q ^ 1][v] = __fdividef(en, (float)a.xtdat[v]);
+  *mag = max(*mag, fbits(fabsf(en)));
   return fbits(dl);
+}
+
+// The L-inf change and correction size of a sweep (every thread calls it).
+__device__ __forceinline__ void reduce32(State* st, unsigned int dl, unsigned int mag) {
+  const int q = st->k32 & 1;
+  block_max_u32(dl, &st->el32_bits[q]);
+  block_max_u32(mag, &st->e32max_bits[q]);
 }
 
 // LOW: one warp per 32 consecutive ids, one lane per vertex, one launch per
@@ -37,17 +51,17 @@ __global__ void __launch_bounds__(kThreads) k32_low(SolveArgs a, const uint32_t*
   const int q = st->k32 & 1;
   const float* __restrict__ ce = a.ce[q];
   const uint32_t words = (a.n + 31) >> 5;
-  unsigned int emax = 0;
+  unsigned int emax = 0, mag = 0;
   for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t v = (w << 5) | lane_id();
     if (v >= a.n || !((a.low_bm[w] >> lane_id()) & 1u)) continue;
     const uint32_t s = off[v], e = off[v + 1];
     if (!FIRST && !LAST && s == e) continue;
     const float acc = lane_row_sum(ce, edg, s, e, FIRST ? 0.f : a.acc32[v]);
-    if (LAST) emax = max(emax, finish32(a, v, acc, q));
+    if (LAST) emax = max(emax, finish32(a, v, acc, q, &mag));
     else a.acc32[v] = acc;
   }
-  if (LAST) block_max_u32(emax, &st->el32_bits[st->k32 & 1]);
+  if (LAST) reduce32(st, emax, mag);
 }
 
 // MID: warp per vertex, lane-strided sums folded by shuffles.
@@ -57,7 +71,7 @@ __global__ void __launch_bounds__(kThreads) k32_mid(SolveArgs a, uint32_t begin,
   const int q = st->k32 & 1;
   const float* __restrict__ ce = a.ce[q];
   const uint32_t lane = lane_id();
-  unsigned int emax = 0;
+  unsigned int emax = 0, mag = 0;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t v = a.cls_list[begin + i];
     const uint32_t s = a.xtoff[v], d = a.xtoff[v + 1] - s;
@@ -66,9 +80,9 @@ __global__ void __launch_bounds__(kThreads) k32_mid(SolveArgs a, uint32_t begin,
     for (uint32_t t = lane; t < d; t += 32) acc += __ldg(ce + __ldg(ed + t));
 #pragma unroll
     for (int o = 16; o; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) emax = max(emax, finish32(a, v, acc, q));
+    if (lane == 0) emax = max(emax, finish32(a, v, acc, q, &mag));
   }
-  block_max_u32(emax, &st->el32_bits[st->k32 & 1]);
+  reduce32(st, emax, mag);
 }
 
 // HIGH: block per vertex.
@@ -78,7 +92,7 @@ __global__ void __launch_bounds__(256) k32_high(SolveArgs a, uint32_t begin, uin
   if (st->done || st->inner_done) return;
   const int q = st->k32 & 1;
   const float* __restrict__ ce = a.ce[q];
-  unsigned int emax = 0;
+  unsigned int emax = 0, mag = 0;
   for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
     const uint32_t v = a.cls_list[begin + i];
     const uint32_t s = a.xtoff[v], d = a.xtoff[v + 1] - s;
@@ -93,11 +107,11 @@ __global__ void __launch_bounds__(256) k32_high(SolveArgs a, uint32_t begin, uin
       float x = threadIdx.x < 8 ? part[threadIdx.x] : 0.f;
 #pragma unroll
       for (int o = 4; o; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-      if (threadIdx.x == 0) emax = max(emax, finish32(a, v, x, q));
+      if (threadIdx.x == 0) emax = max(emax, finish32(a, v, x, q, &mag));
     }
     __syncthreads();
   }
-  block_max_u32(emax, &st->el32_bits[st->k32 & 1]);
+  reduce32(st, emax, mag);
 }
 
 // After the FP64 sweep: its L-inf decides (:689); otherwise start a round of
@@ -118,16 +132,38 @@ __global__ void k_refine_finalize64(State* st) {
   st->k32 = 0;
   st->inner_done = 0;
   st->el32_bits[0] = st->el32_bits[1] = 0;
+  st->e32max_bits[0] = st->e32max_bits[1] = 0;
 }
 
 __global__ void k_finalize32(State* st) {
   if (st->done || st->inner_done) return;
   const int q = st->k32 & 1;
   const float dl = __uint_as_float(st->el32_bits[q]);
+  const float em = __uint_as_float(st->e32max_bits[q]);
   st->iter += 1;
   st->k32 += 1;
   st->el32_bits[q ^ 1] = 0;
-  if (dl < (float)st->tol || st->iter >= st->max_iter) st->inner_done = 1;
+  st->e32max_bits[q ^ 1] = 0;
+  if (dl < (float)st->tol || dl < em * 0x1p-18f || st->iter >= st->max_iter) st->inner_done = 1;
+}
+
+// Round 0: x_b = 0, rho = C0, e_0 = the initial ranks (FP32), ce_0 = e_0 / d.
+__global__ void k_refine_round0(SolveArgs a) {
+  const float c0 = (float)a.C0;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
+    const float x = (float)a.r[0][v];
+    a.r[0][v] = 0.0;
+    a.rho[v] = c0;
+    a.e[0][v] = x;
+    a.ce[0][v] = __fdividef(x, (float)a.xtdat[v]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    State* st = a.st;
+    st->k32 = 0;
+    st->inner_done = st->done;
+    st->el32_bits[0] = st->el32_bits[1] = 0;
+    st->e32max_bits[0] = st->e32max_bits[1] = 0;
+  }
 }
 
 // x_b += e (FP64), c_b = x_b / outdeg.
@@ -170,6 +206,10 @@ bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, const ChunkL
 void launch_refine_finalize64(const SolveArgs& a, cudaStream_t s) { k_refine_finalize64<<<1, 1, 0, s>>>(a.st); }
 
 void launch_finalize32(const SolveArgs& a, cudaStream_t s) { k_finalize32<<<1, 1, 0, s>>>(a.st); }
+
+void launch_refine_round0(const SolveArgs& a, int sms, cudaStream_t s) {
+  k_refine_round0<<<cap_grid32((a.n + kThreads - 1) / kThreads, sms * 16), kThreads, 0, s>>>(a);
+}
 
 void launch_refine_commit(const SolveArgs& a, int sms, cudaStream_t s) {
   k_refine_commit<<<cap_grid32((a.n + kThreads - 1) / kThreads, sms * 16), kThreads, 0, s>>>(a);
