@@ -164,11 +164,19 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def chunk_passes(args, n, default_width=(200 << 20) // 8):
+    """Launches of the LOW-class FP64 kernel per sweep: one per source chunk
+    (the library's default chunk holds 200 MB of FP64 contributions)."""
+    w = args.chunk or default_width
+    return -(-n // w) if w < n else 1
+
+
 def ncu_traffic(kernel, workload):
-    """DRAM bytes per launch from the committed ncu summary, if any."""
+    """DRAM bytes per sweep (the source-chunk launches of one sweep together,
+    the unit of roofline.achieved) from the committed ncu summary, if any."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     try:
-        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+        m = re.search(r"traffic_bytes_per_sweep:\s*([0-9.eE+]+)", open(path).read())
         return float(m.group(1)) if m else None
     except OSError:
         return None
@@ -362,7 +370,7 @@ def run_ours(args):
     roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": ncu_traffic(names[dom], "weblike50m"), "alg_bytes_per_sweep": bytes_per_sweep,
-                "sweep_ms": sweep_ms, "launches_per_sweep": upd_n[dom] / max(sweeps, 1),
+                "sweep_ms": sweep_ms, "launches_per_sweep": chunk_passes(args, n) if dom == 0 else 1,
                 "share_of_step": upd_ms[dom] / ms}
     # all three update kernels together, same byte model
     all_bytes = sum((20 * cls_v[c] + 12 * cls_e[c]) * sweeps for c in range(3) if upd_n[c])
