@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--static-only", action="store_true", help="upload only the in-CSR; skip DF-P and the CPU leg")
     p.add_argument("--chunk", type=int, default=0, help="source-chunk width of the gathers (0: library default)")
+    p.add_argument("--no-grid", action="store_true", help="skip the high-diameter grid workload")
+    p.add_argument("--grid-side", type=int, default=4096)
     p.add_argument("--no-ppr", action="store_true", help="skip the batched personalized PageRank workload")
     p.add_argument("--ppr-scale", type=int, default=22)
     p.add_argument("--no-adjoint", action="store_true", help="skip the weighted PageRank adjoint workload")
@@ -221,6 +223,45 @@ def run_reference(args):
                                       f"{threads} OpenMP threads"},
            "e2e": {"value": v, "unit": "GE/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def run_grid(args, pg, ctx, local):
+    """High-diameter road-like graph: side x side grid, 4-neighbour edges both
+    ways, 5% random diagonal shortcuts, self-loops; Static, then one batch of
+    1e-4|E| applied on the device and DT / DF / DF-P from the Static ranks."""
+    import numpy as np
+    import torch
+    dev = f"cuda:{local}"
+    t = time.perf_counter()
+    xoff, xedg = pg.graphs.grid(args.grid_side, 0.05, seed=args.seed)
+    xt = pg.graphs.transpose(xoff, xedg)
+    n, m = len(xoff) - 1, len(xedg)
+    g = pg.Graph(ctx, *xt, xoff, xedg)
+    log(f"grid graph: {args.grid_side}^2 n={n} m={m} in {time.perf_counter() - t:.1f}s")
+    ranks = torch.empty(n, dtype=torch.float64, device=dev)
+    pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr())
+    st0 = pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr())
+    q = ranks.clone()
+    size = int(1e-4 * m)
+    du, dv, iu, iv = pg.graphs.random_batch(xoff, xedg, size // 5, size - size // 5, seed=args.seed + 3)
+    g.apply_batch(du, dv, iu, iv)
+    bt = [torch.from_numpy(np.asarray(a, dtype=np.uint32).view(np.int32)).to(dev) for a in (du, dv, iu, iv)]
+    bp = (bt[0].data_ptr(), bt[1].data_ptr(), len(du), bt[2].data_ptr(), bt[3].data_ptr(), len(iu))
+    out = torch.empty_like(q)
+    res = {}
+    st1 = pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr())
+    for name, mode in (("dt", pg.DYNAMIC_TRAVERSAL), ("df", pg.DYNAMIC_FRONTIER), ("dfp", pg.PRUNE_DYNAMIC_FRONTIER)):
+        pg.solve_device(ctx, g, mode, q.data_ptr(), out.data_ptr(), bp)
+        r = pg.solve_device(ctx, g, mode, q.data_ptr(), out.data_ptr(), bp)
+        res[name] = {"ms": r["time_ms"], "iterations": r["iterations"], "marking_ms": r["marking_time_ms"],
+                     "affected_initial": r["affected_initial"], "speedup_vs_static": st1["time_ms"] / r["time_ms"],
+                     "linf_vs_static": float((out - ranks).abs().max())}
+    g.close()
+    return {"workload": f"grid {args.grid_side}^2: {n} vertices, {m} edges (4-neighbour both ways, 5% diagonal "
+                        "shortcuts, self-loops), batch 1e-4|E| (80% insertions)",
+            "static_ms": st0["time_ms"], "static_iterations": st0["iterations"],
+            "static_ge_s": m * st0["iterations"] / (st0["time_ms"] / 1e3) / 1e9,
+            "static_after_batch_ms": st1["time_ms"], **res}
 
 
 def run_ppr(args, pg, ctx, local):
@@ -453,7 +494,10 @@ def run_ours(args):
                "dfp_linf_vs_static": err}
         log(f"dfp: {dfp}")
 
-    ppr = adj = None
+    ppr = adj = grid = None
+    if rank == 0 and not args.no_grid and not args.static_only:
+        grid = run_grid(args, pg, ctx, local)
+        log(f"grid: {grid}")
     if rank == 0 and not args.no_ppr and not args.static_only:
         ppr = run_ppr(args, pg, ctx, local)
         log(f"ppr: {ppr}")
@@ -474,7 +518,7 @@ def run_ours(args):
                "e2e": {"value": e2e_value, "unit": "GE/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "ms_per_step": e2e_ms_max},
                "roofline": roofline, "clocks": clk.summary(), "fp32_refine": fp32, "dfp": dfp,
-               "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
+               "grid": grid, "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     g.close()
     ctx.close()

@@ -82,9 +82,9 @@ static void free_ws(prx_context* c) {
   for (int p = 0; p < 2; ++p) {
     cudaFree(c->r[p]); c->r[p] = nullptr;
     cudaFree(c->c[p]); c->c[p] = nullptr;
-    cudaFree(c->fr[p]); c->fr[p] = nullptr;
     for (int k = 0; k < NCLS; ++k) { cudaFree(c->lists[p][k]); c->lists[p][k] = nullptr; }
   }
+  for (auto& f : c->fr) { cudaFree(f); f = nullptr; }
   cudaFree(c->acc64); c->acc64 = nullptr;
   cudaFree(c->acc32); c->acc32 = nullptr;
   cudaFree(c->flags); c->flags = nullptr;
@@ -142,7 +142,7 @@ static int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
     TRY_CUDA_ST(cudaMalloc(&c->xb, sizeof(uint32_t) * cap));
     TRY_CUDA_ST(cudaMalloc(&c->naff, sizeof(uint32_t) * words));
     TRY_CUDA_ST(cudaMalloc(&c->xl, sizeof(uint32_t) * cap));
-    for (int p = 0; p < 2; ++p) TRY_CUDA_ST(cudaMalloc(&c->fr[p], sizeof(uint32_t) * cap));
+    for (auto& f : c->fr) TRY_CUDA_ST(cudaMalloc(&f, sizeof(uint32_t) * cap));
     for (int k = MID; k < NCLS; ++k) TRY_CUDA_ST(cudaMalloc(&c->lists[0][k], sizeof(uint32_t) * cap));
   }
   c->ws_n = cap;
@@ -184,10 +184,10 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
   a.xoff = g.xoff; a.xedg = g.xedg;
   a.xtoff = g.xtoff; a.xtedg = g.xtedg; a.xtdat = g.xtdat;
   a.cls_list = g.cls_list;
+  for (int k = 0; k < 3; ++k) a.fr[k] = c->fr[k];
   for (int p = 0; p < 2; ++p) {
     a.r[p] = c->r[p];
     a.c[p] = c->c[p];
-    a.fr[p] = c->fr[p];
     for (int k = 0; k < NCLS; ++k) a.list[p][k] = c->lists[p][k];
   }
   for (int k = 0; k < 3; ++k) a.bm[k] = c->bm[k];
@@ -228,16 +228,20 @@ static int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint3
   c->launches += 3;
   TRY_CUDA_ST(cudaMemsetAsync(&c->st->xbcnt, 0, sizeof(uint32_t), s));
   if (mode == PRX_DYNAMIC_TRAVERSAL) {
+    // Closure by BFS levels, all enqueued without a host round trip per
+    // level: a level whose frontier is empty returns at once, so levels go
+    // out in batches of 1, 2, 4, ..., 1024 and the host reads the frontier
+    // length once per batch (a graph of diameter 8k needs ~15 reads).
     launch_frontier_from_bitmap(a, c->sms, s);
     c->launches += 1;
-    for (int cur = 0;; cur ^= 1) {
-      TRY_CUDA_ST(cudaMemsetAsync(&c->st->fcnt[cur ^ 1], 0, sizeof(uint32_t), s));
-      launch_expand_frontier(a, cur, c->sms, s);
-      c->launches += 1;
-      TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1].fcnt[cur ^ 1], &c->st->fcnt[cur ^ 1], sizeof(uint32_t),
+    uint32_t level = 0;
+    for (uint32_t k = 1;; k = std::min<uint32_t>(2 * k, 1024)) {
+      for (uint32_t i = 0; i < k; ++i) launch_expand_level(a, level++, c->sms, s);
+      c->launches += k;
+      TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1].fcnt[level % 3], &c->st->fcnt[level % 3], sizeof(uint32_t),
                                   cudaMemcpyDeviceToHost, s));
       TRY_CUDA_ST(cudaStreamSynchronize(s));
-      if (c->st_host[1].fcnt[cur ^ 1] == 0) break;
+      if (c->st_host[1].fcnt[level % 3] == 0) break;
     }
   }
   TRY_CUDA_ST(cudaMemsetAsync(&c->st->xcnt, 0, sizeof(uint32_t), s));

@@ -33,7 +33,7 @@ struct prx_context {
   uint32_t* naff = nullptr;
   uint32_t* lists[2][NCLS] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   uint32_t* xl = nullptr;
-  uint32_t* fr[2] = {nullptr, nullptr};
+  uint32_t* fr[3] = {nullptr, nullptr, nullptr};
   // FP32 refinement (grown on first use)
   uint32_t ws32_n = 0;
   float* rho = nullptr;

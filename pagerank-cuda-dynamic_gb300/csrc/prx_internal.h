@@ -37,7 +37,7 @@ struct State {
   double last_delta;
   uint32_t cnt[2][NCLS];          // dynamic: queued MID / HIGH vertices (cnt[0][MID], cnt[0][HIGH])
   uint32_t xcnt;                  // vertices whose out-neighbours must be marked
-  uint32_t fcnt[2];               // DT closure frontier lengths
+  uint32_t fcnt[3];               // DT closure frontier lengths, rotating over levels
   uint32_t err;                   // device-detected error code, 0 = none
   unsigned long long edges;       // in-edges gathered (statistic)
   unsigned long long affected;    // vertices marked before the first iteration
@@ -122,7 +122,7 @@ struct SolveArgs {
   uint32_t* xl;                   // marking: queued sources
   uint32_t* xb;                   // high out-degree vertices to expand block-wide
   uint32_t* nf[2];                // DF / DF-P: bitmap of vertices whose change exceeded D, by parity
-  uint32_t* fr[2];                // DT closure frontiers
+  uint32_t* fr[3];                // DT closure frontiers: level L reads fr[L % 3], fills fr[(L+1) % 3]
   float* rho;                     // FP32 refinement: residual of the base ranks
   float* e[2];                    // FP32 refinement: correction, ping-pong
   float* ce[2];                   // FP32 refinement: correction / outdeg, ping-pong
@@ -171,7 +171,8 @@ void launch_mark_seed(const SolveArgs& a, const uint32_t* delu, const uint32_t* 
                       const uint32_t* insu, uint64_t ni, int sms, cudaStream_t s);
 void launch_expand_seeds(const SolveArgs& a, int sms, cudaStream_t s);
 void launch_frontier_from_bitmap(const SolveArgs& a, int sms, cudaStream_t s);
-void launch_expand_frontier(const SolveArgs& a, int cur, int sms, cudaStream_t s);
+// One DT closure level (no-op once the frontier is empty).
+void launch_expand_level(const SolveArgs& a, uint32_t level, int sms, cudaStream_t s);
 void launch_popcount(const uint32_t* bm, uint32_t n, unsigned long long* out, int sms, cudaStream_t s);
 void launch_flags_from_bitmap(const uint32_t* bm, uint8_t* out, uint32_t n, cudaStream_t s);
 void launch_state_reset(State* st, int max_iter, double tol, cudaStream_t s);

@@ -63,17 +63,21 @@ __global__ void __launch_bounds__(kThreads) k_frontier_from_bitmap(SolveArgs a) 
   }
 }
 
-// One closure level: newly reached vertices go to bitmap 0 and frontier cur^1.
-__global__ void __launch_bounds__(kThreads) k_expand_frontier(SolveArgs a, int cur) {
+// Closure level L: the out-neighbours of frontier L % 3 not yet reached go to
+// bitmap 0 and frontier (L+1) % 3.  The counter of frontier (L+2) % 3 -- the
+// one level L+1 fills -- is zeroed here: level L-1 was its last reader.
+__global__ void __launch_bounds__(kThreads) k_expand_level(SolveArgs a, uint32_t level) {
   State* st = a.st;
+  const uint32_t cur = level % 3, nxt = (level + 1) % 3, clr = (level + 2) % 3;
   const uint32_t count = st->fcnt[cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->fcnt[clr] = 0;
   const uint32_t lane = lane_id();
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t u = a.fr[cur][i];
     const uint32_t e = a.xoff[u + 1];
     for (uint32_t j = a.xoff[u] + lane; j < e; j += 32) {
       const uint32_t w = a.xedg[j];
-      if (test_and_set(a.bm[0], w)) push(a.fr[cur ^ 1], &st->fcnt[cur ^ 1], w);
+      if (test_and_set(a.bm[0], w)) push(a.fr[nxt], &st->fcnt[nxt], w);
     }
   }
 }
@@ -99,7 +103,7 @@ __global__ void k_state_reset(State* st, int max_iter, double tol) {
   for (int p = 0; p < 2; ++p)
     for (int c = 0; c < NCLS; ++c) st->cnt[p][c] = 0;
   st->xcnt = 0;
-  st->fcnt[0] = st->fcnt[1] = 0;
+  st->fcnt[0] = st->fcnt[1] = st->fcnt[2] = 0;
   st->err = 0;
   st->edges = 0;
   st->affected = 0;
@@ -128,8 +132,8 @@ void launch_frontier_from_bitmap(const SolveArgs& a, int sms, cudaStream_t s) {
   k_frontier_from_bitmap<<<sms * 4, kThreads, 0, s>>>(a);
 }
 
-void launch_expand_frontier(const SolveArgs& a, int cur, int sms, cudaStream_t s) {
-  k_expand_frontier<<<sms * 4, kThreads, 0, s>>>(a, cur);
+void launch_expand_level(const SolveArgs& a, uint32_t level, int sms, cudaStream_t s) {
+  k_expand_level<<<sms * 4, kThreads, 0, s>>>(a, level);
 }
 
 void launch_popcount(const uint32_t* bm, uint32_t n, unsigned long long* out, int sms, cudaStream_t s) {
