@@ -61,7 +61,9 @@ typedef enum {
 } prx_precision;
 
 typedef enum {
-  PRX_LOOP_AUTO = 0,    /* CUDA graph with a device-side while loop if possible */
+  PRX_LOOP_AUTO = 0,    /* CUDA graph with a device-side while loop if possible:
+                           Static / ND / DT / DF / DF-P without per-launch
+                           timing; otherwise the host-driven loop           */
   PRX_LOOP_HOST = 1,    /* host-driven loop, convergence read back in batches   */
   PRX_LOOP_GRAPH = 2    /* CUDA graph with a conditional while node             */
 } prx_loop;

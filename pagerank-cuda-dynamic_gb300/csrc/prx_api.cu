@@ -304,6 +304,65 @@ static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArg
   return PRX_OK;
 }
 
+// ---- the iteration loop as one CUDA graph ----------------------------------
+// A conditional WHILE node whose body is one iteration (the update launches,
+// the expansion and k_finalize) followed by k_loop_cond, which keeps the loop
+// going while the solve is not done.  k_loop_cond counts the bodies itself
+// and stops after `cap` of them whatever the other kernels did, so the loop
+// ends even if k_finalize never ran: at most max_iterations + 1 bodies run.
+__global__ void k_loop_cond(cudaGraphConditionalHandle h, State* st, int cap) {
+  const int rounds = ++st->graph_rounds;
+  cudaGraphSetConditional(h, (!st->done && rounds < cap) ? 1u : 0u);
+}
+
+static int run_graph_loop(prx_context* c, const prx_graph* gr, const SolveArgs& a, int mode, const ChunkLayout* lay,
+                          int max_iter) {
+  cudaStream_t s = c->stream;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int st = PRX_OK;
+  auto fail = [&](cudaError_t e, const char* what) {
+    set_error(std::string("prx_solve (graph loop): ") + what + ": " + cudaGetErrorString(e));
+    st = e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
+  };
+  cudaError_t e = cudaGraphCreate(&graph, 0);
+  cudaGraphConditionalHandle h{};
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+  cudaGraphNodeParams p{};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (e == cudaSuccess) e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &p);
+  const uint64_t l0 = c->launches;
+  uint64_t per_body = 0;
+  if (e == cudaSuccess) {
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      const int st_enq = enqueue_iteration(c, gr, a, mode, false, lay);
+      const int cap = (max_iter < (1 << 30) ? max_iter : (1 << 30)) + 2;
+      k_loop_cond<<<1, 1, 0, s>>>(h, a.st, cap);
+      per_body = c->launches - l0 + 1;
+      const cudaError_t e_launch = cudaGetLastError();
+      cudaGraph_t captured = nullptr;
+      e = cudaStreamEndCapture(s, &captured);  // always leave capture mode
+      if (st_enq) st = st_enq;
+      if (e == cudaSuccess) e = e_launch;
+    }
+  }
+  if (e == cudaSuccess && !st) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e == cudaSuccess && !st) e = cudaGraphLaunch(exec, s);
+  if (e == cudaSuccess && !st) e = cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && !st) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess && !st) fail(e, "build or launch");
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  c->launches = l0 + per_body * (uint64_t)(st ? 0 : c->st_host[1].graph_rounds);
+  return st;
+}
+
 // FP32 refinement loop (prx_refine.cu).  *final_parity: 1 when the last FP64
 // sweep converged (its output in r[1]), 0 when the cap stopped an FP32 round
 // (the committed ranks in r[0]).
@@ -420,6 +479,8 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
     TRY_CUDA_ST(cudaEventRecord(c->ev[2], s));
     if (refine) {
       if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity))) return st;
+    } else if (o.loop != PRX_LOOP_HOST && !timing) {
+      if ((st = run_graph_loop(c, gr, a, mode, lay64, o.max_iterations))) return st;
     } else {
       for (int k = 1;; k = std::min(2 * k, 16)) {
         for (int i = 0; i < k; ++i) {

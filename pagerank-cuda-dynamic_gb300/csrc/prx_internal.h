@@ -49,6 +49,7 @@ struct State {
   int rounds;                     // FP64 residual sweeps run
   unsigned int el32_bits[2];      // L-inf change of the FP32 sweep with parity k32 & 1 (bits of a float >= 0)
   unsigned int e32max_bits[2];    // L-inf of the correction it produced (personalized PageRank)
+  int graph_rounds;               // bodies run by the CUDA-graph loop (its own bound)
 };
 
 // Internal mode of the update kernels: the FP64 residual sweep of the FP32

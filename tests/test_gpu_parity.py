@@ -164,6 +164,29 @@ def test_chunked_gathers_bit_exact(pg, ctx, kind, width):
     g.close()
 
 
+@pytest.mark.parametrize("kind", ["web200k", "hubs"])
+def test_host_and_graph_loops_agree(pg, ctx, kind):
+    # the iteration loop as one CUDA graph (conditional while node) and the
+    # host-driven loop give the oracle's ranks and iteration counts, also
+    # under small iteration caps
+    xoff, xedg = _synthetic(pg, kind)
+    m = len(xedg)
+    batch = pg.graphs.random_batch(xoff, xedg, max(1, int(2e-4 * m)), max(1, int(8e-4 * m)), seed=23)
+    xt = O.transpose(xoff, xedg)
+    q, _ = O.solve("static", None, None, *xt)
+    yoff, yedg = pg.graphs.apply_batch(xoff, xedg, *batch)
+    yt = O.transpose(yoff, yedg)
+    g, _ = _graph(pg, ctx, yoff, yedg, yt)
+    for cap in (500, 0, 1, 3):
+        for mode in MODES:
+            want, it_w = _oracle(mode, yoff, yedg, yt, batch, q, O.options(max_iterations=cap))
+            for loop in (pg.LOOP_HOST, pg.LOOP_GRAPH):
+                got, res = _gpu(pg, ctx, g, mode, batch, q, pg.options(loop=loop, max_iterations=cap))
+                assert res["iterations"] == it_w, (kind, mode, cap, loop)
+                np.testing.assert_array_equal(got, want, err_msg=f"{kind} {mode} cap={cap} loop={loop}")
+    g.close()
+
+
 def test_graph_outlives_context(pg):
     # destroying a context first must leave its graphs destroyable
     c = pg.Context(0)
