@@ -376,7 +376,11 @@ def run_ours(args):
     g = pg.Graph(ctx, *xt) if args.static_only else pg.Graph(ctx, *xt, xoff, xedg)
     cls_v, cls_e = g.class_stats()
     ranks = torch.empty(n, dtype=torch.float64, device=f"cuda:{local}")
-    opts = pg.options(timing=1, chunk_vertices=args.chunk)
+    # the timed solves run as the library runs by default (the iteration loop
+    # as one CUDA graph); the per-launch timing of the roofline comes from
+    # separate solves with timing on (host-driven loop, same kernels)
+    opts = pg.options(chunk_vertices=args.chunk)
+    topts = pg.options(timing=1, chunk_vertices=args.chunk)
     log(f"classes: vertices {cls_v} edges {cls_e}")
     for _ in range(args.warmup):
         pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr(), opts=opts)
@@ -399,9 +403,11 @@ def run_ours(args):
     # previous + new rank 16 per vertex; index 4 + gathered contribution 8 per edge)
     # Each iteration sweeps every class once; the LOW class may take several
     # launches per sweep (one per source chunk), so time per sweep.
-    upd_ms = [sum(r["update_ms"][c] for r in results) for c in range(3)]
-    upd_n = [sum(r["update_launches"][c] for r in results) for c in range(3)]
-    sweeps = sum(iters)
+    timed = [pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr(), opts=topts) for _ in range(args.steps)]
+    upd_ms = [sum(r["update_ms"][c] for r in timed) for c in range(3)]
+    upd_n = [sum(r["update_launches"][c] for r in timed) for c in range(3)]
+    sweeps = sum(r["iterations"] for r in timed)
+    timed_ms = sum(r["time_ms"] for r in timed)
     dom = max(range(3), key=lambda c: upd_ms[c])
     names = ("k_update_low", "k_update_mid", "k_update_high")
     bytes_per_sweep = 20 * cls_v[dom] + 12 * cls_e[dom]
@@ -412,7 +418,7 @@ def run_ours(args):
                 "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": ncu_traffic(names[dom], "weblike50m"), "alg_bytes_per_sweep": bytes_per_sweep,
                 "sweep_ms": sweep_ms, "launches_per_sweep": chunk_passes(args, n) if dom == 0 else 1,
-                "share_of_step": upd_ms[dom] / ms}
+                "share_of_step": upd_ms[dom] / timed_ms}
     # all three update kernels together, same byte model
     all_bytes = sum((20 * cls_v[c] + 12 * cls_e[c]) * sweeps for c in range(3) if upd_n[c])
     roofline["all_update_kernels_gbs"] = all_bytes / (sum(upd_ms) / 1e3) / 1e9 if sum(upd_ms) else None
@@ -483,6 +489,14 @@ def run_ours(args):
         r_dfp2 = pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp,
                                  opts=pg.options())
         err = float((out - ranks).abs().max())
+        out64 = out.clone()
+        # the same with FP32 ranks and FP64 refinement (DF-P, DF)
+        o32 = pg.options(precision=pg.FP32_REFINE)
+        pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=o32)
+        r_dfp32 = pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=o32)
+        err32_dfp = float((out - out64).abs().max())
+        err32_static = float((out - ranks).abs().max())
+        r_df32 = pg.solve_device(ctx, g, pg.DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=o32)
         dfp = {"batch": {"deletions": len(du), "insertions": len(iu)}, "apply_ms": apply_ms,
                "dfp_ms": r_dfp2["time_ms"], "dfp_iterations": r_dfp2["iterations"],
                "dfp_marking_ms": r_dfp2["marking_time_ms"], "dfp_computation_ms": r_dfp2["computation_time_ms"],
@@ -491,7 +505,13 @@ def run_ours(args):
                "static_ms": r_st["time_ms"], "static_iterations": r_st["iterations"],
                "dfp_speedup_vs_static": r_st["time_ms"] / max(r_dfp2["time_ms"], 1e-9),
                "df_speedup_vs_static": r_st["time_ms"] / max(r_df["time_ms"], 1e-9),
-               "dfp_linf_vs_static": err}
+               "dfp_linf_vs_static": err,
+               "dfp_fp32_refine_ms": r_dfp32["time_ms"], "dfp_fp32_refine_iterations": r_dfp32["iterations"],
+               "dfp_fp32_refine_speedup_vs_dfp_fp64": r_dfp2["time_ms"] / r_dfp32["time_ms"],
+               "dfp_fp32_refine_speedup_vs_static": r_st["time_ms"] / r_dfp32["time_ms"],
+               "dfp_fp32_refine_linf_vs_dfp_fp64": err32_dfp, "dfp_fp32_refine_linf_vs_static": err32_static,
+               "df_fp32_refine_ms": r_df32["time_ms"],
+               "df_fp32_refine_speedup_vs_df_fp64": r_df["time_ms"] / r_df32["time_ms"]}
         log(f"dfp: {dfp}")
 
     ppr = adj = grid = None

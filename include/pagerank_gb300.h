@@ -57,7 +57,12 @@ typedef enum {
   PRX_FP64 = 0,         /* the drop-in: ranks and contributions in FP64, the
                            reference's summation order, bit-exact to the oracle */
   PRX_FP32_REFINE = 1   /* FP32 storage / gathers / accumulation of a correction,
-                           FP64 base ranks, FP64 residual and convergence test */
+                           FP64 base ranks, FP64 residual and convergence test.
+                           DT / DF / DF-P first run their iterations on FP32
+                           ranks, then FP64 sweeps over all vertices refine
+                           that result until the L-inf test passes: the answer
+                           is the converged ranks to the tolerance, not the
+                           FP64 path's answer bit for bit */
 } prx_precision;
 
 typedef enum {

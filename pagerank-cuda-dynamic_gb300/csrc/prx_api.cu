@@ -92,6 +92,7 @@ static void free_ws(prx_context* c) {
   for (auto& b : c->nf) { cudaFree(b); b = nullptr; }
   cudaFree(c->xb); c->xb = nullptr;
   cudaFree(c->naff); c->naff = nullptr;
+  cudaFree(c->ever); c->ever = nullptr;
   cudaFree(c->xl); c->xl = nullptr;
   c->ws_n = 0;
   c->ws_dyn = false;
@@ -141,6 +142,7 @@ static int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
     for (auto& b : c->nf) TRY_CUDA_ST(cudaMalloc(&b, sizeof(uint32_t) * words));
     TRY_CUDA_ST(cudaMalloc(&c->xb, sizeof(uint32_t) * cap));
     TRY_CUDA_ST(cudaMalloc(&c->naff, sizeof(uint32_t) * words));
+    TRY_CUDA_ST(cudaMalloc(&c->ever, sizeof(uint32_t) * words));
     TRY_CUDA_ST(cudaMalloc(&c->xl, sizeof(uint32_t) * cap));
     for (auto& f : c->fr) TRY_CUDA_ST(cudaMalloc(&f, sizeof(uint32_t) * cap));
     for (int k = MID; k < NCLS; ++k) TRY_CUDA_ST(cudaMalloc(&c->lists[0][k], sizeof(uint32_t) * cap));
@@ -197,6 +199,7 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
   for (int p = 0; p < 2; ++p) { a.e[p] = c->e32[p]; a.ce[p] = c->ce32[p]; }
   a.low_bm = g.low_bm;
   a.rcp = g.rcp;
+  a.ever = c->ever;
   a.acc64 = c->acc64;
   a.acc32 = c->acc32;
   // expand by pulling once more than 1/16 of the vertices changed by > D
@@ -291,11 +294,12 @@ static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArg
                              const ChunkLayout* lay) {
   cudaStream_t s = c->stream;
   for (int cls = 0; cls < NCLS; ++cls) {
-    const int st = launch_update_timed(c, timing, cls,
+    const int slot = (mode & MODE_F32) ? NCLS + cls : cls;  // FP32 sweeps are timed apart
+    const int st = launch_update_timed(c, timing, slot,
                                        [&] { return launch_update_class(a, gr->g, mode, cls, lay, c->sms, s); });
     if (st) return st;
   }
-  if (mode >= PRX_DYNAMIC_FRONTIER) {
+  if ((mode & ~MODE_F32) >= PRX_DYNAMIC_FRONTIER) {
     launch_expand_iteration(a, c->sms, s);  // push or pull, chosen on the device
     c->launches += 3;
   }
@@ -367,7 +371,7 @@ static int run_graph_loop(prx_context* c, const prx_graph* gr, const SolveArgs& 
 // sweep converged (its output in r[1]), 0 when the cap stopped an FP32 round
 // (the committed ranks in r[0]).
 static int run_refine_loop(prx_context* c, const prx_graph* gr, const SolveArgs& a, bool timing, int max_iter,
-                           const ChunkLayout* lay64, const ChunkLayout* lay32, int* final_parity) {
+                           const ChunkLayout* lay64, const ChunkLayout* lay32, int* final_parity, bool round0) {
   cudaStream_t s = c->stream;
   int st;
   // one round of FP32 correction sweeps until they stop, then x_b += e
@@ -398,10 +402,16 @@ static int run_refine_loop(prx_context* c, const prx_graph* gr, const SolveArgs&
     *final_parity = 0;  // no sweep: the initial ranks
     return PRX_OK;
   }
-  // round 0: FP32 sweeps of the ranks themselves from the initial ranks
-  launch_refine_round0(a, c->sms, s);
-  c->launches += 1;
-  if ((st = fp32_round())) return st;
+  // round 0: FP32 sweeps of the ranks themselves from the initial ranks (the
+  // dynamic modes start from the committed result of their FP32 phase instead)
+  if (round0) {
+    launch_refine_round0(a, c->sms, s);
+    c->launches += 1;
+    if ((st = fp32_round())) return st;
+  } else {
+    TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
+    TRY_CUDA_ST(cudaStreamSynchronize(s));
+  }
   if (c->st_host[1].iter >= max_iter) {
     TRY_CUDA_ST(cudaStreamSynchronize(s));
     *final_parity = 0;
@@ -442,7 +452,6 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   if (dyn && !g.xoff) FAIL(PRX_ESTATE, "prx_solve: dynamic modes need the out-CSR (xoff/xedg) of the graph");
   if (o.precision != PRX_FP64 && o.precision != PRX_FP32_REFINE) FAIL(PRX_EINVAL, "prx_solve: unknown precision");
   const bool refine = o.precision == PRX_FP32_REFINE;
-  if (refine && dyn) FAIL(PRX_EINVAL, "prx_solve: PRX_FP32_REFINE is available for Static and ND");
   int st = ensure_ws(c, g.n, dyn);
   if (st) return st;
   if (refine && (st = ensure_ws32(c, g.n))) return st;
@@ -470,6 +479,11 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
     launch_state_reset(c->st, o.max_iterations, o.tolerance, s);
     launch_init_ranks(a, (mode == PRX_STATIC) ? nullptr : q_dev, dyn, s);
     c->launches += 2;
+    if (refine && dyn) {
+      launch_init_ranks32(a, q_dev, s);
+      TRY_CUDA_ST(cudaMemsetAsync(c->ever, 0, sizeof(uint32_t) * (((size_t)g.n + 31) / 32), s));
+      c->launches += 1;
+    }
     TRY_CUDA_ST(cudaEventRecord(c->ev[1], s));
     if (dyn) {
       st = run_marking(c, a, mode, du, dv, nd, iu, ni);
@@ -477,22 +491,35 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
       TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[0], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
     }
     TRY_CUDA_ST(cudaEventRecord(c->ev[2], s));
-    if (refine) {
-      if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity))) return st;
-    } else if (o.loop != PRX_LOOP_HOST && !timing) {
-      if ((st = run_graph_loop(c, gr, a, mode, lay64, o.max_iterations))) return st;
-    } else {
+    // iterations of `m` until done: one CUDA graph, or host-driven batches
+    auto iterate = [&](int m, const ChunkLayout* lay) -> int {
+      if (o.loop != PRX_LOOP_HOST && !timing) return run_graph_loop(c, gr, a, m, lay, o.max_iterations);
       for (int k = 1;; k = std::min(2 * k, 16)) {
         for (int i = 0; i < k; ++i) {
-          st = enqueue_iteration(c, gr, a, mode, timing, lay64);
-          if (st) return st;
+          const int e = enqueue_iteration(c, gr, a, m, timing, lay);
+          if (e) return e;
         }
         TRY_CUDA_ST(cudaGetLastError());
         TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
         TRY_CUDA_ST(cudaStreamSynchronize(s));
-        if (timing && (st = drain_timing(c))) return st;
-        if (c->st_host[1].done) break;
+        if (timing) {
+          const int e = drain_timing(c);
+          if (e) return e;
+        }
+        if (c->st_host[1].done) return PRX_OK;
       }
+    };
+    if (refine && dyn) {
+      // DT / DF / DF-P with FP32 ranks, then the FP64 refinement of the result
+      // (an FP64 residual sweep over all vertices decides convergence)
+      if ((st = iterate(mode | MODE_F32, lay32))) return st;
+      launch_commit_dyn32(a, c->st_host[1].iter & 1, s);
+      c->launches += 1;
+      if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity, false))) return st;
+    } else if (refine) {
+      if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity, true))) return st;
+    } else if ((st = iterate(mode, lay64))) {
+      return st;
     }
     TRY_CUDA_ST(cudaEventRecord(c->ev[3], s));
     TRY_CUDA_ST(cudaEventSynchronize(c->ev[3]));

@@ -31,6 +31,7 @@ struct prx_context {
   uint32_t* nf[2] = {nullptr, nullptr};
   uint32_t* xb = nullptr;
   uint32_t* naff = nullptr;
+  uint32_t* ever = nullptr;   // FP32 dynamic phase: vertices updated at least once
   uint32_t* lists[2][NCLS] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   uint32_t* xl = nullptr;
   uint32_t* fr[3] = {nullptr, nullptr, nullptr};

@@ -56,6 +56,10 @@ struct State {
 // refinement (reads the base ranks r[0] / c[0], writes the next iterate to
 // r[1] and the residual, as FP32, to rho and e[0] / ce[0]).
 constexpr int MODE_REFINE64 = 10;
+// Flag added to DT / DF / DF-P: the same iterations on FP32 ranks and
+// contributions (the refinement workspace's e[] and ce[]), the first phase of
+// those modes under PRX_FP32_REFINE.
+constexpr int MODE_F32 = 0x20;
 
 // In-edges of the LOW class regrouped by source chunk: chunk k holds, for
 // every vertex v, the in-edges whose source lies in [k*width, (k+1)*width),
@@ -129,6 +133,7 @@ struct SolveArgs {
   float* ce[2];                   // FP32 refinement: correction / outdeg, ping-pong
   const uint32_t* low_bm;         // LOW-class bitmap
   const double* rcp;              // RN(1 / outdeg)
+  uint32_t* ever;                 // FP32 dynamic phase: vertices updated at least once
   double* acc64;                  // partial row sums carried between chunk passes (FP64)
   float* acc32;                   // the same for the FP32 sweeps
   State* st;
@@ -140,6 +145,12 @@ struct SolveArgs {
 
 // ---- launchers (prx_update.cu) ------------------------------------------
 void launch_init_ranks(const SolveArgs& a, const double* q, bool dynamic, cudaStream_t s);
+// FP32 dynamic phase: e[0] = e[1] = (float)q, ce = e / outdeg.
+void launch_init_ranks32(const SolveArgs& a, const double* q, cudaStream_t s);
+// After it: r[0] = (double)e[parity] where `ever` is set (else q, already in
+// r[0]), c[0] = r[0] / outdeg; then the control block is reopened for the
+// FP64 refinement (done only if the iteration cap was reached).
+void launch_commit_dyn32(const SolveArgs& a, int parity, cudaStream_t s);
 // Rank update of one in-degree class; false if nothing was launched.  For
 // LOW, `lay` (may be null: no chunking) selects the chunk layout and one
 // launch per chunk is made.

@@ -33,16 +33,38 @@
 // unaffected vertex, :94-96).  Three bitmaps rotate: cur (k), nxt (k+1),
 // prev (k-1); the LOW kernel clears prev after reading it, which makes it the
 // empty nxt of iteration k+1.
+#include <type_traits>
 #include "prx_device.cuh"
 
 namespace prx {
 
 template <int MODE> struct ModeTraits {
-  static constexpr bool REFINE = MODE == MODE_REFINE64;
-  static constexpr bool DYN = !REFINE && MODE >= PRX_DYNAMIC_TRAVERSAL;
-  static constexpr bool FRONTIER = DYN && MODE >= PRX_DYNAMIC_FRONTIER;
-  static constexpr bool PRUNE = MODE == PRX_PRUNE_DYNAMIC_FRONTIER;
+  static constexpr bool F32 = (MODE & MODE_F32) != 0;
+  static constexpr int BASE = MODE & ~MODE_F32;
+  static constexpr bool REFINE = BASE == MODE_REFINE64;
+  static constexpr bool DYN = !REFINE && BASE >= PRX_DYNAMIC_TRAVERSAL;
+  static constexpr bool FRONTIER = DYN && BASE >= PRX_DYNAMIC_FRONTIER;
+  static constexpr bool PRUNE = BASE == PRX_PRUNE_DYNAMIC_FRONTIER;
+  using V = typename std::conditional<F32, float, double>::type;  // rank / contribution type
 };
+
+// Rank, contribution and carried-sum arrays of a mode: FP64 r / c / acc64,
+// or for the FP32 dynamic phase e / ce / acc32.
+template <int MODE>
+__device__ __forceinline__ typename ModeTraits<MODE>::V* ranks_of(const SolveArgs& a, int p) {
+  if constexpr (ModeTraits<MODE>::F32) return a.e[p];
+  else return a.r[p];
+}
+template <int MODE>
+__device__ __forceinline__ typename ModeTraits<MODE>::V* contribs_of(const SolveArgs& a, int p) {
+  if constexpr (ModeTraits<MODE>::F32) return a.ce[p];
+  else return a.c[p];
+}
+template <int MODE>
+__device__ __forceinline__ typename ModeTraits<MODE>::V* carried_of(const SolveArgs& a) {
+  if constexpr (ModeTraits<MODE>::F32) return a.acc32;
+  else return a.acc64;
+}
 
 // Data parity read by an iteration: the refinement's FP64 sweep always reads
 // the base ranks (parity 0) and writes parity 1.
@@ -56,39 +78,62 @@ __device__ __forceinline__ void set_bit(uint32_t* bm, uint32_t w) {
   if (!(bm[w >> 5] & bit)) atomicOr(&bm[w >> 5], bit);
 }
 
-// Finish vertex v given its contribution sum.  Returns |a_v - r_v| as bits.
-// survive (dynamic): v stays affected next iteration; changed (DF / DF-P):
-// its relative change exceeded the frontier tolerance, so its out-neighbours
-// become affected (:106-107, expanded after the sweep as at :686-687).
+// Finish vertex v given its contribution sum.  Returns |a_v - r_v| as bits
+// (of a double; an FP32 change converts exactly).  survive (dynamic): v stays
+// affected next iteration; changed (DF / DF-P): its relative change exceeded
+// the frontier tolerance, so its out-neighbours become affected (:106-107,
+// expanded after the sweep as at :686-687).  FP32 phase: *mag is raised to
+// |a_v| (bits of a float).
 template <int MODE>
-__device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, uint32_t v, double cv, int p,
-                                                            bool& survive, bool& changed) {
+__device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, uint32_t v,
+                                                            typename ModeTraits<MODE>::V cv, int p, bool& survive,
+                                                            bool& changed, unsigned int& mag) {
   using T = ModeTraits<MODE>;
   const uint32_t d = a.xtdat[v];
-  const double y = a.rcp[v];
-  const double rv = a.r[p][v];
-  double av;
-  if (T::PRUNE) av = fma(a.P, cv - div_count(rv, d, y), a.C0) * (1 / (1 - div_count(a.P, d, y)));
-  else          av = fma(a.P, cv, a.C0);
-  const double ev = fabs(av - rv);
-  a.r[p ^ 1][v] = av;
-  if (T::REFINE) {
-    // residual of the base ranks, the first FP32 correction and its contribution
-    const float rho = (float)(av - rv);
-    a.rho[v] = rho;
-    a.e[0][v] = rho;
-    a.ce[0][v] = __fdividef(rho, (float)d);
+  if constexpr (T::F32) {
+    const float P = (float)a.P, C0 = (float)a.C0, df = (float)d;
+    const float rv = a.e[p][v];
+    float av;
+    if (T::PRUNE) av = fmaf(P, cv - rv / df, C0) * (1.f / (1.f - P / df));
+    else          av = fmaf(P, cv, C0);
+    const float ev = fabsf(av - rv);
+    a.e[p ^ 1][v] = av;
+    a.ce[p ^ 1][v] = av / df;
+    mag = max(mag, __float_as_uint(fabsf(av)));
+    survive = true;
+    changed = false;
+    if (T::FRONTIER) {
+      const float rel = ev / fmaxf(rv, av);
+      if (T::PRUNE && rel <= (float)a.C) survive = false;
+      changed = rel > (float)a.D;
+    }
+    return dbits((double)ev);
   } else {
-    a.c[p ^ 1][v] = div_count(av, d, y);
+    const double y = a.rcp[v];
+    const double rv = a.r[p][v];
+    double av;
+    if (T::PRUNE) av = fma(a.P, cv - div_count(rv, d, y), a.C0) * (1 / (1 - div_count(a.P, d, y)));
+    else          av = fma(a.P, cv, a.C0);
+    const double ev = fabs(av - rv);
+    a.r[p ^ 1][v] = av;
+    if (T::REFINE) {
+      // residual of the base ranks, the first FP32 correction and its contribution
+      const float rho = (float)(av - rv);
+      a.rho[v] = rho;
+      a.e[0][v] = rho;
+      a.ce[0][v] = __fdividef(rho, (float)d);
+    } else {
+      a.c[p ^ 1][v] = div_count(av, d, y);
+    }
+    survive = true;
+    changed = false;
+    if (T::FRONTIER) {
+      const double rel = ev / fmax(rv, av);
+      if (T::PRUNE && rel <= a.C) survive = false;  // :106
+      changed = rel > a.D;                          // :107
+    }
+    return dbits(ev);
   }
-  survive = true;
-  changed = false;
-  if (T::FRONTIER) {
-    const double rel = ev / fmax(rv, av);
-    if (T::PRUNE && rel <= a.C) survive = false;  // :106
-    changed = rel > a.D;                          // :107
-  }
-  return dbits(ev);
 }
 
 // ---- LOW: one warp per 32 consecutive vertex ids ------------------------------
@@ -105,10 +150,11 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const uint
   using T = ModeTraits<MODE>;
   constexpr bool FIRST = PASS == PASS_ONLY || PASS == PASS_FIRST;
   constexpr bool LAST = PASS == PASS_ONLY || PASS == PASS_LAST;
+  using V = typename T::V;
   State* st = a.st;
   if (st->done) return;
   const int iter = st->iter, p = data_parity<MODE>(st);
-  const double* __restrict__ c = a.c[p];
+  const V* __restrict__ c = contribs_of<MODE>(a, p);
   uint32_t *cur = nullptr, *nxt = nullptr, *prev = nullptr;
   if (T::DYN) {
     cur = a.bm[iter % 3];
@@ -118,6 +164,7 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const uint
   const uint32_t lane = lane_id();
   const uint32_t words = (a.n + 31) >> 5;
   unsigned long long emax = 0, edges = 0;
+  unsigned int mag = 0;
   for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t v = (w << 5) | lane;
     bool mine = v < a.n;
@@ -126,10 +173,11 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const uint
       if (FIRST) {
         const uint32_t pw = prev[w];
         if (((pw & ~cw) >> lane) & 1u) {  // updated last iteration, not this one: refresh parity p^1
-          a.r[p ^ 1][v] = a.r[p][v];
-          a.c[p ^ 1][v] = a.c[p][v];
+          ranks_of<MODE>(a, p ^ 1)[v] = ranks_of<MODE>(a, p)[v];
+          contribs_of<MODE>(a, p ^ 1)[v] = contribs_of<MODE>(a, p)[v];
         }
         if (lane == 0) {
+          if (T::F32 && cw) atomicOr(&a.ever[w], cw);
           if (pw) prev[w] = 0;  // becomes the empty nxt of iteration k+1
           // nf[p^1] was filled and expanded by iteration k-1; clear it for k+1
           if (T::FRONTIER && a.nf[p ^ 1][w]) a.nf[p ^ 1][w] = 0;
@@ -150,15 +198,15 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const uint
     const uint32_t s = mine ? off[v] : 0, e = mine ? off[v + 1] : 0;
     mine = low && (FIRST || LAST || s < e);
     bool survive = false, changed = false;
-    double acc = 0.0;
-    if (mine) acc = lane_row_sum(c, edg, s, e, FIRST ? 0.0 : a.acc64[v]);
+    V acc = V(0);
+    if (mine) acc = lane_row_sum(c, edg, s, e, FIRST ? V(0) : carried_of<MODE>(a)[v]);
     if (mine) {
       edges += e - s;
       if (LAST) {
-        const unsigned long long ev = finish_vertex<MODE>(a, v, acc, p, survive, changed);
+        const unsigned long long ev = finish_vertex<MODE>(a, v, acc, p, survive, changed, mag);
         emax = ev > emax ? ev : emax;
       } else {
-        a.acc64[v] = acc;
+        carried_of<MODE>(a)[v] = acc;
       }
     }
     if (LAST && T::DYN) {
@@ -174,6 +222,7 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const uint
     }
   }
   if (LAST) block_max_bits(emax, &st->el_bits[iter & 1]);
+  if (LAST && T::F32) block_max_u32(mag, &st->e32max_bits[iter & 1]);
   if (T::DYN) block_sum_u64(edges, &st->edges);
 }
 
@@ -192,10 +241,10 @@ __device__ __forceinline__ void list_of(const SolveArgs& a, int cls, uint32_t be
 }
 
 template <int MODE>
-__device__ __forceinline__ void finish_listed(const SolveArgs& a, uint32_t v, double x, int p,
-                                              unsigned long long& emax) {
+__device__ __forceinline__ void finish_listed(const SolveArgs& a, uint32_t v, typename ModeTraits<MODE>::V x, int p,
+                                              unsigned long long& emax, unsigned int& mag) {
   bool survive, changed;
-  const unsigned long long ev = finish_vertex<MODE>(a, v, x, p, survive, changed);
+  const unsigned long long ev = finish_vertex<MODE>(a, v, x, p, survive, changed, mag);
   emax = ev > emax ? ev : emax;
   if (ModeTraits<MODE>::DYN && survive) atomicOr(&a.bm[(a.st->iter + 1) % 3][v >> 5], 1u << (v & 31u));
   if (ModeTraits<MODE>::FRONTIER && changed) {
@@ -213,18 +262,20 @@ __global__ void __launch_bounds__(kThreads) k_update_mid(SolveArgs a, uint32_t b
   const uint32_t* list;
   uint32_t count;
   list_of<MODE>(a, MID, begin, count_static, list, count);
-  const double* __restrict__ c = a.c[p];
+  using V = typename T::V;
+  const V* __restrict__ c = contribs_of<MODE>(a, p);
   const uint32_t lane = lane_id();
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   unsigned long long emax = 0, edges = 0;
+  unsigned int mag = 0;
   for (uint32_t i = warp; i < count; i += nwarps) {
     const uint32_t v = list[i];
     const uint32_t s = a.xtoff[v], d = a.xtoff[v + 1] - s;
     const uint32_t* __restrict__ ed = a.xtedg + s;
-    double ps[8];
+    V ps[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) ps[k] = 0.0;
+    for (int k = 0; k < 8; ++k) ps[k] = V(0);
     for (uint32_t base = 0; base < d; base += 256) {
       uint32_t u[8];
 #pragma unroll
@@ -232,9 +283,9 @@ __global__ void __launch_bounds__(kThreads) k_update_mid(SolveArgs a, uint32_t b
         const uint32_t t = base + lane + 32u * k;
         u[k] = t < d ? __ldg(ed + t) : 0u;
       }
-      double x[8];
+      V x[8];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) x[k] = (base + lane + 32u * k < d) ? __ldg(c + u[k]) : 0.0;
+      for (int k = 0; k < 8; ++k) x[k] = (base + lane + 32u * k < d) ? __ldg(c + u[k]) : V(0);
 #pragma unroll
       for (int k = 0; k < 8; ++k) ps[k] += x[k];
     }
@@ -242,15 +293,16 @@ __global__ void __launch_bounds__(kThreads) k_update_mid(SolveArgs a, uint32_t b
     ps[0] += ps[4]; ps[1] += ps[5]; ps[2] += ps[6]; ps[3] += ps[7];  // t < 128: += t+128
     ps[0] += ps[2]; ps[1] += ps[3];                                  // t < 64:  += t+64
     ps[0] += ps[1];                                                  // t < 32:  += t+32
-    double x = ps[0];
+    V x = ps[0];
 #pragma unroll
     for (int o = 16; o; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if (lane == 0) {
-      finish_listed<MODE>(a, v, x, p, emax);
+      finish_listed<MODE>(a, v, x, p, emax, mag);
       edges += d;
     }
   }
   block_max_bits(emax, &a.st->el_bits[a.st->iter & 1]);
+  if (T::F32) block_max_u32(mag, &a.st->e32max_bits[a.st->iter & 1]);
   if (T::DYN) block_sum_u64(edges, &a.st->edges);
 }
 
@@ -258,26 +310,28 @@ __global__ void __launch_bounds__(kThreads) k_update_mid(SolveArgs a, uint32_t b
 template <int MODE>
 __global__ void __launch_bounds__(256) k_update_high(SolveArgs a, uint32_t begin, uint32_t count_static) {
   using T = ModeTraits<MODE>;
-  __shared__ double part[256];
+  using V = typename T::V;
+  __shared__ V part[256];
   if (a.st->done) return;
   const int p = data_parity<MODE>(a.st);
   const uint32_t* list;
   uint32_t count;
   list_of<MODE>(a, HIGH, begin, count_static, list, count);
-  const double* __restrict__ c = a.c[p];
+  const V* __restrict__ c = contribs_of<MODE>(a, p);
   const uint32_t t = threadIdx.x;
   unsigned long long emax = 0, edges = 0;
+  unsigned int mag = 0;
   for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
     const uint32_t v = list[i];
     const uint32_t s = a.xtoff[v], d = a.xtoff[v + 1] - s;
     const uint32_t* __restrict__ ed = a.xtedg + s;
-    double acc = 0.0;
+    V acc = V(0);
     uint32_t j = t;
     for (; j + 7 * 256 < d; j += 8 * 256) {
       uint32_t u[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) u[k] = __ldg(ed + j + 256 * k);
-      double x[8];
+      V x[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) x[k] = __ldg(c + u[k]);
 #pragma unroll
@@ -291,17 +345,18 @@ __global__ void __launch_bounds__(256) k_update_high(SolveArgs a, uint32_t begin
     if (t < 64) part[t] += part[t + 64];
     __syncthreads();
     if (t < 32) {
-      double x = part[t] + part[t + 32];
+      V x = part[t] + part[t + 32];
 #pragma unroll
       for (int o = 16; o; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
       if (t == 0) {
-        finish_listed<MODE>(a, v, x, p, emax);
+        finish_listed<MODE>(a, v, x, p, emax, mag);
         edges += d;
       }
     }
     __syncthreads();
   }
   block_max_bits(emax, &a.st->el_bits[a.st->iter & 1]);
+  if (T::F32) block_max_u32(mag, &a.st->e32max_bits[a.st->iter & 1]);
   if (T::DYN) block_sum_u64(edges, &a.st->edges);
 }
 
@@ -391,14 +446,19 @@ __global__ void k_init_ranks(SolveArgs a, const double* __restrict__ q, int both
   }
 }
 
-template <bool DYN>
+template <bool DYN, bool F32>
 __global__ void k_finalize(State* st) {
   if (st->done) return;
   const int p = st->iter & 1;
   const double el = __longlong_as_double((long long)st->el_bits[p]);
   st->last_delta = el;
   st->iter += 1;
-  if (el < st->tol || st->iter >= st->max_iter) st->done = 1;  // pagerankLoopCuU :680,689
+  bool stop = el < st->tol || st->iter >= st->max_iter;  // pagerankLoopCuU :680,689
+  if (F32) {  // FP32 phase: also stop at what FP32 ranks can resolve
+    stop = stop || el < (double)__uint_as_float(st->e32max_bits[p]) * 0x1p-18;
+    st->e32max_bits[p ^ 1] = 0;
+  }
+  if (stop) st->done = 1;
   st->el_bits[p ^ 1] = 0;
   if (DYN) {
     st->cnt[0][MID] = st->cnt[0][HIGH] = 0;
@@ -413,6 +473,47 @@ static inline int cap_grid(uint64_t want, int cap) { return (int)(want < (uint64
 
 void launch_init_ranks(const SolveArgs& a, const double* q, bool dynamic, cudaStream_t s) {
   k_init_ranks<<<cap_grid((a.n + kThreads - 1) / kThreads, 152 * 16), kThreads, 0, s>>>(a, q, dynamic ? 1 : 0);
+}
+
+__global__ void k_init_ranks32(SolveArgs a, const double* __restrict__ q) {
+  const float r0 = 1.0f / (float)a.n;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
+    const float r = q ? (float)q[v] : r0;
+    const float c = r / (float)a.xtdat[v];
+    a.e[0][v] = a.e[1][v] = r;
+    a.ce[0][v] = a.ce[1][v] = c;
+  }
+}
+
+void launch_init_ranks32(const SolveArgs& a, const double* q, cudaStream_t s) {
+  k_init_ranks32<<<cap_grid((a.n + kThreads - 1) / kThreads, 152 * 16), kThreads, 0, s>>>(a, q);
+}
+
+__global__ void k_commit_dyn32(SolveArgs a, int parity) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
+    double x = a.r[0][v];
+    if ((a.ever[v >> 5] >> (v & 31u)) & 1u) {
+      x = (double)a.e[parity][v];
+      a.r[0][v] = x;
+    }
+    a.c[0][v] = div_count(x, a.xtdat[v], a.rcp[v]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {  // reopen the loop for the FP64 refinement
+    State* st = a.st;
+    st->done = st->iter >= st->max_iter;
+    st->el_bits[0] = st->el_bits[1] = 0;
+    st->k32 = 0;
+    st->inner_done = 0;
+    st->el32_bits[0] = st->el32_bits[1] = 0;
+    st->e32max_bits[0] = st->e32max_bits[1] = 0;
+    st->cnt[0][MID] = st->cnt[0][HIGH] = 0;
+    st->nfcnt = 0;
+    st->xbcnt = 0;
+  }
+}
+
+void launch_commit_dyn32(const SolveArgs& a, int parity, cudaStream_t s) {
+  k_commit_dyn32<<<cap_grid((a.n + kThreads - 1) / kThreads, 152 * 16), kThreads, 0, s>>>(a, parity);
 }
 
 template <int MODE>
@@ -457,7 +558,12 @@ bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cl
     case PRX_NAIVE_DYNAMIC: return update_class_t<PRX_STATIC>(a, g, cls, lay, sms, s);
     case PRX_DYNAMIC_TRAVERSAL: return update_class_t<PRX_DYNAMIC_TRAVERSAL>(a, g, cls, lay, sms, s);
     case PRX_DYNAMIC_FRONTIER: return update_class_t<PRX_DYNAMIC_FRONTIER>(a, g, cls, lay, sms, s);
-    default: return update_class_t<PRX_PRUNE_DYNAMIC_FRONTIER>(a, g, cls, lay, sms, s);
+    case PRX_PRUNE_DYNAMIC_FRONTIER: return update_class_t<PRX_PRUNE_DYNAMIC_FRONTIER>(a, g, cls, lay, sms, s);
+    case PRX_DYNAMIC_TRAVERSAL | MODE_F32:
+      return update_class_t<PRX_DYNAMIC_TRAVERSAL | MODE_F32>(a, g, cls, lay, sms, s);
+    case PRX_DYNAMIC_FRONTIER | MODE_F32:
+      return update_class_t<PRX_DYNAMIC_FRONTIER | MODE_F32>(a, g, cls, lay, sms, s);
+    default: return update_class_t<PRX_PRUNE_DYNAMIC_FRONTIER | MODE_F32>(a, g, cls, lay, sms, s);
   }
 }
 
@@ -479,8 +585,9 @@ void launch_expand_big(const SolveArgs& a, int target, int sms, cudaStream_t s) 
 }
 
 void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s) {
-  if (mode < PRX_DYNAMIC_TRAVERSAL) k_finalize<false><<<1, 1, 0, s>>>(a.st);
-  else k_finalize<true><<<1, 1, 0, s>>>(a.st);
+  if (mode & MODE_F32) k_finalize<true, true><<<1, 1, 0, s>>>(a.st);
+  else if (mode < PRX_DYNAMIC_TRAVERSAL) k_finalize<false, false><<<1, 1, 0, s>>>(a.st);
+  else k_finalize<true, false><<<1, 1, 0, s>>>(a.st);
 }
 
 }  // namespace prx

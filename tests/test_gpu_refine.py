@@ -82,11 +82,64 @@ def test_refine_caps_and_tolerances(pg, ctx):
     g.close()
 
 
-def test_refine_rejects_dynamic_modes_for_now(pg, ctx):
-    xoff, xedg = pg.graphs.rmat(8, 8, seed=1)
+@pytest.mark.parametrize("kind", ["web200k", "hubs", "rmat16"])
+def test_refine_dynamic_modes(pg, ctx, kind):
+    # DT / DF / DF-P with FP32 ranks, then FP64 sweeps over all vertices until
+    # the L-inf test passes.  The answer is the converged (Static) ranks to the
+    # refinement bound; its distance from the FP64 path's answer is at most
+    # that path's own distance from them (pruned vertices keep stale ranks
+    # there) plus the bound.  Same initial affected set, both loops.
+    from test_gpu_parity import _synthetic
+    xoff, xedg = _synthetic(pg, kind)
+    m = len(xedg)
+    batch = pg.graphs.random_batch(xoff, xedg, max(1, int(2e-4 * m)), max(1, int(8e-4 * m)), seed=29)
+    du, dv, iu, iv = batch
     xt = O.transpose(xoff, xedg)
-    g = pg.Graph(ctx, *xt, xoff, xedg)
-    e = np.zeros(0, np.uint32)
-    with pytest.raises(pg.PrxError):
-        pg.solve(ctx, g, pg.DYNAMIC_FRONTIER, (e, e), (e, e), None, pg.options(precision=pg.FP32_REFINE))
-    g.close()
+    q, _ = O.solve("static", None, None, *xt)
+    yoff, yedg = pg.graphs.apply_batch(xoff, xedg, *batch)
+    yt = O.transpose(yoff, yedg)
+    g = pg.Graph(ctx, *yt, yoff, yedg)
+    try:
+        conv, _ = O.solve("static", None, None, *yt)
+        for mode in ("dynamic_traversal", "dynamic_frontier", "prune_dynamic_frontier"):
+            want, _ = O.solve(mode, yoff, yedg, *yt, du, dv, iu, iv, q=q)
+            own = np.abs(want - conv).max()
+            _, r64 = pg.solve(ctx, g, pg.MODES[mode], (du, dv), (iu, iv), q)
+            for loop in (pg.LOOP_GRAPH, pg.LOOP_HOST):
+                o = pg.options(precision=pg.FP32_REFINE, loop=loop)
+                got, res = pg.solve(ctx, g, pg.MODES[mode], (du, dv), (iu, iv), q, o)
+                assert np.abs(got - conv).max() <= bound(conv), (kind, mode, loop)
+                assert np.abs(got - want).max() <= own + bound(want), (kind, mode, loop)
+                assert res["refinements"] >= 1 and res["last_delta"] < 1e-10
+                assert res["affected_initial"] == r64["affected_initial"]
+    finally:
+        g.close()
+
+
+def test_refine_dynamic_caps_and_empty_batch(pg, ctx):
+    xoff, xedg = pg.graphs.rmat(12, 16, seed=5)
+    m = len(xedg)
+    batch = pg.graphs.random_batch(xoff, xedg, 20, 80, seed=31)
+    du, dv, iu, iv = batch
+    xt = O.transpose(xoff, xedg)
+    q, _ = O.solve("static", None, None, *xt)
+    yoff, yedg = pg.graphs.apply_batch(xoff, xedg, *batch)
+    yt = O.transpose(yoff, yedg)
+    g = pg.Graph(ctx, *yt, yoff, yedg)
+    try:
+        for L in (0, 1, 3):
+            got, res = pg.solve(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, (du, dv), (iu, iv), q,
+                                pg.options(precision=pg.FP32_REFINE, max_iterations=L))
+            assert res["iterations"] == L and np.all(np.isfinite(got))
+            if L == 0:
+                np.testing.assert_array_equal(got, q)
+        e = np.zeros(0, np.uint32)
+        want, _ = O.solve("prune_dynamic_frontier", yoff, yedg, *yt, e, e, e, e, q=q)
+        got, res = pg.solve(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, (e, e), (e, e), q,
+                            pg.options(precision=pg.FP32_REFINE))
+        assert res["affected_initial"] == 0
+        conv, _ = O.solve("static", None, None, *yt)
+        assert np.abs(got - conv).max() <= bound(conv)
+        assert np.abs(got - want).max() <= np.abs(want - conv).max() + bound(want)
+    finally:
+        g.close()
