@@ -55,6 +55,9 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--static-only", action="store_true", help="upload only the in-CSR; skip DF-P and the CPU leg")
     p.add_argument("--chunk", type=int, default=0, help="source-chunk width of the gathers (0: library default)")
+    p.add_argument("--loop", default="auto", choices=("auto", "host"),
+                   help="iteration loop of the Static / dynamic solves: auto (one CUDA graph) or host (kernels "
+                        "visible one by one to a profiler)")
     p.add_argument("--no-grid", action="store_true", help="skip the high-diameter grid workload")
     p.add_argument("--grid-side", type=int, default=4096)
     p.add_argument("--no-ppr", action="store_true", help="skip the batched personalized PageRank workload")
@@ -164,6 +167,15 @@ def measured_peak():
             return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def loop_opts(pg, args):
+    """Options factory honouring --loop."""
+    def make(**kw):
+        if args.loop == "host":
+            kw["loop"] = pg.LOOP_HOST
+        return pg.options(**kw)
+    return make
 
 
 def chunk_passes(args, n, default_width=(200 << 20) // 8):
@@ -379,7 +391,7 @@ def run_ours(args):
     # the timed solves run as the library runs by default (the iteration loop
     # as one CUDA graph); the per-launch timing of the roofline comes from
     # separate solves with timing on (host-driven loop, same kernels)
-    opts = pg.options(chunk_vertices=args.chunk)
+    opts = loop_opts(pg, args)(chunk_vertices=args.chunk)
     topts = pg.options(timing=1, chunk_vertices=args.chunk)
     log(f"classes: vertices {cls_v} edges {cls_e}")
     for _ in range(args.warmup):
@@ -483,15 +495,16 @@ def run_ours(args):
               for a in (du, dv, iu, iv)]
         out = torch.empty_like(q)
         bp = (bt[0].data_ptr(), bt[1].data_ptr(), len(du), bt[2].data_ptr(), bt[3].data_ptr(), len(iu))
-        r_dfp = pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=pg.options())
-        r_df = pg.solve_device(ctx, g, pg.DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=pg.options())
-        r_st = pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr(), opts=pg.options())
+        lo = loop_opts(pg, args)
+        r_dfp = pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=lo())
+        r_df = pg.solve_device(ctx, g, pg.DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=lo())
+        r_st = pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr(), opts=lo())
         r_dfp2 = pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp,
-                                 opts=pg.options())
+                                 opts=lo())
         err = float((out - ranks).abs().max())
         out64 = out.clone()
         # the same with FP32 ranks and FP64 refinement (DF-P, DF)
-        o32 = pg.options(precision=pg.FP32_REFINE)
+        o32 = lo(precision=pg.FP32_REFINE)
         pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=o32)
         r_dfp32 = pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=o32)
         err32_dfp = float((out - out64).abs().max())

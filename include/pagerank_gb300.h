@@ -270,7 +270,10 @@ int prx_adjoint(prx_context* ctx, prx_graph* g, const double* t, const double* r
  * device, the dividends a and out-degrees d (d = 1 .. dmax, `per` values of a
  * per d, spread over 2^-40 .. 2^2) for which the library's three-operation
  * division by a precomputed reciprocal differs from the IEEE division a / d.
- * The solvers divide ranks by out-degrees that way. */
+ * The solvers divide ranks by out-degrees that way.  Each sample also checks
+ * the multiply-first comparisons of a relative change with a tolerance
+ * (DF / DF-P) against the comparison of the correctly rounded quotient, in
+ * the band where the two are closest. */
 int prx_selftest_division(prx_context* ctx, uint32_t dmax, uint32_t per, unsigned long long* mismatches);
 
 /* Static FP64 PageRank that allocates no memory.  No counterpart in the

@@ -93,6 +93,7 @@ static void free_ws(prx_context* c) {
   cudaFree(c->xb); c->xb = nullptr;
   cudaFree(c->naff); c->naff = nullptr;
   cudaFree(c->ever); c->ever = nullptr;
+  cudaFree(c->pf); c->pf = nullptr;
   cudaFree(c->xl); c->xl = nullptr;
   c->ws_n = 0;
   c->ws_dyn = false;
@@ -143,6 +144,7 @@ static int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
     TRY_CUDA_ST(cudaMalloc(&c->xb, sizeof(uint32_t) * cap));
     TRY_CUDA_ST(cudaMalloc(&c->naff, sizeof(uint32_t) * words));
     TRY_CUDA_ST(cudaMalloc(&c->ever, sizeof(uint32_t) * words));
+    TRY_CUDA_ST(cudaMalloc(&c->pf, sizeof(double) * cap));
     TRY_CUDA_ST(cudaMalloc(&c->xl, sizeof(uint32_t) * cap));
     for (auto& f : c->fr) TRY_CUDA_ST(cudaMalloc(&f, sizeof(uint32_t) * cap));
     for (int k = MID; k < NCLS; ++k) TRY_CUDA_ST(cudaMalloc(&c->lists[0][k], sizeof(uint32_t) * cap));
@@ -200,6 +202,7 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
   a.low_bm = g.low_bm;
   a.rcp = g.rcp;
   a.ever = c->ever;
+  a.pf = c->pf;
   a.acc64 = c->acc64;
   a.acc32 = c->acc32;
   // expand by pulling once more than 1/16 of the vertices changed by > D
@@ -479,6 +482,10 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
     launch_state_reset(c->st, o.max_iterations, o.tolerance, s);
     launch_init_ranks(a, (mode == PRX_STATIC) ? nullptr : q_dev, dyn, s);
     c->launches += 2;
+    if (mode == PRX_PRUNE_DYNAMIC_FRONTIER && !refine) {
+      launch_prune_factor(a, s);
+      c->launches += 1;
+    }
     if (refine && dyn) {
       launch_init_ranks32(a, q_dev, s);
       TRY_CUDA_ST(cudaMemsetAsync(c->ever, 0, sizeof(uint32_t) * (((size_t)g.n + 31) / 32), s));

@@ -32,6 +32,7 @@ struct prx_context {
   uint32_t* xb = nullptr;
   uint32_t* naff = nullptr;
   uint32_t* ever = nullptr;   // FP32 dynamic phase: vertices updated at least once
+  double* pf = nullptr;       // DF-P: 1 / (1 - P/d) per vertex
   uint32_t* lists[2][NCLS] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   uint32_t* xl = nullptr;
   uint32_t* fr[3] = {nullptr, nullptr, nullptr};

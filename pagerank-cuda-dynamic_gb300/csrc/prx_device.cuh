@@ -111,6 +111,26 @@ __device__ __forceinline__ double div_count(double a, uint32_t d, double y) {
   return fma(r, y, q);
 }
 
+// RN(x / m) <= c and RN(x / m) > c for x >= 0, m >= 0 -- the comparisons of
+// a relative change with a tolerance -- decided by one multiplication unless
+// x lies within 2^-48 of c*m, where the quotient is formed as written.  Away
+// from that band the rounded quotient is on the same side of c as the exact
+// one (the product's rounding is < 2^-52 relative), so the result always
+// equals the comparison of the correctly rounded quotient, NaN (0/0)
+// included.
+__device__ __forceinline__ bool quot_le(double x, double m, double c) {
+  const double cm = c * m;
+  if (x < cm * (1.0 - 0x1p-48)) return true;
+  if (x > cm * (1.0 + 0x1p-48)) return false;
+  return x / m <= c;
+}
+__device__ __forceinline__ bool quot_gt(double x, double m, double c) {
+  const double cm = c * m;
+  if (x > cm * (1.0 + 0x1p-48)) return true;
+  if (x < cm * (1.0 - 0x1p-48)) return false;
+  return x / m > c;
+}
+
 // Sum of c[edg[j]] for j in [s, e) added front to back onto acc.  The edge
 // ids are read as aligned 16-byte groups of four (edg must be 16-byte
 // aligned and allocated per edge_slots); ids outside [s, e) in the first and

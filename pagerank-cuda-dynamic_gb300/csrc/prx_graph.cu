@@ -146,6 +146,13 @@ __global__ void k_selftest_div(uint32_t dmax, uint32_t per, unsigned long long* 
     const double a = __longlong_as_double((long long)(((uint64_t)ex << 52) | (z & 0xFFFFFFFFFFFFFull)));
     const double y = 1.0 / (double)d;
     if (dbits(div_count(a, d, y)) != dbits(a / (double)d)) ++mine;
+    // the tolerance comparisons of a relative change, around their tie band:
+    // x = c*m*(1 + t 2^-50) for t in [-2^8, 2^8), c = 1e-6 * (1 + small)
+    const double m = a;
+    const double c = 1e-6 * (1.0 + (double)(z & 0xffff) * 0x1p-20);
+    const double t = (double)((int)((z >> 16) & 0x1ff) - 256);
+    const double x = c * m * (1.0 + t * 0x1p-50);
+    if (quot_le(x, m, c) != (x / m <= c) || quot_gt(x, m, c) != (x / m > c)) ++mine;
   }
   if (mine) atomicAdd(bad, mine);
 }

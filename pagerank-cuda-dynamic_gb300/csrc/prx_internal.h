@@ -134,6 +134,7 @@ struct SolveArgs {
   const uint32_t* low_bm;         // LOW-class bitmap
   const double* rcp;              // RN(1 / outdeg)
   uint32_t* ever;                 // FP32 dynamic phase: vertices updated at least once
+  double* pf;                     // DF-P: 1 / (1 - P/d) per vertex (launch_prune_factor)
   double* acc64;                  // partial row sums carried between chunk passes (FP64)
   float* acc32;                   // the same for the FP32 sweeps
   State* st;
@@ -147,6 +148,8 @@ struct SolveArgs {
 void launch_init_ranks(const SolveArgs& a, const double* q, bool dynamic, cudaStream_t s);
 // FP32 dynamic phase: e[0] = e[1] = (float)q, ce = e / outdeg.
 void launch_init_ranks32(const SolveArgs& a, const double* q, cudaStream_t s);
+// DF-P: the per-vertex factor 1 / (1 - P/d) of the closed-form update, into pf.
+void launch_prune_factor(const SolveArgs& a, cudaStream_t s);
 // After it: r[0] = (double)e[parity] where `ever` is set (else q, already in
 // r[0]), c[0] = r[0] / outdeg; then the control block is reopened for the
 // FP64 refinement (done only if the iteration cap was reached).

@@ -102,17 +102,17 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
     mag = max(mag, __float_as_uint(fabsf(av)));
     survive = true;
     changed = false;
-    if (T::FRONTIER) {
-      const float rel = ev / fmaxf(rv, av);
-      if (T::PRUNE && rel <= (float)a.C) survive = false;
-      changed = rel > (float)a.D;
+    if (T::FRONTIER) {  // relative change against the tolerances, without the division
+      const float m = fmaxf(rv, av);
+      if (T::PRUNE && ev <= (float)a.C * m) survive = false;
+      changed = ev > (float)a.D * m;
     }
     return dbits((double)ev);
   } else {
     const double y = a.rcp[v];
     const double rv = a.r[p][v];
     double av;
-    if (T::PRUNE) av = fma(a.P, cv - div_count(rv, d, y), a.C0) * (1 / (1 - div_count(a.P, d, y)));
+    if (T::PRUNE) av = fma(a.P, cv - div_count(rv, d, y), a.C0) * a.pf[v];  // pf: 1 / (1 - P/d)
     else          av = fma(a.P, cv, a.C0);
     const double ev = fabs(av - rv);
     a.r[p ^ 1][v] = av;
@@ -127,10 +127,10 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
     }
     survive = true;
     changed = false;
-    if (T::FRONTIER) {
-      const double rel = ev / fmax(rv, av);
-      if (T::PRUNE && rel <= a.C) survive = false;  // :106
-      changed = rel > a.D;                          // :107
+    if (T::FRONTIER) {  // rel = ev / max(rv, av) compared with C and D
+      const double m = fmax(rv, av);
+      if (T::PRUNE && quot_le(ev, m, a.C)) survive = false;  // :106
+      changed = quot_gt(ev, m, a.D);                          // :107
     }
     return dbits(ev);
   }
@@ -483,6 +483,17 @@ __global__ void k_init_ranks32(SolveArgs a, const double* __restrict__ q) {
     a.e[0][v] = a.e[1][v] = r;
     a.ce[0][v] = a.ce[1][v] = c;
   }
+}
+
+// The DF-P factor with the same operations as the reference's
+// (1 / (1 - P/d)) inline in the update (:104), so its bits are the same.
+__global__ void k_prune_factor(SolveArgs a) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x)
+    a.pf[v] = 1 / (1 - div_count(a.P, a.xtdat[v], a.rcp[v]));
+}
+
+void launch_prune_factor(const SolveArgs& a, cudaStream_t s) {
+  k_prune_factor<<<cap_grid((a.n + kThreads - 1) / kThreads, 152 * 16), kThreads, 0, s>>>(a);
 }
 
 void launch_init_ranks32(const SolveArgs& a, const double* q, cudaStream_t s) {
