@@ -216,6 +216,78 @@ __global__ void k_chunk_scatter(const uint32_t* __restrict__ xtoff, const uint32
   }
 }
 
+// Scatter for K <= kScatterK chunks, coalesced: a warp takes 32 consecutive
+// rows (lane i: row v0+i), whose edges are one contiguous range, and walks it
+// 32 edges at a time.  Each edge finds its row by a binary search over the
+// lanes' row starts (the last row starting at or before it: empty rows are
+// skipped that way) and its destination -- chunk k's piece of the row, which
+// is a consecutive run since rows are sorted by source -- by shuffles from
+// that row's lane.  Edges of non-LOW rows are read and dropped.
+constexpr int kScatterK = 8;
+__global__ void __launch_bounds__(256) k_chunk_scatter_w(const uint32_t* __restrict__ xtoff,
+                                                         const uint32_t* __restrict__ xtedg,
+                                                         const uint32_t* __restrict__ low_bm, uint32_t n,
+                                                         uint32_t width, int K, const uint32_t* __restrict__ off,
+                                                         uint32_t* __restrict__ edg) {
+  const size_t row = (size_t)n + 1;
+  const uint32_t lane = lane_id();
+  const uint32_t groups = (n + 31) >> 5;
+  for (uint32_t gi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gi < groups;
+       gi += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t v = (gi << 5) + lane;
+    const uint32_t s = xtoff[min(v, n)];
+    const uint32_t end = xtoff[min((gi << 5) + 32u, n)];
+    const bool low = v < n && ((low_bm[v >> 5] >> (v & 31u)) & 1u);
+    uint32_t dst[kScatterK], rs[kScatterK];
+    uint32_t run = 0;
+#pragma unroll
+    for (int k = 0; k < kScatterK; ++k) {
+      dst[k] = 0;
+      rs[k] = run;
+      if (low && k < K) {
+        dst[k] = off[k * row + v];
+        run += off[k * row + v + 1] - dst[k];
+      }
+    }
+    // four 32-edge windows per step, their loads issued together
+    for (uint32_t base = __shfl_sync(0xffffffffu, s, 0); base < end; base += 128) {
+      uint32_t uu[4];
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const uint32_t j = base + 32u * w + lane;
+        uu[w] = j < end ? __ldg(xtedg + j) : 0u;
+      }
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const uint32_t j = base + 32u * w + lane;
+        uint32_t r = 0;
+#pragma unroll
+        for (int step = 16; step; step >>= 1) {
+          const uint32_t cand = r + step;
+          if (__shfl_sync(0xffffffffu, s, cand) <= j) r = cand;
+        }
+        const bool rlow = __shfl_sync(0xffffffffu, (int)low, r) != 0;
+        const uint32_t sr = __shfl_sync(0xffffffffu, s, r);
+        const bool act = j < end && rlow;
+        const uint32_t u = uu[w];
+        const uint32_t k = act ? u / width : 0u;
+        uint32_t d = 0, rr = 0;
+#pragma unroll
+        for (int kk = 0; kk < kScatterK; ++kk) {
+          if (kk >= K) break;
+          const uint32_t dk = __shfl_sync(0xffffffffu, dst[kk], r);
+          const uint32_t rk = __shfl_sync(0xffffffffu, rs[kk], r);
+          if (k == (uint32_t)kk) {
+            d = dk;
+            rr = rk;
+          }
+        }
+        if (act) edg[d + (j - sr - rr)] = u;
+      }
+    }
+  }
+}
+
 void free_chunks(GraphDev& g) {
   for (auto& l : g.lay) {
     cudaFree(l.off);
@@ -251,7 +323,9 @@ cudaError_t ensure_chunks(GraphDev& g, uint32_t width, uint32_t keep, int sms, c
   k_chunk_count<<<grid, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, g.n, width, K, l.off);
   e = exclusive_scan_u32(l.off, (uint32_t)len, s);
   if (e == cudaSuccess) {
-    k_chunk_scatter<<<grid, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, g.n, width, K, l.off, l.edg);
+    if (K <= kScatterK)
+      k_chunk_scatter_w<<<grid, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, g.n, width, K, l.off, l.edg);
+    else k_chunk_scatter<<<grid, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, g.n, width, K, l.off, l.edg);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) {
