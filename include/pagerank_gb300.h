@@ -266,6 +266,28 @@ int prx_adjoint(prx_context* ctx, prx_graph* g, const double* t, const double* r
                 const prx_options* o, double* lambda, double* grad_w, double* grad_t, double* grad_alpha,
                 prx_result* res);
 
+/* ---- autotuning (no counterpart in the reference) ---------------------- */
+
+typedef struct {
+  uint32_t mid_max;           /* in-degree above which a vertex gets a block, not a warp */
+  uint32_t chunk_vertices64;  /* source-chunk width of the FP64 sweeps (>= n: none)    */
+  uint32_t chunk_vertices32;  /* the same for the FP32 sweeps of PRX_FP32_REFINE        */
+  float    ms_per_iteration64;
+  float    ms_per_iteration32;
+  int      trials;            /* trial solves run (0 when taken from the cache)         */
+  int      cached;            /* 1: picks reused for a graph of the same signature      */
+} prx_tune_result;
+
+/* Times short Static solves on g (FP64 and FP32 refinement, 3 iterations
+ * each, best of two) over the MID / HIGH in-degree boundary (1024, 4096,
+ * 16384) and the source-chunk widths (none, 200/128/64 MB of FP64
+ * contributions, 96/48/24 MB of FP32 ones), and keeps the fastest on g: later
+ * solves with chunk_vertices = 0 use them.  Results do not depend on these
+ * parameters.  Picks are cached per graph signature (n, m, in-degree class
+ * sizes) in the process and, when cache_path is not NULL, in that text file
+ * (read before, rewritten after). */
+int prx_autotune(prx_context* ctx, prx_graph* g, const char* cache_path, prx_tune_result* out);
+
 /* Diagnostic with no counterpart in the reference: counts, on the context's
  * device, the dividends a and out-degrees d (d = 1 .. dmax, `per` values of a
  * per d, spread over 2^-40 .. 2^2) for which the library's three-operation

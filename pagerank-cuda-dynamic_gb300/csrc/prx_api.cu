@@ -464,8 +464,12 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   // FP64 sweep (bound by GB300's FP64 add rate as much as by HBM) gains from
   // two chunks only (200 MB of contributions each), the FP32 sweep from
   // 48 MB chunks.
-  const uint32_t w64 = o.chunk_vertices ? o.chunk_vertices : (200u << 20) / sizeof(double);
-  const uint32_t w32 = o.chunk_vertices ? o.chunk_vertices : (48u << 20) / sizeof(float);
+  const uint32_t w64 = o.chunk_vertices ? o.chunk_vertices
+                      : g.tuned_w64          ? g.tuned_w64
+                                             : (200u << 20) / sizeof(double);
+  const uint32_t w32 = o.chunk_vertices ? o.chunk_vertices
+                      : g.tuned_w32          ? g.tuned_w32
+                                             : (48u << 20) / sizeof(float);
   const ChunkLayout *lay64 = nullptr, *lay32 = nullptr;
   TRY_CUDA_ST(ensure_chunks(gr->g, w64, refine ? w32 : w64, c->sms, c->stream, &lay64));
   if (refine) TRY_CUDA_ST(ensure_chunks(gr->g, w32, w64, c->sms, c->stream, &lay32));

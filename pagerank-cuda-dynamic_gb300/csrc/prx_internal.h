@@ -88,6 +88,8 @@ struct GraphDev {
   uint32_t cls_begin[NCLS + 1] = {0, 0, 0, 0};
   uint64_t cls_edges[NCLS] = {0, 0, 0};  // in-edges per class
   uint32_t mid_max = kDefaultMidMax;
+  uint32_t tuned_w64 = 0;         // source-chunk widths picked by prx_autotune (0: library default)
+  uint32_t tuned_w32 = 0;
   uint32_t* low_bm = nullptr;     // bitmap of the LOW class
   double* rcp = nullptr;          // RN(1 / outdeg) per vertex, for div_count
   float* rcp32 = nullptr;         // the same in FP32 (personalized PageRank sweeps)

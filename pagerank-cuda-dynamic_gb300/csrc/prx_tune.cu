@@ -1,0 +1,175 @@
+// prx_tune.cu -- autotuner for the execution parameters that do not change
+// results: the MID / HIGH in-degree boundary (warp or block per vertex, both
+// in the reference's 256-way order) and the source-chunk widths of the FP64
+// and FP32 sweeps of the in-degree <= 64 rows.  No counterpart in the
+// reference, which uses fixed thresholds (inc/pagerankCuda.hxx:625-638).
+//
+// Each candidate is timed by short solves on the graph itself (Static, 3
+// iterations, FP64 or FP32 refinement, the default loop), best of two.  The
+// picks are stored on the graph and cached per graph signature (n, m and the
+// in-degree class sizes), in the process and optionally in a text file, so a
+// graph of the same shape built again is tuned without trials.
+#include <algorithm>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+#include "prx_ctx.h"
+
+namespace {
+
+struct Pick {
+  uint32_t mid_max, w64, w32;
+  float ms64, ms32;
+};
+
+std::mutex g_tune_mu;
+std::map<std::string, Pick> g_tune_cache;
+
+std::string signature(const GraphDev& g) {
+  char buf[160];
+  snprintf(buf, sizeof buf, "n%u_m%llu_low%u_%llu", g.n, (unsigned long long)g.m, g.cls_begin[1] - g.cls_begin[0],
+           (unsigned long long)g.cls_edges[LOW]);
+  return buf;
+}
+
+void load_file(const char* path) {
+  if (!path) return;
+  FILE* f = fopen(path, "r");
+  if (!f) return;
+  char key[160];
+  Pick p{};
+  while (fscanf(f, "%159s %u %u %u %f %f", key, &p.mid_max, &p.w64, &p.w32, &p.ms64, &p.ms32) == 6)
+    g_tune_cache[key] = p;
+  fclose(f);
+}
+
+void save_file(const char* path) {
+  if (!path) return;
+  FILE* f = fopen(path, "w");
+  if (!f) return;
+  for (const auto& kv : g_tune_cache)
+    fprintf(f, "%s %u %u %u %.4f %.4f\n", kv.first.c_str(), kv.second.mid_max, kv.second.w64, kv.second.w32,
+            kv.second.ms64, kv.second.ms32);
+  fclose(f);
+}
+
+// ms per iteration of a short Static solve (best of two), or < 0 on error.
+float trial(prx_context* c, prx_graph* gr, double* ranks, int precision, uint32_t width, int* status) {
+  prx_options o;
+  prx_options_default(&o);
+  o.max_iterations = 3;
+  o.precision = precision;
+  o.chunk_vertices = width;
+  o.tolerance = 0.0;  // run all three iterations
+  float best = -1.f;
+  for (int rep = 0; rep < 2; ++rep) {
+    prx_result r{};
+    const int st = prx_solve_device(c, gr, PRX_STATIC, nullptr, nullptr, 0, nullptr, nullptr, 0, nullptr, &o, ranks, &r);
+    if (st) {
+      *status = st;
+      return -1.f;
+    }
+    const float ms = r.computation_time_ms / (r.iterations ? r.iterations : 1);
+    if (best < 0 || ms < best) best = ms;
+  }
+  return best;
+}
+
+}  // namespace
+
+extern "C" {
+
+int prx_autotune(prx_context* c, prx_graph* gr, const char* cache_path, prx_tune_result* out) {
+  if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_autotune: bad context or graph");
+  GraphDev& g = gr->g;
+  prx_tune_result res{};
+  res.mid_max = g.mid_max;
+  if (g.n == 0) {
+    if (out) *out = res;
+    return PRX_OK;
+  }
+  TRY_CUDA_ST(cudaSetDevice(c->device));
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  load_file(cache_path);
+  const std::string key = signature(g);
+  auto it = g_tune_cache.find(key);
+  if (it != g_tune_cache.end()) {
+    const Pick& p = it->second;
+    if (p.mid_max != g.mid_max) {
+      g.mid_max = p.mid_max;
+      TRY_CUDA_ST(build_classes(g, c->sms, c->stream));
+      TRY_CUDA_ST(cudaStreamSynchronize(c->stream));
+    }
+    g.tuned_w64 = p.w64;
+    g.tuned_w32 = p.w32;
+    res = {p.mid_max, p.w64, p.w32, p.ms64, p.ms32, 0, 1};
+    if (out) *out = res;
+    return PRX_OK;
+  }
+  double* ranks = nullptr;
+  TRY_CUDA_ST(cudaMalloc(&ranks, sizeof(double) * g.n));
+  int st = PRX_OK, trials = 0;
+  // 1. MID / HIGH boundary, with the default chunk widths
+  const uint32_t mids[] = {1024u, 4096u, 16384u};
+  uint32_t best_mid = g.mid_max;
+  float best = -1.f;
+  for (uint32_t mm : mids) {
+    if (g.mid_max != mm) {
+      g.mid_max = mm;
+      if (build_classes(g, c->sms, c->stream) != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        st = PRX_ECUDA;
+        break;
+      }
+    }
+    const float ms = trial(c, gr, ranks, PRX_FP64, 0, &st);
+    ++trials;
+    if (st) break;
+    if (best < 0 || ms < best) {
+      best = ms;
+      best_mid = mm;
+    }
+  }
+  if (!st && g.mid_max != best_mid) {
+    g.mid_max = best_mid;
+    if (build_classes(g, c->sms, c->stream) != cudaSuccess || cudaStreamSynchronize(c->stream) != cudaSuccess)
+      st = PRX_ECUDA;
+  }
+  // 2. source-chunk widths: no chunking and chunks of 200, 128, 64 MB (FP64)
+  //    or 96, 48, 24 MB (FP32) of contributions
+  uint32_t w64 = 0, w32 = 0;
+  float ms64 = -1.f, ms32 = -1.f;
+  if (!st) {
+    g.tuned_w64 = g.tuned_w32 = 0;
+    const uint32_t c64[] = {g.n, (200u << 20) / 8, (128u << 20) / 8, (64u << 20) / 8};
+    const uint32_t c32[] = {g.n, (96u << 20) / 4, (48u << 20) / 4, (24u << 20) / 4};
+    for (int pass = 0; pass < 2 && !st; ++pass) {
+      const uint32_t* cand = pass ? c32 : c64;
+      float& bms = pass ? ms32 : ms64;
+      uint32_t& bw = pass ? w32 : w64;
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t w = cand[k];
+        if (k > 0 && w >= g.n) continue;  // the same as no chunking
+        const float ms = trial(c, gr, ranks, pass ? PRX_FP32_REFINE : PRX_FP64, w, &st);
+        ++trials;
+        if (st) break;
+        if (bms < 0 || ms < bms) {
+          bms = ms;
+          bw = w;
+        }
+      }
+    }
+  }
+  cudaFree(ranks);
+  if (st) return st;
+  g.tuned_w64 = w64;
+  g.tuned_w32 = w32;
+  g_tune_cache[key] = {g.mid_max, w64, w32, ms64, ms32};
+  save_file(cache_path);
+  res = {g.mid_max, w64, w32, ms64, ms32, trials, 0};
+  if (out) *out = res;
+  return PRX_OK;
+}
+
+}  // extern "C"

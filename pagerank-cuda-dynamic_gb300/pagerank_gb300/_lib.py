@@ -51,6 +51,15 @@ class PprResult(C.Structure):
     as_dict = Result.as_dict
 
 
+class TuneResult(C.Structure):
+    """prx_tune_result (autotuner picks; no counterpart in the reference)."""
+    _fields_ = [("mid_max", C.c_uint32), ("chunk_vertices64", C.c_uint32), ("chunk_vertices32", C.c_uint32),
+                ("ms_per_iteration64", C.c_float), ("ms_per_iteration32", C.c_float), ("trials", C.c_int),
+                ("cached", C.c_int)]
+
+    as_dict = Result.as_dict
+
+
 class HostCsr(C.Structure):
     _fields_ = [("n", C.c_uint32), ("m", C.c_uint64), ("off", C.POINTER(C.c_uint32)),
                 ("edg", C.POINTER(C.c_uint32))]
@@ -69,7 +78,7 @@ EXPORTS = (
     "prx_graph_download",
     "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_selftest_division",
     "prx_solve_ppr_batched", "prx_solve_ppr_batched_device", "prx_graph_set_weights", "prx_solve_weighted",
-    "prx_adjoint",
+    "prx_adjoint", "prx_autotune",
     "prx_host_csr_free",
     "prx_gen_rmat", "prx_gen_weblike", "prx_gen_grid", "prx_gen_batch", "prx_host_tidy_batch",
     "prx_host_apply_batch", "prx_host_transpose", "prx_host_free",
@@ -114,6 +123,7 @@ def load(build_if_missing=True):
         "prx_solve_ppr_batched_device": (i32, [vp, vp, C.c_uint32, vp, vp, C.POINTER(Options), vp,
                                                C.POINTER(PprResult)]),
         "prx_graph_set_weights": (i32, [vp, vp, vp]),
+        "prx_autotune": (i32, [vp, vp, C.c_char_p, C.POINTER(TuneResult)]),
         "prx_solve_weighted": (i32, [vp, vp, vp, vp, C.POINTER(Options), vp, C.POINTER(Result)]),
         "prx_adjoint": (i32, [vp, vp, vp, vp, vp, C.POINTER(Options), vp, vp, vp, C.POINTER(dbl),
                               C.POINTER(Result)]),

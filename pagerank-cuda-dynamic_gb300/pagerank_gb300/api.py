@@ -16,7 +16,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import Options, PprResult, Result, check, load
+from ._lib import Options, PprResult, Result, TuneResult, check, load
 
 
 def options(**kw):
@@ -205,6 +205,15 @@ def solve_ppr_batched_device(ctx, g, seed_sets, ranks_ptr, opts=None):
     check(load().prx_solve_ppr_batched_device(ctx.handle, g.handle, len(off) - 1, off.ctypes.data, _p(seeds),
                                               C.byref(opts or options()), ranks_ptr, C.byref(res)),
           "prx_solve_ppr_batched_device")
+    return res.as_dict()
+
+
+def autotune(ctx, g, cache_path=None):
+    """Pick the MID / HIGH boundary and source-chunk widths for g by trial
+    solves (prx_autotune) -> dict of the picks."""
+    res = TuneResult()
+    path = None if cache_path is None else str(cache_path).encode()
+    check(load().prx_autotune(ctx.handle, g.handle, path, C.byref(res)), "prx_autotune")
     return res.as_dict()
 
 

@@ -258,3 +258,32 @@ def test_reciprocal_division_matches_ieee(pg, ctx):
     # sparser sweep of large out-degrees.
     assert pg.selftest_division(ctx, 1 << 17, 256) == 0
     assert pg.selftest_division(ctx, 1 << 24, 4) == 0
+
+
+def test_autotune_keeps_results_and_caches(pg, ctx, tmp_path):
+    # the tuner only picks execution parameters: ranks and iteration counts
+    # stay the oracle's; a graph of the same signature reuses the picks, also
+    # through the cache file
+    xoff, xedg = _synthetic(pg, "hubs")
+    m = len(xedg)
+    batch = pg.graphs.random_batch(xoff, xedg, max(1, int(2e-4 * m)), max(1, int(8e-4 * m)), seed=37)
+    xt = O.transpose(xoff, xedg)
+    q, _ = O.solve("static", None, None, *xt)
+    yoff, yedg = pg.graphs.apply_batch(xoff, xedg, *batch)
+    yt = O.transpose(yoff, yedg)
+    g, _ = _graph(pg, ctx, yoff, yedg, yt)
+    path = tmp_path / "tune.txt"
+    t = pg.autotune(ctx, g, path)
+    assert t["trials"] > 0 and t["cached"] == 0 and t["mid_max"] in (1024, 4096, 16384)
+    for mode in MODES:
+        want, it_w = _oracle(mode, yoff, yedg, yt, batch, q)
+        got, res = _gpu(pg, ctx, g, mode, batch, q)
+        assert res["iterations"] == it_w, mode
+        np.testing.assert_array_equal(got, want, err_msg=mode)
+    g2, _ = _graph(pg, ctx, yoff, yedg, yt)
+    t2 = pg.autotune(ctx, g2)
+    assert t2["cached"] == 1 and t2["trials"] == 0 and t2["mid_max"] == t["mid_max"]
+    lines = path.read_text().split()
+    assert len(lines) >= 6 and int(lines[1]) == t["mid_max"]
+    g2.close()
+    g.close()
