@@ -237,6 +237,75 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m):
+    import numpy as np
+    import torch
+    dev = f"cuda:{local}"
+    sizes = (1e-5, 1e-4, 1e-3)
+    parts = [(sz, int(sz * m)) for sz in sizes for _ in range(3)]
+    nd_all = sum(c // 5 for _, c in parts)
+    ni_all = sum(c - c // 5 for _, c in parts)
+    du, dv, iu, iv = pg.graphs.random_batch(xoff, xedg, nd_all, ni_all, seed=args.seed + 1)
+    rng = np.random.default_rng(args.seed + 2)
+    pd, pi = rng.permutation(len(du)), rng.permutation(len(iu))
+    lo = loop_opts(pg, args)
+    o32 = lo(precision=pg.FP32_REFINE)
+    q = ranks.clone()
+    out = torch.empty_like(q)
+    rows = []
+    od = oi = 0
+    for sz, cnt in parts:
+        kd = np.sort(pd[od:od + cnt // 5])
+        ki = np.sort(pi[oi:oi + cnt - cnt // 5])
+        od += cnt // 5
+        oi += cnt - cnt // 5
+        b = (du[kd], dv[kd], iu[ki], iv[ki])
+        t = time.perf_counter()
+        g.apply_batch(*b)
+        apply_ms = (time.perf_counter() - t) * 1e3
+        bt = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint32).view(np.int32)).to(dev) for a in b]
+        bp = (bt[0].data_ptr(), bt[1].data_ptr(), len(kd), bt[2].data_ptr(), bt[3].data_ptr(), len(ki))
+        row = {"size": sz, "deletions": int(len(kd)), "insertions": int(len(ki)), "apply_ms": apply_ms}
+        r = pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr(), opts=lo())
+        row["static"] = {"ms": r["time_ms"], "iterations": r["iterations"]}
+        for name, mode, o in (("nd", pg.NAIVE_DYNAMIC, lo()), ("dt", pg.DYNAMIC_TRAVERSAL, lo()),
+                              ("df", pg.DYNAMIC_FRONTIER, lo()), ("dfp", pg.PRUNE_DYNAMIC_FRONTIER, lo()),
+                              ("df_fp32_refine", pg.DYNAMIC_FRONTIER, o32),
+                              ("dfp_fp32_refine", pg.PRUNE_DYNAMIC_FRONTIER, o32)):
+            pg.solve_device(ctx, g, mode, q.data_ptr(), out.data_ptr(), bp, opts=o)
+            r = pg.solve_device(ctx, g, mode, q.data_ptr(), out.data_ptr(), bp, opts=o)
+            row[name] = {"ms": r["time_ms"], "iterations": r["iterations"], "marking_ms": r["marking_time_ms"],
+                         "affected_initial": r["affected_initial"], "edges": r["edges_processed"],
+                         "speedup_vs_static": row["static"]["ms"] / r["time_ms"],
+                         "linf_vs_static": float((out - ranks).abs().max())}
+            if name == "dfp":
+                out64 = out.clone()
+            if name == "dfp_fp32_refine":
+                row[name]["linf_vs_dfp_fp64"] = float((out - out64).abs().max())
+                row[name]["speedup_vs_dfp_fp64"] = row["dfp"]["ms"] / r["time_ms"]
+        rows.append(row)
+        log(f"batch {sz:g}: " + ", ".join(f"{k} {row[k]['ms']:.1f} ms" for k in
+                                          ("static", "nd", "dt", "df", "dfp", "dfp_fp32_refine")))
+        q.copy_(ranks)  # the next batch starts from this graph's converged ranks
+    summary = {}
+    for sz in sizes:
+        rs = [x for x in rows if x["size"] == sz]
+        summary[f"{sz:g}"] = {k: statistics.median(x[k]["speedup_vs_static"] for x in rs)
+                              for k in ("nd", "dt", "df", "dfp", "df_fp32_refine", "dfp_fp32_refine")}
+    first = next(x for x in rows if x["size"] == 1e-4)
+    d, d32 = first["dfp"], first["dfp_fp32_refine"]
+    dfp = {"batch": {"deletions": first["deletions"], "insertions": first["insertions"]},
+           "apply_ms": first["apply_ms"], "dfp_ms": d["ms"], "dfp_iterations": d["iterations"],
+           "dfp_marking_ms": d["marking_ms"], "dfp_affected_initial": d["affected_initial"],
+           "dfp_edges": d["edges"], "df_ms": first["df"]["ms"], "static_ms": first["static"]["ms"],
+           "dfp_speedup_vs_static": d["speedup_vs_static"], "df_speedup_vs_static": first["df"]["speedup_vs_static"],
+           "dfp_linf_vs_static": d["linf_vs_static"], "dfp_fp32_refine_ms": d32["ms"],
+           "dfp_fp32_refine_speedup_vs_dfp_fp64": d32["speedup_vs_dfp_fp64"],
+           "dfp_fp32_refine_speedup_vs_static": d32["speedup_vs_static"],
+           "dfp_fp32_refine_linf_vs_dfp_fp64": d32["linf_vs_dfp_fp64"]}
+    return {"batches": rows, "median_speedup_vs_static": summary}, dfp
+
+
 def run_grid(args, pg, ctx, local):
     """High-diameter road-like graph: side x side grid, 4-neighbour edges both
     ways, 5% random diagonal shortcuts, self-loops; Static, then one batch of
@@ -488,49 +557,13 @@ def run_ours(args):
     e2e_value = ws * m * statistics.median(e2e_it) / (e2e_ms_max / 1e3) / 1e9
     log(f"e2e: {e2e_ms} ms")
 
-    # ---- DF-P after one 1e-4|E| batch applied on the device ------------------
-    dfp = None
+    # ---- dynamic modes over consecutive batches applied on the device ----------
+    # Batch sizes 1e-5, 1e-4, 1e-3 |E| (80% insertions), three consecutive
+    # batches each: one tidy batch drawn from the original graph, split into
+    # nine disjoint sorted parts, so every part is tidy for the graph it meets.
+    dfp = dynamic = None
     if not args.no_dfp:
-        q = ranks.clone()
-        size = int(1e-4 * m)
-        du, dv, iu, iv = pg.graphs.random_batch(xoff, xedg, size // 5, size - size // 5, seed=args.seed + 1)
-        t = time.perf_counter()
-        g.apply_batch(du, dv, iu, iv)
-        apply_ms = (time.perf_counter() - t) * 1e3
-        bt = [torch.from_numpy(np.asarray(a, dtype=np.uint32).view(np.int32)).to(f"cuda:{local}")
-              for a in (du, dv, iu, iv)]
-        out = torch.empty_like(q)
-        bp = (bt[0].data_ptr(), bt[1].data_ptr(), len(du), bt[2].data_ptr(), bt[3].data_ptr(), len(iu))
-        lo = loop_opts(pg, args)
-        r_dfp = pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=lo())
-        r_df = pg.solve_device(ctx, g, pg.DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=lo())
-        r_st = pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr(), opts=lo())
-        r_dfp2 = pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp,
-                                 opts=lo())
-        err = float((out - ranks).abs().max())
-        out64 = out.clone()
-        # the same with FP32 ranks and FP64 refinement (DF-P, DF)
-        o32 = lo(precision=pg.FP32_REFINE)
-        pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=o32)
-        r_dfp32 = pg.solve_device(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=o32)
-        err32_dfp = float((out - out64).abs().max())
-        err32_static = float((out - ranks).abs().max())
-        r_df32 = pg.solve_device(ctx, g, pg.DYNAMIC_FRONTIER, q.data_ptr(), out.data_ptr(), bp, opts=o32)
-        dfp = {"batch": {"deletions": len(du), "insertions": len(iu)}, "apply_ms": apply_ms,
-               "dfp_ms": r_dfp2["time_ms"], "dfp_iterations": r_dfp2["iterations"],
-               "dfp_marking_ms": r_dfp2["marking_time_ms"], "dfp_computation_ms": r_dfp2["computation_time_ms"],
-               "dfp_affected_initial": r_dfp2["affected_initial"], "dfp_edges": r_dfp2["edges_processed"],
-               "df_ms": r_df["time_ms"], "df_iterations": r_df["iterations"],
-               "static_ms": r_st["time_ms"], "static_iterations": r_st["iterations"],
-               "dfp_speedup_vs_static": r_st["time_ms"] / max(r_dfp2["time_ms"], 1e-9),
-               "df_speedup_vs_static": r_st["time_ms"] / max(r_df["time_ms"], 1e-9),
-               "dfp_linf_vs_static": err,
-               "dfp_fp32_refine_ms": r_dfp32["time_ms"], "dfp_fp32_refine_iterations": r_dfp32["iterations"],
-               "dfp_fp32_refine_speedup_vs_dfp_fp64": r_dfp2["time_ms"] / r_dfp32["time_ms"],
-               "dfp_fp32_refine_speedup_vs_static": r_st["time_ms"] / r_dfp32["time_ms"],
-               "dfp_fp32_refine_linf_vs_dfp_fp64": err32_dfp, "dfp_fp32_refine_linf_vs_static": err32_static,
-               "df_fp32_refine_ms": r_df32["time_ms"],
-               "df_fp32_refine_speedup_vs_df_fp64": r_df["time_ms"] / r_df32["time_ms"]}
+        dynamic, dfp = run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m)
         log(f"dfp: {dfp}")
 
     ppr = adj = grid = None
@@ -557,7 +590,7 @@ def run_ours(args):
                "e2e": {"value": e2e_value, "unit": "GE/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "ms_per_step": e2e_ms_max},
                "roofline": roofline, "clocks": clk.summary(), "fp32_refine": fp32, "dfp": dfp,
-               "autotune": tune, "grid": grid, "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
+               "dynamic": dynamic, "autotune": tune, "grid": grid, "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     g.close()
     ctx.close()
