@@ -83,6 +83,12 @@ def make_graph(args, pg):
     return xoff, xedg, xt
 
 
+def replica_value(ws, edges, iterations, ms):
+    """Whole-job GE/s of ws replicas, each solving its own copy of a graph of
+    `edges` edges for `iterations` sweeps in total, timed by the slowest (ms)."""
+    return ws * edges * iterations / (ms / 1e3) / 1e9
+
+
 def dist_setup(args):
     import torch
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -102,11 +108,13 @@ def barrier(ws):
 
 
 def max_over_ranks(ws, x):
+    """Largest x over the replicas (the slowest replica's time)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -484,7 +492,7 @@ def run_ours(args):
     barrier(ws)
     ms = max_over_ranks(ws, e0.elapsed_time(e1))
     iters = [r["iterations"] for r in results]
-    value = ws * m * sum(iters) / (ms / 1e3) / 1e9
+    value = replica_value(ws, m, sum(iters), ms)
     launches = int(sum(r["kernel_launches"] for r in results))
     # roofline of the dominant update kernel (FP64 algorithmic bytes: offsets 4,
     # previous + new rank 16 per vertex; index 4 + gathered contribution 8 per edge)
