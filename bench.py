@@ -256,6 +256,21 @@ def run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m):
     du, dv, iu, iv = pg.graphs.random_batch(xoff, xedg, nd_all, ni_all, seed=args.seed + 1)
     rng = np.random.default_rng(args.seed + 2)
     pd, pi = rng.permutation(len(du)), rng.permutation(len(iu))
+    # tidying a raw 1e-3 |E| batch (shuffled, 10% repeats) against this graph:
+    # on the device (prx_graph_tidy_batch) and on the host (the same rules)
+    kd, ki = pd[: int(2e-4 * m)], pi[: int(8e-4 * m)]
+    kd = np.concatenate([kd, kd[: len(kd) // 10]])
+    ki = np.concatenate([ki, ki[: len(ki) // 10]])
+    raw = (du[kd], dv[kd], iu[ki], iv[ki])
+    g.tidy_batch(*raw)
+    t0 = time.perf_counter()
+    tidy_dev = g.tidy_batch(*raw)
+    t1 = time.perf_counter()
+    tidy_host = pg.graphs.tidy_batch(xoff, xedg, *raw)
+    t2 = time.perf_counter()
+    tidy = {"raw_edges": int(len(kd) + len(ki)), "device_ms": (t1 - t0) * 1e3, "host_ms": (t2 - t1) * 1e3,
+            "same": all(np.array_equal(a, b) for a, b in zip(tidy_dev, tidy_host))}
+    log(f"tidy: {tidy}")
     lo = loop_opts(pg, args)
     o32 = lo(precision=pg.FP32_REFINE)
     q = ranks.clone()
@@ -311,7 +326,7 @@ def run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m):
            "dfp_fp32_refine_speedup_vs_dfp_fp64": d32["speedup_vs_dfp_fp64"],
            "dfp_fp32_refine_speedup_vs_static": d32["speedup_vs_static"],
            "dfp_fp32_refine_linf_vs_dfp_fp64": d32["linf_vs_dfp_fp64"]}
-    return {"batches": rows, "median_speedup_vs_static": summary}, dfp
+    return {"batches": rows, "median_speedup_vs_static": summary, "tidy": tidy}, dfp
 
 
 def run_grid(args, pg, ctx, local):

@@ -192,6 +192,18 @@ int prx_solve_device(prx_context* ctx, prx_graph* g, int mode,
                      const double* q, const prx_options* o,
                      double* ranks_out, prx_result* res);
 
+/* tidyBatchUpdateU (inc/batch.hxx:152-208), on the device: against graph g
+ * (created with its out-CSR, before the batch is applied), keep the
+ * deletions that exist and the insertions that do not, sort each list by
+ * (u, v) and drop duplicates.  Host arrays in and out; the outputs need room
+ * for nd / ni edges, and *out_nd / *out_ni receive the tidied lengths.  The
+ * result is what prx_graph_apply_batch takes. */
+int prx_graph_tidy_batch(prx_context* ctx, prx_graph* g,
+                         const uint32_t* del_u, const uint32_t* del_v, uint64_t nd,
+                         const uint32_t* ins_u, const uint32_t* ins_v, uint64_t ni,
+                         uint32_t* out_del_u, uint32_t* out_del_v, uint64_t* out_nd,
+                         uint32_t* out_ins_u, uint32_t* out_ins_v, uint64_t* out_ni);
+
 /* Run only the initial affected-vertex marking of a dynamic mode
  * (pagerankAffectedFrontierCuW :405-412 for DF / DF-P,
  * pagerankAffectedTraversalCuW :438-456 for DT) and copy the flags (n bytes,

@@ -1,0 +1,259 @@
+// prx_tidy.cu -- batch tidying on the device: the reference's
+// tidyBatchUpdateU (inc/batch.hxx:152-208), which runs on the host there:
+// keep the deletions that exist in the graph and the insertions that do not,
+// sort each list by (u, v) and drop duplicates.
+//
+//   1. existence: binary search of v in u's out-row (rows are ascending);
+//   2. keys: a kept deletion is its out-CSR position (the positions order
+//      like (u, v)); a kept insertion is u * 2^b + v with b = bits(n - 1);
+//   3. an LSD radix sort of the keys, 8-bit digits, stable (our own: per-block
+//      digit histograms, a digit-major scan, and a scatter that ranks equal
+//      digits in element order with __match_any_sync);
+//   4. unique: first occurrences kept (scan of flags), decoded back to (u, v).
+#include <algorithm>
+#include "prx_ctx.h"
+#include "prx_device.cuh"
+
+namespace prx {
+
+constexpr int kRadix = 256;
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;                       // elements per thread per tile
+constexpr int kSortTile = kSortThreads * kSortItems;
+
+// Position of edge (u, v) in the out-CSR, or UINT32_MAX.
+__device__ __forceinline__ uint32_t edge_position(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg,
+                                                  uint32_t u, uint32_t v) {
+  uint32_t lo = xoff[u], hi = xoff[u + 1];
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (xedg[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < xoff[u + 1] && xedg[lo] == v) ? lo : 0xffffffffu;
+}
+
+// keep[i] = 1 for kept edges; key[i] = the edge's sort key.
+__global__ void k_tidy_keys(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg,
+                            const uint32_t* __restrict__ u, const uint32_t* __restrict__ v, uint32_t count,
+                            int deletions, int vbits, uint32_t* __restrict__ keep,
+                            unsigned long long* __restrict__ key) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const uint32_t p = edge_position(xoff, xedg, u[i], v[i]);
+    if (deletions) {
+      keep[i] = p != 0xffffffffu;
+      key[i] = p;
+    } else {
+      keep[i] = p == 0xffffffffu;
+      key[i] = ((unsigned long long)u[i] << vbits) | v[i];
+    }
+  }
+}
+
+// out[pos[i]] = in[i] where flag[i] (pos: exclusive scan of flag).
+__global__ void k_compact64(const unsigned long long* __restrict__ in, const uint32_t* __restrict__ flag,
+                            const uint32_t* __restrict__ pos, uint32_t count, unsigned long long* __restrict__ out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+    if (flag[i]) out[pos[i]] = in[i];
+}
+
+// Radix pass, step 1: per-tile digit counts, digit-major: hist[d * tiles + b].
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long long* __restrict__ key,
+                                                             uint32_t count, int shift, uint32_t tiles,
+                                                             uint32_t* __restrict__ hist) {
+  __shared__ uint32_t cnt[kRadix];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t base = blockIdx.x * kSortTile;
+  for (int r = 0; r < kSortItems; ++r) {
+    const uint32_t i = base + r * kSortThreads + threadIdx.x;
+    if (i < count) atomicAdd(&cnt[(key[i] >> shift) & (kRadix - 1)], 1u);
+  }
+  __syncthreads();
+  hist[threadIdx.x * tiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// Radix pass, step 2 (after the scan of hist): stable scatter.  The tile's
+// elements go round by round (round r: elements r*256 + t); within a round an
+// element's rank among equal digits is the count in lower warps plus its rank
+// in its warp (__match_any_sync), so element order is kept.
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned long long* __restrict__ in,
+                                                                uint32_t count, int shift, uint32_t tiles,
+                                                                const uint32_t* __restrict__ start,
+                                                                unsigned long long* __restrict__ out) {
+  constexpr int kWarps = kSortThreads / 32;
+  __shared__ uint32_t base[kRadix];
+  __shared__ uint32_t wcnt[kWarps][kRadix];
+  const uint32_t t = threadIdx.x, w = t >> 5, lane = t & 31u;
+  base[t] = start[t * tiles + blockIdx.x];
+  for (int r = 0; r < kSortItems; ++r) {
+    for (int k = 0; k < kWarps; ++k) wcnt[k][t] = 0;
+    __syncthreads();
+    const uint32_t i = blockIdx.x * kSortTile + r * kSortThreads + t;
+    const bool act = i < count;
+    const unsigned long long x = act ? in[i] : 0ull;
+    const uint32_t d = act ? (uint32_t)((x >> shift) & (kRadix - 1)) : (uint32_t)kRadix;  // kRadix: none
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t below = __popc(peers & ((1u << lane) - 1u));
+    if (act && below == 0) wcnt[w][d] = __popc(peers);
+    __syncthreads();
+    if (act) {
+      uint32_t pos = base[d] + below;
+      for (uint32_t k = 0; k < w; ++k) pos += wcnt[k][d];
+      out[pos] = x;
+    }
+    __syncthreads();
+    uint32_t add = 0;
+    for (int k = 0; k < kWarps; ++k) add += wcnt[k][t];
+    base[t] += add;
+  }
+}
+
+// flag[i] = 1 for the first of equal adjacent keys.
+__global__ void k_first_flags(const unsigned long long* __restrict__ key, uint32_t count, uint32_t* __restrict__ flag) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+    flag[i] = (i == 0 || key[i] != key[i - 1]) ? 1u : 0u;
+}
+
+// Decode the unique keys at pos[i] (flag[i]) into (u, v).
+__global__ void k_decode(const unsigned long long* __restrict__ key, const uint32_t* __restrict__ flag,
+                         const uint32_t* __restrict__ pos, uint32_t count, int deletions, int vbits,
+                         const uint32_t* __restrict__ xoff, uint32_t n, const uint32_t* __restrict__ xedg,
+                         uint32_t* __restrict__ ou, uint32_t* __restrict__ ov) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    if (!flag[i]) continue;
+    const unsigned long long k = key[i];
+    uint32_t u, v;
+    if (deletions) {  // out-CSR position: v from the edge, u the row holding it
+      const uint32_t p = (uint32_t)k;
+      v = xedg[p];
+      uint32_t lo = 0, hi = n;  // last row whose start is <= p
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (xoff[mid] <= p) lo = mid;
+        else hi = mid - 1;
+      }
+      u = lo;
+    } else {
+      u = (uint32_t)(k >> vbits);
+      v = (uint32_t)(k & ((1ull << vbits) - 1));
+    }
+    ou[pos[i]] = u;
+    ov[pos[i]] = v;
+  }
+}
+
+static int grid_of(uint64_t work, int sms) {
+  const uint64_t b = (work + 255) / 256;
+  return (int)std::max<uint64_t>(1, std::min<uint64_t>(b, (uint64_t)sms * 16));
+}
+
+}  // namespace prx
+
+// Device buffers of one tidy call.
+struct TidyBufs {
+  uint32_t *u = nullptr, *v = nullptr, *flag = nullptr, *pos = nullptr, *hist = nullptr;
+  unsigned long long *key = nullptr, *key2 = nullptr;
+  void release() {
+    cudaFree(u); cudaFree(v); cudaFree(flag); cudaFree(pos); cudaFree(hist); cudaFree(key); cudaFree(key2);
+  }
+};
+
+// Tidy one list (deletions or insertions) of `count` edges from host arrays
+// into host arrays; *kept receives the tidied length.
+static int tidy_list(prx_context* c, const GraphDev& g, const uint32_t* hu, const uint32_t* hv, uint64_t count64,
+                     bool deletions, uint32_t* ou, uint32_t* ov, uint64_t* kept) {
+  *kept = 0;
+  if (count64 == 0) return PRX_OK;
+  if (count64 >= 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_tidy_batch: batch too large");
+  const uint32_t count = (uint32_t)count64;
+  cudaStream_t s = c->stream;
+  int vbits = 1;
+  while (vbits < 32 && (1ull << vbits) < g.n) ++vbits;
+  const int key_bits = deletions ? 32 : std::min(64, 2 * vbits);
+  const uint32_t tiles = (count + kSortTile - 1) / kSortTile;
+  TidyBufs b;
+  auto fail = [&](cudaError_t e) {
+    b.release();
+    set_error(std::string("prx_graph_tidy_batch: ") + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
+  };
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc(&b.u, 4ull * count);
+  if (e == cudaSuccess) e = cudaMalloc(&b.v, 4ull * count);
+  if (e == cudaSuccess) e = cudaMalloc(&b.flag, 4ull * (count + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b.pos, 4ull * (count + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b.hist, 4ull * ((size_t)kRadix * tiles + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b.key, 8ull * count);
+  if (e == cudaSuccess) e = cudaMalloc(&b.key2, 8ull * count);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b.u, hu, 4ull * count, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b.v, hv, 4ull * count, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return fail(e);
+  const int grid = grid_of(count, c->sms);
+  // 1-2. existence and keys, then compaction of the kept keys
+  k_tidy_keys<<<grid, 256, 0, s>>>(g.xoff, g.xedg, b.u, b.v, count, deletions ? 1 : 0, vbits, b.flag, b.key);
+  e = cudaMemcpyAsync(b.pos, b.flag, 4ull * count, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.pos + count, 0, 4, s);
+  if (e == cudaSuccess) e = exclusive_scan_u32(b.pos, count + 1, s);
+  uint32_t m2 = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&m2, b.pos + count, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) k_compact64<<<grid, 256, 0, s>>>(b.key, b.flag, b.pos, count, b.key2);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(e);
+  if (m2 == 0) {
+    b.release();
+    return PRX_OK;
+  }
+  // 3. radix sort of key2[0 .. m2), ping-ponging with key
+  const uint32_t t2 = (m2 + kSortTile - 1) / kSortTile;
+  unsigned long long *src = b.key2, *dst = b.key;
+  for (int shift = 0; shift < key_bits; shift += 8) {
+    k_radix_hist<<<t2, kSortThreads, 0, s>>>(src, m2, shift, t2, b.hist);
+    e = exclusive_scan_u32(b.hist, (uint32_t)(kRadix * t2), s);
+    if (e != cudaSuccess) return fail(e);
+    k_radix_scatter<<<t2, kSortThreads, 0, s>>>(src, m2, shift, t2, b.hist, dst);
+    std::swap(src, dst);
+  }
+  // 4. unique and decode
+  const int g2 = grid_of(m2, c->sms);
+  k_first_flags<<<g2, 256, 0, s>>>(src, m2, b.flag);
+  e = cudaMemcpyAsync(b.pos, b.flag, 4ull * m2, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.pos + m2, 0, 4, s);
+  if (e == cudaSuccess) e = exclusive_scan_u32(b.pos, m2 + 1, s);
+  uint32_t m3 = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&m3, b.pos + m2, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    k_decode<<<g2, 256, 0, s>>>(src, b.flag, b.pos, m2, deletions ? 1 : 0, vbits, g.xoff, g.n, g.xedg, b.u, b.v);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && m3) e = cudaMemcpyAsync(ou, b.u, 4ull * m3, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && m3) e = cudaMemcpyAsync(ov, b.v, 4ull * m3, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(e);
+  b.release();
+  *kept = m3;
+  return PRX_OK;
+}
+
+extern "C" {
+
+int prx_graph_tidy_batch(prx_context* c, prx_graph* gr, const uint32_t* du, const uint32_t* dv, uint64_t nd,
+                         const uint32_t* iu, const uint32_t* iv, uint64_t ni, uint32_t* out_du, uint32_t* out_dv,
+                         uint64_t* out_nd, uint32_t* out_iu, uint32_t* out_iv, uint64_t* out_ni) {
+  if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_graph_tidy_batch: bad context or graph");
+  const GraphDev& g = gr->g;
+  if (!g.xoff) FAIL(PRX_ESTATE, "prx_graph_tidy_batch: graph has no out-CSR");
+  if (!out_nd || !out_ni) FAIL(PRX_EINVAL, "prx_graph_tidy_batch: NULL output length");
+  if ((nd && (!du || !dv || !out_du || !out_dv)) || (ni && (!iu || !iv || !out_iu || !out_iv)))
+    FAIL(PRX_EINVAL, "prx_graph_tidy_batch: NULL array with a non-zero length");
+  for (uint64_t i = 0; i < nd; ++i)
+    if (du[i] >= g.n || dv[i] >= g.n) FAIL(PRX_EINVAL, "prx_graph_tidy_batch: deletion vertex id out of range");
+  for (uint64_t i = 0; i < ni; ++i)
+    if (iu[i] >= g.n || iv[i] >= g.n) FAIL(PRX_EINVAL, "prx_graph_tidy_batch: insertion vertex id out of range");
+  TRY_CUDA_ST(cudaSetDevice(c->device));
+  int st = tidy_list(c, g, du, dv, nd, true, out_du, out_dv, out_nd);
+  if (st) return st;
+  return tidy_list(c, g, iu, iv, ni, false, out_iu, out_iv, out_ni);
+}
+
+}  // extern "C"

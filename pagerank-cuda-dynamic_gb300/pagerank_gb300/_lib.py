@@ -78,7 +78,7 @@ EXPORTS = (
     "prx_graph_download",
     "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_selftest_division",
     "prx_solve_ppr_batched", "prx_solve_ppr_batched_device", "prx_graph_set_weights", "prx_solve_weighted",
-    "prx_adjoint", "prx_autotune",
+    "prx_adjoint", "prx_autotune", "prx_graph_tidy_batch",
     "prx_host_csr_free",
     "prx_gen_rmat", "prx_gen_weblike", "prx_gen_grid", "prx_gen_batch", "prx_host_tidy_batch",
     "prx_host_apply_batch", "prx_host_transpose", "prx_host_free",
@@ -124,6 +124,8 @@ def load(build_if_missing=True):
                                                C.POINTER(PprResult)]),
         "prx_graph_set_weights": (i32, [vp, vp, vp]),
         "prx_autotune": (i32, [vp, vp, C.c_char_p, C.POINTER(TuneResult)]),
+        "prx_graph_tidy_batch": (i32, [vp, vp, vp, vp, u64, vp, vp, u64, vp, vp, C.POINTER(u64), vp, vp,
+                                       C.POINTER(u64)]),
         "prx_solve_weighted": (i32, [vp, vp, vp, vp, C.POINTER(Options), vp, C.POINTER(Result)]),
         "prx_adjoint": (i32, [vp, vp, vp, vp, vp, C.POINTER(Options), vp, vp, vp, C.POINTER(dbl),
                               C.POINTER(Result)]),

@@ -108,6 +108,17 @@ class Graph:
         check(load().prx_graph_apply_batch(self._h, _p(du), _p(dv), len(du), _p(iu), _p(iv), len(iu)),
               "prx_graph_apply_batch")
 
+    def tidy_batch(self, del_u, del_v, ins_u, ins_v):
+        """prx_graph_tidy_batch: the tidied (del_u, del_v, ins_u, ins_v) for this graph."""
+        du, dv, iu, iv = (_u32(a) for a in (del_u, del_v, ins_u, ins_v))
+        od, odv = np.zeros(max(len(du), 1), np.uint32), np.zeros(max(len(du), 1), np.uint32)
+        oi, oiv = np.zeros(max(len(iu), 1), np.uint32), np.zeros(max(len(iu), 1), np.uint32)
+        nd, ni = C.c_uint64(), C.c_uint64()
+        check(load().prx_graph_tidy_batch(self.ctx.handle, self._h, _p(du), _p(dv), len(du), _p(iu), _p(iv), len(iu),
+                                          od.ctypes.data, odv.ctypes.data, C.byref(nd), oi.ctypes.data,
+                                          oiv.ctypes.data, C.byref(ni)), "prx_graph_tidy_batch")
+        return od[:nd.value], odv[:nd.value], oi[:ni.value], oiv[:ni.value]
+
     def download(self):
         n, m = self.size()
         xoff, xtoff = np.zeros(n + 1, np.uint32), np.zeros(n + 1, np.uint32)

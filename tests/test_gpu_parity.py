@@ -287,3 +287,45 @@ def test_autotune_keeps_results_and_caches(pg, ctx, tmp_path):
     assert len(lines) >= 6 and int(lines[1]) == t["mid_max"]
     g2.close()
     g.close()
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_device_tidy_matches_reference_golden(pg, ctx, case):
+    # the raw batch tidied on the device against x equals the reference's own
+    # tidyBatchUpdateU output stored in the fixture
+    z = load_golden(case)
+    g = pg.Graph(ctx, z["xt_off"], z["xt_edg"], z["xt_dat"], z["x_off"], z["x_edg"])
+    du, dv, iu, iv = g.tidy_batch(z["raw_del_u"], z["raw_del_v"], z["raw_ins_u"], z["raw_ins_v"])
+    np.testing.assert_array_equal(du, z["del_u"])
+    np.testing.assert_array_equal(dv, z["del_v"])
+    np.testing.assert_array_equal(iu, z["ins_u"])
+    np.testing.assert_array_equal(iv, z["ins_v"])
+    g.close()
+
+
+@pytest.mark.parametrize("kind", ["rmat16", "hubs", "web200k"])
+def test_device_tidy_matches_host_tidy(pg, ctx, kind):
+    xoff, xedg = _synthetic(pg, kind)
+    n, m = len(xoff) - 1, len(xedg)
+    rng = np.random.default_rng(41)
+    src = np.repeat(np.arange(n, dtype=np.uint32), np.diff(xoff.astype(np.int64)))
+    pick = rng.integers(0, m, 30000)
+    # deletions: existing edges with repeats, plus random pairs (mostly absent)
+    du = np.concatenate([src[pick], rng.integers(0, n, 5000).astype(np.uint32)])
+    dv = np.concatenate([xedg[pick], rng.integers(0, n, 5000).astype(np.uint32)])
+    # insertions: random pairs with repeats, plus some existing edges
+    iu0 = rng.integers(0, n, 40000).astype(np.uint32)
+    iv0 = rng.integers(0, n, 40000).astype(np.uint32)
+    iu = np.concatenate([iu0, iu0[:3000], src[pick[:2000]]])
+    iv = np.concatenate([iv0, iv0[:3000], xedg[pick[:2000]]])
+    perm = rng.permutation(len(du))
+    du, dv = du[perm], dv[perm]
+    g = pg.Graph(ctx, *O.transpose(xoff, xedg), xoff, xedg)
+    got = g.tidy_batch(du, dv, iu, iv)
+    want = pg.graphs.tidy_batch(xoff, xedg, du, dv, iu, iv)
+    for a, b in zip(got, want):
+        np.testing.assert_array_equal(a, b)
+    g.apply_batch(*got)  # the result is a valid batch for the device apply
+    e = np.zeros(0, np.uint32)
+    assert all(len(a) == 0 for a in g.tidy_batch(e, e, e, e))
+    g.close()
