@@ -204,6 +204,17 @@ int prx_graph_tidy_batch(prx_context* ctx, prx_graph* g,
                          uint32_t* out_del_u, uint32_t* out_del_v, uint64_t* out_nd,
                          uint32_t* out_ins_u, uint32_t* out_ins_v, uint64_t* out_ni);
 
+/* Build a graph on the device from an edge list (0-based ids < n, any order,
+ * duplicates allowed): the out-CSR (rows ascending, duplicates merged), the
+ * in-CSR and the out-degrees -- what the reference assembles on the host
+ * with readTemporalOmpW (inc/snap.hxx:158-166, main.cu:167),
+ * addSelfLoopsOmp (inc/selfLoop.hxx:60-66, main.cu:169; here when
+ * self_loops != 0, a loop on every vertex) and transposeWithDegreeOmp
+ * (inc/transpose.hxx:110-134, main.cu:170).  u, v: host arrays of `count`
+ * ids.  Equivalent to prx_graph_create with those CSRs. */
+int prx_graph_create_from_edges(prx_context* ctx, uint32_t n, const uint32_t* u, const uint32_t* v,
+                                uint64_t count, int self_loops, prx_graph** out);
+
 /* Run only the initial affected-vertex marking of a dynamic mode
  * (pagerankAffectedFrontierCuW :405-412 for DF / DF-P,
  * pagerankAffectedTraversalCuW :438-456 for DT) and copy the flags (n bytes,
@@ -368,6 +379,27 @@ int prx_host_apply_batch(const prx_host_csr* x,
                          const uint32_t* delu, const uint32_t* delv, uint64_t nd,
                          const uint32_t* insu, const uint32_t* insv, uint64_t ni,
                          prx_host_csr* y);
+/* Edge-list readers.  Ids in the files are 1-based; the arrays returned are
+ * 0-based, allocated by the library (free with prx_host_free).
+ *
+ * SNAP temporal text ("u v [t]" per line), read in consecutive pieces as the
+ * reference's driver does (main.cu:167 reads the first 90% of the lines,
+ * main.cu:83 each batch): prx_edge_reader_next reads the next `size` lines
+ * (fewer at the end of the file); a line that does not start with two
+ * unsigned integers ends the piece, as in readTemporalDo
+ * (inc/snap.hxx:41-52).  Ids must lie in 1..rows (PRX_EINVAL otherwise);
+ * symmetric != 0 adds (v, u) after each (u, v). */
+typedef struct prx_edge_reader prx_edge_reader;
+int prx_edge_reader_open(const char* path, prx_edge_reader** out);
+int prx_edge_reader_next(prx_edge_reader* r, uint32_t rows, uint64_t size, int symmetric,
+                         uint32_t** u, uint32_t** v, uint64_t* count, uint64_t* lines);
+int prx_edge_reader_close(prx_edge_reader* r);
+/* MatrixMarket coordinate file (readMtxDo, inc/mtx.hxx:119-135; header by
+ * readMtxHeader, inc/mtx.hxx:39-54): n = max(rows, cols); a symmetric or
+ * skew-symmetric matrix gives both (u, v) and (v, u); a file that is not
+ * "matrix coordinate" gives n = 0 and no edges; reading stops at the first
+ * line without two unsigned integers.  Ids must lie in 1..n. */
+int prx_read_mtx(const char* path, uint32_t* n, uint32_t** u, uint32_t** v, uint64_t* count);
 /* In-CSR (sources ascending) and out-degrees of x; xtdat has n entries. */
 int prx_host_transpose(const prx_host_csr* x, prx_host_csr* xt, uint32_t* xtdat);
 void prx_host_free(void* p);

@@ -1,4 +1,6 @@
-// prx_tidy.cu -- batch tidying on the device: the reference's
+// prx_tidy.cu -- batch tidying and graph ingest on the device.
+//
+// Tidying: the reference's
 // tidyBatchUpdateU (inc/batch.hxx:152-208), which runs on the host there:
 // keep the deletions that exist in the graph and the insertions that do not,
 // sort each list by (u, v) and drop duplicates.
@@ -10,6 +12,14 @@
 //      digit histograms, a digit-major scan, and a scatter that ranks equal
 //      digits in element order with __match_any_sync);
 //   4. unique: first occurrences kept (scan of flags), decoded back to (u, v).
+//
+// Ingest (prx_graph_create_from_edges): the reference builds its DiGraph from
+// an edge list on the host (readTemporalOmpW, inc/snap.hxx:158-166; edges
+// merged into sorted neighbour sets), adds a self-loop to every vertex
+// (addSelfLoopsOmp, inc/selfLoop.hxx:60-66) and transposes it with the
+// out-degrees (transposeWithDegreeOmp, inc/transpose.hxx:110-134).  Here:
+// keys u * 2^b + v (plus v * 2^b + v for the self-loops), radix sort, unique,
+// row starts from the sorted keys; the transpose the same from v * 2^b + u.
 #include <algorithm>
 #include "prx_ctx.h"
 #include "prx_device.cuh"
@@ -143,9 +153,80 @@ __global__ void k_decode(const unsigned long long* __restrict__ key, const uint3
   }
 }
 
+// Stable LSD radix sort of keys[0 .. count) on their low `bits` bits, 8 at a
+// time, ping-ponging with tmp; *out is the buffer holding the result.  hist:
+// 256 * ceil(count / kSortTile) + 1 words.
+static cudaError_t radix_sort_u64(unsigned long long* keys, unsigned long long* tmp, uint32_t count, int bits,
+                                  uint32_t* hist, cudaStream_t s, unsigned long long** out) {
+  const uint32_t tiles = (count + kSortTile - 1) / kSortTile;
+  unsigned long long *src = keys, *dst = tmp;
+  for (int shift = 0; shift < bits && count; shift += 8) {
+    k_radix_hist<<<tiles, kSortThreads, 0, s>>>(src, count, shift, tiles, hist);
+    const cudaError_t e = exclusive_scan_u32(hist, (uint32_t)(kRadix * tiles), s);
+    if (e != cudaSuccess) return e;
+    k_radix_scatter<<<tiles, kSortThreads, 0, s>>>(src, count, shift, tiles, hist, dst);
+    std::swap(src, dst);
+  }
+  *out = src;
+  return cudaGetLastError();
+}
+
 static int grid_of(uint64_t work, int sms) {
   const uint64_t b = (work + 255) / 256;
   return (int)std::max<uint64_t>(1, std::min<uint64_t>(b, (uint64_t)sms * 16));
+}
+
+// Edge keys of the ingest: u * 2^b + v for the listed edges, then v * 2^b + v
+// for every vertex when self-loops are added.  An id >= n sets *bad (its key
+// is clamped into range; the caller fails the call).
+__global__ void k_ingest_keys(const uint32_t* __restrict__ u, const uint32_t* __restrict__ v, uint32_t count,
+                              uint32_t n, int self_loops, int vbits, unsigned long long* __restrict__ key,
+                              uint32_t* __restrict__ bad) {
+  const uint32_t total = count + (self_loops ? n : 0);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    if (i < count) {
+      uint32_t a = u[i], b = v[i];
+      if (a >= n || b >= n) {
+        *bad = 1u;
+        a = min(a, n - 1);
+        b = min(b, n - 1);
+      }
+      key[i] = ((unsigned long long)a << vbits) | b;
+    } else {
+      key[i] = ((unsigned long long)(i - count) << vbits) | (i - count);
+    }
+  }
+}
+
+// Unique sorted keys: low halves to edg, and the swapped keys (transpose).
+__global__ void k_ingest_split(const unsigned long long* __restrict__ key, const uint32_t* __restrict__ flag,
+                               const uint32_t* __restrict__ pos, uint32_t count, int vbits, int make_swapped,
+                               unsigned long long* __restrict__ uniq, unsigned long long* __restrict__ swapped) {
+  const unsigned long long mask = (1ull << vbits) - 1;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    if (!flag[i]) continue;
+    const unsigned long long k = key[i];
+    uniq[pos[i]] = k;
+    if (make_swapped) swapped[pos[i]] = ((k & mask) << vbits) | (k >> vbits);
+  }
+}
+
+// CSR of unique sorted keys: edg[i] = low part, off[w] = first key with high
+// part >= w (each off entry written once, by the key that closes the gap).
+__global__ void k_ingest_csr(const unsigned long long* __restrict__ key, uint32_t count, int vbits, uint32_t n,
+                             uint32_t* __restrict__ off, uint32_t* __restrict__ edg) {
+  const unsigned long long mask = (1ull << vbits) - 1;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= count; i += gridDim.x * blockDim.x) {
+    const long long cur = i < count ? (long long)(key[i] >> vbits) : (long long)n;
+    const long long prev = i > 0 ? (long long)(key[i - 1] >> vbits) : -1;
+    for (long long w = prev + 1; w <= cur; ++w) off[w] = i;
+    if (i < count) edg[i] = (uint32_t)(key[i] & mask);
+  }
+}
+
+__global__ void k_ingest_degree(const uint32_t* __restrict__ off, uint32_t n, uint32_t* __restrict__ deg) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    deg[v] = off[v + 1] - off[v];
 }
 
 }  // namespace prx
@@ -204,16 +285,10 @@ static int tidy_list(prx_context* c, const GraphDev& g, const uint32_t* hu, cons
     b.release();
     return PRX_OK;
   }
-  // 3. radix sort of key2[0 .. m2), ping-ponging with key
-  const uint32_t t2 = (m2 + kSortTile - 1) / kSortTile;
-  unsigned long long *src = b.key2, *dst = b.key;
-  for (int shift = 0; shift < key_bits; shift += 8) {
-    k_radix_hist<<<t2, kSortThreads, 0, s>>>(src, m2, shift, t2, b.hist);
-    e = exclusive_scan_u32(b.hist, (uint32_t)(kRadix * t2), s);
-    if (e != cudaSuccess) return fail(e);
-    k_radix_scatter<<<t2, kSortThreads, 0, s>>>(src, m2, shift, t2, b.hist, dst);
-    std::swap(src, dst);
-  }
+  // 3. radix sort of key2[0 .. m2)
+  unsigned long long* src = nullptr;
+  e = radix_sort_u64(b.key2, b.key, m2, key_bits, b.hist, s, &src);
+  if (e != cudaSuccess) return fail(e);
   // 4. unique and decode
   const int g2 = grid_of(m2, c->sms);
   k_first_flags<<<g2, 256, 0, s>>>(src, m2, b.flag);
@@ -236,6 +311,104 @@ static int tidy_list(prx_context* c, const GraphDev& g, const uint32_t* hu, cons
 }
 
 extern "C" {
+
+int prx_graph_create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, const uint32_t* v, uint64_t count64,
+                                int self_loops, prx_graph** out) {
+  if (!c || !out) FAIL(PRX_EINVAL, "prx_graph_create_from_edges: NULL context or output");
+  *out = nullptr;
+  if (count64 && (!u || !v)) FAIL(PRX_EINVAL, "prx_graph_create_from_edges: NULL edge arrays");
+  const uint64_t total64 = count64 + (self_loops ? n : 0);
+  if (total64 >= 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_create_from_edges: too many edges (offsets are 32-bit)");
+  if (count64 && n == 0) FAIL(PRX_EINVAL, "prx_graph_create_from_edges: edges given with n = 0");
+  TRY_CUDA_ST(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  const uint32_t count = (uint32_t)count64, total = (uint32_t)total64;
+  int vbits = 1;
+  while (vbits < 32 && (1ull << vbits) < n) ++vbits;
+  prx_graph* gr = new prx_graph();
+  gr->ctx = c;
+  GraphDev& g = gr->g;
+  g.device = c->device;
+  g.n = n;
+  TidyBufs b;
+  unsigned long long *uniq = nullptr, *swp = nullptr;
+  uint32_t* bad = nullptr;
+  auto release = [&]() {
+    b.release();
+    b = TidyBufs();
+    cudaFree(uniq);
+    cudaFree(swp);
+    cudaFree(bad);
+    uniq = swp = nullptr;
+    bad = nullptr;
+  };
+  auto fail = [&](cudaError_t e) {
+    release();
+    prx_graph_destroy(gr);
+    set_error(std::string("prx_graph_create_from_edges: ") + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
+  };
+  const size_t cap = total ? total : 1;
+  const uint32_t tiles = (total + kSortTile - 1) / kSortTile;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess && count) e = cudaMalloc(&b.u, 4ull * count);
+  if (e == cudaSuccess && count) e = cudaMalloc(&b.v, 4ull * count);
+  if (e == cudaSuccess) e = cudaMalloc(&b.flag, 4ull * (cap + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b.pos, 4ull * (cap + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b.hist, 4ull * ((size_t)kRadix * tiles + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b.key, 8ull * cap);
+  if (e == cudaSuccess) e = cudaMalloc(&b.key2, 8ull * cap);
+  if (e == cudaSuccess) e = cudaMalloc(&uniq, 8ull * cap);
+  if (e == cudaSuccess) e = cudaMalloc(&swp, 8ull * cap);
+  if (e == cudaSuccess) e = cudaMalloc(&bad, 4);
+  if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, 4, s);
+  if (e == cudaSuccess && count) e = cudaMemcpyAsync(b.u, u, 4ull * count, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && count) e = cudaMemcpyAsync(b.v, v, 4ull * count, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return fail(e);
+  const int grid = grid_of(cap, c->sms);
+  // sorted unique (u, v): the out-CSR
+  k_ingest_keys<<<grid, 256, 0, s>>>(b.u, b.v, count, n, self_loops ? 1 : 0, vbits, b.key, bad);
+  unsigned long long* sorted = nullptr;
+  e = radix_sort_u64(b.key, b.key2, total, 2 * vbits, b.hist, s, &sorted);
+  if (e != cudaSuccess) return fail(e);
+  k_first_flags<<<grid, 256, 0, s>>>(sorted, total, b.flag);
+  e = cudaMemcpyAsync(b.pos, b.flag, 4ull * total, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.pos + total, 0, 4, s);
+  if (e == cudaSuccess) e = exclusive_scan_u32(b.pos, total + 1, s);
+  uint32_t m = 0, bad_h = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&m, b.pos + total, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad_h, bad, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) k_ingest_split<<<grid, 256, 0, s>>>(sorted, b.flag, b.pos, total, vbits, 1, uniq, swp);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(e);
+  if (bad_h) {
+    release();
+    prx_graph_destroy(gr);
+    FAIL(PRX_EINVAL, "prx_graph_create_from_edges: vertex id out of range");
+  }
+  g.m = g.m_cap = m;
+  if (e == cudaSuccess) e = cudaMalloc(&g.xoff, 4ull * ((size_t)n + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&g.xedg, 4ull * (m ? m : 1));
+  if (e == cudaSuccess) e = cudaMalloc(&g.xtoff, 4ull * ((size_t)n + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&g.xtedg, 4ull * edge_slots(m));
+  if (e == cudaSuccess) e = cudaMalloc(&g.xtdat, 4ull * (n ? n : 1));
+  if (e != cudaSuccess) return fail(e);
+  const int g2 = grid_of((uint64_t)m + 1, c->sms);
+  k_ingest_csr<<<g2, 256, 0, s>>>(uniq, m, vbits, n, g.xoff, g.xedg);
+  k_ingest_degree<<<grid_of(n, c->sms), 256, 0, s>>>(g.xoff, n, g.xtdat);
+  // the transpose: the swapped keys sorted
+  e = radix_sort_u64(swp, b.key, m, 2 * vbits, b.hist, s, &sorted);
+  if (e != cudaSuccess) return fail(e);
+  k_ingest_csr<<<g2, 256, 0, s>>>(sorted, m, vbits, n, g.xtoff, g.xtedg);
+  e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  release();
+  if (e == cudaSuccess) e = build_classes(g, c->sms, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(e);
+  *out = gr;
+  return PRX_OK;
+}
 
 int prx_graph_tidy_batch(prx_context* c, prx_graph* gr, const uint32_t* du, const uint32_t* dv, uint64_t nd,
                          const uint32_t* iu, const uint32_t* iv, uint64_t ni, uint32_t* out_du, uint32_t* out_dv,

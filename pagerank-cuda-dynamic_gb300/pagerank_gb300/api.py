@@ -88,6 +88,21 @@ class Graph:
         xtoff, xtedg, xtdat = transpose(off, edg)
         return cls(ctx, xtoff, xtedg, xtdat, off if dynamic else None, edg if dynamic else None, validate)
 
+    @classmethod
+    def from_edges(cls, ctx, n, u, v, self_loops=True):
+        """prx_graph_create_from_edges: sort, merge and transpose an edge list
+        (0-based ids < n) on the device, with a self-loop on every vertex when
+        self_loops is set (main.cu:167-170 of the reference, on the host there)."""
+        u, v = _u32(u), _u32(v)
+        if len(u) != len(v):
+            raise ValueError("u and v differ in length")
+        g = cls.__new__(cls)
+        g.ctx = ctx
+        g._h = C.c_void_p()
+        check(load().prx_graph_create_from_edges(ctx.handle, int(n), _p(u), _p(v), len(u), int(bool(self_loops)),
+                                                 C.byref(g._h)), "prx_graph_create_from_edges")
+        return g
+
     @property
     def handle(self):
         return self._h

@@ -1,4 +1,5 @@
-"""Host graph utilities of the C ABI: synthetic generators, batches, transpose.
+"""Host graph utilities of the C ABI: synthetic generators, batches, transpose,
+edge-list readers (SNAP temporal text, MatrixMarket).
 
 Arrays made by the library are wrapped without copying: the numpy array keeps
 an owner object alive that frees the C buffer when the last view goes away.
@@ -112,3 +113,46 @@ def apply_batch(off, edg, del_u, del_v, ins_u, ins_v):
           "prx_host_apply_batch")
     del keep
     return _take_csr(h)
+
+
+class EdgeReader:
+    """SNAP temporal edge list read in consecutive pieces (prx_edge_reader_*),
+    as the reference's driver reads its input (main.cu:167, main.cu:83)."""
+
+    def __init__(self, path):
+        self._h = C.c_void_p()
+        check(load().prx_edge_reader_open(str(path).encode(), C.byref(self._h)), "prx_edge_reader_open")
+
+    def next(self, rows, size, symmetric=False):
+        """Next `size` lines -> (u, v, lines): 0-based ids, lines consumed."""
+        u, v = C.POINTER(C.c_uint32)(), C.POINTER(C.c_uint32)()
+        cnt, lines = C.c_uint64(), C.c_uint64()
+        check(load().prx_edge_reader_next(self._h, int(rows), int(size), int(bool(symmetric)), C.byref(u),
+                                          C.byref(v), C.byref(cnt), C.byref(lines)), "prx_edge_reader_next")
+        return _take(u, cnt.value), _take(v, cnt.value), lines.value
+
+    def close(self):
+        if self._h:
+            load().prx_edge_reader_close(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def read_mtx(path):
+    """MatrixMarket coordinate file -> (n, u, v), 0-based; symmetric files give both directions."""
+    n = C.c_uint32()
+    u, v = C.POINTER(C.c_uint32)(), C.POINTER(C.c_uint32)()
+    cnt = C.c_uint64()
+    check(load().prx_read_mtx(str(path).encode(), C.byref(n), C.byref(u), C.byref(v), C.byref(cnt)), "prx_read_mtx")
+    return n.value, _take(u, cnt.value), _take(v, cnt.value)

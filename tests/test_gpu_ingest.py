@@ -1,0 +1,137 @@
+"""Device-side graph ingest (prx_graph_create_from_edges) against the CSRs the
+reference's own graph builder made: the golden graphs (tests/golden/*.npz)
+from shuffled, duplicated edge lists, and main.cu's whole flow on a SNAP
+temporal file (reader -> base graph with self-loops -> per batch: tidy,
+apply, transpose; tests/golden/readers/readers.npz)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_cases, load_golden
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+READERS = os.path.join(GOLDEN, "readers")
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import pagerank_gb300
+    pagerank_gb300.load()
+    return pagerank_gb300
+
+
+def edges_of(off, edg):
+    off = np.asarray(off, np.int64)
+    u = np.repeat(np.arange(len(off) - 1, dtype=np.uint32), np.diff(off))
+    return u, np.asarray(edg, np.uint32)
+
+
+def assert_graph(g, off, edg, toff, tedg, tdat):
+    xoff, xedg, xtoff, xtedg, xtdat = g.download()
+    assert np.array_equal(xoff, off) and np.array_equal(xedg, edg)
+    assert np.array_equal(xtoff, toff) and np.array_equal(xtedg, tedg)
+    assert np.array_equal(xtdat, tdat)
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_ingest_golden_graphs(pg, ctx, case):
+    z = load_golden(case)
+    n = int(z["n"])
+    u, v = edges_of(z["x_off"], z["x_edg"])
+    rng = np.random.default_rng(3)
+    # shuffled, with a third of the edges repeated
+    rep = rng.random(len(u)) < 0.33
+    uu, vv = np.concatenate([u, u[rep]]), np.concatenate([v, v[rep]])
+    p = rng.permutation(len(uu))
+    want = (z["x_off"], z["x_edg"], z["xt_off"], z["xt_edg"], z["xt_dat"])
+    g = pg.Graph.from_edges(ctx, n, uu[p], vv[p], self_loops=False)
+    assert_graph(g, *want)
+    g.close()
+    # the golden graphs hold a self-loop on every vertex: drop them and let
+    # the ingest add them back
+    keep = uu[p] != vv[p]
+    g = pg.Graph.from_edges(ctx, n, uu[p][keep], vv[p][keep], self_loops=True)
+    assert_graph(g, *want)
+    g.close()
+
+
+def test_ingest_reference_pipeline(pg, ctx):
+    z = np.load(os.path.join(READERS, "readers.npz"))
+    z = {k: z[k] for k in z.files}
+    rows, size, frac = int(z["pipe_rows"]), int(z["pipe_size"]), float(z["pipe_frac"])
+    with pg.graphs.EdgeReader(os.path.join(READERS, "temporal_small.txt")) as r:
+        u, v, _ = r.next(rows, int(0.90 * size))
+        x = pg.Graph.from_edges(ctx, rows, u, v, self_loops=True)
+        assert_graph(x, z["pipe_x_off"], z["pipe_x_edg"], z["pipe_xt_off"], z["pipe_xt_edg"], z["pipe_xt_dat"])
+        xoff, xedg = z["pipe_x_off"], z["pipe_x_edg"]
+        for b in range(int(z["pipe_batches"])):
+            bu, bv, _ = r.next(rows, int(frac * size))
+            du, dv, iu, iv = x.tidy_batch([], [], bu, bv)
+            assert np.array_equal(iu, z[f"pipe_ins_u{b}"] - 1) and np.array_equal(iv, z[f"pipe_ins_v{b}"] - 1)
+            y = pg.Graph.from_edges(ctx, rows, *edges_of(xoff, xedg), self_loops=False)
+            y.apply_batch(du, dv, iu, iv)
+            assert_graph(y, z[f"pipe_y{b}_off"], z[f"pipe_y{b}_edg"], z[f"pipe_yt{b}_off"], z[f"pipe_yt{b}_edg"],
+                         z[f"pipe_yt_dat{b}"])
+            # the same graph straight from the edge list of x plus the batch
+            xu, xv = edges_of(xoff, xedg)
+            y2 = pg.Graph.from_edges(ctx, rows, np.concatenate([xu, bu]), np.concatenate([xv, bv]),
+                                     self_loops=False)
+            assert_graph(y2, z[f"pipe_y{b}_off"], z[f"pipe_y{b}_edg"], z[f"pipe_yt{b}_off"],
+                         z[f"pipe_yt{b}_edg"], z[f"pipe_yt_dat{b}"])
+            y.close()
+            y2.close()
+        x.close()
+
+
+def numpy_csr(n, u, v, self_loops):
+    u, v = np.asarray(u, np.uint64), np.asarray(v, np.uint64)
+    if self_loops:
+        s = np.arange(n, dtype=np.uint64)
+        u, v = np.concatenate([u, s]), np.concatenate([v, s])
+    k = np.unique(u * np.uint64(n) + v) if len(u) else np.zeros(0, np.uint64)
+    su, sv = (k // np.uint64(n)).astype(np.uint32), (k % np.uint64(n)).astype(np.uint32)
+    off = np.zeros(n + 1, np.uint32)
+    np.cumsum(np.bincount(su, minlength=n), out=off[1:])
+    toff, tedg, tdat = O.transpose(off, sv)
+    return off, sv, toff, tedg, tdat
+
+
+@pytest.mark.parametrize("n,m,self_loops", [(1, 0, True), (1, 5, False), (7, 0, False), (1000, 30000, True),
+                                            (65537, 2_500_000, True), (300_001, 4_000_000, False)])
+def test_ingest_random_vs_numpy(pg, ctx, n, m, self_loops):
+    rng = np.random.default_rng(n + m)
+    # skewed sources (a few long rows) and a band of isolated high ids
+    hi = max(1, int(n * 0.9))
+    u = np.minimum(rng.zipf(1.6, m) - 1, hi - 1).astype(np.uint32)
+    v = rng.integers(0, hi, m).astype(np.uint32)
+    g = pg.Graph.from_edges(ctx, n, u, v, self_loops=self_loops)
+    assert_graph(g, *numpy_csr(n, u, v, self_loops))
+    assert g.size() == (n, int(numpy_csr(n, u, v, self_loops)[0][-1]))
+    g.close()
+
+
+def test_ingest_solves_like_host_built_graph(pg, ctx):
+    off, edg = pg.graphs.rmat(12, 16, seed=9)
+    u, v = edges_of(off, edg)
+    p = np.random.default_rng(1).permutation(len(u))
+    g = pg.Graph.from_edges(ctx, len(off) - 1, u[p], v[p], self_loops=False)
+    r, res = pg.pagerank_static(ctx, g)
+    want, it = O.solve("static", None, None, *O.transpose(off, edg))
+    assert res["iterations"] == it and np.array_equal(r, want)
+    g.close()
+
+
+def test_ingest_errors(pg, ctx):
+    with pytest.raises(pg.PrxError):
+        pg.Graph.from_edges(ctx, 10, [1, 2, 10], [3, 4, 5])     # id 10 >= n
+    with pytest.raises(pg.PrxError):
+        pg.Graph.from_edges(ctx, 0, [0], [0])
+    g = pg.Graph.from_edges(ctx, 0, [], [], self_loops=True)   # empty graph
+    assert g.size() == (0, 0)
+    g.close()
+    g = pg.Graph.from_edges(ctx, 4, [1], [2])                 # context still usable after the errors
+    assert g.size() == (4, 5)
+    g.close()
