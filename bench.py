@@ -66,6 +66,8 @@ def parse():
     p.add_argument("--adjoint-scale", type=int, default=20)
     p.add_argument("--adjoint-fd-edges", type=int, default=200, help="edges checked by finite differences")
     p.add_argument("--adjoint-batches", type=int, default=2, help="dynamic batches of 1e-4|E| after the first solve")
+    p.add_argument("--no-ingest", action="store_true", help="skip the device graph ingest from the edge list")
+    p.add_argument("--ingest-steps", type=int, default=2)
     a = p.parse_args()
     if a.static_only:
         a.no_dfp = a.no_cpu = True
@@ -467,6 +469,57 @@ def run_adjoint(args, pg, ctx, local):
             "rounds": rounds, "fd_max_rel_err": max(x["fd_max_rel_err"] for x in rounds)}
 
 
+def run_ingest(args, pg, ctx, local, xoff, xedg):
+    """Device graph ingest (prx_graph_create_from_edges[_device]) of the bench
+    graph's own edge list plus a self-loop on every vertex, as the reference
+    builds its graph from the file (main.cu:167-170): edge arrays resident on
+    the device, and host arrays (pageable, copied inside the call).  A
+    1/8 sample is also ingested in row order and shuffled (the sort does the
+    same passes for any order; the shuffled run shows what order costs)."""
+    import numpy as np
+    import torch
+    n, m = len(xoff) - 1, len(xedg)
+    dev = f"cuda:{local}"
+    u = np.repeat(np.arange(n, dtype=np.uint32), np.diff(np.asarray(xoff, np.int64)))
+    v = np.asarray(xedg, np.uint32)
+
+    def timed(fn, steps):
+        ms = []
+        for _ in range(steps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            g2 = fn()
+            ms.append((time.perf_counter() - t) * 1e3)
+            got = g2.size()
+            g2.close()
+            assert got[0] == n, got
+        return ms, got[1]
+
+    du = torch.from_numpy(u.view(np.int32)).to(dev)
+    dv = torch.from_numpy(v.view(np.int32)).to(dev)
+    dev_ms, m_dev = timed(lambda: pg.Graph.from_device_edges(ctx, n, du, dv, self_loops=True), args.ingest_steps)
+    k = m // 8
+    a = 2_654_435_761 % k or 1
+    while np.gcd(a, k) != 1:
+        a += 1
+    perm = (np.arange(k, dtype=np.uint64) * np.uint64(a)) % np.uint64(k)
+    su, sv = du[:k], dv[:k]
+    pu = torch.from_numpy(u[:k][perm].view(np.int32)).to(dev)
+    pv = torch.from_numpy(v[:k][perm].view(np.int32)).to(dev)
+    sorted_ms, ms1 = timed(lambda: pg.Graph.from_device_edges(ctx, n, su, sv, self_loops=True), args.ingest_steps)
+    shuf_ms, ms2 = timed(lambda: pg.Graph.from_device_edges(ctx, n, pu, pv, self_loops=True), args.ingest_steps)
+    assert ms1 == ms2, (ms1, ms2)
+    del du, dv, su, sv, pu, pv
+    torch.cuda.empty_cache()
+    host_ms, m_host = timed(lambda: pg.Graph.from_edges(ctx, n, u, v, self_loops=True), 1)
+    assert m_dev == m_host == m, (m_dev, m_host, m)
+    dmed = statistics.median(dev_ms)
+    return {"workload": f"edge list of the bench graph ({m} edges in row order, {n} vertices) plus a self-loop "
+                        "on every vertex -> out-CSR, in-CSR, out-degrees on the device",
+            "device_ms": dev_ms, "host_arrays_ms": host_ms, "edges_per_s_device": m / (dmed / 1e3),
+            "h2d_bytes": 8 * m, "sample_edges": k, "sample_row_order_ms": sorted_ms, "sample_shuffled_ms": shuf_ms}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -589,7 +642,10 @@ def run_ours(args):
         dynamic, dfp = run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m)
         log(f"dfp: {dfp}")
 
-    ppr = adj = grid = None
+    ppr = adj = grid = ingest = None
+    if rank == 0 and not args.no_ingest and not args.static_only:
+        ingest = run_ingest(args, pg, ctx, local, xoff, xedg)
+        log(f"ingest: {ingest}")
     if rank == 0 and not args.no_grid and not args.static_only:
         grid = run_grid(args, pg, ctx, local)
         log(f"grid: {grid}")
@@ -613,7 +669,7 @@ def run_ours(args):
                "e2e": {"value": e2e_value, "unit": "GE/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "ms_per_step": e2e_ms_max},
                "roofline": roofline, "clocks": clk.summary(), "fp32_refine": fp32, "dfp": dfp,
-               "dynamic": dynamic, "autotune": tune, "grid": grid, "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
+               "dynamic": dynamic, "autotune": tune, "ingest": ingest, "grid": grid, "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     g.close()
     ctx.close()

@@ -204,6 +204,16 @@ int prx_graph_tidy_batch(prx_context* ctx, prx_graph* g,
                          uint32_t* out_del_u, uint32_t* out_del_v, uint64_t* out_nd,
                          uint32_t* out_ins_u, uint32_t* out_ins_v, uint64_t* out_ni);
 
+/* A random batch drawn and tidied on the device: nd_req deletions of
+ * uniformly chosen existing non-self-loop edges and ni_req insertions of
+ * uniform pairs, then tidied as prx_graph_tidy_batch does.  The same draws
+ * (counter-based hashes of seed and index) and so the same batch as the host
+ * generator prx_gen_batch on the graph's out-CSR.  Host output arrays with
+ * room for nd_req / ni_req edges. */
+int prx_graph_gen_batch(prx_context* ctx, prx_graph* g, uint64_t nd_req, uint64_t ni_req, uint64_t seed,
+                        uint32_t* del_u, uint32_t* del_v, uint64_t* nd,
+                        uint32_t* ins_u, uint32_t* ins_v, uint64_t* ni);
+
 /* Build a graph on the device from an edge list (0-based ids < n, any order,
  * duplicates allowed): the out-CSR (rows ascending, duplicates merged), the
  * in-CSR and the out-degrees -- what the reference assembles on the host
@@ -214,6 +224,9 @@ int prx_graph_tidy_batch(prx_context* ctx, prx_graph* g,
  * ids.  Equivalent to prx_graph_create with those CSRs. */
 int prx_graph_create_from_edges(prx_context* ctx, uint32_t n, const uint32_t* u, const uint32_t* v,
                                 uint64_t count, int self_loops, prx_graph** out);
+/* Same, with u and v in DEVICE memory (left unchanged). */
+int prx_graph_create_from_edges_device(prx_context* ctx, uint32_t n, const uint32_t* u, const uint32_t* v,
+                                       uint64_t count, int self_loops, prx_graph** out);
 
 /* Run only the initial affected-vertex marking of a dynamic mode
  * (pagerankAffectedFrontierCuW :405-412 for DF / DF-P,
@@ -400,6 +413,13 @@ int prx_edge_reader_close(prx_edge_reader* r);
  * "matrix coordinate" gives n = 0 and no edges; reading stops at the first
  * line without two unsigned integers.  Ids must lie in 1..n. */
 int prx_read_mtx(const char* path, uint32_t* n, uint32_t** u, uint32_t** v, uint64_t* count);
+/* One result line in the reference driver's log format (main.cu:54-61):
+ * "{-<del>/+<ins> batchf, <batch> batchi, <threads> threads} -> {<time>ms,
+ * <init>ms init, <mark>ms mark, <comp>ms comp, <iter> iter, <err> err}
+ * <technique>", without a newline.  Returns what snprintf returns (the
+ * length the full line needs), or -PRX_EINVAL. */
+int prx_format_glog(char* buf, size_t len, double deletions_fraction, double insertions_fraction,
+                    int batch_index, int threads, const prx_result* r, double err, const char* technique);
 /* In-CSR (sources ascending) and out-degrees of x; xtdat has n entries. */
 int prx_host_transpose(const prx_host_csr* x, prx_host_csr* xt, uint32_t* xtdat);
 void prx_host_free(void* p);

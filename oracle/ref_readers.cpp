@@ -14,7 +14,7 @@
 //       first 90% of the lines, addSelfLoopsOmp, transposeWithDegreeOmp; then
 //       per batch: the next batch_fraction * size lines as insertions,
 //       tidyBatchUpdateU and applyBatchUpdateOmpU on a copy of x,
-//       transposeWithDegreeOmp.
+//       transposeWithDegreeOmp, and the copy becomes x.
 // Output (stdout): records "name u count" followed by count unsigned values.
 // Vertex keys are printed as read (1-based); CSRs are over vertexKeys().
 #define BUILD 0
@@ -131,6 +131,7 @@ int main(int argc, char** argv) {
       putCsr("y" + i, y);
       putCsr("yt" + i, yt);
       putDat("yt_dat" + i, yt);
+      swap(x, y);  // the batches accumulate (main.cu:143)
     }
     return 0;
   }

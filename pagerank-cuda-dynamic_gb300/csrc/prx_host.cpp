@@ -12,20 +12,14 @@
 #include <vector>
 #include <omp.h>
 #include "pagerank_gb300.h"
+#include "prx_hash.h"
 
 namespace {
 
-inline uint64_t mix64(uint64_t z) {
-  z += 0x9E3779B97F4A7C15ull;
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  return z ^ (z >> 31);
-}
-inline uint64_t rnd(uint64_t seed, uint64_t stream, uint64_t i) {
-  return mix64(mix64(seed ^ (stream * 0xD1B54A32D192ED03ull)) + i);
-}
+using prx_hash::below;
+using prx_hash::mix64;
+using prx_hash::rnd;
 inline double u01(uint64_t x) { return (double)(x >> 11) * (1.0 / 9007199254740992.0); }  // [0, 1)
-inline uint32_t below(uint64_t x, uint64_t n) { return (uint32_t)(((x >> 32) * n) >> 32); }  // [0, n) for n < 2^32
 
 template <class T>
 T* xmalloc(size_t cnt) {
@@ -265,8 +259,8 @@ int prx_gen_batch(const prx_host_csr* x, uint64_t nd_req, uint64_t ni_req, uint6
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < (int64_t)nd_req; ++i) {
     // a uniformly chosen existing edge; self-loops are kept (no dead ends)
-    for (uint64_t t = 0; t < 32 && m; ++t) {
-      const uint64_t e = ((rnd(seed, 5, (uint64_t)i * 32 + t) >> 11) % m);
+    for (uint64_t t = 0; t < prx_hash::kDelTries && m; ++t) {
+      const uint64_t e = ((rnd(seed, prx_hash::kDelStream, (uint64_t)i * prx_hash::kDelTries + t) >> 11) % m);
       const uint32_t u = (uint32_t)(std::upper_bound(x->off, x->off + n + 1, (uint32_t)e) - x->off - 1);
       const uint32_t v = x->edg[e];
       if (u == v) continue;
@@ -282,7 +276,7 @@ int prx_gen_batch(const prx_host_csr* x, uint64_t nd_req, uint64_t ni_req, uint6
   *nd = k;
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < (int64_t)ni_req; ++i) {
-    const uint64_t h = rnd(seed, 6, (uint64_t)i);
+    const uint64_t h = rnd(seed, prx_hash::kInsStream, (uint64_t)i);
     (*iu)[i] = below(h, n);
     (*iv)[i] = below(mix64(h), n);
   }

@@ -286,4 +286,16 @@ int prx_read_mtx(const char* path, uint32_t* n, uint32_t** u, uint32_t** v, uint
   return hand_out(U, V, u, v, count);
 }
 
+int prx_format_glog(char* buf, size_t len, double deletions_fraction, double insertions_fraction, int batch_index,
+                    int threads, const prx_result* r, double err, const char* technique) {
+  // main.cu:56-59
+  if (!r || !technique) return -PRX_EINVAL;
+  return std::snprintf(buf, len,
+                       "{-%.3e/+%.3e batchf, %03d batchi, %03d threads} -> {%09.1fms, %09.1fms init, %09.1fms mark, "
+                       "%09.1fms comp, %03d iter, %.2e err} %s",
+                       deletions_fraction, insertions_fraction, batch_index, threads, (double)r->time_ms,
+                       (double)r->initialization_time_ms, (double)r->marking_time_ms,
+                       (double)r->computation_time_ms, r->iterations, err, technique);
+}
+
 }  // extern "C"

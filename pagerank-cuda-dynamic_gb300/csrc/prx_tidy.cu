@@ -23,6 +23,7 @@
 #include <algorithm>
 #include "prx_ctx.h"
 #include "prx_device.cuh"
+#include "prx_hash.h"
 
 namespace prx {
 
@@ -43,12 +44,18 @@ __device__ __forceinline__ uint32_t edge_position(const uint32_t* __restrict__ x
   return (lo < xoff[u + 1] && xedg[lo] == v) ? lo : 0xffffffffu;
 }
 
-// keep[i] = 1 for kept edges; key[i] = the edge's sort key.
-__global__ void k_tidy_keys(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg,
+// keep[i] = 1 for kept edges; key[i] = the edge's sort key.  Ids >= n (the
+// device batch generator's empty slots) are never kept.
+__global__ void k_tidy_keys(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg, uint32_t n,
                             const uint32_t* __restrict__ u, const uint32_t* __restrict__ v, uint32_t count,
                             int deletions, int vbits, uint32_t* __restrict__ keep,
                             unsigned long long* __restrict__ key) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    if (u[i] >= n || v[i] >= n) {
+      keep[i] = 0;
+      key[i] = 0;
+      continue;
+    }
     const uint32_t p = edge_position(xoff, xedg, u[i], v[i]);
     if (deletions) {
       keep[i] = p != 0xffffffffu;
@@ -153,14 +160,14 @@ __global__ void k_decode(const unsigned long long* __restrict__ key, const uint3
   }
 }
 
-// Stable LSD radix sort of keys[0 .. count) on their low `bits` bits, 8 at a
-// time, ping-ponging with tmp; *out is the buffer holding the result.  hist:
-// 256 * ceil(count / kSortTile) + 1 words.
-static cudaError_t radix_sort_u64(unsigned long long* keys, unsigned long long* tmp, uint32_t count, int bits,
+// Stable LSD radix sort of keys[0 .. count) on their bits [lo, hi), 8 at a
+// time (keys must be below 2^hi), ping-ponging with tmp; *out is the buffer
+// holding the result.  hist: 256 * ceil(count / kSortTile) + 1 words.
+static cudaError_t radix_sort_u64(unsigned long long* keys, unsigned long long* tmp, uint32_t count, int lo, int hi,
                                   uint32_t* hist, cudaStream_t s, unsigned long long** out) {
   const uint32_t tiles = (count + kSortTile - 1) / kSortTile;
   unsigned long long *src = keys, *dst = tmp;
-  for (int shift = 0; shift < bits && count; shift += 8) {
+  for (int shift = lo; shift < hi && count; shift += 8) {
     k_radix_hist<<<tiles, kSortThreads, 0, s>>>(src, count, shift, tiles, hist);
     const cudaError_t e = exclusive_scan_u32(hist, (uint32_t)(kRadix * tiles), s);
     if (e != cudaSuccess) return e;
@@ -211,22 +218,73 @@ __global__ void k_ingest_split(const unsigned long long* __restrict__ key, const
   }
 }
 
-// CSR of unique sorted keys: edg[i] = low part, off[w] = first key with high
-// part >= w (each off entry written once, by the key that closes the gap).
-__global__ void k_ingest_csr(const unsigned long long* __restrict__ key, uint32_t count, int vbits, uint32_t n,
-                             uint32_t* __restrict__ off, uint32_t* __restrict__ edg) {
-  const unsigned long long mask = (1ull << vbits) - 1;
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= count; i += gridDim.x * blockDim.x) {
-    const long long cur = i < count ? (long long)(key[i] >> vbits) : (long long)n;
-    const long long prev = i > 0 ? (long long)(key[i - 1] >> vbits) : -1;
-    for (long long w = prev + 1; w <= cur; ++w) off[w] = i;
-    if (i < count) edg[i] = (uint32_t)(key[i] & mask);
+// Row starts of unique sorted keys: off[w] = number of keys whose high part
+// (the row) is below w, by binary search (rows without keys need no
+// special case, however long the run of them).
+__global__ void k_ingest_offsets(const unsigned long long* __restrict__ key, uint32_t count, int vbits, uint32_t n,
+                                 uint32_t* __restrict__ off) {
+  for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w <= n; w += gridDim.x * blockDim.x) {
+    const unsigned long long first = (unsigned long long)w << vbits;  // smallest key of row w
+    uint32_t lo = 0, hi = count;
+    while (lo < hi) {
+      const uint32_t mid = lo + ((hi - lo) >> 1);
+      if (key[mid] < first) lo = mid + 1;
+      else hi = mid;
+    }
+    off[w] = lo;
   }
+}
+
+// Column ids of unique sorted keys: edg[i] = low part of key[i].
+__global__ void k_ingest_columns(const unsigned long long* __restrict__ key, uint32_t count, int vbits,
+                                 uint32_t* __restrict__ edg) {
+  const unsigned long long mask = (1ull << vbits) - 1;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+    edg[i] = (uint32_t)(key[i] & mask);
 }
 
 __global__ void k_ingest_degree(const uint32_t* __restrict__ off, uint32_t n, uint32_t* __restrict__ deg) {
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
     deg[v] = off[v + 1] - off[v];
+}
+
+// Raw random batch, the same draws as the host generator prx_gen_batch:
+// deletion i is the first non-self-loop edge among kDelTries uniform draws
+// (n, n when all are self-loops: dropped by the tidy); insertion i is a
+// uniform pair.
+__global__ void k_gen_deletions(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg, uint32_t n,
+                                uint64_t m, uint64_t seed, uint32_t count, uint32_t* __restrict__ du,
+                                uint32_t* __restrict__ dv) {
+  using namespace prx_hash;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    uint32_t ou = n, ov = n;
+    for (uint64_t t = 0; t < kDelTries && m; ++t) {
+      const uint64_t e = (rnd(seed, kDelStream, (uint64_t)i * kDelTries + t) >> 11) % m;
+      uint32_t lo = 0, hi = n;  // last row whose start is <= e
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (xoff[mid] <= e) lo = mid;
+        else hi = mid - 1;
+      }
+      const uint32_t v = xedg[e];
+      if (lo == v) continue;
+      ou = lo;
+      ov = v;
+      break;
+    }
+    du[i] = ou;
+    dv[i] = ov;
+  }
+}
+
+__global__ void k_gen_insertions(uint32_t n, uint64_t seed, uint32_t count, uint32_t* __restrict__ iu,
+                                 uint32_t* __restrict__ iv) {
+  using namespace prx_hash;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const uint64_t h = rnd(seed, kInsStream, i);
+    iu[i] = below(h, n);
+    iv[i] = below(mix64(h), n);
+  }
 }
 
 }  // namespace prx
@@ -240,39 +298,31 @@ struct TidyBufs {
   }
 };
 
-// Tidy one list (deletions or insertions) of `count` edges from host arrays
-// into host arrays; *kept receives the tidied length.
-static int tidy_list(prx_context* c, const GraphDev& g, const uint32_t* hu, const uint32_t* hv, uint64_t count64,
-                     bool deletions, uint32_t* ou, uint32_t* ov, uint64_t* kept) {
-  *kept = 0;
-  if (count64 == 0) return PRX_OK;
-  if (count64 >= 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_tidy_batch: batch too large");
-  const uint32_t count = (uint32_t)count64;
+// Tidy one list (deletions or insertions) of `count` edges already in b.u /
+// b.v on the device into host arrays; *kept receives the tidied length.
+// Frees every buffer of b.
+static int tidy_core(prx_context* c, const GraphDev& g, TidyBufs& b, uint32_t count, bool deletions, uint32_t* ou,
+                     uint32_t* ov, uint64_t* kept) {
   cudaStream_t s = c->stream;
   int vbits = 1;
   while (vbits < 32 && (1ull << vbits) < g.n) ++vbits;
   const int key_bits = deletions ? 32 : std::min(64, 2 * vbits);
   const uint32_t tiles = (count + kSortTile - 1) / kSortTile;
-  TidyBufs b;
   auto fail = [&](cudaError_t e) {
     b.release();
     set_error(std::string("prx_graph_tidy_batch: ") + cudaGetErrorString(e));
     return e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
   };
   cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess) e = cudaMalloc(&b.u, 4ull * count);
-  if (e == cudaSuccess) e = cudaMalloc(&b.v, 4ull * count);
   if (e == cudaSuccess) e = cudaMalloc(&b.flag, 4ull * (count + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b.pos, 4ull * (count + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b.hist, 4ull * ((size_t)kRadix * tiles + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b.key, 8ull * count);
   if (e == cudaSuccess) e = cudaMalloc(&b.key2, 8ull * count);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(b.u, hu, 4ull * count, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(b.v, hv, 4ull * count, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail(e);
   const int grid = grid_of(count, c->sms);
   // 1-2. existence and keys, then compaction of the kept keys
-  k_tidy_keys<<<grid, 256, 0, s>>>(g.xoff, g.xedg, b.u, b.v, count, deletions ? 1 : 0, vbits, b.flag, b.key);
+  k_tidy_keys<<<grid, 256, 0, s>>>(g.xoff, g.xedg, g.n, b.u, b.v, count, deletions ? 1 : 0, vbits, b.flag, b.key);
   e = cudaMemcpyAsync(b.pos, b.flag, 4ull * count, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b.pos + count, 0, 4, s);
   if (e == cudaSuccess) e = exclusive_scan_u32(b.pos, count + 1, s);
@@ -287,7 +337,7 @@ static int tidy_list(prx_context* c, const GraphDev& g, const uint32_t* hu, cons
   }
   // 3. radix sort of key2[0 .. m2)
   unsigned long long* src = nullptr;
-  e = radix_sort_u64(b.key2, b.key, m2, key_bits, b.hist, s, &src);
+  e = radix_sort_u64(b.key2, b.key, m2, 0, key_bits, b.hist, s, &src);
   if (e != cudaSuccess) return fail(e);
   // 4. unique and decode
   const int g2 = grid_of(m2, c->sms);
@@ -310,10 +360,31 @@ static int tidy_list(prx_context* c, const GraphDev& g, const uint32_t* hu, cons
   return PRX_OK;
 }
 
-extern "C" {
+// Tidy one list of `count` edges from host arrays into host arrays.
+static int tidy_list(prx_context* c, const GraphDev& g, const uint32_t* hu, const uint32_t* hv, uint64_t count64,
+                     bool deletions, uint32_t* ou, uint32_t* ov, uint64_t* kept) {
+  *kept = 0;
+  if (count64 == 0) return PRX_OK;
+  if (count64 >= 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_tidy_batch: batch too large");
+  const uint32_t count = (uint32_t)count64;
+  TidyBufs b;
+  cudaError_t e = cudaMalloc(&b.u, 4ull * count);
+  if (e == cudaSuccess) e = cudaMalloc(&b.v, 4ull * count);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b.u, hu, 4ull * count, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b.v, hv, 4ull * count, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) {
+    b.release();
+    set_error(std::string("prx_graph_tidy_batch: ") + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
+  }
+  return tidy_core(c, g, b, count, deletions, ou, ov, kept);
+}
 
-int prx_graph_create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, const uint32_t* v, uint64_t count64,
-                                int self_loops, prx_graph** out) {
+// prx_graph_create_from_edges[_device].  Device memory: the edge arrays (host
+// edges only), 3 key buffers of 8 bytes per edge, 2 scan buffers of 4 bytes
+// per edge, then the graph.
+static int create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, const uint32_t* v, uint64_t count64,
+                             int self_loops, bool on_device, prx_graph** out) {
   if (!c || !out) FAIL(PRX_EINVAL, "prx_graph_create_from_edges: NULL context or output");
   *out = nullptr;
   if (count64 && (!u || !v)) FAIL(PRX_EINVAL, "prx_graph_create_from_edges: NULL edge arrays");
@@ -330,16 +401,15 @@ int prx_graph_create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, c
   GraphDev& g = gr->g;
   g.device = c->device;
   g.n = n;
-  TidyBufs b;
-  unsigned long long *uniq = nullptr, *swp = nullptr;
+  TidyBufs b;                          // u, v (host edges), flag, pos, hist, key, key2
+  unsigned long long* key3 = nullptr;
   uint32_t* bad = nullptr;
   auto release = [&]() {
     b.release();
     b = TidyBufs();
-    cudaFree(uniq);
-    cudaFree(swp);
+    cudaFree(key3);
     cudaFree(bad);
-    uniq = swp = nullptr;
+    key3 = nullptr;
     bad = nullptr;
   };
   auto fail = [&](cudaError_t e) {
@@ -351,26 +421,31 @@ int prx_graph_create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, c
   const size_t cap = total ? total : 1;
   const uint32_t tiles = (total + kSortTile - 1) / kSortTile;
   cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess && count) e = cudaMalloc(&b.u, 4ull * count);
-  if (e == cudaSuccess && count) e = cudaMalloc(&b.v, 4ull * count);
+  const uint32_t *du = u, *dv = v;
+  if (!on_device && count) {
+    if (e == cudaSuccess) e = cudaMalloc(&b.u, 4ull * count);
+    if (e == cudaSuccess) e = cudaMalloc(&b.v, 4ull * count);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b.u, u, 4ull * count, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b.v, v, 4ull * count, cudaMemcpyHostToDevice, s);
+    du = b.u;
+    dv = b.v;
+  }
   if (e == cudaSuccess) e = cudaMalloc(&b.flag, 4ull * (cap + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b.pos, 4ull * (cap + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b.hist, 4ull * ((size_t)kRadix * tiles + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b.key, 8ull * cap);
   if (e == cudaSuccess) e = cudaMalloc(&b.key2, 8ull * cap);
-  if (e == cudaSuccess) e = cudaMalloc(&uniq, 8ull * cap);
-  if (e == cudaSuccess) e = cudaMalloc(&swp, 8ull * cap);
+  if (e == cudaSuccess) e = cudaMalloc(&key3, 8ull * cap);
   if (e == cudaSuccess) e = cudaMalloc(&bad, 4);
   if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, 4, s);
-  if (e == cudaSuccess && count) e = cudaMemcpyAsync(b.u, u, 4ull * count, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess && count) e = cudaMemcpyAsync(b.v, v, 4ull * count, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail(e);
   const int grid = grid_of(cap, c->sms);
   // sorted unique (u, v): the out-CSR
-  k_ingest_keys<<<grid, 256, 0, s>>>(b.u, b.v, count, n, self_loops ? 1 : 0, vbits, b.key, bad);
+  k_ingest_keys<<<grid, 256, 0, s>>>(du, dv, count, n, self_loops ? 1 : 0, vbits, b.key, bad);
   unsigned long long* sorted = nullptr;
-  e = radix_sort_u64(b.key, b.key2, total, 2 * vbits, b.hist, s, &sorted);
+  e = radix_sort_u64(b.key, b.key2, total, 0, 2 * vbits, b.hist, s, &sorted);
   if (e != cudaSuccess) return fail(e);
+  unsigned long long* uniq = sorted == b.key ? b.key2 : b.key;  // the sort's spare buffer
   k_first_flags<<<grid, 256, 0, s>>>(sorted, total, b.flag);
   e = cudaMemcpyAsync(b.pos, b.flag, 4ull * total, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b.pos + total, 0, 4, s);
@@ -378,7 +453,7 @@ int prx_graph_create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, c
   uint32_t m = 0, bad_h = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&m, b.pos + total, 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(&bad_h, bad, 4, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) k_ingest_split<<<grid, 256, 0, s>>>(sorted, b.flag, b.pos, total, vbits, 1, uniq, swp);
+  if (e == cudaSuccess) k_ingest_split<<<grid, 256, 0, s>>>(sorted, b.flag, b.pos, total, vbits, 1, uniq, key3);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return fail(e);
   if (bad_h) {
@@ -393,13 +468,17 @@ int prx_graph_create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, c
   if (e == cudaSuccess) e = cudaMalloc(&g.xtedg, 4ull * edge_slots(m));
   if (e == cudaSuccess) e = cudaMalloc(&g.xtdat, 4ull * (n ? n : 1));
   if (e != cudaSuccess) return fail(e);
-  const int g2 = grid_of((uint64_t)m + 1, c->sms);
-  k_ingest_csr<<<g2, 256, 0, s>>>(uniq, m, vbits, n, g.xoff, g.xedg);
-  k_ingest_degree<<<grid_of(n, c->sms), 256, 0, s>>>(g.xoff, n, g.xtdat);
-  // the transpose: the swapped keys sorted
-  e = radix_sort_u64(swp, b.key, m, 2 * vbits, b.hist, s, &sorted);
+  const int gm = grid_of(m, c->sms), gn = grid_of((uint64_t)n + 1, c->sms);
+  k_ingest_offsets<<<gn, 256, 0, s>>>(uniq, m, vbits, n, g.xoff);
+  k_ingest_columns<<<gm, 256, 0, s>>>(uniq, m, vbits, g.xedg);
+  k_ingest_degree<<<gn, 256, 0, s>>>(g.xoff, n, g.xtdat);
+  // the transpose: the swapped keys v * 2^b + u arrive ordered by u, so a
+  // stable sort on their high half (v) alone orders them by (v, u); the
+  // spare buffer is the old sorted one
+  e = radix_sort_u64(key3, sorted, m, vbits, 2 * vbits, b.hist, s, &sorted);
   if (e != cudaSuccess) return fail(e);
-  k_ingest_csr<<<g2, 256, 0, s>>>(sorted, m, vbits, n, g.xtoff, g.xtedg);
+  k_ingest_offsets<<<gn, 256, 0, s>>>(sorted, m, vbits, n, g.xtoff);
+  k_ingest_columns<<<gm, 256, 0, s>>>(sorted, m, vbits, g.xtedg);
   e = cudaStreamSynchronize(s);
   if (e == cudaSuccess) e = cudaGetLastError();
   release();
@@ -408,6 +487,18 @@ int prx_graph_create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, c
   if (e != cudaSuccess) return fail(e);
   *out = gr;
   return PRX_OK;
+}
+
+extern "C" {
+
+int prx_graph_create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, const uint32_t* v, uint64_t count,
+                                int self_loops, prx_graph** out) {
+  return create_from_edges(c, n, u, v, count, self_loops, false, out);
+}
+
+int prx_graph_create_from_edges_device(prx_context* c, uint32_t n, const uint32_t* u, const uint32_t* v,
+                                       uint64_t count, int self_loops, prx_graph** out) {
+  return create_from_edges(c, n, u, v, count, self_loops, true, out);
 }
 
 int prx_graph_tidy_batch(prx_context* c, prx_graph* gr, const uint32_t* du, const uint32_t* dv, uint64_t nd,
@@ -427,6 +518,42 @@ int prx_graph_tidy_batch(prx_context* c, prx_graph* gr, const uint32_t* du, cons
   int st = tidy_list(c, g, du, dv, nd, true, out_du, out_dv, out_nd);
   if (st) return st;
   return tidy_list(c, g, iu, iv, ni, false, out_iu, out_iv, out_ni);
+}
+
+int prx_graph_gen_batch(prx_context* c, prx_graph* gr, uint64_t nd_req, uint64_t ni_req, uint64_t seed,
+                        uint32_t* out_du, uint32_t* out_dv, uint64_t* out_nd, uint32_t* out_iu, uint32_t* out_iv,
+                        uint64_t* out_ni) {
+  if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_graph_gen_batch: bad context or graph");
+  const GraphDev& g = gr->g;
+  if (!g.xoff) FAIL(PRX_ESTATE, "prx_graph_gen_batch: graph has no out-CSR");
+  if (!out_nd || !out_ni || (nd_req && (!out_du || !out_dv)) || (ni_req && (!out_iu || !out_iv)))
+    FAIL(PRX_EINVAL, "prx_graph_gen_batch: NULL output");
+  if (g.n == 0) FAIL(PRX_EINVAL, "prx_graph_gen_batch: empty graph");
+  if (nd_req >= 0xffffffffull || ni_req >= 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_gen_batch: batch too large");
+  TRY_CUDA_ST(cudaSetDevice(c->device));
+  *out_nd = *out_ni = 0;
+  for (int del = 1; del >= 0; --del) {
+    const uint32_t count = (uint32_t)(del ? nd_req : ni_req);
+    if (!count) continue;
+    TidyBufs b;
+    cudaError_t e = cudaMalloc(&b.u, 4ull * count);
+    if (e == cudaSuccess) e = cudaMalloc(&b.v, 4ull * count);
+    if (e == cudaSuccess) {
+      const int grid = grid_of(count, c->sms);
+      if (del) k_gen_deletions<<<grid, 256, 0, c->stream>>>(g.xoff, g.xedg, g.n, g.m, seed, count, b.u, b.v);
+      else k_gen_insertions<<<grid, 256, 0, c->stream>>>(g.n, seed, count, b.u, b.v);
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+      b.release();
+      set_error(std::string("prx_graph_gen_batch: ") + cudaGetErrorString(e));
+      return e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
+    }
+    const int st = del ? tidy_core(c, g, b, count, true, out_du, out_dv, out_nd)
+                       : tidy_core(c, g, b, count, false, out_iu, out_iv, out_ni);
+    if (st) return st;
+  }
+  return PRX_OK;
 }
 
 }  // extern "C"

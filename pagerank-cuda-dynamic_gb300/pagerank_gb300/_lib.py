@@ -79,7 +79,8 @@ EXPORTS = (
     "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_selftest_division",
     "prx_solve_ppr_batched", "prx_solve_ppr_batched_device", "prx_graph_set_weights", "prx_solve_weighted",
     "prx_adjoint", "prx_autotune", "prx_graph_tidy_batch", "prx_graph_create_from_edges",
-    "prx_edge_reader_open", "prx_edge_reader_next", "prx_edge_reader_close", "prx_read_mtx",
+    "prx_graph_create_from_edges_device", "prx_graph_gen_batch",
+    "prx_edge_reader_open", "prx_edge_reader_next", "prx_edge_reader_close", "prx_read_mtx", "prx_format_glog",
     "prx_host_csr_free",
     "prx_gen_rmat", "prx_gen_weblike", "prx_gen_grid", "prx_gen_batch", "prx_host_tidy_batch",
     "prx_host_apply_batch", "prx_host_transpose", "prx_host_free",
@@ -128,10 +129,13 @@ def load(build_if_missing=True):
         "prx_graph_tidy_batch": (i32, [vp, vp, vp, vp, u64, vp, vp, u64, vp, vp, C.POINTER(u64), vp, vp,
                                        C.POINTER(u64)]),
         "prx_graph_create_from_edges": (i32, [vp, C.c_uint32, vp, vp, u64, i32, C.POINTER(vp)]),
+        "prx_graph_create_from_edges_device": (i32, [vp, C.c_uint32, vp, vp, u64, i32, C.POINTER(vp)]),
+        "prx_graph_gen_batch": (i32, [vp, vp, u64, u64, u64, vp, vp, C.POINTER(u64), vp, vp, C.POINTER(u64)]),
         "prx_edge_reader_open": (i32, [C.c_char_p, C.POINTER(vp)]),
         "prx_edge_reader_next": (i32, [vp, C.c_uint32, u64, i32, C.POINTER(u32p), C.POINTER(u32p), C.POINTER(u64),
                                        C.POINTER(u64)]),
         "prx_edge_reader_close": (i32, [vp]),
+        "prx_format_glog": (i32, [C.c_char_p, C.c_size_t, dbl, dbl, i32, i32, C.POINTER(Result), dbl, C.c_char_p]),
         "prx_read_mtx": (i32, [C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(u32p), C.POINTER(u32p),
                                C.POINTER(u64)]),
         "prx_solve_weighted": (i32, [vp, vp, vp, vp, C.POINTER(Options), vp, C.POINTER(Result)]),

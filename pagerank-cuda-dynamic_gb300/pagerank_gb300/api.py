@@ -103,6 +103,24 @@ class Graph:
                                                  C.byref(g._h)), "prx_graph_create_from_edges")
         return g
 
+    @classmethod
+    def from_device_edges(cls, ctx, n, u, v, self_loops=True):
+        """prx_graph_create_from_edges_device: u, v are int32/uint32 CUDA
+        tensors (torch) of equal length, already resident on the device."""
+        if u.numel() != v.numel() or u.element_size() != 4 or v.element_size() != 4:
+            raise ValueError("u and v must be 4-byte integer tensors of equal length")
+        if not (u.is_cuda and v.is_cuda and u.is_contiguous() and v.is_contiguous()):
+            raise ValueError("u and v must be contiguous CUDA tensors")
+        import torch
+        torch.cuda.current_stream(u.device).synchronize()   # the library works on its own stream
+        g = cls.__new__(cls)
+        g.ctx = ctx
+        g._h = C.c_void_p()
+        check(load().prx_graph_create_from_edges_device(ctx.handle, int(n), u.data_ptr() or None,
+                                                        v.data_ptr() or None, u.numel(), int(bool(self_loops)),
+                                                        C.byref(g._h)), "prx_graph_create_from_edges_device")
+        return g
+
     @property
     def handle(self):
         return self._h
@@ -132,6 +150,18 @@ class Graph:
         check(load().prx_graph_tidy_batch(self.ctx.handle, self._h, _p(du), _p(dv), len(du), _p(iu), _p(iv), len(iu),
                                           od.ctypes.data, odv.ctypes.data, C.byref(nd), oi.ctypes.data,
                                           oiv.ctypes.data, C.byref(ni)), "prx_graph_tidy_batch")
+        return od[:nd.value], odv[:nd.value], oi[:ni.value], oiv[:ni.value]
+
+    def gen_batch(self, n_del, n_ins, seed=7):
+        """prx_graph_gen_batch: a random batch drawn and tidied on the device ->
+        (del_u, del_v, ins_u, ins_v); the same as graphs.random_batch on this
+        graph's out-CSR."""
+        od, odv = np.zeros(max(n_del, 1), np.uint32), np.zeros(max(n_del, 1), np.uint32)
+        oi, oiv = np.zeros(max(n_ins, 1), np.uint32), np.zeros(max(n_ins, 1), np.uint32)
+        nd, ni = C.c_uint64(), C.c_uint64()
+        check(load().prx_graph_gen_batch(self.ctx.handle, self._h, int(n_del), int(n_ins), int(seed), od.ctypes.data,
+                                         odv.ctypes.data, C.byref(nd), oi.ctypes.data, oiv.ctypes.data,
+                                         C.byref(ni)), "prx_graph_gen_batch")
         return od[:nd.value], odv[:nd.value], oi[:ni.value], oiv[:ni.value]
 
     def download(self):

@@ -9,7 +9,8 @@ compiled against the headers of puzzlef/pagerank-cuda-dynamic by
   pieces_<file>_u<i>/_v<i>    readTemporalDo (inc/snap.hxx:41-52) per piece
   mtx_<file>_header/_u/_v     readMtxDo (inc/mtx.hxx:119-135), 1-based ids
   pipe_*                      main.cu's graph flow (x, xt, then per batch
-                              raw and tidied insertions, y, yt), 0-based CSRs
+                              raw and tidied insertions, y, yt; each y is
+                              the next batch's x), 0-based CSRs
 
 Run from the repository root where the reference headers exist:
     make -C oracle ref && python tests/golden/make_readers_golden.py

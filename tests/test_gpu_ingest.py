@@ -67,7 +67,7 @@ def test_ingest_reference_pipeline(pg, ctx):
         x = pg.Graph.from_edges(ctx, rows, u, v, self_loops=True)
         assert_graph(x, z["pipe_x_off"], z["pipe_x_edg"], z["pipe_xt_off"], z["pipe_xt_edg"], z["pipe_xt_dat"])
         xoff, xedg = z["pipe_x_off"], z["pipe_x_edg"]
-        for b in range(int(z["pipe_batches"])):
+        for b in range(int(z["pipe_batches"])):   # each batch applies to the graph the last one made
             bu, bv, _ = r.next(rows, int(frac * size))
             du, dv, iu, iv = x.tidy_batch([], [], bu, bv)
             assert np.array_equal(iu, z[f"pipe_ins_u{b}"] - 1) and np.array_equal(iv, z[f"pipe_ins_v{b}"] - 1)
@@ -81,8 +81,9 @@ def test_ingest_reference_pipeline(pg, ctx):
                                      self_loops=False)
             assert_graph(y2, z[f"pipe_y{b}_off"], z[f"pipe_y{b}_edg"], z[f"pipe_yt{b}_off"],
                          z[f"pipe_yt{b}_edg"], z[f"pipe_yt_dat{b}"])
-            y.close()
+            x.close()
             y2.close()
+            x, (xoff, xedg) = y, (z[f"pipe_y{b}_off"], z[f"pipe_y{b}_edg"])
         x.close()
 
 
@@ -113,6 +114,20 @@ def test_ingest_random_vs_numpy(pg, ctx, n, m, self_loops):
     g.close()
 
 
+def test_ingest_from_device_edges(pg, ctx):
+    import torch
+    rng = np.random.default_rng(11)
+    n, m = 50_000, 800_000
+    u = rng.integers(0, n, m).astype(np.uint32)
+    v = rng.integers(0, n, m).astype(np.uint32)
+    du = torch.from_numpy(u.view(np.int32)).cuda()
+    dv = torch.from_numpy(v.view(np.int32)).cuda()
+    g = pg.Graph.from_device_edges(ctx, n, du, dv, self_loops=True)
+    assert_graph(g, *numpy_csr(n, u, v, True))
+    g.close()
+    assert torch.equal(du.cpu(), torch.from_numpy(u.view(np.int32)))   # inputs left unchanged
+
+
 def test_ingest_solves_like_host_built_graph(pg, ctx):
     off, edg = pg.graphs.rmat(12, 16, seed=9)
     u, v = edges_of(off, edg)
@@ -135,3 +150,22 @@ def test_ingest_errors(pg, ctx):
     g = pg.Graph.from_edges(ctx, 4, [1], [2])                 # context still usable after the errors
     assert g.size() == (4, 5)
     g.close()
+
+
+def test_experiment_driver_runs_main_cu_flow(pg):
+    """python -m pagerank_gb300.experiment on the temporal fixture: graph
+    sizes as the reference's builder gives them, one result line per technique
+    and batch in main.cu's format, every error small."""
+    from pagerank_gb300 import experiment, report
+    z = np.load(os.path.join(READERS, "readers.npz"))
+    lines = experiment.run(os.path.join(READERS, "temporal_small.txt"), int(z["pipe_rows"]), int(z["pipe_size"]),
+                           float(z["pipe_frac"]), batches=int(z["pipe_batches"]), partition=True, out=lambda s: None)
+    text = "\n".join(lines)
+    assert f"size: {len(z['pipe_x_edg'])} [directed] {{}} (selfLoopAllVertices)" in text
+    for b in range(int(z["pipe_batches"])):
+        assert f"size: {len(z[f'pipe_y{b}_edg'])} [directed] {{}} (insertions={len(z[f'pipe_ins_u{b}'])})" in text
+    rows = report.parse_log(text)
+    assert len(rows) == 10 * int(z["pipe_batches"])
+    assert {r["technique"] for r in rows} == {t + p for t, _ in experiment.TECHNIQUES for p in ("", "Partition")}
+    for r in rows:   # L1 over 500 vertices; tolerance 1e-10 (L-inf), frontier / prune tolerances 1e-6
+        assert r["error"] < (1e-6 if "Frontier" not in r["technique"] else 1e-5) and r["iterations"] >= 1, r

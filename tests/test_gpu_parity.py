@@ -329,3 +329,20 @@ def test_device_tidy_matches_host_tidy(pg, ctx, kind):
     e = np.zeros(0, np.uint32)
     assert all(len(a) == 0 for a in g.tidy_batch(e, e, e, e))
     g.close()
+
+
+@pytest.mark.parametrize("kind", ["rmat", "grid"])
+def test_device_batch_generation_matches_host(pg, ctx, kind):
+    """prx_graph_gen_batch draws the same raw batch as the host generator
+    (same counter-based hashes) and tidies it on the device."""
+    if kind == "rmat":
+        xoff, xedg = pg.graphs.rmat(14, 8, seed=3)
+    else:
+        xoff, xedg = pg.graphs.grid(128, seed=3)
+    g = pg.Graph.from_out_csr(ctx, xoff, xedg)
+    for nd, ni, seed in [(0, 0, 1), (5, 0, 2), (0, 7, 3), (300, 1200, 4), (20000, 80000, 5)]:
+        want = pg.graphs.random_batch(xoff, xedg, nd, ni, seed=seed)
+        got = g.gen_batch(nd, ni, seed=seed)
+        for a, b in zip(got, want):
+            assert np.array_equal(a, b), (nd, ni, seed)
+    g.close()
