@@ -10,7 +10,7 @@
 //      like (u, v)); a kept insertion is u * 2^b + v with b = bits(n - 1);
 //   3. an LSD radix sort of the keys, 8-bit digits, stable (our own: per-block
 //      digit histograms, a digit-major scan, and a scatter that ranks equal
-//      digits in element order with __match_any_sync);
+//      digits in element order with warp ballots);
 //   4. unique: first occurrences kept (scan of flags), decoded back to (u, v).
 //
 // Ingest (prx_graph_create_from_edges): the reference builds its DiGraph from
@@ -29,7 +29,7 @@ namespace prx {
 
 constexpr int kRadix = 256;
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 8;                       // elements per thread per tile
+constexpr int kSortItems = 16;                      // elements per thread per tile
 constexpr int kSortTile = kSortThreads * kSortItems;
 
 // Position of edge (u, v) in the out-CSR, or UINT32_MAX.
@@ -74,55 +74,128 @@ __global__ void k_compact64(const unsigned long long* __restrict__ in, const uin
     if (flag[i]) out[pos[i]] = in[i];
 }
 
+// Lanes of the warp holding the same 8-bit digit d as this lane, among the
+// lanes where act is set: eight ballots, one per digit bit.
+__device__ __forceinline__ unsigned digit_peers(uint32_t d, bool act) {
+  unsigned peers = __ballot_sync(0xffffffffu, act);
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const unsigned m = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? m : ~m;
+  }
+  return peers;
+}
+
+// Element order within a tile (both radix steps): warp w owns the
+// kSortItems * 32 consecutive keys from tile0 + w * kSortItems * 32, read 32
+// at a time (round r: tile0 + w * kSortItems * 32 + r * 32 + lane).
+
 // Radix pass, step 1: per-tile digit counts, digit-major: hist[d * tiles + b].
+// Each warp counts into its own shared histogram.
 __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long long* __restrict__ key,
                                                              uint32_t count, int shift, uint32_t tiles,
                                                              uint32_t* __restrict__ hist) {
-  __shared__ uint32_t cnt[kRadix];
-  cnt[threadIdx.x] = 0;
+  constexpr int kWarps = kSortThreads / 32;
+  __shared__ uint32_t cnt[kWarps][kRadix];
+  const uint32_t t = threadIdx.x, w = t >> 5, lane = t & 31u;
+  for (int k = 0; k < kWarps; ++k) cnt[k][t] = 0;
   __syncthreads();
-  const uint32_t base = blockIdx.x * kSortTile;
+  const uint32_t base = blockIdx.x * kSortTile + w * (kSortItems * 32) + lane;
+  unsigned long long k[kSortItems];  // all loads in flight before the first use
+#pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
-    const uint32_t i = base + r * kSortThreads + threadIdx.x;
-    if (i < count) atomicAdd(&cnt[(key[i] >> shift) & (kRadix - 1)], 1u);
+    const uint32_t i = base + r * 32;
+    k[r] = i < count ? key[i] : 0ull;
   }
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r)
+    if (base + r * 32 < count) atomicAdd(&cnt[w][(k[r] >> shift) & (kRadix - 1)], 1u);
   __syncthreads();
-  hist[threadIdx.x * tiles + blockIdx.x] = cnt[threadIdx.x];
+  uint32_t sum = 0;
+  for (int q = 0; q < kWarps; ++q) sum += cnt[q][t];
+  hist[t * tiles + blockIdx.x] = sum;
 }
 
-// Radix pass, step 2 (after the scan of hist): stable scatter.  The tile's
-// elements go round by round (round r: elements r*256 + t); within a round an
-// element's rank among equal digits is the count in lower warps plus its rank
-// in its warp (__match_any_sync), so element order is kept.
-__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned long long* __restrict__ in,
+// Radix pass, step 2 (after the exclusive scan of hist, so start[d * tiles +
+// b] is where tile b's keys of digit d go): stable scatter.  Each warp ranks
+// its keys among equal digits round by round (earlier rounds: a running
+// per-warp count; within the round: lanes below with the same digit, from
+// digit_peers); the tile is then laid out by digit in shared memory (digit
+// start in the tile + keys of that digit in lower warps + rank) and written
+// out in that order, so the keys of one digit leave as one contiguous,
+// coalesced run.
+__global__ void __launch_bounds__(kSortThreads, 3) k_radix_scatter(const unsigned long long* __restrict__ in,
                                                                 uint32_t count, int shift, uint32_t tiles,
                                                                 const uint32_t* __restrict__ start,
                                                                 unsigned long long* __restrict__ out) {
   constexpr int kWarps = kSortThreads / 32;
-  __shared__ uint32_t base[kRadix];
-  __shared__ uint32_t wcnt[kWarps][kRadix];
+  __shared__ unsigned long long sk[kSortTile];
+  __shared__ uint32_t gbase[kRadix];          // global start of this tile's digit-d run
+  __shared__ uint32_t tstart[kRadix];         // start of digit d within the tile
+  __shared__ uint32_t wrun[kWarps][kRadix];   // per warp: keys of digit d so far, then before this warp
+  __shared__ uint32_t wsum[kWarps];
   const uint32_t t = threadIdx.x, w = t >> 5, lane = t & 31u;
-  base[t] = start[t * tiles + blockIdx.x];
+  const uint32_t tile0 = blockIdx.x * kSortTile;
+  const size_t idx = (size_t)t * tiles + blockIdx.x;
+  const uint32_t s0 = start[idx];
+  const uint32_t s1 = idx + 1 < (size_t)kRadix * tiles ? start[idx + 1] : count;
+  const uint32_t c = s1 - s0;   // this tile's keys of digit t
+  gbase[t] = s0;
+  for (int k = 0; k < kWarps; ++k) wrun[k][t] = 0;
+  const uint32_t base = tile0 + w * (kSortItems * 32) + lane;
+  unsigned long long kr[kSortItems];  // all loads in flight before the first use
+#pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
-    for (int k = 0; k < kWarps; ++k) wcnt[k][t] = 0;
-    __syncthreads();
-    const uint32_t i = blockIdx.x * kSortTile + r * kSortThreads + t;
-    const bool act = i < count;
-    const unsigned long long x = act ? in[i] : 0ull;
-    const uint32_t d = act ? (uint32_t)((x >> shift) & (kRadix - 1)) : (uint32_t)kRadix;  // kRadix: none
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t below = __popc(peers & ((1u << lane) - 1u));
-    if (act && below == 0) wcnt[w][d] = __popc(peers);
-    __syncthreads();
-    if (act) {
-      uint32_t pos = base[d] + below;
-      for (uint32_t k = 0; k < w; ++k) pos += wcnt[k][d];
-      out[pos] = x;
+    const uint32_t i = base + r * 32;
+    kr[r] = i < count ? in[i] : 0ull;
+  }
+  __syncthreads();
+  uint32_t rank[kSortItems];
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const bool act = base + r * 32 < count;
+    const uint32_t d = (uint32_t)((kr[r] >> shift) & (kRadix - 1));
+    const unsigned peers = digit_peers(d, act);
+    const uint32_t below = __popc(peers & lt);
+    rank[r] = act ? wrun[w][d] + below : 0;
+    __syncwarp();
+    if (act && below == 0) wrun[w][d] += __popc(peers);
+    __syncwarp();
+  }
+  // exclusive block scan of c over the 256 digits -> tstart; per digit, the
+  // keys in lower warps -> wrun
+  uint32_t x = c;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  uint32_t before = 0;
+  for (uint32_t k = 0; k < w; ++k) before += wsum[k];
+  tstart[t] = before + x - c;
+  uint32_t acc = 0;
+  for (int k = 0; k < kWarps; ++k) {
+    const uint32_t v = wrun[k][t];
+    wrun[k][t] = acc;
+    acc += v;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    if (base + r * 32 < count) {
+      const uint32_t d = (uint32_t)((kr[r] >> shift) & (kRadix - 1));
+      sk[tstart[d] + wrun[w][d] + rank[r]] = kr[r];
     }
-    __syncthreads();
-    uint32_t add = 0;
-    for (int k = 0; k < kWarps; ++k) add += wcnt[k][t];
-    base[t] += add;
+  }
+  __syncthreads();
+  const uint32_t nt = count - tile0 < (uint32_t)kSortTile ? count - tile0 : (uint32_t)kSortTile;
+  for (uint32_t j = t; j < nt; j += kSortThreads) {
+    const unsigned long long key = sk[j];
+    const uint32_t d = (uint32_t)((key >> shift) & (kRadix - 1));
+    out[gbase[d] + (j - tstart[d])] = key;
   }
 }
 
