@@ -21,6 +21,7 @@ import json
 import os
 import re
 import statistics
+import tempfile
 import subprocess
 import sys
 import time
@@ -514,10 +515,42 @@ def run_ingest(args, pg, ctx, local, xoff, xedg):
     host_ms, m_host = timed(lambda: pg.Graph.from_edges(ctx, n, u, v, self_loops=True), 1)
     assert m_dev == m_host == m, (m_dev, m_host, m)
     dmed = statistics.median(dev_ms)
+    # the shuffled sample as SNAP temporal text ("u v" lines, 1-based): parsed
+    # on the device from host memory, and from a file in memory (tmpfs) by the
+    # device parser and by the host reader (16 threads)
+    t = time.perf_counter()
+    text = pg.graphs.format_edges(u[:k][perm], v[:k][perm])
+    fmt_s = time.perf_counter() - t
+    text_ms, m_text = timed(lambda: pg.Graph.from_text(ctx, text, n, None, self_loops=True)[0], args.ingest_steps)
+    assert m_text == ms2, (m_text, ms2)
+    shm = "/dev/shm" if os.path.isdir("/dev/shm") else None
+    fd, path = tempfile.mkstemp(suffix=".txt", dir=shm)
+    try:
+        with os.fdopen(fd, "wb") as f:
+            f.write(text)
+        nbytes = len(text)
+        del text
+
+        def from_file():
+            with pg.graphs.EdgeReader(path) as r:
+                return pg.Graph.from_reader(ctx, r, n, k, self_loops=True)[0]
+        file_ms, m_file = timed(from_file, 1)
+        assert m_file == ms2, (m_file, ms2)
+        t = time.perf_counter()
+        with pg.graphs.EdgeReader(path) as r:
+            hu, hv, hl = r.next(n, k)
+        host_parse_ms = (time.perf_counter() - t) * 1e3
+        assert hl == k and len(hu) == k
+        del hu, hv
+    finally:
+        os.unlink(path)
     return {"workload": f"edge list of the bench graph ({m} edges in row order, {n} vertices) plus a self-loop "
                         "on every vertex -> out-CSR, in-CSR, out-degrees on the device",
             "device_ms": dev_ms, "host_arrays_ms": host_ms, "edges_per_s_device": m / (dmed / 1e3),
-            "h2d_bytes": 8 * m, "sample_edges": k, "sample_row_order_ms": sorted_ms, "sample_shuffled_ms": shuf_ms}
+            "h2d_bytes": 8 * m, "sample_edges": k, "sample_row_order_ms": sorted_ms, "sample_shuffled_ms": shuf_ms,
+            "text": {"lines": k, "bytes": nbytes, "format_s": fmt_s, "device_parse_and_build_ms": text_ms,
+                     "device_parse_and_build_from_file_ms": file_ms, "file": "tmpfs" if shm else "disk",
+                     "host_parse_only_ms": host_parse_ms, "host_threads": os.cpu_count()}}
 
 
 def run_ours(args):

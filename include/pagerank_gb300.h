@@ -413,6 +413,29 @@ int prx_edge_reader_close(prx_edge_reader* r);
  * "matrix coordinate" gives n = 0 and no edges; reading stops at the first
  * line without two unsigned integers.  Ids must lie in 1..n. */
 int prx_read_mtx(const char* path, uint32_t* n, uint32_t** u, uint32_t** v, uint64_t* count);
+/* The edges as text, "u v\n" per edge with 1-based ids (what the readers
+ * take); *text is allocated by the library, free with prx_host_free. */
+int prx_format_edges(const uint32_t* u, const uint32_t* v, uint64_t count, char** text, uint64_t* bytes);
+
+/* Edge-list text parsed on the DEVICE and built into a graph there (the
+ * same lines and the same edges as the host readers above, then what
+ * prx_graph_create_from_edges does with them).  Symmetric != 0 adds (v, u)
+ * after each (u, v); self_loops != 0 adds a loop on every vertex.
+ *
+ * prx_graph_create_from_text: up to `size` lines of text[0 .. bytes), host
+ * memory, ids in 1..rows, the last line may lack its newline; *lines and
+ * *used receive the lines and bytes consumed (either may be NULL).
+ * prx_edge_reader_next_graph: the next `size` lines of an open reader, as
+ * prx_edge_reader_next reads them (the reference's first 90% read,
+ * main.cu:167, builds its graph this way).
+ * prx_graph_create_from_mtx: a whole MatrixMarket coordinate file, n =
+ * max(rows, cols) (*n_out may be NULL). */
+int prx_graph_create_from_text(prx_context* ctx, const char* text, uint64_t bytes, uint32_t rows, uint64_t size,
+                               int symmetric, int self_loops, prx_graph** out, uint64_t* lines, uint64_t* used);
+int prx_edge_reader_next_graph(prx_edge_reader* r, prx_context* ctx, uint32_t rows, uint64_t size, int symmetric,
+                               int self_loops, prx_graph** out, uint64_t* lines);
+int prx_graph_create_from_mtx(prx_context* ctx, const char* path, int self_loops, prx_graph** out,
+                              uint32_t* n_out);
 /* One result line in the reference driver's log format (main.cu:54-61):
  * "{-<del>/+<ins> batchf, <batch> batchi, <threads> threads} -> {<time>ms,
  * <init>ms init, <mark>ms mark, <comp>ms comp, <iter> iter, <err> err}

@@ -19,30 +19,14 @@
 #include <vector>
 #include <omp.h>
 #include "pagerank_gb300.h"
+#include "prx_reader.h"
 
 namespace prx {
 void set_error(const std::string& msg);
 }
 
-struct prx_edge_reader {
-  FILE* f = nullptr;
-  std::vector<char> buf;
-  size_t beg = 0, end = 0;  // unread bytes: buf[beg .. end)
-  bool eof = false;
-};
+namespace prx_io {
 
-namespace {
-
-constexpr size_t kBufBytes = 64u << 20;
-constexpr size_t kBlockLines = 1u << 20;
-
-int fail(int code, const std::string& msg) {
-  prx::set_error(msg);
-  return code;
-}
-
-// Move the unread bytes to the front and read more (the buffer doubles when a
-// single line fills it).  Sets eof when nothing more could be read.
 void fill(prx_edge_reader* r) {
   if (r->beg > 0) {
     std::memmove(r->buf.data(), r->buf.data() + r->beg, r->end - r->beg);
@@ -53,6 +37,52 @@ void fill(prx_edge_reader* r) {
   const size_t got = std::fread(r->buf.data() + r->end, 1, r->buf.size() - r->end, r->f);
   r->end += got;
   if (got == 0) r->eof = true;
+}
+
+}  // namespace prx_io
+
+namespace {
+
+using prx_io::fill;
+bool read_line(prx_edge_reader* r, std::string& line);
+bool parse_u64(const char*& p, const char* e, uint64_t& out);
+
+}  // namespace
+
+namespace prx_io {
+
+int mtx_header(prx_edge_reader* r, uint64_t* order, bool* symmetric) {
+  // comment lines start with '%', the banner with "%%"; the first other line
+  // holds rows, cols and the entry count
+  std::string line, h0, h1, h2, h3, h4;
+  for (;;) {
+    if (!read_line(r, line)) line.clear();
+    if (line.rfind('%', 0) != 0) break;
+    if (line.rfind("%%", 0) != 0) continue;
+    std::istringstream ss(line);
+    ss >> h0 >> h1 >> h2 >> h3 >> h4;
+  }
+  *order = 0;
+  *symmetric = false;
+  if (h1 != "matrix" || h2 != "coordinate") return PRX_OK;
+  *symmetric = h4 == "symmetric" || h4 == "skew-symmetric";
+  uint64_t rows = 0, cols = 0, size = 0;
+  const char* p = line.data();
+  const char* e = p + line.size();
+  if (parse_u64(p, e, rows) && parse_u64(p, e, cols) && parse_u64(p, e, size)) *order = std::max(rows, cols);
+  return PRX_OK;
+}
+
+}  // namespace prx_io
+
+namespace {
+
+constexpr size_t kBufBytes = 64u << 20;
+constexpr size_t kBlockLines = 1u << 20;
+
+int fail(int code, const std::string& msg) {
+  prx::set_error(msg);
+  return code;
 }
 
 // One line (without its '\n') as std::getline gives it; false at the end.
@@ -79,7 +109,7 @@ inline bool is_space(char c) { return c == ' ' || c == '\t' || c == '\r' || c ==
 
 // Unsigned decimal after optional whitespace and '+', like operator>> into an
 // unsigned integer; false if there are no digits or the value overflows.
-inline bool parse_u64(const char*& p, const char* e, uint64_t& out) {
+bool parse_u64(const char*& p, const char* e, uint64_t& out) {
   while (p < e && is_space(*p)) ++p;
   if (p < e && *p == '+') ++p;
   if (p >= e || *p < '0' || *p > '9') return false;
@@ -248,42 +278,66 @@ int prx_read_mtx(const char* path, uint32_t* n, uint32_t** u, uint32_t** v, uint
   prx_edge_reader* r = nullptr;
   int rc = prx_edge_reader_open(path, &r);
   if (rc != PRX_OK) return rc;
-  // header: comment lines start with '%', the banner with "%%"; the first
-  // other line holds rows, cols and the entry count
-  std::string line, h0, h1, h2, h3, h4;
-  for (;;) {
-    if (!read_line(r, line)) line.clear();
-    if (line.rfind('%', 0) != 0) break;
-    if (line.rfind("%%", 0) != 0) continue;
-    std::istringstream ss(line);
-    ss >> h0 >> h1 >> h2 >> h3 >> h4;
-  }
+  uint64_t order = 0;
+  bool symmetric = false;
+  rc = prx_io::mtx_header(r, &order, &symmetric);
+  if (rc == PRX_OK && order >= 0xffffffffull) rc = fail(PRX_ERANGE, "prx_read_mtx: more than 2^32 - 2 vertices");
   std::vector<uint32_t> U, V;
-  if (h1 == "matrix" && h2 == "coordinate") {
-    const bool symmetric = h4 == "symmetric" || h4 == "skew-symmetric";
-    uint64_t rows = 0, cols = 0, size = 0;
-    const char* p = line.data();
-    const char* e = p + line.size();
-    if (!(parse_u64(p, e, rows) && parse_u64(p, e, cols) && parse_u64(p, e, size))) rows = cols = 0;
-    const uint64_t order = std::max(rows, cols);
-    if (order >= 0xffffffffull) {
-      prx_edge_reader_close(r);
-      return fail(PRX_ERANGE, "prx_read_mtx: more than 2^32 - 2 vertices");
-    }
-    if (order > 0) {
-      uint64_t got = 0;
-      U.reserve((size_t)std::min<uint64_t>(size, 1u << 24) * (symmetric ? 2 : 1));
-      V.reserve(U.capacity());
-      rc = read_edges(r, order, UINT64_MAX, symmetric, U, V, &got);
-      if (rc != PRX_OK) {
-        prx_edge_reader_close(r);
-        return rc;
-      }
-      *n = (uint32_t)order;
-    }
+  if (rc == PRX_OK && order > 0) {
+    uint64_t got = 0;
+    rc = read_edges(r, order, UINT64_MAX, symmetric, U, V, &got);
+    if (rc == PRX_OK) *n = (uint32_t)order;
   }
   prx_edge_reader_close(r);
+  if (rc != PRX_OK) return rc;
   return hand_out(U, V, u, v, count);
+}
+
+int prx_format_edges(const uint32_t* u, const uint32_t* v, uint64_t count, char** text, uint64_t* bytes) {
+  // "u v\n" per edge, ids written 1-based (the readers' input format)
+  if (!text || !bytes || (count && (!u || !v))) return fail(PRX_EINVAL, "prx_format_edges: NULL argument");
+  *text = nullptr;
+  *bytes = 0;
+  auto digits = [](uint64_t x) {
+    int d = 1;
+    while (x >= 10) {
+      x /= 10;
+      ++d;
+    }
+    return d;
+  };
+  constexpr int64_t kBlock = 1 << 16;
+  const int64_t blocks = (int64_t)((count + kBlock - 1) / kBlock);
+  std::vector<uint64_t> off((size_t)blocks + 1, 0);
+#pragma omp parallel for schedule(static)
+  for (int64_t b = 0; b < blocks; ++b) {
+    uint64_t len = 0;
+    for (uint64_t i = (uint64_t)b * kBlock; i < std::min<uint64_t>(count, (uint64_t)(b + 1) * kBlock); ++i)
+      len += digits((uint64_t)u[i] + 1) + digits((uint64_t)v[i] + 1) + 2;
+    off[b + 1] = len;
+  }
+  for (int64_t b = 0; b < blocks; ++b) off[b + 1] += off[b];
+  char* out = (char*)std::malloc(off[blocks] ? off[blocks] : 1);
+  if (!out) return fail(PRX_ENOMEM, "prx_format_edges: host allocation failed");
+#pragma omp parallel for schedule(static)
+  for (int64_t b = 0; b < blocks; ++b) {
+    char* p = out + off[b];
+    for (uint64_t i = (uint64_t)b * kBlock; i < std::min<uint64_t>(count, (uint64_t)(b + 1) * kBlock); ++i) {
+      for (int k = 0; k < 2; ++k) {
+        uint64_t x = (uint64_t)(k ? v[i] : u[i]) + 1;
+        const int d = digits(x);
+        for (int q = d - 1; q >= 0; --q) {
+          p[q] = (char)('0' + x % 10);
+          x /= 10;
+        }
+        p += d;
+        *p++ = k ? '\n' : ' ';
+      }
+    }
+  }
+  *text = out;
+  *bytes = off[blocks];
+  return PRX_OK;
 }
 
 int prx_format_glog(char* buf, size_t len, double deletions_fraction, double insertions_fraction, int batch_index,

@@ -81,6 +81,7 @@ EXPORTS = (
     "prx_adjoint", "prx_autotune", "prx_graph_tidy_batch", "prx_graph_create_from_edges",
     "prx_graph_create_from_edges_device", "prx_graph_gen_batch",
     "prx_edge_reader_open", "prx_edge_reader_next", "prx_edge_reader_close", "prx_read_mtx", "prx_format_glog",
+    "prx_graph_create_from_text", "prx_edge_reader_next_graph", "prx_graph_create_from_mtx", "prx_format_edges",
     "prx_host_csr_free",
     "prx_gen_rmat", "prx_gen_weblike", "prx_gen_grid", "prx_gen_batch", "prx_host_tidy_batch",
     "prx_host_apply_batch", "prx_host_transpose", "prx_host_free",
@@ -135,6 +136,11 @@ def load(build_if_missing=True):
         "prx_edge_reader_next": (i32, [vp, C.c_uint32, u64, i32, C.POINTER(u32p), C.POINTER(u32p), C.POINTER(u64),
                                        C.POINTER(u64)]),
         "prx_edge_reader_close": (i32, [vp]),
+        "prx_graph_create_from_text": (i32, [vp, C.c_char_p, u64, C.c_uint32, u64, i32, i32, C.POINTER(vp),
+                                             C.POINTER(u64), C.POINTER(u64)]),
+        "prx_edge_reader_next_graph": (i32, [vp, vp, C.c_uint32, u64, i32, i32, C.POINTER(vp), C.POINTER(u64)]),
+        "prx_format_edges": (i32, [vp, vp, u64, C.POINTER(C.c_void_p), C.POINTER(u64)]),
+        "prx_graph_create_from_mtx": (i32, [vp, C.c_char_p, i32, C.POINTER(vp), C.POINTER(C.c_uint32)]),
         "prx_format_glog": (i32, [C.c_char_p, C.c_size_t, dbl, dbl, i32, i32, C.POINTER(Result), dbl, C.c_char_p]),
         "prx_read_mtx": (i32, [C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(u32p), C.POINTER(u32p),
                                C.POINTER(u64)]),

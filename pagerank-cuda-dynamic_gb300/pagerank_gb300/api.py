@@ -104,6 +104,48 @@ class Graph:
         return g
 
     @classmethod
+    def _wrap(cls, ctx):
+        g = cls.__new__(cls)
+        g.ctx = ctx
+        g._h = C.c_void_p()
+        return g
+
+    @classmethod
+    def from_text(cls, ctx, text, rows, size=None, symmetric=False, self_loops=True):
+        """prx_graph_create_from_text: SNAP temporal text (bytes, 1-based ids)
+        parsed and built on the device -> (graph, lines consumed, bytes consumed)."""
+        if not isinstance(text, bytes):
+            text = bytes(text)
+        g = cls._wrap(ctx)
+        lines, used = C.c_uint64(), C.c_uint64()
+        size = (1 << 64) - 1 if size is None else int(size)
+        check(load().prx_graph_create_from_text(ctx.handle, text, len(text), int(rows), size,
+                                                int(bool(symmetric)), int(bool(self_loops)), C.byref(g._h),
+                                                C.byref(lines), C.byref(used)), "prx_graph_create_from_text")
+        return g, lines.value, used.value
+
+    @classmethod
+    def from_reader(cls, ctx, reader, rows, size, symmetric=False, self_loops=True):
+        """prx_edge_reader_next_graph: the next `size` lines of an EdgeReader,
+        parsed and built on the device -> (graph, lines consumed)."""
+        g = cls._wrap(ctx)
+        lines = C.c_uint64()
+        check(load().prx_edge_reader_next_graph(reader._h, ctx.handle, int(rows), int(size), int(bool(symmetric)),
+                                                int(bool(self_loops)), C.byref(g._h), C.byref(lines)),
+              "prx_edge_reader_next_graph")
+        return g, lines.value
+
+    @classmethod
+    def from_mtx(cls, ctx, path, self_loops=True):
+        """prx_graph_create_from_mtx: a MatrixMarket coordinate file parsed and
+        built on the device -> (graph, n)."""
+        g = cls._wrap(ctx)
+        n = C.c_uint32()
+        check(load().prx_graph_create_from_mtx(ctx.handle, str(path).encode(), int(bool(self_loops)),
+                                               C.byref(g._h), C.byref(n)), "prx_graph_create_from_mtx")
+        return g, n.value
+
+    @classmethod
     def from_device_edges(cls, ctx, n, u, v, self_loops=True):
         """prx_graph_create_from_edges_device: u, v are int32/uint32 CUDA
         tensors (torch) of equal length, already resident on the device."""

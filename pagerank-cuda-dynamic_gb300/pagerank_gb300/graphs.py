@@ -156,3 +156,18 @@ def read_mtx(path):
     cnt = C.c_uint64()
     check(load().prx_read_mtx(str(path).encode(), C.byref(n), C.byref(u), C.byref(v), C.byref(cnt)), "prx_read_mtx")
     return n.value, _take(u, cnt.value), _take(v, cnt.value)
+
+
+def format_edges(u, v):
+    """prx_format_edges: "u v\\n" lines with 1-based ids -> bytes."""
+    u = np.ascontiguousarray(u, dtype=np.uint32)
+    v = np.ascontiguousarray(v, dtype=np.uint32)
+    if len(u) != len(v):
+        raise ValueError("u and v differ in length")
+    ptr, n = C.c_void_p(), C.c_uint64()
+    check(load().prx_format_edges(u.ctypes.data if len(u) else None, v.ctypes.data if len(v) else None, len(u),
+                                  C.byref(ptr), C.byref(n)), "prx_format_edges")
+    try:
+        return (C.c_char * n.value).from_address(ptr.value).raw if n.value else b""
+    finally:
+        load().prx_host_free(ptr)

@@ -169,3 +169,107 @@ def test_experiment_driver_runs_main_cu_flow(pg):
     assert {r["technique"] for r in rows} == {t + p for t, _ in experiment.TECHNIQUES for p in ("", "Partition")}
     for r in rows:   # L1 over 500 vertices; tolerance 1e-10 (L-inf), frontier / prune tolerances 1e-6
         assert r["error"] < (1e-6 if "Frontier" not in r["technique"] else 1e-5) and r["iterations"] >= 1, r
+
+
+# ---- edge-list text parsed on the device --------------------------------------
+
+def graph_of(pg, ctx, n, u, v, self_loops):
+    g = pg.Graph.from_edges(ctx, n, u, v, self_loops=self_loops)
+    d = g.download()
+    g.close()
+    return d
+
+
+def same_graph(g, want):
+    got = g.download()
+    g.close()
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))
+
+
+@pytest.mark.parametrize("stem", ["temporal_small", "temporal_edge"])
+def test_device_parse_pieces_match_host_reader(pg, ctx, stem):
+    """prx_edge_reader_next_graph reads the same lines as prx_edge_reader_next,
+    piece by piece, bad lines included (the fixtures are pinned to the
+    reference's readTemporalDo)."""
+    z = np.load(os.path.join(READERS, "readers.npz"))
+    rows = int(z[f"pieces_{stem}_rows"])
+    path = os.path.join(READERS, stem + ".txt")
+    with pg.graphs.EdgeReader(path) as rh, pg.graphs.EdgeReader(path) as rd:
+        for i, size in enumerate(z[f"pieces_{stem}_sizes"].tolist()):
+            u, v, lines = rh.next(rows, size)
+            assert np.array_equal(u, z[f"pieces_{stem}_u{i}"] - 1)
+            g, dlines = pg.Graph.from_reader(ctx, rd, rows, size, self_loops=False)
+            assert dlines == lines, (i, dlines, lines)
+            same_graph(g, graph_of(pg, ctx, rows, u, v, False))
+
+
+def test_device_parse_reference_pipeline(pg, ctx):
+    z = np.load(os.path.join(READERS, "readers.npz"))
+    rows, size = int(z["pipe_rows"]), int(z["pipe_size"])
+    with pg.graphs.EdgeReader(os.path.join(READERS, "temporal_small.txt")) as r:
+        g, lines = pg.Graph.from_reader(ctx, r, rows, int(0.90 * size), self_loops=True)
+    assert lines == int(0.90 * size)
+    same_graph(g, (z["pipe_x_off"], z["pipe_x_edg"], z["pipe_xt_off"], z["pipe_xt_edg"], z["pipe_xt_dat"]))
+    text = open(os.path.join(READERS, "temporal_small.txt"), "rb").read()
+    g, lines, used = pg.Graph.from_text(ctx, text, rows, int(0.90 * size), self_loops=True)
+    assert lines == int(0.90 * size) and text[:used].count(b"\n") == lines
+    same_graph(g, (z["pipe_x_off"], z["pipe_x_edg"], z["pipe_xt_off"], z["pipe_xt_edg"], z["pipe_xt_dat"]))
+
+
+@pytest.mark.parametrize("stem", ["general", "symmetric", "skew", "rect", "array", "crlf"])
+def test_device_parse_mtx(pg, ctx, stem):
+    path = os.path.join(READERS, stem + ".mtx")
+    n, u, v = pg.graphs.read_mtx(path)
+    g, gn = pg.Graph.from_mtx(ctx, path, self_loops=True)
+    assert gn == n
+    same_graph(g, graph_of(pg, ctx, n, u, v, True))
+
+
+def test_device_parse_large_text(pg, ctx):
+    """~6M lines (~75 MB: more than the reader's 64 MB buffer), read whole and
+    in irregular pieces, against the edges themselves."""
+    rng = np.random.default_rng(8)
+    rows, m = 2_000_000, 6_000_000
+    u = rng.integers(0, rows, m).astype(np.uint32)
+    v = rng.integers(0, rows, m).astype(np.uint32)
+    text = pg.graphs.format_edges(u, v)
+    g, lines, used = pg.Graph.from_text(ctx, text, rows, None, self_loops=True)
+    assert lines == m and used == len(text)
+    same_graph(g, numpy_csr(rows, u, v, True))
+    p = os.path.join(os.environ.get("TMPDIR", "/tmp"), f"prx_big_{os.getpid()}.txt")
+    with open(p, "wb") as f:
+        f.write(text)
+    try:
+        at = 0
+        with pg.graphs.EdgeReader(p) as r:
+            for s in (1, 2_500_000, 3, 3_400_000, 1000):
+                g, lines = pg.Graph.from_reader(ctx, r, rows, s, self_loops=False)
+                k = min(s, m - at)
+                assert lines == k
+                same_graph(g, numpy_csr(rows, u[at:at + k], v[at:at + k], False))
+                at += k
+    finally:
+        os.unlink(p)
+
+
+def test_device_parse_edge_cases(pg, ctx):
+    g, lines, used = pg.Graph.from_text(ctx, b"", 5, None)
+    assert lines == 0 and used == 0 and g.size() == (5, 5)
+    g.close()
+    g, lines, used = pg.Graph.from_text(ctx, b"1 2\n3 4", 4, None, self_loops=False)   # no final newline
+    assert lines == 2 and used == 7
+    same_graph(g, graph_of(pg, ctx, 4, [0, 2], [1, 3], False))
+    g, lines, used = pg.Graph.from_text(ctx, b"1 2\nx\n3 4\n", 4, None, self_loops=False)
+    assert lines == 2 and used == 6                                                    # stops after "x"
+    same_graph(g, graph_of(pg, ctx, 4, [0], [1], False))
+    g, lines, used = pg.Graph.from_text(ctx, b"1 2\n3 4\n", 4, 1, self_loops=False)
+    assert lines == 1 and used == 4
+    g.close()
+    g, lines, used = pg.Graph.from_text(ctx, b"1 2\n", 0, None)                        # rows == 0: nothing read
+    assert lines == 0 and g.size() == (0, 0)
+    g.close()
+    with pytest.raises(pg.PrxError):
+        pg.Graph.from_text(ctx, b"1 2\n3 9\n", 8, None)                                # id 9 > rows
+    g, lines, _ = pg.Graph.from_text(ctx, b"1 2\n3 x\n3 9\n", 8, None, self_loops=False)   # id 9 after the stop
+    assert lines == 2
+    g.close()
