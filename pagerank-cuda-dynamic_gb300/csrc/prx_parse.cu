@@ -5,8 +5,9 @@
 // the bytes go to the device in chunks and are parsed there:
 //   1. k_nl_count: newlines per 64 KB block (16-byte loads, byte compares);
 //   2. an exclusive scan of the block counts gives each block its first line;
-//   3. k_parse_lines: a thread owns 256 bytes; a line is parsed by the thread
-//      owning the newline before it (line 0 by thread 0).  Ids are 1-based in
+//   3. k_parse_lines: each block lists the starts of the lines after its
+//      newlines in shared memory, and its threads parse consecutive lines of
+//      the list together (line 0 by the first thread).  Ids are 1-based in
 //      the text and stored 0-based; the first line that does not start with
 //      two unsigned integers and the first id outside 1..rows are found with
 //      atomicMin, so the result is the same line sequence the host reader
@@ -113,12 +114,22 @@ __device__ void parse_line(const ParseArgs& a, uint64_t k, uint64_t s) {
   }
 }
 
+// Parse pass.  A thread parsing the lines after its own newlines would leave
+// the lanes of a warp in different lines at different times (each lane owns
+// a different number of newlines per word), so the lines would be parsed one
+// lane at a time.  Instead the block first lists the starts of the lines
+// that follow its newlines in shared memory (kLineCap at a time), then the
+// threads take consecutive lines from the list together.
+constexpr int kLineCap = 8192;
+
 __global__ void __launch_bounds__(kParseThreads) k_parse_lines(ParseArgs a) {
   __shared__ uint32_t ws[kParseThreads / 32];
-  const uint64_t seg0 = (uint64_t)blockIdx.x * kParseBlock + (uint64_t)threadIdx.x * kParseBytes;
-  const uint4* seg = reinterpret_cast<const uint4*>(a.text + seg0);
+  __shared__ uint32_t starts[kLineCap];  // block-relative start of each listed line
+  const uint64_t block0 = (uint64_t)blockIdx.x * kParseBlock;
+  const uint32_t off0 = threadIdx.x * kParseBytes;  // this thread's bytes, block-relative
+  const uint4* seg = reinterpret_cast<const uint4*>(a.text + block0 + off0);
   const uint32_t c = nl_in_segment(seg);
-  // newlines before this thread's segment: block base + exclusive scan in the block
+  // newlines of this block before this thread's bytes, and in the whole block
   const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   uint32_t x = c;
   for (int o = 1; o < 32; o <<= 1) {
@@ -127,24 +138,39 @@ __global__ void __launch_bounds__(kParseThreads) k_parse_lines(ParseArgs a) {
   }
   if (lane == 31) ws[w] = x;
   __syncthreads();
-  uint64_t j = a.nl_base[blockIdx.x] + x - c;
-  for (uint32_t k = 0; k < w; ++k) j += ws[k];
-  if (seg0 == 0 && a.limit > 0) parse_line(a, 0, 0);
-  if (c == 0) return;
-  for (int q = 0; q < kParseBytes / 16; ++q) {
-    const uint4 vv = seg[q];
-    const uint32_t wd[4] = {vv.x, vv.y, vv.z, vv.w};
-    for (int e = 0; e < 4; ++e) {
-      uint32_t m = __vcmpeq4(wd[e], 0x0A0A0A0Au);
-      while (m) {
-        const int bit = __ffs(m) - 1;  // lowest byte first: the text's order
-        m &= ~(0xFFu << bit);
-        const uint64_t pos = seg0 + q * 16 + e * 4 + (bit >> 3);
-        const uint64_t k = j + 1;      // the line after newline number j
-        ++j;
-        if (k < a.limit && k < a.lines) parse_line(a, k, pos + 1);
+  uint32_t ex = x - c, total = 0;
+  for (int k = 0; k < kParseThreads / 32; ++k) {
+    if (k < (int)w) ex += ws[k];
+    total += ws[k];
+  }
+  const uint64_t j0 = a.nl_base[blockIdx.x];  // newlines before this block
+  if (block0 == 0 && threadIdx.x == 0 && a.limit > 0) parse_line(a, 0, 0);
+  for (uint32_t lo = 0; lo < total; lo += kLineCap) {
+    const uint32_t hi = lo + kLineCap;
+    if (c && ex < hi && ex + c > lo) {
+      uint32_t q = ex;  // block-local number of the next newline of this thread
+      for (int v16 = 0; v16 < kParseBytes / 16 && q < hi; ++v16) {
+        const uint4 vv = seg[v16];
+        const uint32_t wd[4] = {vv.x, vv.y, vv.z, vv.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          uint32_t m = __vcmpeq4(wd[e], 0x0A0A0A0Au);
+          while (m) {
+            const int bit = __ffs(m) - 1;  // lowest byte first: the text's order
+            m &= ~(0xFFu << bit);
+            if (q >= lo && q < hi) starts[q - lo] = off0 + v16 * 16 + e * 4 + (bit >> 3) + 1;
+            ++q;
+          }
+        }
       }
     }
+    __syncthreads();
+    const uint32_t cnt = (total < hi ? total : hi) - lo;
+    for (uint32_t i = threadIdx.x; i < cnt; i += kParseThreads) {
+      const uint64_t k = j0 + lo + i + 1;  // the line after block newline lo + i
+      if (k < a.limit && k < a.lines) parse_line(a, k, block0 + starts[i]);
+    }
+    __syncthreads();
   }
 }
 
