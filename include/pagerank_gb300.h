@@ -150,8 +150,11 @@ int prx_graph_create(prx_context* ctx, uint32_t n, uint64_t m,
                      const uint32_t* xtoff, const uint32_t* xtedg,
                      const uint32_t* xtdat, int validate, prx_graph** out);
 /* A graph may be destroyed before or after its context; every other call on
- * a graph needs its context alive. */
+ * a graph needs its context alive.  Graph arrays come from a pool of this
+ * library that keeps freed memory for the next graph on the device;
+ * prx_release_cached_memory gives that memory back to the driver. */
 int prx_graph_destroy(prx_graph* g);
+int prx_release_cached_memory(int device);
 /* Current vertex / edge counts (m changes with prx_graph_apply_batch). */
 int prx_graph_size(const prx_graph* g, uint32_t* n, uint64_t* m);
 /* Vertices and in-edges in each in-degree class of the rank update:

@@ -607,7 +607,7 @@ int prx_graph_create(prx_context* c, uint32_t n, uint64_t m, const uint32_t* xof
   g.m_cap = m;
   cudaStream_t s = c->stream;
   auto upload = [&](uint32_t** dst, const uint32_t* src, size_t cnt, size_t slots = 0) -> cudaError_t {
-    cudaError_t e = cudaMalloc(dst, sizeof(uint32_t) * (slots > cnt ? slots : (cnt ? cnt : 1)));
+    cudaError_t e = graph_alloc(dst, sizeof(uint32_t) * (slots > cnt ? slots : (cnt ? cnt : 1)), s);
     if (e == cudaSuccess && cnt) e = cudaMemcpyAsync(*dst, src, sizeof(uint32_t) * cnt, cudaMemcpyHostToDevice, s);
     return e;
   };
@@ -624,6 +624,13 @@ int prx_graph_create(prx_context* c, uint32_t n, uint64_t m, const uint32_t* xof
     return e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
   }
   *out = gr;
+  return PRX_OK;
+}
+
+int prx_release_cached_memory(int device) {
+  TRY_CUDA_ST(cudaSetDevice(device));
+  TRY_CUDA_ST(cudaDeviceSynchronize());
+  TRY_CUDA_ST(graph_pool_trim(device));
   return PRX_OK;
 }
 

@@ -133,11 +133,11 @@ cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd64, ui
     if (hflag) { err = cudaErrorInvalidValue; goto done; }
     k_batch_deltas<<<grid, kThreads, 0, s>>>(du, dv, nd, iu, iv, ni, dout, din, tout, tin);
   }
-  PRX_CU(cudaMalloc(&noff, sizeof(uint32_t) * ((size_t)n + 1)));
-  PRX_CU(cudaMalloc(&ntoff, sizeof(uint32_t) * ((size_t)n + 1)));
-  PRX_CU(cudaMalloc(&nedg, sizeof(uint32_t) * (m2 ? m2 : 1)));
-  PRX_CU(cudaMalloc(&ntedg, sizeof(uint32_t) * edge_slots(m2)));
-  PRX_CU(cudaMalloc(&ndat, sizeof(uint32_t) * (n ? n : 1)));
+  PRX_CU(graph_alloc(&noff, sizeof(uint32_t) * ((size_t)n + 1), s));
+  PRX_CU(graph_alloc(&ntoff, sizeof(uint32_t) * ((size_t)n + 1), s));
+  PRX_CU(graph_alloc(&nedg, sizeof(uint32_t) * (m2 ? m2 : 1), s));
+  PRX_CU(graph_alloc(&ntedg, sizeof(uint32_t) * edge_slots(m2), s));
+  PRX_CU(graph_alloc(&ndat, sizeof(uint32_t) * (n ? n : 1), s));
   k_new_degree<<<grid, kThreads, 0, s>>>(g.xoff, dout, n, noff);
   k_new_degree<<<grid, kThreads, 0, s>>>(g.xtoff, din, n, ntoff);
   PRX_CU(exclusive_scan_u32(noff, n + 1, s));

@@ -6,10 +6,60 @@
 // inside every timed solve (:812-813).  Here one stable 3-way partition
 // (LOW / MID / HIGH, ids ascending within each class) is built once per graph
 // version with three kernels of our own and reused by every solve on it.
+#include <mutex>
 #include <vector>
 #include "prx_device.cuh"
 
 namespace prx {
+
+namespace {
+constexpr int kMaxDevices = 64;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+std::mutex g_pool_mu;
+
+cudaError_t pool_of(int dev, cudaMemPool_t* out) {
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = cudaMemPoolCreate(&pool, &props);
+    if (e != cudaSuccess) return e;
+    uint64_t keep = ~0ull;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e != cudaSuccess) {
+      cudaMemPoolDestroy(pool);
+      return e;
+    }
+    g_pool[dev] = pool;
+  }
+  *out = g_pool[dev];
+  return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t graph_alloc(void** p, size_t bytes, cudaStream_t s) {
+  *p = nullptr;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  cudaMemPool_t pool = nullptr;
+  if (e == cudaSuccess) e = pool_of(dev, &pool);
+  if (e == cudaSuccess) e = cudaMallocFromPoolAsync(p, bytes ? bytes : 1, pool, s);
+  return e;
+}
+
+cudaError_t graph_pool_trim(int dev) {
+  cudaMemPool_t pool = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    if (dev < 0 || dev >= kMaxDevices || !g_pool[dev]) return cudaSuccess;
+    pool = g_pool[dev];
+  }
+  return cudaMemPoolTrimTo(pool, 0);
+}
 
 constexpr uint32_t kTileV = 2048;            // vertices per tile (256 threads x 8)
 constexpr int kFieldBits = 21;               // per-class count within a tile, packed into a u64
@@ -312,8 +362,8 @@ cudaError_t ensure_chunks(GraphDev& g, uint32_t width, uint32_t keep, int sms, c
   const int K = (int)((g.n + (uint64_t)width - 1) / width);
   const size_t len = (size_t)K * ((size_t)g.n + 1);
   if (len > 0xffffffffull) return cudaErrorInvalidValue;
-  cudaError_t e = cudaMalloc(&l.off, sizeof(uint32_t) * len);
-  if (e == cudaSuccess) e = cudaMalloc(&l.edg, sizeof(uint32_t) * edge_slots(g.cls_edges[LOW]));
+  cudaError_t e = graph_alloc(&l.off, sizeof(uint32_t) * len, s);
+  if (e == cudaSuccess) e = graph_alloc(&l.edg, sizeof(uint32_t) * edge_slots(g.cls_edges[LOW]), s);
   if (e != cudaSuccess) {
     cudaFree(l.off); cudaFree(l.edg);
     l = ChunkLayout();
@@ -343,21 +393,21 @@ cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
   const uint32_t n = g.n;
   free_chunks(g);
   if (!g.low_bm) {
-    cudaError_t e = cudaMalloc(&g.low_bm, sizeof(uint32_t) * (((size_t)n + 31) / 32 + 1));
+    cudaError_t e = graph_alloc(&g.low_bm, sizeof(uint32_t) * (((size_t)n + 31) / 32 + 1), s);
     if (e != cudaSuccess) return e;
   }
   if (!g.rcp) {
-    cudaError_t e = cudaMalloc(&g.rcp, sizeof(double) * (n ? n : 1));
+    cudaError_t e = graph_alloc(&g.rcp, sizeof(double) * (n ? n : 1), s);
     if (e != cudaSuccess) return e;
   }
   if (!g.rcp32) {
-    cudaError_t e = cudaMalloc(&g.rcp32, sizeof(float) * (n ? n : 1));
+    cudaError_t e = graph_alloc(&g.rcp32, sizeof(float) * (n ? n : 1), s);
     if (e != cudaSuccess) return e;
   }
   if (n) k_low_bitmap<<<sms * 4, 256, 0, s>>>(g.xtoff, n, g.low_bm);
   if (n) k_reciprocals<<<sms * 4, 256, 0, s>>>(g.xtdat, n, g.rcp, g.rcp32);
   if (!g.cls_list) {
-    cudaError_t e = cudaMalloc(&g.cls_list, sizeof(uint32_t) * (n ? n : 1));
+    cudaError_t e = graph_alloc(&g.cls_list, sizeof(uint32_t) * (n ? n : 1), s);
     if (e != cudaSuccess) return e;
   }
   return build_class_lists(g.xtoff, n, g.mid_max, g.cls_list, g.cls_begin, g.cls_edges, sms, s);

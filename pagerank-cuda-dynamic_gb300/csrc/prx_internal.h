@@ -203,6 +203,18 @@ cudaError_t build_class_lists(const uint32_t* off, uint32_t n, uint32_t mid_max,
 // b: device array [du | dv | iu | iv | tdk | tdv | tik | tiv]; t* = batch sorted by (v, u)
 cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd, uint64_t ni, int sms, cudaStream_t s);
 cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t len, cudaStream_t s);
+
+// Graph arrays come from a stream-ordered pool of this library that keeps
+// freed memory (release threshold: unlimited), so a graph built after another
+// one was destroyed reuses its pages instead of mapping new ones.  Allocated
+// on stream s and usable there at once; cudaFree returns them to the pool.
+cudaError_t graph_alloc(void** p, size_t bytes, cudaStream_t s);
+template <class T>
+cudaError_t graph_alloc(T** p, size_t bytes, cudaStream_t s) {
+  return graph_alloc(reinterpret_cast<void**>(p), bytes, s);
+}
+// Give the pool's free memory on device dev back to the driver.
+cudaError_t graph_pool_trim(int dev);
 // Mismatches of div_count against the IEEE division (prx_selftest_division).
 cudaError_t selftest_division(uint32_t dmax, uint32_t per, unsigned long long* bad_host, int sms, cudaStream_t s);
 

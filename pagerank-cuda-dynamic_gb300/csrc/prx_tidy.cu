@@ -535,11 +535,11 @@ static int create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, cons
     FAIL(PRX_EINVAL, "prx_graph_create_from_edges: vertex id out of range");
   }
   g.m = g.m_cap = m;
-  if (e == cudaSuccess) e = cudaMalloc(&g.xoff, 4ull * ((size_t)n + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&g.xedg, 4ull * (m ? m : 1));
-  if (e == cudaSuccess) e = cudaMalloc(&g.xtoff, 4ull * ((size_t)n + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&g.xtedg, 4ull * edge_slots(m));
-  if (e == cudaSuccess) e = cudaMalloc(&g.xtdat, 4ull * (n ? n : 1));
+  if (e == cudaSuccess) e = graph_alloc(&g.xoff, 4ull * ((size_t)n + 1), s);
+  if (e == cudaSuccess) e = graph_alloc(&g.xedg, 4ull * (m ? m : 1), s);
+  if (e == cudaSuccess) e = graph_alloc(&g.xtoff, 4ull * ((size_t)n + 1), s);
+  if (e == cudaSuccess) e = graph_alloc(&g.xtedg, 4ull * edge_slots(m), s);
+  if (e == cudaSuccess) e = graph_alloc(&g.xtdat, 4ull * (n ? n : 1), s);
   if (e != cudaSuccess) return fail(e);
   const int gm = grid_of(m, c->sms), gn = grid_of((uint64_t)n + 1, c->sms);
   k_ingest_offsets<<<gn, 256, 0, s>>>(uniq, m, vbits, n, g.xoff);

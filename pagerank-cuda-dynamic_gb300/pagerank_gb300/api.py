@@ -263,6 +263,11 @@ def solve_device(ctx, g, mode, q_ptr, ranks_ptr, batch_ptrs=(None, None, 0, None
     return res.as_dict()
 
 
+def release_cached_memory(device=0):
+    """prx_release_cached_memory: give the graph pool's free memory on a device back to the driver."""
+    check(load().prx_release_cached_memory(int(device)), "prx_release_cached_memory")
+
+
 def mark_affected(ctx, g, mode, deletions, insertions):
     """Initial affected flags of a dynamic mode -> uint8[n]."""
     n, _ = g.size()

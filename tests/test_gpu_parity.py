@@ -346,3 +346,18 @@ def test_device_batch_generation_matches_host(pg, ctx, kind):
         for a, b in zip(got, want):
             assert np.array_equal(a, b), (nd, ni, seed)
     g.close()
+
+
+def test_graph_pool_reuse_and_release(pg, ctx):
+    """Graphs built one after another reuse the pool's memory; results do not
+    change, and releasing the cached memory leaves later graphs working."""
+    xoff, xedg = pg.graphs.rmat(14, 8, seed=5)
+    xt = O.transpose(xoff, xedg)
+    want, it = O.solve("static", None, None, *xt)
+    for k in range(3):
+        g = pg.Graph(ctx, *xt, xoff, xedg)
+        r, res = pg.pagerank_static(ctx, g, pg.options(chunk_vertices=4096))
+        assert res["iterations"] == it and np.array_equal(r, want)
+        g.close()
+        if k == 1:
+            pg.release_cached_memory(0)
