@@ -68,6 +68,8 @@ def parse():
     p.add_argument("--adjoint-fd-edges", type=int, default=200, help="edges checked by finite differences")
     p.add_argument("--adjoint-batches", type=int, default=2, help="dynamic batches of 1e-4|E| after the first solve")
     p.add_argument("--no-ingest", action="store_true", help="skip the device graph ingest from the edge list")
+    p.add_argument("--no-offsets64", action="store_true",
+                   help="skip the 64-bit-offset graph (four copies of the bench graph, 4x its edges)")
     p.add_argument("--ingest-steps", type=int, default=2)
     a = p.parse_args()
     if a.static_only:
@@ -553,6 +555,52 @@ def run_ingest(args, pg, ctx, local, xoff, xedg):
                      "host_parse_only_ms": host_parse_ms, "host_threads": os.cpu_count()}}
 
 
+def run_offsets64(args, pg, ctx, local, xt):
+    """64-bit offsets: four disjoint copies of the bench graph's in-CSR (4x its
+    edges: past 2^32) through prx_graph_create64, Static FP64 for 10 sweeps
+    (tolerance 0) against the same sweeps on one copy.  A copy's ranks must be
+    exactly a quarter of the single graph's: 1/n, C0 and every contribution
+    scale by exactly 1/4, so every sum does too."""
+    import numpy as np
+    import torch
+    xtoff, xtedg, xtdat = (np.asarray(a) for a in xt)
+    n, m = len(xtoff) - 1, len(xtedg)
+    dev = f"cuda:{local}"
+    copies = 4
+    t = time.perf_counter()
+    toff = np.empty(copies * n + 1, np.uint64)
+    tedg = np.empty(copies * m, np.uint32)
+    for k in range(copies):
+        toff[k * n:(k + 1) * n] = xtoff[:-1].astype(np.uint64) + np.uint64(k * m)
+        np.add(xtedg, np.uint32(k * n), out=tedg[k * m:(k + 1) * m])
+    toff[-1] = copies * m
+    tdat = np.tile(xtdat, copies)
+    build_s = time.perf_counter() - t
+    t = time.perf_counter()
+    g4 = pg.Graph.from_csr64(ctx, toff, tedg, tdat)
+    create_s = time.perf_counter() - t
+    del tedg
+    o = pg.options(tolerance=0.0, max_iterations=10)
+    r1 = torch.empty(n, dtype=torch.float64, device=dev)
+    r4 = torch.empty(copies * n, dtype=torch.float64, device=dev)
+    g1 = pg.Graph(ctx, *xt)   # the bench graph as generated (the dynamic section changed g)
+    res1 = pg.solve_device(ctx, g1, pg.STATIC, None, r1.data_ptr(), opts=pg.options(tolerance=0.0, max_iterations=10,
+                                                                                     chunk_vertices=n))
+    g1.close()
+    res4 = [pg.solve_device(ctx, g4, pg.STATIC, None, r4.data_ptr(), opts=o) for _ in range(3)]
+    exact = all(torch.equal(r4[k * n:(k + 1) * n], r1 / 4) for k in range(copies))
+    ms4 = statistics.median(r["time_ms"] for r in res4)
+    g4.close()
+    del r4
+    torch.cuda.empty_cache()
+    return {"workload": f"{copies} disjoint copies of the bench graph: {copies * n} vertices, {copies * m} edges "
+                        f"(2^32 = 4294967296), Static FP64, 10 sweeps, tolerance 0",
+            "edges": copies * m, "build_s": build_s, "create_s": create_s, "ms": ms4,
+            "ge_s": copies * m * res4[0]["iterations"] / (ms4 / 1e3) / 1e9,
+            "single_copy_unchunked_ms": res1["time_ms"], "iterations": res4[0]["iterations"],
+            "copy_ranks_exactly_quarter_of_single": bool(exact)}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -675,7 +723,10 @@ def run_ours(args):
         dynamic, dfp = run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m)
         log(f"dfp: {dfp}")
 
-    ppr = adj = grid = ingest = None
+    ppr = adj = grid = ingest = big = None
+    if rank == 0 and not args.no_offsets64 and not args.static_only:
+        big = run_offsets64(args, pg, ctx, local, xt)
+        log(f"offsets64: {big}")
     if rank == 0 and not args.no_ingest and not args.static_only:
         ingest = run_ingest(args, pg, ctx, local, xoff, xedg)
         log(f"ingest: {ingest}")
@@ -702,7 +753,7 @@ def run_ours(args):
                "e2e": {"value": e2e_value, "unit": "GE/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "ms_per_step": e2e_ms_max},
                "roofline": roofline, "clocks": clk.summary(), "fp32_refine": fp32, "dfp": dfp,
-               "dynamic": dynamic, "autotune": tune, "ingest": ingest, "grid": grid, "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
+               "dynamic": dynamic, "autotune": tune, "offsets64": big, "ingest": ingest, "grid": grid, "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     g.close()
     ctx.close()

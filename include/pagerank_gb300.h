@@ -149,6 +149,21 @@ int prx_graph_create(prx_context* ctx, uint32_t n, uint64_t m,
                      const uint32_t* xoff, const uint32_t* xedg,
                      const uint32_t* xtoff, const uint32_t* xtedg,
                      const uint32_t* xtdat, int validate, prx_graph** out);
+/* The same with 64-bit offsets, for graphs of 2^32 edges or more (288 GB of
+ * HBM holds about 20 billion FP64 edges).  Rows are cut into segments of
+ * 2^seg_shift rows whose edges are addressed with 32-bit offsets from the
+ * segment's start; seg_shift 0 picks it (one segment, the plain CSR, while
+ * m < 2^32), 1..32 forces it (PRX_ERANGE if a segment would hold 2^32 edges
+ * or more).  Graphs with more than one segment support every solver mode,
+ * the FP32 refinement, marking, autotuning and download; batch apply, tidy
+ * and generation, personalized PageRank and edge weights return PRX_ERANGE,
+ * and the source-chunked gathers are not used. */
+int prx_graph_create64(prx_context* ctx, uint32_t n, uint64_t m,
+                       const uint64_t* xoff, const uint32_t* xedg,
+                       const uint64_t* xtoff, const uint32_t* xtedg,
+                       const uint32_t* xtdat, int validate, uint32_t seg_shift, prx_graph** out);
+int prx_graph_download64(prx_graph* g, uint64_t* xoff, uint32_t* xedg,
+                         uint64_t* xtoff, uint32_t* xtedg, uint32_t* xtdat);
 /* A graph may be destroyed before or after its context; every other call on
  * a graph needs its context alive.  Graph arrays come from a pool of this
  * library that keeps freed memory for the next graph on the device;

@@ -187,6 +187,7 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
   std::memset(&a, 0, sizeof(a));
   a.xoff = g.xoff; a.xedg = g.xedg;
   a.xtoff = g.xtoff; a.xtedg = g.xtedg; a.xtdat = g.xtdat;
+  a.xbase = g.xbase; a.xtbase = g.xtbase; a.seg_shift = g.seg_shift;
   a.cls_list = g.cls_list;
   for (int k = 0; k < 3; ++k) a.fr[k] = c->fr[k];
   for (int p = 0; p < 2; ++p) {
@@ -563,6 +564,49 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   return PRX_OK;
 }
 
+// Segmented 32-bit offsets from 64-bit ones: entry i of segment k (rows
+// [k * 2^S, ...), 2^S + 1 entries each) is off64[v] - off64[k * 2^S] with
+// v = k * 2^S + i.
+__global__ void k_segment_offsets(const unsigned long long* __restrict__ off64, uint32_t n, uint32_t shift,
+                                  uint64_t entries, uint32_t* __restrict__ off) {
+  const uint64_t per = (1ull << shift) + 1;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < entries; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = i / per, j = i - k * per;
+    const uint64_t v = (k << shift) + j;
+    off[i] = v <= n ? (uint32_t)(off64[v] - off64[k << shift]) : 0u;
+  }
+}
+
+// Row segments for 64-bit offsets (see GraphDev): the largest shift <= 30
+// whose segments all hold fewer than 2^32 - 8 edges in every CSR given, or
+// `want` if it is not 0; 32 (one segment) when m < 2^32 and want is 0.
+static int pick_shift(uint32_t n, uint64_t m, const uint64_t* a, const uint64_t* b, uint32_t want, uint32_t* out) {
+  auto fits = [&](uint32_t S) {
+    if (S >= 32) return m < 0xfffffff8ull;
+    for (uint64_t v0 = 0; v0 < n; v0 += 1ull << S) {
+      const uint64_t v1 = std::min<uint64_t>(n, v0 + (1ull << S));
+      if (a[v1] - a[v0] >= 0xfffffff8ull) return false;
+      if (b && b[v1] - b[v0] >= 0xfffffff8ull) return false;
+    }
+    return true;
+  };
+  if (want) {
+    if (want > 32 || !fits(want)) FAIL(PRX_ERANGE, "prx_graph_create64: a row segment holds 2^32 edges or more");
+    *out = want;
+    return PRX_OK;
+  }
+  if (fits(32)) {
+    *out = 32;
+    return PRX_OK;
+  }
+  for (uint32_t S = 30; S >= 1; --S)
+    if (fits(S)) {
+      *out = S;
+      return PRX_OK;
+    }
+  FAIL(PRX_ERANGE, "prx_graph_create64: a row holds 2^32 edges or more");
+}
+
 static int check_batch_ids(uint32_t n, const uint32_t* du, const uint32_t* dv, uint64_t nd, const uint32_t* iu,
                            const uint32_t* iv, uint64_t ni) {
   if ((nd && (!du || !dv)) || (ni && !iu)) FAIL(PRX_EINVAL, "batch: NULL array with a non-zero length");
@@ -634,6 +678,135 @@ int prx_release_cached_memory(int device) {
   return PRX_OK;
 }
 
+int prx_graph_create64(prx_context* c, uint32_t n, uint64_t m, const uint64_t* xoff, const uint32_t* xedg,
+                       const uint64_t* xtoff, const uint32_t* xtedg, const uint32_t* xtdat, int validate,
+                       uint32_t seg_shift, prx_graph** out) {
+  if (!c || !out) FAIL(PRX_EINVAL, "prx_graph_create64: NULL context or out");
+  *out = nullptr;
+  if (!xtoff || (n && !xtdat) || (m && !xtedg))
+    FAIL(PRX_EINVAL, "prx_graph_create64: xtoff, xtedg and xtdat are required");
+  if ((xedg && !xoff) || (xoff && m && !xedg)) FAIL(PRX_EINVAL, "prx_graph_create64: give both xoff and xedg or neither");
+  if (xtoff[0] != 0 || xtoff[n] != m) FAIL(PRX_EINVAL, "prx_graph_create64: xtoff must start at 0 and end at m");
+  if (xoff && (xoff[0] != 0 || xoff[n] != m)) FAIL(PRX_EINVAL, "prx_graph_create64: xoff must start at 0 and end at m");
+  if (validate) {
+    for (uint32_t v = 0; v < n; ++v) {
+      if (xtoff[v + 1] < xtoff[v]) FAIL(PRX_EINVAL, "prx_graph_create64: xtoff not monotone");
+      if (xoff && xoff[v + 1] < xoff[v]) FAIL(PRX_EINVAL, "prx_graph_create64: xoff not monotone");
+      if (xoff && xtdat[v] != xoff[v + 1] - xoff[v]) FAIL(PRX_EINVAL, "prx_graph_create64: xtdat != out-degree");
+    }
+    for (uint64_t i = 0; i < m; ++i) {
+      if (xtedg[i] >= n) FAIL(PRX_EINVAL, "prx_graph_create64: xtedg id out of range");
+      if (xedg && xedg[i] >= n) FAIL(PRX_EINVAL, "prx_graph_create64: xedg id out of range");
+    }
+  }
+  uint32_t S = 32;
+  int st = pick_shift(n, m, xtoff, xoff, seg_shift, &S);
+  if (st) return st;
+  TRY_CUDA_ST(cudaSetDevice(c->device));
+  prx_graph* gr = new prx_graph();
+  gr->ctx = c;
+  GraphDev& g = gr->g;
+  g.device = c->device;
+  g.n = n;
+  g.m = g.m_cap = m;
+  g.seg_shift = S;
+  g.nseg = n ? (uint32_t)(((uint64_t)n + (1ull << S) - 1) >> S) : 1;
+  if (S >= 32) g.nseg = 1;
+  cudaStream_t s = c->stream;
+  const uint64_t entries = (uint64_t)n + g.nseg;
+  unsigned long long* tmp = nullptr;
+  // one CSR: segment bases (edge positions rounded up to 16 bytes), offsets, edges
+  auto build = [&](const uint64_t* off64, const uint32_t* edg, uint32_t** doff, uint32_t** dedg,
+                   unsigned long long** dbase, std::vector<uint64_t>& seg0, std::vector<uint64_t>& pos) -> cudaError_t {
+    seg0.assign(g.nseg, 0);
+    pos.assign(g.nseg, 0);
+    uint64_t slots = 0;
+    for (uint32_t k = 0; k < g.nseg; ++k) {
+      const uint64_t v0 = std::min<uint64_t>(n, (uint64_t)k << (S >= 32 ? 0 : S));
+      seg0[k] = off64[S >= 32 ? 0 : v0];
+      pos[k] = (slots + 3) & ~3ull;
+      const uint64_t v1 = S >= 32 ? n : std::min<uint64_t>(n, v0 + (1ull << S));
+      slots = pos[k] + (off64[v1] - seg0[k]);
+    }
+    cudaError_t e = graph_alloc(doff, 4 * entries, s);
+    if (e == cudaSuccess) e = graph_alloc(dedg, 4 * (((slots + 3) & ~3ull) + 4), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(tmp, off64, 8 * ((uint64_t)n + 1), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      k_segment_offsets<<<c->sms * 8, 256, 0, s>>>(tmp, n, S >= 32 ? 63 : S, entries, *doff);
+    for (uint32_t k = 0; k < g.nseg && e == cudaSuccess; ++k) {
+      const uint64_t v0 = S >= 32 ? 0 : std::min<uint64_t>(n, (uint64_t)k << S);
+      const uint64_t v1 = S >= 32 ? n : std::min<uint64_t>(n, v0 + (1ull << S));
+      const uint64_t cnt = off64[v1] - off64[v0];
+      if (cnt) e = cudaMemcpyAsync(*dedg + pos[k], edg + off64[v0], 4 * cnt, cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess && g.nseg > 1) {
+      e = graph_alloc(dbase, 8 * (uint64_t)g.nseg, s);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(*dbase, pos.data(), 8 * (uint64_t)g.nseg, cudaMemcpyHostToDevice, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host arrays above are the caller's
+    return e;
+  };
+  cudaError_t e = cudaMalloc(&tmp, 8 * ((uint64_t)n + 1));
+  if (e == cudaSuccess) e = build(xtoff, xtedg, &g.xtoff, &g.xtedg, &g.xtbase, g.xtseg0, g.xtpos);
+  if (e == cudaSuccess && xoff) e = build(xoff, xedg, &g.xoff, &g.xedg, &g.xbase, g.xseg0, g.xpos);
+  if (e == cudaSuccess) e = graph_alloc(&g.xtdat, 4 * (uint64_t)(n ? n : 1), s);
+  if (e == cudaSuccess && n) e = cudaMemcpyAsync(g.xtdat, xtdat, 4 * (uint64_t)n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = build_classes(g, c->sms, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(tmp);
+  if (e != cudaSuccess) {
+    set_error(std::string("prx_graph_create64: ") + cudaGetErrorString(e));
+    prx_graph_destroy(gr);
+    return e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
+  }
+  *out = gr;
+  return PRX_OK;
+}
+
+int prx_graph_download64(prx_graph* gr, uint64_t* xoff, uint32_t* xedg, uint64_t* xtoff, uint32_t* xtedg,
+                         uint32_t* xtdat) {
+  if (!gr) FAIL(PRX_EINVAL, "prx_graph_download64: NULL graph");
+  const GraphDev& g = gr->g;
+  cudaStream_t s = gr->ctx->stream;
+  TRY_CUDA_ST(cudaSetDevice(gr->ctx->device));
+  if ((xoff || xedg) && !g.xoff) FAIL(PRX_ESTATE, "prx_graph_download64: graph has no out-CSR");
+  const uint64_t entries = (uint64_t)g.n + g.nseg;
+  std::vector<uint32_t> rel(entries);
+  auto one = [&](const uint32_t* doff, const uint32_t* dedg, const std::vector<uint64_t>& seg0,
+                 const std::vector<uint64_t>& pos, uint64_t* off, uint32_t* edg) -> int {
+    if (g.nseg == 1) {  // plain CSR
+      if (off) {
+        TRY_CUDA_ST(cudaMemcpyAsync(rel.data(), doff, 4 * entries, cudaMemcpyDeviceToHost, s));
+        TRY_CUDA_ST(cudaStreamSynchronize(s));
+        for (uint64_t v = 0; v < entries; ++v) off[v] = rel[v];
+      }
+      if (edg && g.m) TRY_CUDA_ST(cudaMemcpyAsync(edg, dedg, 4 * g.m, cudaMemcpyDeviceToHost, s));
+      return PRX_OK;
+    }
+    TRY_CUDA_ST(cudaMemcpyAsync(rel.data(), doff, 4 * entries, cudaMemcpyDeviceToHost, s));
+    TRY_CUDA_ST(cudaStreamSynchronize(s));
+    const uint32_t S = g.seg_shift;
+    for (uint32_t k = 0; k < g.nseg; ++k) {
+      const uint64_t v0 = (uint64_t)k << S, v1 = std::min<uint64_t>(g.n, v0 + (1ull << S));
+      for (uint64_t v = v0; v <= v1; ++v) {
+        const uint64_t o = seg0[k] + rel[v + k];
+        if (off) off[v] = o;
+        if (v == v1 && edg && o > seg0[k])
+          TRY_CUDA_ST(cudaMemcpyAsync(edg + seg0[k], dedg + pos[k], 4 * (o - seg0[k]), cudaMemcpyDeviceToHost, s));
+      }
+    }
+    return PRX_OK;
+  };
+  int st = PRX_OK;
+  if (xoff || xedg) st = one(g.xoff, g.xedg, g.xseg0, g.xpos, xoff, xedg);
+  if (st == PRX_OK && (xtoff || xtedg)) st = one(g.xtoff, g.xtedg, g.xtseg0, g.xtpos, xtoff, xtedg);
+  if (st) return st;
+  if (xtdat && g.n) TRY_CUDA_ST(cudaMemcpyAsync(xtdat, g.xtdat, 4 * (size_t)g.n, cudaMemcpyDeviceToHost, s));
+  TRY_CUDA_ST(cudaStreamSynchronize(s));
+  return PRX_OK;
+}
+
 int prx_graph_destroy(prx_graph* gr) {
   // Does not touch the context, which may already be destroyed: cudaFree
   // waits for the device's outstanding work on these arrays.
@@ -641,6 +814,7 @@ int prx_graph_destroy(prx_graph* gr) {
   cudaSetDevice(gr->g.device);
   GraphDev& g = gr->g;
   cudaFree(g.xoff); cudaFree(g.xedg); cudaFree(g.xtoff); cudaFree(g.xtedg); cudaFree(g.xtdat); cudaFree(g.cls_list);
+  cudaFree(g.xbase); cudaFree(g.xtbase);
   cudaFree(g.low_bm);
   cudaFree(g.rcp);
   cudaFree(g.rcp32);
@@ -674,6 +848,16 @@ int prx_graph_download(prx_graph* gr, uint32_t* xoff, uint32_t* xedg, uint32_t* 
   cudaStream_t s = gr->ctx->stream;
   TRY_CUDA_ST(cudaSetDevice(gr->ctx->device));
   if ((xoff || xedg) && !g.xoff) FAIL(PRX_ESTATE, "prx_graph_download: graph has no out-CSR");
+  if (g.nseg > 1) {  // row segments: rebuild the offsets, 32-bit when they fit
+    if (g.m >= 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_download: 2^32 edges or more; use prx_graph_download64");
+    std::vector<uint64_t> o((xoff ? (size_t)g.n + 1 : 0)), ot((xtoff ? (size_t)g.n + 1 : 0));
+    const int st = prx_graph_download64(gr, xoff ? o.data() : nullptr, xedg, xtoff ? ot.data() : nullptr, xtedg,
+                                        xtdat);
+    if (st) return st;
+    for (size_t v = 0; v < o.size(); ++v) xoff[v] = (uint32_t)o[v];
+    for (size_t v = 0; v < ot.size(); ++v) xtoff[v] = (uint32_t)ot[v];
+    return PRX_OK;
+  }
   if (xoff) TRY_CUDA_ST(cudaMemcpyAsync(xoff, g.xoff, 4 * ((size_t)g.n + 1), cudaMemcpyDeviceToHost, s));
   if (xedg && g.m) TRY_CUDA_ST(cudaMemcpyAsync(xedg, g.xedg, 4 * g.m, cudaMemcpyDeviceToHost, s));
   if (xtoff) TRY_CUDA_ST(cudaMemcpyAsync(xtoff, g.xtoff, 4 * ((size_t)g.n + 1), cudaMemcpyDeviceToHost, s));
@@ -689,6 +873,7 @@ int prx_graph_apply_batch(prx_graph* gr, const uint32_t* du, const uint32_t* dv,
   GraphDev& g = gr->g;
   prx_context* c = gr->ctx;
   if (!g.xoff) FAIL(PRX_ESTATE, "prx_graph_apply_batch: graph has no out-CSR");
+  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_graph_apply_batch: not for graphs with row segments (64-bit offsets)");
   if (ni && !iv) FAIL(PRX_EINVAL, "prx_graph_apply_batch: insertions need targets");
   int st = check_batch_ids(g.n, du, dv, nd, iu, iv, ni);
   if (st) return st;

@@ -8,9 +8,24 @@ namespace prx {
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
+// Row segments (see GraphDev): index of row v's begin in the offsets, and
+// the start of its segment's edges.  shift 32 / base null: the plain CSR.
+__device__ __forceinline__ uint64_t seg_index(uint32_t v, uint32_t shift) {
+  return (uint64_t)v + ((uint64_t)v >> shift);
+}
+__device__ __forceinline__ const uint32_t* seg_edges(const uint32_t* edg, const unsigned long long* base, uint32_t shift,
+                                                     uint32_t v) {
+  return base ? edg + base[(uint64_t)v >> shift] : edg;
+}
+__device__ __forceinline__ uint32_t row_len(const uint32_t* __restrict__ off, uint32_t shift, uint32_t v) {
+  const uint64_t i = seg_index(v, shift);
+  return off[i + 1] - off[i];
+}
+
 // In-degree class of v (see kLowMax).
-__device__ __forceinline__ int in_class(const uint32_t* __restrict__ xtoff, uint32_t v, uint32_t mid_max) {
-  const uint32_t d = xtoff[v + 1] - xtoff[v];
+__device__ __forceinline__ int in_class(const uint32_t* __restrict__ xtoff, uint32_t shift, uint32_t v,
+                                        uint32_t mid_max) {
+  const uint32_t d = row_len(xtoff, shift, v);
   return d <= kLowMax ? LOW : (d <= mid_max ? MID : HIGH);
 }
 

@@ -65,8 +65,9 @@ constexpr uint32_t kTileV = 2048;            // vertices per tile (256 threads x
 constexpr int kFieldBits = 21;               // per-class count within a tile, packed into a u64
 constexpr unsigned long long kFieldMask = (1ull << kFieldBits) - 1;
 
-__device__ __forceinline__ unsigned long long cls_code(const uint32_t* __restrict__ xtoff, uint32_t v, uint32_t mid_max) {
-  return 1ull << (kFieldBits * in_class(xtoff, v, mid_max));
+__device__ __forceinline__ unsigned long long cls_code(const uint32_t* __restrict__ xtoff, uint32_t shift, uint32_t v,
+                                                     uint32_t mid_max) {
+  return 1ull << (kFieldBits * in_class(xtoff, shift, v, mid_max));
 }
 
 // Inclusive scan over a 256-thread block; *total receives the block sum.
@@ -92,13 +93,13 @@ __device__ __forceinline__ unsigned long long block_scan_incl(unsigned long long
 }
 
 // Per-tile class counts, class-major: cnt[c * ntiles + tile].
-__global__ void __launch_bounds__(256) k_cls_count(const uint32_t* __restrict__ xtoff, uint32_t n, uint32_t mid_max,
+__global__ void __launch_bounds__(256) k_cls_count(const uint32_t* __restrict__ xtoff, uint32_t shift, uint32_t n, uint32_t mid_max,
                                                    uint32_t ntiles, uint32_t* __restrict__ cnt) {
   const uint32_t v0 = blockIdx.x * kTileV + threadIdx.x * 8;
   unsigned long long x = 0;
 #pragma unroll
   for (int k = 0; k < 8; ++k)
-    if (v0 + k < n) x += cls_code(xtoff, v0 + k, mid_max);
+    if (v0 + k < n) x += cls_code(xtoff, shift, v0 + k, mid_max);
   unsigned long long tot;
   block_scan_incl(x, &tot);
   if (threadIdx.x == 0)
@@ -134,7 +135,7 @@ __global__ void __launch_bounds__(1024) k_cls_scan(uint32_t* cnt, uint32_t ntile
   if (t == 1023) bounds[NCLS] = sh[1023];
 }
 
-__global__ void __launch_bounds__(256) k_cls_scatter(const uint32_t* __restrict__ xtoff, uint32_t n, uint32_t mid_max,
+__global__ void __launch_bounds__(256) k_cls_scatter(const uint32_t* __restrict__ xtoff, uint32_t shift, uint32_t n, uint32_t mid_max,
                                                      uint32_t ntiles, const uint32_t* __restrict__ start,
                                                      uint32_t* __restrict__ out) {
   const uint32_t v0 = blockIdx.x * kTileV + threadIdx.x * 8;
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(256) k_cls_scatter(const uint32_t* __restrict_
   unsigned long long x = 0;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    cls[k] = v0 + k < n ? in_class(xtoff, v0 + k, mid_max) : -1;
+    cls[k] = v0 + k < n ? in_class(xtoff, shift, v0 + k, mid_max) : -1;
     if (cls[k] >= 0) x += 1ull << (kFieldBits * cls[k]);
   }
   unsigned long long tot;
@@ -159,14 +160,14 @@ __global__ void __launch_bounds__(256) k_cls_scatter(const uint32_t* __restrict_
 
 // In-edges per class (statistics for the roofline): one u64 atomic per block
 // and class.
-__global__ void __launch_bounds__(256) k_cls_edges(const uint32_t* __restrict__ xtoff, uint32_t n, uint32_t mid_max,
+__global__ void __launch_bounds__(256) k_cls_edges(const uint32_t* __restrict__ xtoff, uint32_t shift, uint32_t n, uint32_t mid_max,
                                                    unsigned long long* __restrict__ out) {
   __shared__ unsigned long long acc[NCLS];
   if (threadIdx.x < NCLS) acc[threadIdx.x] = 0;
   __syncthreads();
   unsigned long long mine[NCLS] = {0, 0, 0};
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
-    mine[in_class(xtoff, v, mid_max)] += xtoff[v + 1] - xtoff[v];
+    mine[in_class(xtoff, shift, v, mid_max)] += row_len(xtoff, shift, v);
   for (int c = 0; c < NCLS; ++c)
     if (mine[c]) atomicAdd(&acc[c], mine[c]);
   __syncthreads();
@@ -221,12 +222,12 @@ cudaError_t selftest_division(uint32_t dmax, uint32_t per, unsigned long long* b
 }
 
 // Bitmap of the LOW class (warp per 32 ids).
-__global__ void __launch_bounds__(256) k_low_bitmap(const uint32_t* __restrict__ xtoff, uint32_t n,
+__global__ void __launch_bounds__(256) k_low_bitmap(const uint32_t* __restrict__ xtoff, uint32_t shift, uint32_t n,
                                                     uint32_t* __restrict__ bm) {
   const uint32_t words = (n + 31) >> 5;
   for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t v = (w << 5) | (threadIdx.x & 31u);
-    const bool low = v < n && xtoff[v + 1] - xtoff[v] <= kLowMax;
+    const bool low = v < n && row_len(xtoff, shift, v) <= kLowMax;
     const unsigned b = __ballot_sync(0xffffffffu, low);
     if ((threadIdx.x & 31u) == 0) bm[w] = b;
   }
@@ -350,6 +351,7 @@ cudaError_t ensure_chunks(GraphDev& g, uint32_t width, uint32_t keep, int sms, c
                           const ChunkLayout** out) {
   *out = nullptr;
   if (width == 0 || width >= g.n) return cudaSuccess;  // one chunk: the row-major CSR is the layout
+  if (g.nseg > 1) return cudaSuccess;                   // segmented rows: no chunk layouts (32-bit offsets)
   for (auto& l : g.lay)
     if (l.width == width) { *out = &l; return cudaSuccess; }
   // an empty slot, else the one not holding `keep` (still in use by the caller)
@@ -404,16 +406,16 @@ cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
     cudaError_t e = graph_alloc(&g.rcp32, sizeof(float) * (n ? n : 1), s);
     if (e != cudaSuccess) return e;
   }
-  if (n) k_low_bitmap<<<sms * 4, 256, 0, s>>>(g.xtoff, n, g.low_bm);
+  if (n) k_low_bitmap<<<sms * 4, 256, 0, s>>>(g.xtoff, g.seg_shift, n, g.low_bm);
   if (n) k_reciprocals<<<sms * 4, 256, 0, s>>>(g.xtdat, n, g.rcp, g.rcp32);
   if (!g.cls_list) {
     cudaError_t e = graph_alloc(&g.cls_list, sizeof(uint32_t) * (n ? n : 1), s);
     if (e != cudaSuccess) return e;
   }
-  return build_class_lists(g.xtoff, n, g.mid_max, g.cls_list, g.cls_begin, g.cls_edges, sms, s);
+  return build_class_lists(g.xtoff, g.seg_shift, n, g.mid_max, g.cls_list, g.cls_begin, g.cls_edges, sms, s);
 }
 
-cudaError_t build_class_lists(const uint32_t* off, uint32_t n, uint32_t mid_max, uint32_t* list,
+cudaError_t build_class_lists(const uint32_t* off, uint32_t shift, uint32_t n, uint32_t mid_max, uint32_t* list,
                               uint32_t begin[NCLS + 1], uint64_t edges_out[NCLS], int sms, cudaStream_t s) {
   if (n == 0) {
     for (int c = 0; c <= NCLS; ++c) begin[c] = 0;
@@ -430,10 +432,10 @@ cudaError_t build_class_lists(const uint32_t* off, uint32_t n, uint32_t mid_max,
   uint32_t* bounds = cnt + (size_t)NCLS * ntiles;
   unsigned long long* edges = (unsigned long long*)((char*)cnt + ((words * sizeof(uint32_t) + 7) & ~(size_t)7));
   e = cudaMemsetAsync(edges, 0, NCLS * sizeof(unsigned long long), s);
-  k_cls_count<<<ntiles, 256, 0, s>>>(off, n, mid_max, ntiles, cnt);
+  k_cls_count<<<ntiles, 256, 0, s>>>(off, shift, n, mid_max, ntiles, cnt);
   k_cls_scan<<<1, 1024, 0, s>>>(cnt, ntiles, bounds);
-  k_cls_scatter<<<ntiles, 256, 0, s>>>(off, n, mid_max, ntiles, cnt, list);
-  k_cls_edges<<<sms * 4, 256, 0, s>>>(off, n, mid_max, edges);
+  k_cls_scatter<<<ntiles, 256, 0, s>>>(off, shift, n, mid_max, ntiles, cnt, list);
+  k_cls_edges<<<sms * 4, 256, 0, s>>>(off, shift, n, mid_max, edges);
   uint32_t hb[NCLS + 1];
   unsigned long long he[NCLS];
   if (e == cudaSuccess) e = cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s);

@@ -4,6 +4,7 @@
 #include <cstdint>
 #include <cstddef>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 #include "pagerank_gb300.h"
 
@@ -83,6 +84,18 @@ struct GraphDev {
   uint32_t* xedg = nullptr;
   uint32_t* xtoff = nullptr;      // in-CSR
   uint32_t* xtedg = nullptr;
+  // Row segments, for edge arrays of 2^32 entries or more: rows
+  // [k * 2^seg_shift, (k+1) * 2^seg_shift) form segment k, whose offsets are
+  // 32-bit and relative to the segment's first edge, at xbase[k] / xtbase[k]
+  // in the edge array.  Offset entries: n + nseg, row v's begin at
+  // v + (v >> seg_shift) (seg_index).  One segment (seg_shift 32, bases null)
+  // is the plain CSR.
+  uint32_t seg_shift = 32;
+  uint32_t nseg = 1;
+  unsigned long long* xbase = nullptr;
+  unsigned long long* xtbase = nullptr;
+  std::vector<uint64_t> xseg0, xtseg0;  // host: first edge of each segment in the compact order
+  std::vector<uint64_t> xpos, xtpos;    // host: the same as positions in the device arrays
   uint32_t* xtdat = nullptr;      // out-degree
   uint32_t* cls_list = nullptr;   // n ids: LOW ids, then MID, then HIGH (each ascending)
   uint32_t cls_begin[NCLS + 1] = {0, 0, 0, 0};
@@ -119,6 +132,9 @@ struct SolveArgs {
   const uint32_t* xedg;
   const uint32_t* xtoff;
   const uint32_t* xtedg;
+  const unsigned long long* xbase;   // row segments (see GraphDev); null: one segment
+  const unsigned long long* xtbase;
+  uint32_t seg_shift;
   const uint32_t* xtdat;
   const uint32_t* cls_list;       // static classes (see GraphDev)
   double* r[2];                   // FP64 ranks, ping-pong by iteration parity
@@ -198,7 +214,7 @@ void launch_state_reset(State* st, int max_iter, double tol, cudaStream_t s);
 cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s);
 // Ids of the rows of `off` by length class (LOW, MID, HIGH; each ascending)
 // into list (n), their bounds and the edges of each class.
-cudaError_t build_class_lists(const uint32_t* off, uint32_t n, uint32_t mid_max, uint32_t* list,
+cudaError_t build_class_lists(const uint32_t* off, uint32_t shift, uint32_t n, uint32_t mid_max, uint32_t* list,
                               uint32_t begin[NCLS + 1], uint64_t edges[NCLS], int sms, cudaStream_t s);
 // b: device array [du | dv | iu | iv | tdk | tdv | tik | tiv]; t* = batch sorted by (v, u)
 cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd, uint64_t ni, int sms, cudaStream_t s);

@@ -43,12 +43,14 @@ __global__ void __launch_bounds__(kThreads) k_expand_seeds(SolveArgs a) {
   const uint32_t lane = lane_id();
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t u = a.xl[i];
-    const uint32_t b = a.xoff[u], e = a.xoff[u + 1];
+    const uint64_t iu = seg_index(u, a.seg_shift);
+    const uint32_t b = a.xoff[iu], e = a.xoff[iu + 1];
     if (e - b > 1024) {
       if (lane == 0) push(a.xb, &a.st->xbcnt, u);
       continue;
     }
-    for (uint32_t j = b + lane; j < e; j += 32) set_bit(b0, a.xedg[j]);
+    const uint32_t* ed = seg_edges(a.xedg, a.xbase, a.seg_shift, u);
+    for (uint32_t j = b + lane; j < e; j += 32) set_bit(b0, ed[j]);
   }
 }
 
@@ -74,9 +76,11 @@ __global__ void __launch_bounds__(kThreads) k_expand_level(SolveArgs a, uint32_t
   const uint32_t lane = lane_id();
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t u = a.fr[cur][i];
-    const uint32_t e = a.xoff[u + 1];
-    for (uint32_t j = a.xoff[u] + lane; j < e; j += 32) {
-      const uint32_t w = a.xedg[j];
+    const uint64_t iu = seg_index(u, a.seg_shift);
+    const uint32_t e = a.xoff[iu + 1];
+    const uint32_t* ed = seg_edges(a.xedg, a.xbase, a.seg_shift, u);
+    for (uint32_t j = a.xoff[iu] + lane; j < e; j += 32) {
+      const uint32_t w = ed[j];
       if (test_and_set(a.bm[0], w)) push(a.fr[nxt], &st->fcnt[nxt], w);
     }
   }

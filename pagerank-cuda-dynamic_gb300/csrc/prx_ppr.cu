@@ -611,6 +611,7 @@ static int ppr_common(prx_context* c, prx_graph* gr, uint32_t nvec, const uint32
   if (!(o.damping >= 0 && o.damping < 1)) FAIL(PRX_EINVAL, "prx_solve_ppr_batched: damping must be in [0, 1)");
   const GraphDev& g = gr->g;
   if (seed_off[0] != 0) FAIL(PRX_EINVAL, "prx_solve_ppr_batched: seed_off[0] must be 0");
+  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_solve_ppr_batched: not for graphs with row segments (64-bit offsets)");
   for (uint32_t k = 0; k < nvec; ++k)
     if (seed_off[k + 1] <= seed_off[k]) FAIL(PRX_EINVAL, "prx_solve_ppr_batched: every seed set must be non-empty");
   for (uint32_t i = 0; i < seed_off[nvec]; ++i)

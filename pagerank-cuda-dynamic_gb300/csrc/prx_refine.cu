@@ -44,7 +44,8 @@ __device__ __forceinline__ void reduce32(State* st, unsigned int dl, unsigned in
 // LOW: one warp per 32 consecutive ids, one lane per vertex, one launch per
 // source chunk (partial sums carried in acc32), as the FP64 kernel.
 template <bool FIRST, bool LAST>
-__global__ void __launch_bounds__(kThreads) k32_low(SolveArgs a, const uint32_t* __restrict__ off,
+__global__ void __launch_bounds__(kThreads) k32_low(SolveArgs a, const unsigned long long* __restrict__ base,
+                                                    uint32_t shift, const uint32_t* __restrict__ off,
                                                     const uint32_t* __restrict__ edg) {
   State* st = a.st;
   if (st->done || st->inner_done) return;
@@ -55,9 +56,10 @@ __global__ void __launch_bounds__(kThreads) k32_low(SolveArgs a, const uint32_t*
   for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t v = (w << 5) | lane_id();
     if (v >= a.n || !((a.low_bm[w] >> lane_id()) & 1u)) continue;
-    const uint32_t s = off[v], e = off[v + 1];
+    const uint64_t iv = seg_index(v, shift);
+    const uint32_t s = off[iv], e = off[iv + 1];
     if (!FIRST && !LAST && s == e) continue;
-    const float acc = lane_row_sum(ce, edg, s, e, FIRST ? 0.f : a.acc32[v]);
+    const float acc = lane_row_sum(ce, seg_edges(edg, base, shift, v), s, e, FIRST ? 0.f : a.acc32[v]);
     if (LAST) emax = max(emax, finish32(a, v, acc, q, &mag));
     else a.acc32[v] = acc;
   }
@@ -74,8 +76,9 @@ __global__ void __launch_bounds__(kThreads) k32_mid(SolveArgs a, uint32_t begin,
   unsigned int emax = 0, mag = 0;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t v = a.cls_list[begin + i];
-    const uint32_t s = a.xtoff[v], d = a.xtoff[v + 1] - s;
-    const uint32_t* __restrict__ ed = a.xtedg + s;
+    const uint64_t iv = seg_index(v, a.seg_shift);
+    const uint32_t s = a.xtoff[iv], d = a.xtoff[iv + 1] - s;
+    const uint32_t* __restrict__ ed = seg_edges(a.xtedg, a.xtbase, a.seg_shift, v) + s;
     float acc = 0.f;
     for (uint32_t t = lane; t < d; t += 32) acc += __ldg(ce + __ldg(ed + t));
 #pragma unroll
@@ -95,8 +98,9 @@ __global__ void __launch_bounds__(256) k32_high(SolveArgs a, uint32_t begin, uin
   unsigned int emax = 0, mag = 0;
   for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
     const uint32_t v = a.cls_list[begin + i];
-    const uint32_t s = a.xtoff[v], d = a.xtoff[v + 1] - s;
-    const uint32_t* __restrict__ ed = a.xtedg + s;
+    const uint64_t iv = seg_index(v, a.seg_shift);
+    const uint32_t s = a.xtoff[iv], d = a.xtoff[iv + 1] - s;
+    const uint32_t* __restrict__ ed = seg_edges(a.xtedg, a.xtbase, a.seg_shift, v) + s;
     float acc = 0.f;
     for (uint32_t t = threadIdx.x; t < d; t += 256) acc += __ldg(ce + __ldg(ed + t));
 #pragma unroll
@@ -185,15 +189,15 @@ bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, const ChunkL
     const uint64_t words = ((uint64_t)g.n + 31) / 32;
     const int grid = cap_grid32((words + 7) / 8, sms * 8);
     if (!lay || lay->K <= 1) {
-      k32_low<true, true><<<grid, kThreads, 0, s>>>(a, g.xtoff, g.xtedg);
+      k32_low<true, true><<<grid, kThreads, 0, s>>>(a, g.xtbase, g.seg_shift, g.xtoff, g.xtedg);
       return true;
     }
     const size_t row = (size_t)g.n + 1;
     for (int k = 0; k < lay->K; ++k) {
       const uint32_t* off = lay->off + k * row;
-      if (k == 0) k32_low<true, false><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
-      else if (k == lay->K - 1) k32_low<false, true><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
-      else k32_low<false, false><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
+      if (k == 0) k32_low<true, false><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
+      else if (k == lay->K - 1) k32_low<false, true><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
+      else k32_low<false, false><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
     }
   } else if (cls == MID) {
     k32_mid<<<cap_grid32((cnt + 7) / 8, sms * 8), kThreads, 0, s>>>(a, b, cnt);

@@ -580,6 +580,7 @@ int prx_graph_tidy_batch(prx_context* c, prx_graph* gr, const uint32_t* du, cons
   if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_graph_tidy_batch: bad context or graph");
   const GraphDev& g = gr->g;
   if (!g.xoff) FAIL(PRX_ESTATE, "prx_graph_tidy_batch: graph has no out-CSR");
+  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_graph_tidy_batch: not for graphs with row segments (64-bit offsets)");
   if (!out_nd || !out_ni) FAIL(PRX_EINVAL, "prx_graph_tidy_batch: NULL output length");
   if ((nd && (!du || !dv || !out_du || !out_dv)) || (ni && (!iu || !iv || !out_iu || !out_iv)))
     FAIL(PRX_EINVAL, "prx_graph_tidy_batch: NULL array with a non-zero length");
@@ -599,6 +600,7 @@ int prx_graph_gen_batch(prx_context* c, prx_graph* gr, uint64_t nd_req, uint64_t
   if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_graph_gen_batch: bad context or graph");
   const GraphDev& g = gr->g;
   if (!g.xoff) FAIL(PRX_ESTATE, "prx_graph_gen_batch: graph has no out-CSR");
+  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_graph_gen_batch: not for graphs with row segments (64-bit offsets)");
   if (!out_nd || !out_ni || (nd_req && (!out_du || !out_dv)) || (ni_req && (!out_iu || !out_iv)))
     FAIL(PRX_EINVAL, "prx_graph_gen_batch: NULL output");
   if (g.n == 0) FAIL(PRX_EINVAL, "prx_graph_gen_batch: empty graph");

@@ -145,7 +145,8 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
 enum Pass { PASS_ONLY = 0, PASS_FIRST = 1, PASS_INNER = 2, PASS_LAST = 3 };
 
 template <int MODE, int PASS>
-__global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const uint32_t* __restrict__ off,
+__global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const unsigned long long* __restrict__ base,
+                                                         uint32_t shift, const uint32_t* __restrict__ off,
                                                          const uint32_t* __restrict__ edg) {
   using T = ModeTraits<MODE>;
   constexpr bool FIRST = PASS == PASS_ONLY || PASS == PASS_FIRST;
@@ -188,18 +189,19 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const uint
     }
     const bool low = mine && ((a.low_bm[w] >> lane) & 1u);
     if (T::DYN && FIRST && mine && !low) {  // affected MID / HIGH vertex: its own kernel updates it
-      const uint32_t d = a.xtoff[v + 1] - a.xtoff[v];
+      const uint32_t d = row_len(a.xtoff, a.seg_shift, v);
       const int cls = d <= a.mid_max ? MID : HIGH;
       push(a.list[0][cls], &st->cnt[0][cls], v);
     }
     // One thread per row: a row's terms must be added front to back (the
     // reference's order), and a whole row per lane keeps the warp's FP64 adds
     // for different rows running side by side.
-    const uint32_t s = mine ? off[v] : 0, e = mine ? off[v + 1] : 0;
+    const uint64_t iv = seg_index(v, shift);
+    const uint32_t s = mine ? off[iv] : 0, e = mine ? off[iv + 1] : 0;
     mine = low && (FIRST || LAST || s < e);
     bool survive = false, changed = false;
     V acc = V(0);
-    if (mine) acc = lane_row_sum(c, edg, s, e, FIRST ? V(0) : carried_of<MODE>(a)[v]);
+    if (mine) acc = lane_row_sum(c, seg_edges(edg, base, shift, v), s, e, FIRST ? V(0) : carried_of<MODE>(a)[v]);
     if (mine) {
       edges += e - s;
       if (LAST) {
@@ -271,8 +273,9 @@ __global__ void __launch_bounds__(kThreads) k_update_mid(SolveArgs a, uint32_t b
   unsigned int mag = 0;
   for (uint32_t i = warp; i < count; i += nwarps) {
     const uint32_t v = list[i];
-    const uint32_t s = a.xtoff[v], d = a.xtoff[v + 1] - s;
-    const uint32_t* __restrict__ ed = a.xtedg + s;
+    const uint64_t iv = seg_index(v, a.seg_shift);
+    const uint32_t s = a.xtoff[iv], d = a.xtoff[iv + 1] - s;
+    const uint32_t* __restrict__ ed = seg_edges(a.xtedg, a.xtbase, a.seg_shift, v) + s;
     V ps[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) ps[k] = V(0);
@@ -323,8 +326,9 @@ __global__ void __launch_bounds__(256) k_update_high(SolveArgs a, uint32_t begin
   unsigned int mag = 0;
   for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
     const uint32_t v = list[i];
-    const uint32_t s = a.xtoff[v], d = a.xtoff[v + 1] - s;
-    const uint32_t* __restrict__ ed = a.xtedg + s;
+    const uint64_t iv = seg_index(v, a.seg_shift);
+    const uint32_t s = a.xtoff[iv], d = a.xtoff[iv + 1] - s;
+    const uint32_t* __restrict__ ed = seg_edges(a.xtedg, a.xtbase, a.seg_shift, v) + s;
     V acc = V(0);
     uint32_t j = t;
     for (; j + 7 * 256 < d; j += 8 * 256) {
@@ -379,12 +383,14 @@ __global__ void __launch_bounds__(kThreads) k_expand_push(SolveArgs a) {
   for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
     if (!((nf[w] >> lane) & 1u)) continue;
     const uint32_t u = (w << 5) | lane;
-    const uint32_t b = a.xoff[u], e = a.xoff[u + 1];
+    const uint64_t iu = seg_index(u, a.seg_shift);
+    const uint32_t b = a.xoff[iu], e = a.xoff[iu + 1];
     if (e - b > kLowMax) {
       push(a.xb, &st->xbcnt, u);
       continue;
     }
-    for (uint32_t j = b; j < e; ++j) set_bit(nxt, a.xedg[j]);
+    const uint32_t* ed = seg_edges(a.xedg, a.xbase, a.seg_shift, u);
+    for (uint32_t j = b; j < e; ++j) set_bit(nxt, ed[j]);
   }
 }
 
@@ -403,9 +409,11 @@ __global__ void __launch_bounds__(kThreads) k_expand_pull(SolveArgs a) {
     const uint32_t v = (w << 5) | lane;
     bool hit = false;
     if (v < a.n && !((word >> lane) & 1u)) {
-      const uint32_t e = a.xtoff[v + 1];
-      for (uint32_t j = a.xtoff[v]; j < e && !hit; ++j) {
-        const uint32_t u = a.xtedg[j];
+      const uint64_t iv = seg_index(v, a.seg_shift);
+      const uint32_t e = a.xtoff[iv + 1];
+      const uint32_t* ed = seg_edges(a.xtedg, a.xtbase, a.seg_shift, v);
+      for (uint32_t j = a.xtoff[iv]; j < e && !hit; ++j) {
+        const uint32_t u = ed[j];
         hit = (nf[u >> 5] >> (u & 31u)) & 1u;
       }
     }
@@ -423,8 +431,10 @@ __global__ void __launch_bounds__(256) k_expand_big(SolveArgs a, int target) {
   const uint32_t count = st->xbcnt;
   for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
     const uint32_t u = a.xb[i];
-    const uint32_t e = a.xoff[u + 1];
-    for (uint32_t j = a.xoff[u] + threadIdx.x; j < e; j += blockDim.x) set_bit(bm, a.xedg[j]);
+    const uint64_t iu = seg_index(u, a.seg_shift);
+    const uint32_t e = a.xoff[iu + 1];
+    const uint32_t* ed = seg_edges(a.xedg, a.xbase, a.seg_shift, u);
+    for (uint32_t j = a.xoff[iu] + threadIdx.x; j < e; j += blockDim.x) set_bit(bm, ed[j]);
   }
 }
 
@@ -538,15 +548,15 @@ static bool update_class_t(const SolveArgs& a, const GraphDev& g, int cls, const
     const uint64_t words = ((uint64_t)g.n + 31) / 32;
     const int grid = cap_grid((words + 7) / 8, sms * 8);
     if (!lay || lay->K <= 1) {
-      k_update_low<MODE, PASS_ONLY><<<grid, kThreads, 0, s>>>(a, g.xtoff, g.xtedg);
+      k_update_low<MODE, PASS_ONLY><<<grid, kThreads, 0, s>>>(a, g.xtbase, g.seg_shift, g.xtoff, g.xtedg);
       return true;
     }
     const size_t row = (size_t)g.n + 1;
     for (int k = 0; k < lay->K; ++k) {
       const uint32_t* off = lay->off + k * row;
-      if (k == 0) k_update_low<MODE, PASS_FIRST><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
-      else if (k == lay->K - 1) k_update_low<MODE, PASS_LAST><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
-      else k_update_low<MODE, PASS_INNER><<<grid, kThreads, 0, s>>>(a, off, lay->edg);
+      if (k == 0) k_update_low<MODE, PASS_FIRST><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
+      else if (k == lay->K - 1) k_update_low<MODE, PASS_LAST><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
+      else k_update_low<MODE, PASS_INNER><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
     }
     return true;
   }

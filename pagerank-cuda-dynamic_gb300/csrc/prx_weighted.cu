@@ -323,6 +323,7 @@ int prx_graph_set_weights(prx_context* c, prx_graph* gr, const float* w) {
   if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_graph_set_weights: bad context or graph");
   GraphDev& g = gr->g;
   if (!g.xoff) FAIL(PRX_ESTATE, "prx_graph_set_weights: graph has no out-CSR");
+  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_graph_set_weights: not for graphs with row segments (64-bit offsets)");
   if (!w && g.m) FAIL(PRX_EINVAL, "prx_graph_set_weights: weights are NULL");
   TRY_CUDA_ST(cudaSetDevice(c->device));
   cudaStream_t s = c->stream;
@@ -337,7 +338,7 @@ int prx_graph_set_weights(prx_context* c, prx_graph* gr, const float* w) {
     k_set_weights<<<pull_grid((uint64_t)g.n * 32, 256, c->sms * 16), 256, 0, s>>>(
         g.xoff, g.xedg, g.xtoff, g.xtedg, w, g.n, g.wsum, g.px, g.pt, &c->st->err);
   TRY_CUDA_ST(cudaGetLastError());
-  const cudaError_t e = build_class_lists(g.xoff, g.n, g.mid_max, g.ocls_list, g.ocls_begin, g.ocls_edges, c->sms, s);
+  const cudaError_t e = build_class_lists(g.xoff, 32, g.n, g.mid_max, g.ocls_list, g.ocls_begin, g.ocls_edges, c->sms, s);
   TRY_CUDA_ST(e);
   TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
   TRY_CUDA_ST(cudaStreamSynchronize(s));

@@ -104,6 +104,32 @@ class Graph:
         return g
 
     @classmethod
+    def from_csr64(cls, ctx, xtoff, xtedg, xtdat, xoff=None, xedg=None, seg_shift=0, validate=False):
+        """prx_graph_create64: 64-bit offsets (graphs of 2^32 edges or more);
+        seg_shift 0 picks the row segments, 1..32 forces them."""
+        xtoff = np.ascontiguousarray(xtoff, dtype=np.uint64)
+        xoff = None if xoff is None else np.ascontiguousarray(xoff, dtype=np.uint64)
+        xtedg, xtdat, xedg = (_u32(a) for a in (xtedg, xtdat, xedg))
+        g = cls._wrap(ctx)
+        n, m = len(xtoff) - 1, len(xtedg)
+        check(load().prx_graph_create64(ctx.handle, n, m, _p(xoff), _p(xedg) if xoff is not None else None,
+                                        xtoff.ctypes.data, _p(xtedg), _p(xtdat), int(validate), int(seg_shift),
+                                        C.byref(g._h)), "prx_graph_create64")
+        return g
+
+    def download64(self, out_csr=True):
+        """prx_graph_download64 -> (xoff, xedg, xtoff, xtedg, xtdat) with 64-bit offsets."""
+        n, m = self.size()
+        xoff = np.zeros(n + 1, np.uint64) if out_csr else None
+        xedg = np.zeros(max(m, 1), np.uint32) if out_csr else None
+        xtoff, xtedg = np.zeros(n + 1, np.uint64), np.zeros(max(m, 1), np.uint32)
+        xtdat = np.zeros(max(n, 1), np.uint32)
+        check(load().prx_graph_download64(self._h, None if xoff is None else xoff.ctypes.data,
+                                          None if xedg is None else xedg.ctypes.data, xtoff.ctypes.data,
+                                          xtedg.ctypes.data, xtdat.ctypes.data), "prx_graph_download64")
+        return xoff, None if xedg is None else xedg[:m], xtoff, xtedg[:m], xtdat[:n]
+
+    @classmethod
     def _wrap(cls, ctx):
         g = cls.__new__(cls)
         g.ctx = ctx
