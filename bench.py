@@ -304,6 +304,9 @@ def run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m):
             r = pg.solve_device(ctx, g, mode, q.data_ptr(), out.data_ptr(), bp, opts=o)
             row[name] = {"ms": r["time_ms"], "iterations": r["iterations"], "marking_ms": r["marking_time_ms"],
                          "affected_initial": r["affected_initial"], "edges": r["edges_processed"],
+                         # in-edges gathered / solve time, and their 12 bytes each (FP64: id + contribution)
+                         "touched_ge_s": r["edges_processed"] / (r["time_ms"] / 1e3) / 1e9,
+                         "touched_edge_gbs": 12 * r["edges_processed"] / (r["time_ms"] / 1e3) / 1e9,
                          "speedup_vs_static": row["static"]["ms"] / r["time_ms"],
                          "linf_vs_static": float((out - ranks).abs().max())}
             if name == "dfp":
@@ -325,7 +328,8 @@ def run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m):
     dfp = {"batch": {"deletions": first["deletions"], "insertions": first["insertions"]},
            "apply_ms": first["apply_ms"], "dfp_ms": d["ms"], "dfp_iterations": d["iterations"],
            "dfp_marking_ms": d["marking_ms"], "dfp_affected_initial": d["affected_initial"],
-           "dfp_edges": d["edges"], "df_ms": first["df"]["ms"], "static_ms": first["static"]["ms"],
+           "dfp_edges": d["edges"], "dfp_touched_ge_s": d["touched_ge_s"], "df_ms": first["df"]["ms"],
+           "static_ms": first["static"]["ms"],
            "dfp_speedup_vs_static": d["speedup_vs_static"], "df_speedup_vs_static": first["df"]["speedup_vs_static"],
            "dfp_linf_vs_static": d["linf_vs_static"], "dfp_fp32_refine_ms": d32["ms"],
            "dfp_fp32_refine_speedup_vs_dfp_fp64": d32["speedup_vs_dfp_fp64"],
