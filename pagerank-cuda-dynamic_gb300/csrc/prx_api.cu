@@ -239,16 +239,45 @@ static int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint3
     // level: a level whose frontier is empty returns at once, so levels go
     // out in batches of 1, 2, 4, ..., 1024 and the host reads the frontier
     // length once per batch (a graph of diameter 8k needs ~15 reads).
+    //
+    // Once a frontier holds more than pull_threshold vertices (n/16 by
+    // default; prx_options.expansion 1 never, 2 at once), the rest of the
+    // closure is done by pull rounds until one adds nothing: each vertex not
+    // yet reached scans its in-edges only until it finds a reached one, so a
+    // closure that covers most of the graph no longer walks every out-edge.
     launch_frontier_from_bitmap(a, c->sms, s);
     c->launches += 1;
     uint32_t level = 0;
-    for (uint32_t k = 1;; k = std::min<uint32_t>(2 * k, 1024)) {
+    bool pull = a.pull_threshold == 0;
+    if (!pull && a.pull_threshold != 0xffffffffu) {
+      TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1].fcnt[0], &c->st->fcnt[0], sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                  s));
+      TRY_CUDA_ST(cudaStreamSynchronize(s));
+      pull = c->st_host[1].fcnt[0] > a.pull_threshold;
+    }
+    for (uint32_t k = 1; !pull; k = std::min<uint32_t>(2 * k, 1024)) {
       for (uint32_t i = 0; i < k; ++i) launch_expand_level(a, level++, c->sms, s);
       c->launches += k;
       TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1].fcnt[level % 3], &c->st->fcnt[level % 3], sizeof(uint32_t),
                                   cudaMemcpyDeviceToHost, s));
       TRY_CUDA_ST(cudaStreamSynchronize(s));
-      if (c->st_host[1].fcnt[level % 3] == 0) break;
+      const uint32_t next = c->st_host[1].fcnt[level % 3];
+      if (next == 0) break;
+      pull = next > a.pull_threshold;
+    }
+    if (pull) {
+      // rounds in batches of 1, 2, 4, ..., 64; done when a round of the batch
+      // returned early (pdone) or, all having run, the last one added nothing
+      TRY_CUDA_ST(cudaMemsetAsync(c->st->pcnt, 0, sizeof(c->st->pcnt) + sizeof(c->st->pdone), s));
+      uint32_t round = 0;
+      for (uint32_t k = 1;; k = std::min<uint32_t>(2 * k, 64)) {
+        for (uint32_t i = 0; i < k; ++i) launch_closure_pull(a, round++, c->sms, s);
+        c->launches += k;
+        TRY_CUDA_ST(cudaMemcpyAsync(c->st_host[1].pcnt, c->st->pcnt, sizeof(c->st->pcnt) + sizeof(c->st->pdone),
+                                    cudaMemcpyDeviceToHost, s));
+        TRY_CUDA_ST(cudaStreamSynchronize(s));
+        if (c->st_host[1].pdone || c->st_host[1].pcnt[(round - 1) % 3] == 0) break;
+      }
     }
   }
   TRY_CUDA_ST(cudaMemsetAsync(&c->st->xcnt, 0, sizeof(uint32_t), s));

@@ -39,6 +39,8 @@ struct State {
   uint32_t cnt[2][NCLS];          // dynamic: queued MID / HIGH vertices (cnt[0][MID], cnt[0][HIGH])
   uint32_t xcnt;                  // vertices whose out-neighbours must be marked
   uint32_t fcnt[3];               // DT closure frontier lengths, rotating over levels
+  uint32_t pcnt[3];               // DT closure by pull rounds: vertices each round added, rotating
+  uint32_t pdone;                 // a pull round found that the round before it added nothing
   uint32_t err;                   // device-detected error code, 0 = none
   unsigned long long edges;       // in-edges gathered (statistic)
   unsigned long long affected;    // vertices marked before the first iteration
@@ -206,6 +208,9 @@ void launch_expand_seeds(const SolveArgs& a, int sms, cudaStream_t s);
 void launch_frontier_from_bitmap(const SolveArgs& a, int sms, cudaStream_t s);
 // One DT closure level (no-op once the frontier is empty).
 void launch_expand_level(const SolveArgs& a, uint32_t level, int sms, cudaStream_t s);
+// One DT closure round by pulling: every vertex not yet reached that has a
+// reached in-neighbour joins (no-op once a round added nothing).
+void launch_closure_pull(const SolveArgs& a, uint32_t round, int sms, cudaStream_t s);
 void launch_popcount(const uint32_t* bm, uint32_t n, unsigned long long* out, int sms, cudaStream_t s);
 void launch_flags_from_bitmap(const uint32_t* bm, uint8_t* out, uint32_t n, cudaStream_t s);
 void launch_state_reset(State* st, int max_iter, double tol, cudaStream_t s);

@@ -86,6 +86,57 @@ __global__ void __launch_bounds__(kThreads) k_expand_level(SolveArgs a, uint32_t
   }
 }
 
+// Closure round r by pulling (the reached set is bitmap 0; set semantics, so
+// the order rounds and warps add vertices in does not matter).  Round r adds
+// to pcnt[r % 3] and zeroes pcnt[(r+1) % 3], which round r-2 filled and round
+// r-1 read.  A round after one that added nothing sets pdone and returns, and
+// so does every round after it.  A warp is the only writer of its bitmap
+// word here; other warps may read it while it changes, and a bit seen set
+// early only speeds the closure up.
+__global__ void __launch_bounds__(kThreads) k_closure_pull(SolveArgs a, uint32_t round) {
+  State* st = a.st;
+  if (st->pdone) return;
+  if (round > 0 && st->pcnt[(round - 1) % 3] == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) st->pdone = 1;
+    return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->pcnt[(round + 1) % 3] = 0;
+  uint32_t* reached = a.bm[0];
+  const uint32_t words = (a.n + 31) >> 5;
+  const uint32_t lane = lane_id();
+  unsigned long long added = 0;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t word = reached[w];
+    if (word == 0xffffffffu) continue;
+    const uint32_t v = (w << 5) | lane;
+    bool hit = false;
+    if (v < a.n && !((word >> lane) & 1u)) {
+      const uint64_t iv = seg_index(v, a.seg_shift);
+      const uint32_t e = a.xtoff[iv + 1];
+      const uint32_t* ed = seg_edges(a.xtedg, a.xtbase, a.seg_shift, v);
+      for (uint32_t j = a.xtoff[iv]; j < e && !hit; ++j) {
+        const uint32_t u = ed[j];
+        hit = (reached[u >> 5] >> (u & 31u)) & 1u;
+      }
+    }
+    const unsigned add = __ballot_sync(0xffffffffu, hit);
+    if (lane == 0 && add) {
+      reached[w] = word | add;
+      added += __popc(add);
+    }
+  }
+  unsigned long long total = added;  // block sum, then one atomic per block
+  for (int o = 16; o; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+  __shared__ unsigned long long part[kThreads / 32];
+  if (lane == 0) part[threadIdx.x >> 5] = total;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long b = 0;
+    for (int k = 0; k < kThreads / 32; ++k) b += part[k];
+    if (b) atomicAdd(&st->pcnt[round % 3], (uint32_t)b);
+  }
+}
+
 __global__ void k_popcount(const uint32_t* __restrict__ bm, uint32_t words, unsigned long long* out) {
   unsigned long long x = 0;
   for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x) x += __popc(bm[w]);
@@ -108,6 +159,8 @@ __global__ void k_state_reset(State* st, int max_iter, double tol) {
     for (int c = 0; c < NCLS; ++c) st->cnt[p][c] = 0;
   st->xcnt = 0;
   st->fcnt[0] = st->fcnt[1] = st->fcnt[2] = 0;
+  st->pcnt[0] = st->pcnt[1] = st->pcnt[2] = 0;
+  st->pdone = 0;
   st->err = 0;
   st->edges = 0;
   st->affected = 0;
@@ -139,6 +192,10 @@ void launch_frontier_from_bitmap(const SolveArgs& a, int sms, cudaStream_t s) {
 
 void launch_expand_level(const SolveArgs& a, uint32_t level, int sms, cudaStream_t s) {
   k_expand_level<<<sms * 4, kThreads, 0, s>>>(a, level);
+}
+
+void launch_closure_pull(const SolveArgs& a, uint32_t round, int sms, cudaStream_t s) {
+  k_closure_pull<<<sms * 8, kThreads, 0, s>>>(a, round);
 }
 
 void launch_popcount(const uint32_t* bm, uint32_t n, unsigned long long* out, int sms, cudaStream_t s) {

@@ -129,7 +129,8 @@ def test_frontier_expansion_push_and_pull_agree(pg, ctx, kind):
     yoff, yedg = pg.graphs.apply_batch(xoff, xedg, *batch)
     yt = O.transpose(yoff, yedg)
     g, _ = _graph(pg, ctx, yoff, yedg, yt)
-    for mode in ("dynamic_frontier", "prune_dynamic_frontier"):
+    # DT: the closure by push levels, by pull rounds, or switching between them
+    for mode in ("dynamic_frontier", "prune_dynamic_frontier", "dynamic_traversal"):
         want, it_w = _oracle(mode, yoff, yedg, yt, batch, q)
         for expansion in (0, 1, 2):
             got, res = _gpu(pg, ctx, g, mode, batch, q, pg.options(expansion=expansion))
