@@ -6,6 +6,7 @@
 // inside every timed solve (:812-813).  Here one stable 3-way partition
 // (LOW / MID / HIGH, ids ascending within each class) is built once per graph
 // version with three kernels of our own and reused by every solve on it.
+#include <algorithm>
 #include <mutex>
 #include <vector>
 #include "prx_device.cuh"
@@ -339,50 +340,72 @@ __global__ void __launch_bounds__(256) k_chunk_scatter_w(const uint32_t* __restr
   }
 }
 
+static void free_layout(ChunkLayout& l) {
+  cudaFree(l.off);
+  cudaFree(l.edg);
+  for (auto p : l.seg_off) cudaFree(p);
+  for (auto p : l.seg_edg) cudaFree(p);
+  l = ChunkLayout();
+}
+
 void free_chunks(GraphDev& g) {
-  for (auto& l : g.lay) {
-    cudaFree(l.off);
-    cudaFree(l.edg);
-    l = ChunkLayout();
+  for (auto& l : g.lay) free_layout(l);
+}
+
+// The chunk layout of one CSR of `rows` rows (offsets off[0 .. rows], edges
+// edg, LOW bitmap from its first row): counts, scan, scatter.
+static cudaError_t build_layout(const uint32_t* off, const uint32_t* edg, const uint32_t* low_bm, uint32_t rows,
+                                uint64_t low_edges, uint32_t width, int K, int sms, cudaStream_t s,
+                                uint32_t** lay_off, uint32_t** lay_edg) {
+  const size_t len = (size_t)K * ((size_t)rows + 1);
+  if (len > 0xffffffffull) return cudaErrorInvalidValue;
+  cudaError_t e = graph_alloc(lay_off, sizeof(uint32_t) * len, s);
+  if (e == cudaSuccess) e = graph_alloc(lay_edg, sizeof(uint32_t) * edge_slots(low_edges), s);
+  if (e != cudaSuccess) return e;
+  const int grid = sms * 8;
+  k_chunk_count<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, *lay_off);
+  e = exclusive_scan_u32(*lay_off, (uint32_t)len, s);
+  if (e == cudaSuccess) {
+    if (K <= kScatterK) k_chunk_scatter_w<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, *lay_off, *lay_edg);
+    else k_chunk_scatter<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, *lay_off, *lay_edg);
+    e = cudaGetLastError();
   }
+  return e;
 }
 
 cudaError_t ensure_chunks(GraphDev& g, uint32_t width, uint32_t keep, int sms, cudaStream_t s,
                           const ChunkLayout** out) {
   *out = nullptr;
   if (width == 0 || width >= g.n) return cudaSuccess;  // one chunk: the row-major CSR is the layout
-  if (g.nseg > 1) return cudaSuccess;                   // segmented rows: no chunk layouts (32-bit offsets)
+  if (g.nseg > 1 && g.seg_shift < 5) return cudaSuccess;  // segments must start on a LOW-bitmap word
   for (auto& l : g.lay)
     if (l.width == width) { *out = &l; return cudaSuccess; }
   // an empty slot, else the one not holding `keep` (still in use by the caller)
   ChunkLayout& l = g.lay[0].width == 0 ? g.lay[0]
                    : g.lay[1].width == 0 ? g.lay[1]
                    : (g.lay[0].width == keep ? g.lay[1] : g.lay[0]);
-  cudaFree(l.off);
-  cudaFree(l.edg);
-  l = ChunkLayout();
+  free_layout(l);
   const int K = (int)((g.n + (uint64_t)width - 1) / width);
-  const size_t len = (size_t)K * ((size_t)g.n + 1);
-  if (len > 0xffffffffull) return cudaErrorInvalidValue;
-  cudaError_t e = graph_alloc(&l.off, sizeof(uint32_t) * len, s);
-  if (e == cudaSuccess) e = graph_alloc(&l.edg, sizeof(uint32_t) * edge_slots(g.cls_edges[LOW]), s);
-  if (e != cudaSuccess) {
-    cudaFree(l.off); cudaFree(l.edg);
-    l = ChunkLayout();
-    return e;
+  cudaError_t e = cudaSuccess;
+  if (g.nseg <= 1) {
+    e = build_layout(g.xtoff, g.xtedg, g.low_bm, g.n, g.cls_edges[LOW], width, K, sms, s, &l.off, &l.edg);
+  } else {
+    // one layout per row segment: its rows' offsets are a plain CSR of the
+    // segment's edges; sources keep their global ids, so the chunks are global
+    for (uint32_t q = 0; q < g.nseg && e == cudaSuccess; ++q) {
+      const uint64_t v0 = (uint64_t)q << g.seg_shift;
+      const uint32_t rows = (uint32_t)(std::min<uint64_t>(g.n, v0 + (1ull << g.seg_shift)) - v0);
+      const uint64_t seg_edges_bound =
+          (q + 1 < g.nseg ? g.xtseg0[q + 1] : g.m) - g.xtseg0[q];  // every edge of the segment
+      uint32_t *lo = nullptr, *le = nullptr;
+      e = build_layout(g.xtoff + v0 + q, g.xtedg + g.xtpos[q], g.low_bm + (v0 >> 5), rows, seg_edges_bound, width,
+                       K, sms, s, &lo, &le);
+      l.seg_off.push_back(lo);
+      l.seg_edg.push_back(le);
+    }
   }
-  const int grid = sms * 8;
-  k_chunk_count<<<grid, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, g.n, width, K, l.off);
-  e = exclusive_scan_u32(l.off, (uint32_t)len, s);
-  if (e == cudaSuccess) {
-    if (K <= kScatterK)
-      k_chunk_scatter_w<<<grid, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, g.n, width, K, l.off, l.edg);
-    else k_chunk_scatter<<<grid, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, g.n, width, K, l.off, l.edg);
-    e = cudaGetLastError();
-  }
   if (e != cudaSuccess) {
-    cudaFree(l.off); cudaFree(l.edg);
-    l = ChunkLayout();
+    free_layout(l);
     return e;
   }
   l.width = width;

@@ -73,8 +73,11 @@ constexpr int MODE_F32 = 0x20;
 struct ChunkLayout {
   uint32_t width = 0;             // vertices per source chunk, 0 = slot unused
   int K = 0;                      // number of chunks
-  uint32_t* off = nullptr;
+  uint32_t* off = nullptr;        // K x (n + 1) offsets into edg
   uint32_t* edg = nullptr;
+  // graphs with row segments: one layout per segment (rows [k * 2^S, ...),
+  // K x (rows + 1) offsets each, relative to the segment's own edg)
+  std::vector<uint32_t*> seg_off, seg_edg;
 };
 
 struct GraphDev {

@@ -18,6 +18,7 @@
 //      accumulated in FP32.
 //   3. x_b += e in FP64, back to 1.
 // Every FP64 and FP32 sweep counts as one iteration against max_iterations.
+#include <algorithm>
 #include "prx_device.cuh"
 
 namespace prx {
@@ -44,19 +45,22 @@ __device__ __forceinline__ void reduce32(State* st, unsigned int dl, unsigned in
 // LOW: one warp per 32 consecutive ids, one lane per vertex, one launch per
 // source chunk (partial sums carried in acc32), as the FP64 kernel.
 template <bool FIRST, bool LAST>
-__global__ void __launch_bounds__(kThreads) k32_low(SolveArgs a, const unsigned long long* __restrict__ base,
+__global__ void __launch_bounds__(kThreads) k32_low(SolveArgs a, uint32_t vb, uint32_t ve,
+                                                    const unsigned long long* __restrict__ base,
                                                     uint32_t shift, const uint32_t* __restrict__ off,
                                                     const uint32_t* __restrict__ edg) {
   State* st = a.st;
   if (st->done || st->inner_done) return;
   const int q = st->k32 & 1;
   const float* __restrict__ ce = a.ce[q];
-  const uint32_t words = (a.n + 31) >> 5;
+  // rows [vb, ve) (vb a multiple of 32); off is indexed from row vb
+  const uint32_t words = (uint32_t)(((uint64_t)ve + 31) >> 5);
   unsigned int emax = 0, mag = 0;
-  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
+  for (uint32_t w = (vb >> 5) + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < words;
+       w += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t v = (w << 5) | lane_id();
-    if (v >= a.n || !((a.low_bm[w] >> lane_id()) & 1u)) continue;
-    const uint64_t iv = seg_index(v, shift);
+    if (v >= ve || !((a.low_bm[w] >> lane_id()) & 1u)) continue;
+    const uint64_t iv = seg_index(v, shift) - vb;
     const uint32_t s = off[iv], e = off[iv + 1];
     if (!FIRST && !LAST && s == e) continue;
     const float acc = lane_row_sum(ce, seg_edges(edg, base, shift, v), s, e, FIRST ? 0.f : a.acc32[v]);
@@ -186,18 +190,27 @@ bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, const ChunkL
   const uint32_t b = g.cls_begin[cls], cnt = g.cls_begin[cls + 1] - b;
   if (!cnt) return false;
   if (cls == LOW) {
-    const uint64_t words = ((uint64_t)g.n + 31) / 32;
-    const int grid = cap_grid32((words + 7) / 8, sms * 8);
     if (!lay || lay->K <= 1) {
-      k32_low<true, true><<<grid, kThreads, 0, s>>>(a, g.xtbase, g.seg_shift, g.xtoff, g.xtedg);
+      const uint64_t words = ((uint64_t)g.n + 31) / 32;
+      const int grid = cap_grid32((words + 7) / 8, sms * 8);
+      k32_low<true, true><<<grid, kThreads, 0, s>>>(a, 0, g.n, g.xtbase, g.seg_shift, g.xtoff, g.xtedg);
       return true;
     }
-    const size_t row = (size_t)g.n + 1;
-    for (int k = 0; k < lay->K; ++k) {
-      const uint32_t* off = lay->off + k * row;
-      if (k == 0) k32_low<true, false><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
-      else if (k == lay->K - 1) k32_low<false, true><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
-      else k32_low<false, false><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
+    // one pass per source chunk (per row segment and chunk on segmented rows)
+    const size_t nseg = lay->seg_off.empty() ? 1 : lay->seg_off.size();
+    for (size_t q = 0; q < nseg; ++q) {
+      const uint32_t v0 = nseg == 1 ? 0 : (uint32_t)(q << g.seg_shift);
+      const uint32_t v1 = nseg == 1 ? g.n : (uint32_t)std::min<uint64_t>(g.n, ((uint64_t)q + 1) << g.seg_shift);
+      const uint32_t* offs = nseg == 1 ? lay->off : lay->seg_off[q];
+      const uint32_t* edg = nseg == 1 ? lay->edg : lay->seg_edg[q];
+      const size_t row = (size_t)(v1 - v0) + 1;
+      const int grid = cap_grid32(((uint64_t)(v1 - v0) + 31) / 32 / 8 + 1, sms * 8);
+      for (int k = 0; k < lay->K; ++k) {
+        const uint32_t* off = offs + k * row;
+        if (k == 0) k32_low<true, false><<<grid, kThreads, 0, s>>>(a, v0, v1, nullptr, 32, off, edg);
+        else if (k == lay->K - 1) k32_low<false, true><<<grid, kThreads, 0, s>>>(a, v0, v1, nullptr, 32, off, edg);
+        else k32_low<false, false><<<grid, kThreads, 0, s>>>(a, v0, v1, nullptr, 32, off, edg);
+      }
     }
   } else if (cls == MID) {
     k32_mid<<<cap_grid32((cnt + 7) / 8, sms * 8), kThreads, 0, s>>>(a, b, cnt);

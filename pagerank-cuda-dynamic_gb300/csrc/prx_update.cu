@@ -33,6 +33,7 @@
 // unaffected vertex, :94-96).  Three bitmaps rotate: cur (k), nxt (k+1),
 // prev (k-1); the LOW kernel clears prev after reading it, which makes it the
 // empty nxt of iteration k+1.
+#include <algorithm>
 #include <type_traits>
 #include "prx_device.cuh"
 
@@ -145,7 +146,8 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
 enum Pass { PASS_ONLY = 0, PASS_FIRST = 1, PASS_INNER = 2, PASS_LAST = 3 };
 
 template <int MODE, int PASS>
-__global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const unsigned long long* __restrict__ base,
+__global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, uint32_t vb, uint32_t ve,
+                                                         const unsigned long long* __restrict__ base,
                                                          uint32_t shift, const uint32_t* __restrict__ off,
                                                          const uint32_t* __restrict__ edg) {
   using T = ModeTraits<MODE>;
@@ -163,12 +165,14 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const unsi
     prev = a.bm[(iter + 2) % 3];
   }
   const uint32_t lane = lane_id();
-  const uint32_t words = (a.n + 31) >> 5;
+  // rows [vb, ve) (vb a multiple of 32); off is indexed from row vb
+  const uint32_t words = (uint32_t)(((uint64_t)ve + 31) >> 5);
   unsigned long long emax = 0, edges = 0;
   unsigned int mag = 0;
-  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < words; w += (gridDim.x * blockDim.x) >> 5) {
+  for (uint32_t w = (vb >> 5) + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < words;
+       w += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t v = (w << 5) | lane;
-    bool mine = v < a.n;
+    bool mine = v < ve;
     if (T::DYN) {
       const uint32_t cw = cur[w];
       if (FIRST) {
@@ -196,7 +200,7 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, const unsi
     // One thread per row: a row's terms must be added front to back (the
     // reference's order), and a whole row per lane keeps the warp's FP64 adds
     // for different rows running side by side.
-    const uint64_t iv = seg_index(v, shift);
+    const uint64_t iv = seg_index(v, shift) - vb;
     const uint32_t s = mine ? off[iv] : 0, e = mine ? off[iv + 1] : 0;
     mine = low && (FIRST || LAST || s < e);
     bool survive = false, changed = false;
@@ -545,18 +549,30 @@ static bool update_class_t(const SolveArgs& a, const GraphDev& g, int cls, const
     // static: skip when the graph has no LOW vertex; dynamic: always (the
     // first pass also maintains the bitmaps)
     if (!DYN && g.cls_begin[1] == g.cls_begin[0]) return false;
-    const uint64_t words = ((uint64_t)g.n + 31) / 32;
-    const int grid = cap_grid((words + 7) / 8, sms * 8);
     if (!lay || lay->K <= 1) {
-      k_update_low<MODE, PASS_ONLY><<<grid, kThreads, 0, s>>>(a, g.xtbase, g.seg_shift, g.xtoff, g.xtedg);
+      const uint64_t words = ((uint64_t)g.n + 31) / 32;
+      const int grid = cap_grid((words + 7) / 8, sms * 8);
+      k_update_low<MODE, PASS_ONLY><<<grid, kThreads, 0, s>>>(a, 0, g.n, g.xtbase, g.seg_shift, g.xtoff, g.xtedg);
       return true;
     }
-    const size_t row = (size_t)g.n + 1;
-    for (int k = 0; k < lay->K; ++k) {
-      const uint32_t* off = lay->off + k * row;
-      if (k == 0) k_update_low<MODE, PASS_FIRST><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
-      else if (k == lay->K - 1) k_update_low<MODE, PASS_LAST><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
-      else k_update_low<MODE, PASS_INNER><<<grid, kThreads, 0, s>>>(a, nullptr, 32, off, lay->edg);
+    // one pass per source chunk (per row segment and chunk on segmented rows)
+    const size_t nseg = lay->seg_off.empty() ? 1 : lay->seg_off.size();
+    for (size_t q = 0; q < nseg; ++q) {
+      const uint32_t v0 = nseg == 1 ? 0 : (uint32_t)(q << g.seg_shift);
+      const uint32_t v1 = nseg == 1 ? g.n : (uint32_t)std::min<uint64_t>(g.n, ((uint64_t)q + 1) << g.seg_shift);
+      const uint32_t* offs = nseg == 1 ? lay->off : lay->seg_off[q];
+      const uint32_t* edg = nseg == 1 ? lay->edg : lay->seg_edg[q];
+      const size_t row = (size_t)(v1 - v0) + 1;
+      const int grid = cap_grid(((uint64_t)(v1 - v0) + 31) / 32 / 8 + 1, sms * 8);
+      for (int k = 0; k < lay->K; ++k) {
+        const uint32_t* off = offs + k * row;
+        if (k == 0)
+          k_update_low<MODE, PASS_FIRST><<<grid, kThreads, 0, s>>>(a, v0, v1, nullptr, 32, off, edg);
+        else if (k == lay->K - 1)
+          k_update_low<MODE, PASS_LAST><<<grid, kThreads, 0, s>>>(a, v0, v1, nullptr, 32, off, edg);
+        else
+          k_update_low<MODE, PASS_INNER><<<grid, kThreads, 0, s>>>(a, v0, v1, nullptr, 32, off, edg);
+      }
     }
     return true;
   }

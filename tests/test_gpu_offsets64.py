@@ -56,7 +56,7 @@ def test_segmented_rows_bit_exact_golden(pg, ctx, case, shift):
 
 
 @pytest.mark.parametrize("kind", ["rmat", "web", "grid"])
-@pytest.mark.parametrize("shift", [4, 12])
+@pytest.mark.parametrize("shift", [4, 10, 14])
 def test_segmented_rows_synthetic(pg, ctx, kind, shift):
     """Rows of every in-degree class (thread, warp, block kernels) across
     segment boundaries; Static, DF-P and the FP32 refinement."""
@@ -80,10 +80,16 @@ def test_segmented_rows_synthetic(pg, ctx, kind, shift):
     a, ra = pg.solve(ctx, plain, pg.STATIC, opts=o32)
     b, rb = pg.solve(ctx, seg, pg.STATIC, opts=o32)
     assert ra["iterations"] == rb["iterations"] and np.array_equal(a, b)
-    # chunked gathers are not used on segmented rows; results stay the same
-    b, rb = pg.solve(ctx, seg, pg.STATIC, opts=pg.options(chunk_vertices=1000))
-    a, ra = pg.solve(ctx, plain, pg.STATIC, opts=pg.options(chunk_vertices=1000))
-    assert ra["iterations"] == rb["iterations"] and np.array_equal(a, b)
+    # source chunks: one layout per row segment (segments of 32 rows or more);
+    # 7 chunks (the coalesced scatter) and 20 (the general one)
+    n = len(yoff) - 1
+    for width in (n // 7 + 1, n // 20 + 1):
+        for mode in ("static", "prune_dynamic_frontier"):
+            for prec in (pg.FP64, pg.FP32_REFINE):
+                o = pg.options(chunk_vertices=width, precision=prec)
+                b, rb = pg.solve(ctx, seg, pg.MODES[mode], batch[:2], batch[2:], q, o)
+                a, ra = pg.solve(ctx, plain, pg.MODES[mode], batch[:2], batch[2:], q, o)
+                assert ra["iterations"] == rb["iterations"] and np.array_equal(a, b), (kind, shift, width, mode)
     plain.close()
     seg.close()
 
