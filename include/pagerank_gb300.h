@@ -155,9 +155,9 @@ int prx_graph_create(prx_context* ctx, uint32_t n, uint64_t m,
  * segment's start; seg_shift 0 picks it (one segment, the plain CSR, while
  * m < 2^32), 1..32 forces it (PRX_ERANGE if a segment would hold 2^32 edges
  * or more).  Graphs with more than one segment support every solver mode,
- * the FP32 refinement, marking, autotuning and download; batch apply, tidy
- * and generation, personalized PageRank and edge weights return PRX_ERANGE,
- * and the source-chunked gathers are not used. */
+ * the FP32 refinement, marking, autotuning and download (source chunks are
+ * built per segment, for segments of 32 rows or more); batch apply, tidy and
+ * generation, personalized PageRank and edge weights return PRX_ERANGE. */
 int prx_graph_create64(prx_context* ctx, uint32_t n, uint64_t m,
                        const uint64_t* xoff, const uint32_t* xedg,
                        const uint64_t* xtoff, const uint32_t* xtedg,
