@@ -86,19 +86,20 @@ inline prx_context* context() {
   return t.c;
 }
 
-// Dense CSR of a DiGraph over the vertex keys ks (ascending ids).
+// Dense CSR of a DiGraph over the vertex keys ks (ascending ids); 64-bit
+// offsets, so graphs of 2^32 edges or more go through as well.
 template <class G>
 void csr_of(const G& x, const std::vector<uint32_t>& ks, const std::vector<uint32_t>& dense,
-            std::vector<uint32_t>& off, std::vector<uint32_t>& edg) {
+            std::vector<uint64_t>& off, std::vector<uint32_t>& edg) {
   off.clear();
   edg.clear();
   off.reserve(ks.size() + 1);
   uint64_t o = 0;
   for (uint32_t u : ks) {
-    off.push_back((uint32_t)o);
+    off.push_back(o);
     o += x.degree(u);
   }
-  off.push_back((uint32_t)o);
+  off.push_back(o);
   edg.reserve(o);
   for (uint32_t u : ks) x.forEachEdgeKey(u, [&](auto v) { edg.push_back(dense[v]); });
 }
@@ -115,7 +116,8 @@ PagerankResult<V> invoke(int mode, const G& y, const H& yt, const std::vector<st
     ks.push_back((uint32_t)u);
   });
   const uint32_t N = (uint32_t)ks.size();
-  std::vector<uint32_t> xoff, xedg, xtoff, xtedg, xtdat(N);
+  std::vector<uint64_t> xoff, xtoff;
+  std::vector<uint32_t> xedg, xtedg, xtdat(N);
   if (DYNAMIC) csr_of(y, ks, dense, xoff, xedg);
   csr_of(yt, ks, dense, xtoff, xtedg);
   for (uint32_t i = 0; i < N; ++i) xtdat[i] = (uint32_t)yt.vertexValue(ks[i]);
@@ -129,9 +131,9 @@ PagerankResult<V> invoke(int mode, const G& y, const H& yt, const std::vector<st
   for (const auto& e : insertions) { iu.push_back(dense[std::get<0>(e)]); iv.push_back(dense[std::get<1>(e)]); }
   prx_context* ctx = context();
   prx_graph* g = nullptr;
-  check(prx_graph_create(ctx, N, xtedg.size(), DYNAMIC ? xoff.data() : nullptr, DYNAMIC ? xedg.data() : nullptr,
-                         xtoff.data(), xtedg.data(), xtdat.data(), 0, &g),
-        "prx_graph_create");
+  check(prx_graph_create64(ctx, N, xtedg.size(), DYNAMIC ? xoff.data() : nullptr, DYNAMIC ? xedg.data() : nullptr,
+                           xtoff.data(), xtedg.data(), xtdat.data(), 0, 0, &g),
+        "prx_graph_create64");
   prx_options po;
   prx_options_default(&po);
   po.repeat = o.repeat;
