@@ -117,85 +117,167 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned long
   hist[t * tiles + blockIdx.x] = sum;
 }
 
+// ---- bulk copies (TMA, non-tensor) into shared memory, mbarrier-tracked ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Arrive on bar (its one expected arrival) announcing `bytes` of transfers,
+// then copy `bytes` (a multiple of 16, both addresses 16-byte aligned) from
+// global memory to shared memory; the copy completes the barrier's phase.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase with this parity (try_wait itself suspends for
+// a while per call); false after kWaitLimit calls.
+constexpr uint32_t kWaitLimit = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
 // Radix pass, step 2 (after the exclusive scan of hist, so start[d * tiles +
-// b] is where tile b's keys of digit d go): stable scatter.  Each warp ranks
-// its keys among equal digits round by round (earlier rounds: a running
-// per-warp count; within the round: lanes below with the same digit, from
-// digit_peers); the tile is then laid out by digit in shared memory (digit
-// start in the tile + keys of that digit in lower warps + rank) and written
-// out in that order, so the keys of one digit leave as one contiguous,
-// coalesced run.
-__global__ void __launch_bounds__(kSortThreads, 3) k_radix_scatter(const unsigned long long* __restrict__ in,
-                                                                uint32_t count, int shift, uint32_t tiles,
-                                                                const uint32_t* __restrict__ start,
-                                                                unsigned long long* __restrict__ out) {
+// b] is where tile b's keys of digit d go): stable scatter.  Persistent
+// blocks take tiles b, b + grid, ...; each tile's 32 KB of keys comes in by a
+// bulk copy (cp.async.bulk) into one of two shared-memory stages, the next
+// tile's copy in flight while this one is ranked.  Each warp ranks its keys
+// among equal digits round by round (earlier rounds: a running per-warp
+// count; within the round: lanes below with the same digit, from
+// digit_peers); the tile is laid out by digit in shared memory (digit start
+// in the tile + keys of that digit in lower warps + rank) and written out in
+// that order, so the keys of one digit leave as one contiguous, coalesced
+// run.  in must hold 2 keys of slack past count (the last tile's copy is
+// rounded up to 16 bytes).  A copy that does not arrive within the wait
+// limit sets *err and ends the block.
+constexpr uint32_t kScatterSmem = (3 * kSortTile) * 8 + (2 + kSortThreads / 32) * kRadix * 4 + 64;
+
+__global__ void __launch_bounds__(kSortThreads, 2) k_radix_scatter(const unsigned long long* __restrict__ in,
+                                                                   uint32_t count, int shift, uint32_t tiles,
+                                                                   const uint32_t* __restrict__ start,
+                                                                   unsigned long long* __restrict__ out,
+                                                                   uint32_t* __restrict__ err) {
   constexpr int kWarps = kSortThreads / 32;
-  __shared__ unsigned long long sk[kSortTile];
-  __shared__ uint32_t gbase[kRadix];          // global start of this tile's digit-d run
-  __shared__ uint32_t tstart[kRadix];         // start of digit d within the tile
-  __shared__ uint32_t wrun[kWarps][kRadix];   // per warp: keys of digit d so far, then before this warp
-  __shared__ uint32_t wsum[kWarps];
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned long long* stage = reinterpret_cast<unsigned long long*>(smem);  // [2][kSortTile]
+  unsigned long long* sk = stage + 2 * kSortTile;                          // the tile by digit
+  uint32_t* gbase = reinterpret_cast<uint32_t*>(sk + kSortTile);           // global start of digit d's run
+  uint32_t* tstart = gbase + kRadix;                                       // start of digit d in the tile
+  uint32_t* wrun = tstart + kRadix;                                        // [kWarps][kRadix]
+  uint32_t* wsum = wrun + kWarps * kRadix;                                 // [kWarps]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(wsum + 8);                   // [2]
   const uint32_t t = threadIdx.x, w = t >> 5, lane = t & 31u;
-  const uint32_t tile0 = blockIdx.x * kSortTile;
-  const size_t idx = (size_t)t * tiles + blockIdx.x;
-  const uint32_t s0 = start[idx];
-  const uint32_t s1 = idx + 1 < (size_t)kRadix * tiles ? start[idx + 1] : count;
-  const uint32_t c = s1 - s0;   // this tile's keys of digit t
-  gbase[t] = s0;
-  for (int k = 0; k < kWarps; ++k) wrun[k][t] = 0;
-  const uint32_t base = tile0 + w * (kSortItems * 32) + lane;
-  unsigned long long kr[kSortItems];  // all loads in flight before the first use
-#pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
-    const uint32_t i = base + r * 32;
-    kr[r] = i < count ? in[i] : 0ull;
+  if (t == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init_fence();
   }
   __syncthreads();
-  uint32_t rank[kSortItems];
+  auto issue = [&](uint32_t tile, int buf) {  // thread 0
+    const uint32_t first = tile * kSortTile;
+    const uint32_t nk = min((uint32_t)kSortTile, count - first);
+    bulk_load(stage + buf * kSortTile, in + first, (nk * 8u + 15u) & ~15u, &bar[buf]);
+  };
+  uint32_t parity = 0;  // bit k: the phase parity stage k waits for next
+  uint32_t tile = blockIdx.x, it = 0;
+  if (tile < tiles && t == 0) issue(tile, 0);
   const unsigned lt = (1u << lane) - 1u;
-#pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
-    const bool act = base + r * 32 < count;
-    const uint32_t d = (uint32_t)((kr[r] >> shift) & (kRadix - 1));
-    const unsigned peers = digit_peers(d, act);
-    const uint32_t below = __popc(peers & lt);
-    rank[r] = act ? wrun[w][d] + below : 0;
-    __syncwarp();
-    if (act && below == 0) wrun[w][d] += __popc(peers);
-    __syncwarp();
-  }
-  // exclusive block scan of c over the 256 digits -> tstart; per digit, the
-  // keys in lower warps -> wrun
-  uint32_t x = c;
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= (uint32_t)o) x += y;
-  }
-  if (lane == 31) wsum[w] = x;
-  __syncthreads();
-  uint32_t before = 0;
-  for (uint32_t k = 0; k < w; ++k) before += wsum[k];
-  tstart[t] = before + x - c;
-  uint32_t acc = 0;
-  for (int k = 0; k < kWarps; ++k) {
-    const uint32_t v = wrun[k][t];
-    wrun[k][t] = acc;
-    acc += v;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < kSortItems; ++r) {
-    if (base + r * 32 < count) {
-      const uint32_t d = (uint32_t)((kr[r] >> shift) & (kRadix - 1));
-      sk[tstart[d] + wrun[w][d] + rank[r]] = kr[r];
+  for (; tile < tiles; tile += gridDim.x, ++it) {
+    const int buf = it & 1;
+    const uint32_t next = tile + gridDim.x;
+    // the other stage was last read in the previous tile, before its final barrier
+    if (next < tiles && t == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(next, buf ^ 1);
     }
-  }
-  __syncthreads();
-  const uint32_t nt = count - tile0 < (uint32_t)kSortTile ? count - tile0 : (uint32_t)kSortTile;
-  for (uint32_t j = t; j < nt; j += kSortThreads) {
-    const unsigned long long key = sk[j];
-    const uint32_t d = (uint32_t)((key >> shift) & (kRadix - 1));
-    out[gbase[d] + (j - tstart[d])] = key;
+    const bool ok = mbar_wait(&bar[buf], (parity >> buf) & 1u);
+    parity ^= 1u << buf;
+    if (!__syncthreads_and(ok)) {
+      // give up on this block: record it and let the copy still in flight land
+      if (t == 0) {
+        atomicExch(err, 1u);
+        if (next < tiles) mbar_wait(&bar[buf ^ 1], (parity >> (buf ^ 1)) & 1u);
+      }
+      __syncthreads();
+      return;
+    }
+    const unsigned long long* keys = stage + buf * kSortTile;
+    const uint32_t tile0 = tile * kSortTile;
+    const size_t idx = (size_t)t * tiles + tile;
+    const uint32_t s0 = start[idx];
+    const uint32_t s1 = idx + 1 < (size_t)kRadix * tiles ? start[idx + 1] : count;
+    const uint32_t c = s1 - s0;  // this tile's keys of digit t
+    gbase[t] = s0;
+    for (int k = 0; k < kWarps; ++k) wrun[k * kRadix + t] = 0;
+    __syncthreads();
+    const uint32_t lbase = w * (kSortItems * 32) + lane;  // this lane's first key in the tile
+    uint32_t rank[kSortItems];
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+      const uint32_t li = lbase + r * 32;
+      const bool act = tile0 + li < count;
+      const uint32_t d = (uint32_t)((keys[li] >> shift) & (kRadix - 1));
+      const unsigned peers = digit_peers(d, act);
+      const uint32_t below = __popc(peers & lt);
+      rank[r] = act ? wrun[w * kRadix + d] + below : 0;
+      __syncwarp();
+      if (act && below == 0) wrun[w * kRadix + d] += __popc(peers);
+      __syncwarp();
+    }
+    // exclusive block scan of c over the 256 digits -> tstart; per digit, the
+    // keys in lower warps -> wrun
+    uint32_t x = c;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (uint32_t k = 0; k < w; ++k) before += wsum[k];
+    tstart[t] = before + x - c;
+    uint32_t acc = 0;
+    for (int k = 0; k < kWarps; ++k) {
+      const uint32_t v = wrun[k * kRadix + t];
+      wrun[k * kRadix + t] = acc;
+      acc += v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+      const uint32_t li = lbase + r * 32;
+      if (tile0 + li < count) {
+        const unsigned long long key = keys[li];
+        const uint32_t d = (uint32_t)((key >> shift) & (kRadix - 1));
+        sk[tstart[d] + wrun[w * kRadix + d] + rank[r]] = key;
+      }
+    }
+    __syncthreads();
+    const uint32_t nt = count - tile0 < (uint32_t)kSortTile ? count - tile0 : (uint32_t)kSortTile;
+    for (uint32_t j = t; j < nt; j += kSortThreads) {
+      const unsigned long long key = sk[j];
+      const uint32_t d = (uint32_t)((key >> shift) & (kRadix - 1));
+      out[gbase[d] + (j - tstart[d])] = key;
+    }
+    __syncthreads();  // stage, sk and the counters are free for the next tile
   }
 }
 
@@ -237,18 +319,32 @@ __global__ void k_decode(const unsigned long long* __restrict__ key, const uint3
 // time (keys must be below 2^hi), ping-ponging with tmp; *out is the buffer
 // holding the result.  hist: 256 * ceil(count / kSortTile) + 1 words.
 static cudaError_t radix_sort_u64(unsigned long long* keys, unsigned long long* tmp, uint32_t count, int lo, int hi,
-                                  uint32_t* hist, cudaStream_t s, unsigned long long** out) {
+                                  uint32_t* hist, int sms, cudaStream_t s, unsigned long long** out) {
   const uint32_t tiles = (count + kSortTile - 1) / kSortTile;
   unsigned long long *src = keys, *dst = tmp;
-  for (int shift = lo; shift < hi && count; shift += 8) {
+  *out = src;
+  if (count == 0 || lo >= hi) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, kScatterSmem);
+  uint32_t* err = nullptr;
+  if (e == cudaSuccess) e = cudaMallocAsync(&err, sizeof(uint32_t), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  const uint32_t grid = std::min<uint32_t>(tiles, 2u * (uint32_t)sms);
+  for (int shift = lo; shift < hi && e == cudaSuccess; shift += 8) {
     k_radix_hist<<<tiles, kSortThreads, 0, s>>>(src, count, shift, tiles, hist);
-    const cudaError_t e = exclusive_scan_u32(hist, (uint32_t)(kRadix * tiles), s);
-    if (e != cudaSuccess) return e;
-    k_radix_scatter<<<tiles, kSortThreads, 0, s>>>(src, count, shift, tiles, hist, dst);
+    e = exclusive_scan_u32(hist, (uint32_t)(kRadix * tiles), s);
+    if (e != cudaSuccess) break;
+    k_radix_scatter<<<grid, kSortThreads, kScatterSmem, s>>>(src, count, shift, tiles, hist, dst, err);
     std::swap(src, dst);
   }
+  uint32_t herr = 0;
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFreeAsync(err, s);
+  if (e == cudaSuccess && herr) e = cudaErrorLaunchTimeout;  // a bulk copy never arrived
   *out = src;
-  return cudaGetLastError();
+  return e;
 }
 
 static int grid_of(uint64_t work, int sms) {
@@ -390,8 +486,8 @@ static int tidy_core(prx_context* c, const GraphDev& g, TidyBufs& b, uint32_t co
   if (e == cudaSuccess) e = cudaMalloc(&b.flag, 4ull * (count + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b.pos, 4ull * (count + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b.hist, 4ull * ((size_t)kRadix * tiles + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&b.key, 8ull * count);
-  if (e == cudaSuccess) e = cudaMalloc(&b.key2, 8ull * count);
+  if (e == cudaSuccess) e = cudaMalloc(&b.key, 8ull * (count + 2));   // + 2: radix_sort_u64's slack
+  if (e == cudaSuccess) e = cudaMalloc(&b.key2, 8ull * (count + 2));
   if (e != cudaSuccess) return fail(e);
   const int grid = grid_of(count, c->sms);
   // 1-2. existence and keys, then compaction of the kept keys
@@ -410,7 +506,7 @@ static int tidy_core(prx_context* c, const GraphDev& g, TidyBufs& b, uint32_t co
   }
   // 3. radix sort of key2[0 .. m2)
   unsigned long long* src = nullptr;
-  e = radix_sort_u64(b.key2, b.key, m2, 0, key_bits, b.hist, s, &src);
+  e = radix_sort_u64(b.key2, b.key, m2, 0, key_bits, b.hist, c->sms, s, &src);
   if (e != cudaSuccess) return fail(e);
   // 4. unique and decode
   const int g2 = grid_of(m2, c->sms);
@@ -506,9 +602,9 @@ static int create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, cons
   if (e == cudaSuccess) e = cudaMalloc(&b.flag, 4ull * (cap + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b.pos, 4ull * (cap + 1));
   if (e == cudaSuccess) e = cudaMalloc(&b.hist, 4ull * ((size_t)kRadix * tiles + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&b.key, 8ull * cap);
-  if (e == cudaSuccess) e = cudaMalloc(&b.key2, 8ull * cap);
-  if (e == cudaSuccess) e = cudaMalloc(&key3, 8ull * cap);
+  if (e == cudaSuccess) e = cudaMalloc(&b.key, 8ull * (cap + 2));    // + 2: radix_sort_u64's slack
+  if (e == cudaSuccess) e = cudaMalloc(&b.key2, 8ull * (cap + 2));
+  if (e == cudaSuccess) e = cudaMalloc(&key3, 8ull * (cap + 2));
   if (e == cudaSuccess) e = cudaMalloc(&bad, 4);
   if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, 4, s);
   if (e != cudaSuccess) return fail(e);
@@ -516,7 +612,7 @@ static int create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, cons
   // sorted unique (u, v): the out-CSR
   k_ingest_keys<<<grid, 256, 0, s>>>(du, dv, count, n, self_loops ? 1 : 0, vbits, b.key, bad);
   unsigned long long* sorted = nullptr;
-  e = radix_sort_u64(b.key, b.key2, total, 0, 2 * vbits, b.hist, s, &sorted);
+  e = radix_sort_u64(b.key, b.key2, total, 0, 2 * vbits, b.hist, c->sms, s, &sorted);
   if (e != cudaSuccess) return fail(e);
   unsigned long long* uniq = sorted == b.key ? b.key2 : b.key;  // the sort's spare buffer
   k_first_flags<<<grid, 256, 0, s>>>(sorted, total, b.flag);
@@ -548,7 +644,7 @@ static int create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, cons
   // the transpose: the swapped keys v * 2^b + u arrive ordered by u, so a
   // stable sort on their high half (v) alone orders them by (v, u); the
   // spare buffer is the old sorted one
-  e = radix_sort_u64(key3, sorted, m, vbits, 2 * vbits, b.hist, s, &sorted);
+  e = radix_sort_u64(key3, sorted, m, vbits, 2 * vbits, b.hist, c->sms, s, &sorted);
   if (e != cudaSuccess) return fail(e);
   k_ingest_offsets<<<gn, 256, 0, s>>>(sorted, m, vbits, n, g.xtoff);
   k_ingest_columns<<<gm, 256, 0, s>>>(sorted, m, vbits, g.xtedg);
