@@ -140,6 +140,8 @@ int prx_context_destroy(prx_context* ctx);
 /* The context's stream, as a cudaStream_t cast to void*. */
 void* prx_context_stream(prx_context* ctx);
 
+/* Every graph holds at most 2^32 - 2^24 vertices (PRX_ERANGE above). */
+
 /* Upload a graph (the csrCreate*W / cudaMemcpy part of pagerankInvokeCuda,
  * inc/pagerankCuda.hxx:756-805).  xoff/xedg: out-CSR of the graph, needed by
  * the dynamic modes and prx_graph_apply_batch (may be NULL for Static / ND);

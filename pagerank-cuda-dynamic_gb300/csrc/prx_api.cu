@@ -654,6 +654,7 @@ int prx_graph_create(prx_context* c, uint32_t n, uint64_t m, const uint32_t* xof
   if (!c || !out) FAIL(PRX_EINVAL, "prx_graph_create: NULL context or out");
   *out = nullptr;
   if (m > 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_create: m >= 2^32 does not fit 32-bit offsets");
+  if (n > kMaxVertices) FAIL(PRX_ERANGE, "prx_graph_create: more than 2^32 - 2^24 vertices");
   if (!xtoff || (n && !xtdat) || (m && !xtedg))
     FAIL(PRX_EINVAL, "prx_graph_create: xtoff, xtedg and xtdat are required");
   if ((xedg && !xoff) || (xoff && m && !xedg)) FAIL(PRX_EINVAL, "prx_graph_create: give both xoff and xedg or neither");
@@ -712,6 +713,7 @@ int prx_graph_create64(prx_context* c, uint32_t n, uint64_t m, const uint64_t* x
                        uint32_t seg_shift, prx_graph** out) {
   if (!c || !out) FAIL(PRX_EINVAL, "prx_graph_create64: NULL context or out");
   *out = nullptr;
+  if (n > kMaxVertices) FAIL(PRX_ERANGE, "prx_graph_create64: more than 2^32 - 2^24 vertices");
   if (!xtoff || (n && !xtdat) || (m && !xtedg))
     FAIL(PRX_EINVAL, "prx_graph_create64: xtoff, xtedg and xtdat are required");
   if ((xedg && !xoff) || (xoff && m && !xedg)) FAIL(PRX_EINVAL, "prx_graph_create64: give both xoff and xedg or neither");

@@ -27,6 +27,10 @@ constexpr int kThreads = 256;  // threads per block for all map-like kernels
 // row's last edge may reach 3 ids past the array's end.
 inline size_t edge_slots(uint64_t m) { return (size_t)((m + 3) & ~3ull) + 4; }
 
+// Largest vertex count: 2^32 - 2^24, so no 32-bit grid-stride loop index
+// (strides stay below 2^24 threads) can wrap past n.
+constexpr uint32_t kMaxVertices = 0xFF000000u;
+
 // Device-resident control block of one solve.
 struct State {
   unsigned long long el_bits[2];  // L-inf delta of the iteration with parity p (bits of a double >= 0)

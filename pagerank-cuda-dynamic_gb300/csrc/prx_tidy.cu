@@ -560,6 +560,7 @@ static int create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, cons
   const uint64_t total64 = count64 + (self_loops ? n : 0);
   if (total64 >= 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_create_from_edges: too many edges (offsets are 32-bit)");
   if (count64 && n == 0) FAIL(PRX_EINVAL, "prx_graph_create_from_edges: edges given with n = 0");
+  if (n > kMaxVertices) FAIL(PRX_ERANGE, "prx_graph_create_from_edges: more than 2^32 - 2^24 vertices");
   TRY_CUDA_ST(cudaSetDevice(c->device));
   cudaStream_t s = c->stream;
   const uint32_t count = (uint32_t)count64, total = (uint32_t)total64;
