@@ -534,7 +534,7 @@ static int tidy_list(prx_context* c, const GraphDev& g, const uint32_t* hu, cons
                      bool deletions, uint32_t* ou, uint32_t* ov, uint64_t* kept) {
   *kept = 0;
   if (count64 == 0) return PRX_OK;
-  if (count64 >= 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_tidy_batch: batch too large");
+  if (count64 > kMaxVertices) FAIL(PRX_ERANGE, "prx_graph_tidy_batch: batch too large");
   const uint32_t count = (uint32_t)count64;
   TidyBufs b;
   cudaError_t e = cudaMalloc(&b.u, 4ull * count);
@@ -558,7 +558,8 @@ static int create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, cons
   *out = nullptr;
   if (count64 && (!u || !v)) FAIL(PRX_EINVAL, "prx_graph_create_from_edges: NULL edge arrays");
   const uint64_t total64 = count64 + (self_loops ? n : 0);
-  if (total64 >= 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_create_from_edges: too many edges (offsets are 32-bit)");
+  if (total64 > kMaxVertices)  // 32-bit offsets, and 32-bit grid-stride indices that must not wrap
+    FAIL(PRX_ERANGE, "prx_graph_create_from_edges: too many edges (more than 2^32 - 2^24)");
   if (count64 && n == 0) FAIL(PRX_EINVAL, "prx_graph_create_from_edges: edges given with n = 0");
   if (n > kMaxVertices) FAIL(PRX_ERANGE, "prx_graph_create_from_edges: more than 2^32 - 2^24 vertices");
   TRY_CUDA_ST(cudaSetDevice(c->device));
@@ -701,7 +702,7 @@ int prx_graph_gen_batch(prx_context* c, prx_graph* gr, uint64_t nd_req, uint64_t
   if (!out_nd || !out_ni || (nd_req && (!out_du || !out_dv)) || (ni_req && (!out_iu || !out_iv)))
     FAIL(PRX_EINVAL, "prx_graph_gen_batch: NULL output");
   if (g.n == 0) FAIL(PRX_EINVAL, "prx_graph_gen_batch: empty graph");
-  if (nd_req >= 0xffffffffull || ni_req >= 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_gen_batch: batch too large");
+  if (nd_req > kMaxVertices || ni_req > kMaxVertices) FAIL(PRX_ERANGE, "prx_graph_gen_batch: batch too large");
   TRY_CUDA_ST(cudaSetDevice(c->device));
   *out_nd = *out_ni = 0;
   for (int del = 1; del >= 0; --del) {
