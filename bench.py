@@ -68,6 +68,8 @@ def parse():
     p.add_argument("--adjoint-scale", type=int, default=20)
     p.add_argument("--adjoint-fd-edges", type=int, default=200, help="edges checked by finite differences")
     p.add_argument("--adjoint-batches", type=int, default=2, help="dynamic batches of 1e-4|E| after the first solve")
+    p.add_argument("--batches-per-size", type=int, default=10,
+                   help="consecutive dynamic batches at each of 1e-5, 1e-4, 1e-3 |E|")
     p.add_argument("--no-ingest", action="store_true", help="skip the device graph ingest from the edge list")
     p.add_argument("--no-offsets64", action="store_true",
                    help="skip the 64-bit-offset graph (four copies of the bench graph, 4x its edges)")
@@ -256,7 +258,7 @@ def run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m):
     import torch
     dev = f"cuda:{local}"
     sizes = (1e-5, 1e-4, 1e-3)
-    parts = [(sz, int(sz * m)) for sz in sizes for _ in range(3)]
+    parts = [(sz, int(sz * m)) for sz in sizes for _ in range(args.batches_per_size)]
     nd_all = sum(c // 5 for _, c in parts)
     ni_all = sum(c - c // 5 for _, c in parts)
     du, dv, iu, iv = pg.graphs.random_batch(xoff, xedg, nd_all, ni_all, seed=args.seed + 1)
@@ -724,9 +726,10 @@ def run_ours(args):
     log(f"e2e: {e2e_ms} ms")
 
     # ---- dynamic modes over consecutive batches applied on the device ----------
-    # Batch sizes 1e-5, 1e-4, 1e-3 |E| (80% insertions), three consecutive
-    # batches each: one tidy batch drawn from the original graph, split into
-    # nine disjoint sorted parts, so every part is tidy for the graph it meets.
+    # Batch sizes 1e-5, 1e-4, 1e-3 |E| (80% insertions), ten consecutive
+    # batches each (--batches-per-size): one tidy batch drawn from the original
+    # graph, split into disjoint sorted parts, so every part is tidy for the
+    # graph it meets.
     dfp = dynamic = None
     if not args.no_dfp:
         dynamic, dfp = run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m)
