@@ -916,38 +916,20 @@ int prx_graph_apply_batch(prx_graph* gr, const uint32_t* du, const uint32_t* dv,
   if (!sorted_unique(du, dv, nd) || !sorted_unique(iu, iv, ni))
     FAIL(PRX_EINVAL, "prx_graph_apply_batch: batch must be sorted by (u, v) and unique (tidyBatchUpdateU)");
   if (g.m - nd + ni > 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_apply_batch: edge count would reach 2^32");
-  // The in-CSR wants the batch ordered by (v, u): a stable sort by v of the
-  // (u, v)-sorted lists (LSD radix, two 16-bit digits).
-  std::vector<uint32_t> host(4 * (size_t)(nd + ni));
-  auto by_target = [](const uint32_t* u, const uint32_t* v, uint64_t len, uint32_t* ok, uint32_t* ov) {
-    std::vector<uint32_t> tu(u, u + len), tv(v, v + len), su(len), sv(len);
-    for (int shift = 0; shift < 32; shift += 16) {
-      std::vector<uint64_t> cnt(65537, 0);
-      for (uint64_t i = 0; i < len; ++i) cnt[((tv[i] >> shift) & 0xffff) + 1]++;
-      for (int d = 0; d < 65536; ++d) cnt[d + 1] += cnt[d];
-      for (uint64_t i = 0; i < len; ++i) {
-        const uint64_t p = cnt[(tv[i] >> shift) & 0xffff]++;
-        su[p] = tu[i];
-        sv[p] = tv[i];
-      }
-      tu.swap(su);
-      tv.swap(sv);
-    }
-    std::copy(tv.begin(), tv.end(), ok);
-    std::copy(tu.begin(), tu.end(), ov);
-  };
-  uint32_t* h = host.data();
-  std::copy(du, du + nd, h);
-  std::copy(dv, dv + nd, h + nd);
-  std::copy(iu, iu + ni, h + 2 * nd);
-  std::copy(iv, iv + ni, h + 2 * nd + ni);
-  by_target(du, dv, nd, h + 2 * (nd + ni), h + 2 * (nd + ni) + nd);
-  by_target(iu, iv, ni, h + 2 * (nd + ni) + 2 * nd, h + 2 * (nd + ni) + 2 * nd + ni);
+  // The in-CSR wants the batch ordered by (v, u): the device sorts copies of
+  // the (u, v)-sorted lists by v (batch_by_target).
   TRY_CUDA_ST(cudaSetDevice(c->device));
-  st = ensure_batch(c, host.size());
+  st = ensure_batch(c, 4 * (size_t)(nd + ni));
   if (st) return st;
-  if (!host.empty())
-    TRY_CUDA_ST(cudaMemcpyAsync(c->batch, h, 4 * host.size(), cudaMemcpyHostToDevice, c->stream));
+  uint32_t* b = c->batch;
+  if (nd) TRY_CUDA_ST(cudaMemcpyAsync(b, du, 4 * nd, cudaMemcpyHostToDevice, c->stream));
+  if (nd) TRY_CUDA_ST(cudaMemcpyAsync(b + nd, dv, 4 * nd, cudaMemcpyHostToDevice, c->stream));
+  if (ni) TRY_CUDA_ST(cudaMemcpyAsync(b + 2 * nd, iu, 4 * ni, cudaMemcpyHostToDevice, c->stream));
+  if (ni) TRY_CUDA_ST(cudaMemcpyAsync(b + 2 * nd + ni, iv, 4 * ni, cudaMemcpyHostToDevice, c->stream));
+  uint32_t* t = b + 2 * (nd + ni);
+  TRY_CUDA_ST(batch_by_target(b, b + nd, (uint32_t)nd, g.n, t, t + nd, c->sms, c->stream));
+  TRY_CUDA_ST(batch_by_target(b + 2 * nd, b + 2 * nd + ni, (uint32_t)ni, g.n, t + 2 * nd, t + 2 * nd + ni, c->sms,
+                              c->stream));
   const cudaError_t e = apply_batch_device(g, c->batch, nd, ni, c->sms, c->stream);
   if (e == cudaErrorInvalidValue)
     FAIL(PRX_EINVAL, "prx_graph_apply_batch: batch is not tidy (a deletion is missing or an insertion exists)");

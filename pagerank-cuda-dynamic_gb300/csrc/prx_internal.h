@@ -232,6 +232,18 @@ cudaError_t build_class_lists(const uint32_t* off, uint32_t shift, uint32_t n, u
 cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd, uint64_t ni, int sms, cudaStream_t s);
 cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t len, cudaStream_t s);
 
+// Stable LSD radix sort of keys[0 .. count) on their bits [lo, hi), 8 at a
+// time, ping-ponging with tmp (both with 2 keys of slack past count: the
+// last tile's bulk copy is rounded up to 16 bytes); *out is the buffer that
+// holds the result.  hist: radix_hist_words(count) words.  (prx_tidy.cu)
+size_t radix_hist_words(uint32_t count);
+cudaError_t radix_sort_u64(unsigned long long* keys, unsigned long long* tmp, uint32_t count, int lo, int hi,
+                           uint32_t* hist, int sms, cudaStream_t s, unsigned long long** out);
+// The batch lists ordered by (v, u) for the in-CSR: a stable sort by v of
+// the (u, v)-sorted lists u / v into tk (= v) / tv (= u).  (prx_batch.cu)
+cudaError_t batch_by_target(const uint32_t* u, const uint32_t* v, uint32_t count, uint32_t n, uint32_t* tk,
+                            uint32_t* tv, int sms, cudaStream_t s);
+
 // Graph arrays come from a stream-ordered pool of this library that keeps
 // freed memory (release threshold: unlimited), so a graph built after another
 // one was destroyed reuses its pages instead of mapping new ones.  Allocated

@@ -318,8 +318,10 @@ __global__ void k_decode(const unsigned long long* __restrict__ key, const uint3
 // Stable LSD radix sort of keys[0 .. count) on their bits [lo, hi), 8 at a
 // time (keys must be below 2^hi), ping-ponging with tmp; *out is the buffer
 // holding the result.  hist: 256 * ceil(count / kSortTile) + 1 words.
-static cudaError_t radix_sort_u64(unsigned long long* keys, unsigned long long* tmp, uint32_t count, int lo, int hi,
-                                  uint32_t* hist, int sms, cudaStream_t s, unsigned long long** out) {
+size_t radix_hist_words(uint32_t count) { return (size_t)kRadix * ((count + kSortTile - 1) / kSortTile) + 1; }
+
+cudaError_t radix_sort_u64(unsigned long long* keys, unsigned long long* tmp, uint32_t count, int lo, int hi,
+                           uint32_t* hist, int sms, cudaStream_t s, unsigned long long** out) {
   const uint32_t tiles = (count + kSortTile - 1) / kSortTile;
   unsigned long long *src = keys, *dst = tmp;
   *out = src;
