@@ -134,18 +134,27 @@ __global__ void __launch_bounds__(kThreads) k_merge_rows(const uint32_t* __restr
     const uint32_t oend = ooff[r0 + cnt];
     const uint32_t tw = touched[gi];
     const uint32_t o0 = __shfl_sync(0xffffffffu, os, 0);
-    for (uint32_t pb = o0; pb < oend; pb += 32) {
-      const uint32_t p = pb + lane;
-      // the row of position p: the last of the group's rows starting at or before p
-      uint32_t i = 0;
+    for (uint32_t pb = o0; pb < oend; pb += 128) {  // 4 positions per lane in flight
+      uint32_t val[4];
 #pragma unroll
-      for (uint32_t step = 16; step; step >>= 1) {
-        const uint32_t c = i + step;
-        const uint32_t sc = __shfl_sync(0xffffffffu, os, c < cnt ? c : cnt - 1);
-        if (c < cnt && sc <= p) i = c;
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t p = pb + 32u * q + lane;
+        val[q] = p < oend ? oedg[p] : 0u;
       }
-      const uint32_t si = __shfl_sync(0xffffffffu, os, i), ni_ = __shfl_sync(0xffffffffu, ns, i);
-      if (p < oend && !((tw >> i) & 1u)) nedg[ni_ + (p - si)] = oedg[p];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const uint32_t p = pb + 32u * q + lane;
+        // the row of position p: the last of the group's rows starting at or before p
+        uint32_t i = 0;
+#pragma unroll
+        for (uint32_t step = 16; step; step >>= 1) {
+          const uint32_t c = i + step;
+          const uint32_t sc = __shfl_sync(0xffffffffu, os, c < cnt ? c : cnt - 1);
+          if (c < cnt && sc <= p) i = c;
+        }
+        const uint32_t si = __shfl_sync(0xffffffffu, os, i), ni_ = __shfl_sync(0xffffffffu, ns, i);
+        if (p < oend && !((tw >> i) & 1u)) nedg[ni_ + (p - si)] = val[q];
+      }
     }
     for (uint32_t m = tw; m; m &= m - 1) {           // touched rows, one at a time with the whole warp
       const uint32_t i = __ffs(m) - 1;
