@@ -95,7 +95,8 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
     const float P = (float)a.P, C0 = (float)a.C0, df = (float)d;
     const float rv = a.e[p][v];
     float av;
-    if (T::PRUNE) av = fmaf(P, cv - rv / df, C0) * (1.f / (1.f - P / df));
+    // ce[p][v] is rv / df, formed when rv was (the same division)
+    if (T::PRUNE) av = fmaf(P, cv - a.ce[p][v], C0) * (1.f / (1.f - P / df));
     else          av = fmaf(P, cv, C0);
     const float ev = fabsf(av - rv);
     a.e[p ^ 1][v] = av;
@@ -113,7 +114,8 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
     const double y = a.rcp[v];
     const double rv = a.r[p][v];
     double av;
-    if (T::PRUNE) av = fma(a.P, cv - div_count(rv, d, y), a.C0) * a.pf[v];  // pf: 1 / (1 - P/d)
+    // c[p][v] is div_count(rv, d, y), formed when rv was; pf: 1 / (1 - P/d)
+    if (T::PRUNE) av = fma(a.P, cv - a.c[p][v], a.C0) * a.pf[v];
     else          av = fma(a.P, cv, a.C0);
     const double ev = fabs(av - rv);
     a.r[p ^ 1][v] = av;
