@@ -191,9 +191,9 @@ cudaError_t batch_by_target(const uint32_t* u, const uint32_t* v, uint32_t count
   while (vbits < 32 && (1ull << vbits) < n) ++vbits;
   unsigned long long *key = nullptr, *tmp = nullptr, *sorted = nullptr;
   uint32_t* hist = nullptr;
-  cudaError_t e = cudaMallocAsync(&key, 8ull * (count + 2), s);
-  if (e == cudaSuccess) e = cudaMallocAsync(&tmp, 8ull * (count + 2), s);
-  if (e == cudaSuccess) e = cudaMallocAsync(&hist, 4 * radix_hist_words(count), s);
+  cudaError_t e = graph_alloc(&key, 8ull * (count + 2), s);
+  if (e == cudaSuccess) e = graph_alloc(&tmp, 8ull * (count + 2), s);
+  if (e == cudaSuccess) e = graph_alloc(&hist, 4 * radix_hist_words(count), s);
   const int grid = sms * 4;
   if (e == cudaSuccess) k_target_keys<<<grid, kThreads, 0, s>>>(u, v, count, key);
   // the lists are sorted by (u, v): a stable sort on v alone orders them by (v, u)

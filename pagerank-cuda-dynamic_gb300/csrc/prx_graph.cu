@@ -211,7 +211,7 @@ __global__ void k_selftest_div(uint32_t dmax, uint32_t per, unsigned long long* 
 
 cudaError_t selftest_division(uint32_t dmax, uint32_t per, unsigned long long* bad_host, int sms, cudaStream_t s) {
   unsigned long long* bad = nullptr;
-  cudaError_t e = cudaMalloc(&bad, sizeof(*bad));
+  cudaError_t e = graph_alloc(&bad, sizeof(*bad), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(*bad), s);
   if (e == cudaSuccess) {
     k_selftest_div<<<sms * 8, 256, 0, s>>>(dmax, per, bad);
@@ -450,7 +450,7 @@ cudaError_t build_class_lists(const uint32_t* off, uint32_t shift, uint32_t n, u
   // [class-major tile counts | 4 bounds | pad | 3 u64 edge sums]
   const size_t words = (size_t)NCLS * ntiles + NCLS + 1;
   const size_t bytes = ((words * sizeof(uint32_t) + 7) & ~(size_t)7) + NCLS * sizeof(unsigned long long);
-  cudaError_t e = cudaMallocAsync(&cnt, bytes, s);
+  cudaError_t e = graph_alloc(&cnt, bytes, s);
   if (e != cudaSuccess) return e;
   uint32_t* bounds = cnt + (size_t)NCLS * ntiles;
   unsigned long long* edges = (unsigned long long*)((char*)cnt + ((words * sizeof(uint32_t) + 7) & ~(size_t)7));
@@ -530,7 +530,7 @@ cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t len, cudaStream_t s) {
   if (len == 0) return cudaSuccess;
   const uint32_t ntiles = (len + kTileV - 1) / kTileV;
   uint32_t* sums = nullptr;
-  cudaError_t e = cudaMallocAsync(&sums, sizeof(uint32_t) * ntiles, s);
+  cudaError_t e = graph_alloc(&sums, sizeof(uint32_t) * ntiles, s);
   if (e != cudaSuccess) return e;
   k_scan_tile_sums<<<ntiles, 256, 0, s>>>(data, len, sums);
   k_scan_single<<<1, 1024, 0, s>>>(sums, ntiles);

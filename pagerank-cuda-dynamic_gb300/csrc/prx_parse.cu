@@ -222,8 +222,8 @@ struct DevEdges {
     if (want <= cap) return cudaSuccess;
     uint64_t nc = std::max<uint64_t>(want, cap * 2);
     uint32_t *nu = nullptr, *nv = nullptr;
-    cudaError_t e = cudaMalloc(&nu, 4 * nc);
-    if (e == cudaSuccess) e = cudaMalloc(&nv, 4 * nc);
+    cudaError_t e = graph_alloc(&nu, 4 * nc, s);
+    if (e == cudaSuccess) e = graph_alloc(&nv, 4 * nc, s);
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(nu, u, 4 * n, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(nv, v, 4 * n, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -288,7 +288,7 @@ int parse_chunk(prx_context* c, ParseBufs& B, const char* chunk, uint64_t bytes,
     cudaFree(B.text);
     B.text = nullptr;
     B.text_cap = 0;
-    e = cudaMalloc(&B.text, padded);
+    e = graph_alloc(&B.text, padded, s);
     if (e != cudaSuccess) return parse_fail(e);
     B.text_cap = padded;
   }
@@ -296,12 +296,12 @@ int parse_chunk(prx_context* c, ParseBufs& B, const char* chunk, uint64_t bytes,
     cudaFree(B.nl);
     B.nl = nullptr;
     B.nl_cap = 0;
-    e = cudaMalloc(&B.nl, 4 * (blocks64 + 1));
+    e = graph_alloc(&B.nl, 4 * (blocks64 + 1), s);
     if (e != cudaSuccess) return parse_fail(e);
     B.nl_cap = blocks64 + 1;
   }
   if (!B.word) {
-    e = cudaMalloc(&B.word, 3 * sizeof(unsigned long long));
+    e = graph_alloc(&B.word, 3 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return parse_fail(e);
   }
   e = cudaMemcpyAsync(B.text, chunk, bytes, cudaMemcpyHostToDevice, s);

@@ -328,7 +328,7 @@ cudaError_t radix_sort_u64(unsigned long long* keys, unsigned long long* tmp, ui
   if (count == 0 || lo >= hi) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(k_radix_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, kScatterSmem);
   uint32_t* err = nullptr;
-  if (e == cudaSuccess) e = cudaMallocAsync(&err, sizeof(uint32_t), s);
+  if (e == cudaSuccess) e = graph_alloc(&err, sizeof(uint32_t), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
   const uint32_t grid = std::min<uint32_t>(tiles, 2u * (uint32_t)sms);
@@ -485,11 +485,11 @@ static int tidy_core(prx_context* c, const GraphDev& g, TidyBufs& b, uint32_t co
     return e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
   };
   cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess) e = cudaMalloc(&b.flag, 4ull * (count + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&b.pos, 4ull * (count + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&b.hist, 4ull * ((size_t)kRadix * tiles + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&b.key, 8ull * (count + 2));   // + 2: radix_sort_u64's slack
-  if (e == cudaSuccess) e = cudaMalloc(&b.key2, 8ull * (count + 2));
+  if (e == cudaSuccess) e = graph_alloc(&b.flag, 4ull * (count + 1), s);
+  if (e == cudaSuccess) e = graph_alloc(&b.pos, 4ull * (count + 1), s);
+  if (e == cudaSuccess) e = graph_alloc(&b.hist, 4ull * ((size_t)kRadix * tiles + 1), s);
+  if (e == cudaSuccess) e = graph_alloc(&b.key, 8ull * (count + 2), s);   // + 2: radix_sort_u64's slack
+  if (e == cudaSuccess) e = graph_alloc(&b.key2, 8ull * (count + 2), s);
   if (e != cudaSuccess) return fail(e);
   const int grid = grid_of(count, c->sms);
   // 1-2. existence and keys, then compaction of the kept keys
@@ -539,8 +539,8 @@ static int tidy_list(prx_context* c, const GraphDev& g, const uint32_t* hu, cons
   if (count64 > kMaxVertices) FAIL(PRX_ERANGE, "prx_graph_tidy_batch: batch too large");
   const uint32_t count = (uint32_t)count64;
   TidyBufs b;
-  cudaError_t e = cudaMalloc(&b.u, 4ull * count);
-  if (e == cudaSuccess) e = cudaMalloc(&b.v, 4ull * count);
+  cudaError_t e = graph_alloc(&b.u, 4ull * count, c->stream);
+  if (e == cudaSuccess) e = graph_alloc(&b.v, 4ull * count, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(b.u, hu, 4ull * count, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(b.v, hv, 4ull * count, cudaMemcpyHostToDevice, c->stream);
   if (e != cudaSuccess) {
@@ -596,20 +596,20 @@ static int create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, cons
   cudaError_t e = cudaSuccess;
   const uint32_t *du = u, *dv = v;
   if (!on_device && count) {
-    if (e == cudaSuccess) e = cudaMalloc(&b.u, 4ull * count);
-    if (e == cudaSuccess) e = cudaMalloc(&b.v, 4ull * count);
+    if (e == cudaSuccess) e = graph_alloc(&b.u, 4ull * count, s);
+    if (e == cudaSuccess) e = graph_alloc(&b.v, 4ull * count, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b.u, u, 4ull * count, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b.v, v, 4ull * count, cudaMemcpyHostToDevice, s);
     du = b.u;
     dv = b.v;
   }
-  if (e == cudaSuccess) e = cudaMalloc(&b.flag, 4ull * (cap + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&b.pos, 4ull * (cap + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&b.hist, 4ull * ((size_t)kRadix * tiles + 1));
-  if (e == cudaSuccess) e = cudaMalloc(&b.key, 8ull * (cap + 2));    // + 2: radix_sort_u64's slack
-  if (e == cudaSuccess) e = cudaMalloc(&b.key2, 8ull * (cap + 2));
-  if (e == cudaSuccess) e = cudaMalloc(&key3, 8ull * (cap + 2));
-  if (e == cudaSuccess) e = cudaMalloc(&bad, 4);
+  if (e == cudaSuccess) e = graph_alloc(&b.flag, 4ull * (cap + 1), s);
+  if (e == cudaSuccess) e = graph_alloc(&b.pos, 4ull * (cap + 1), s);
+  if (e == cudaSuccess) e = graph_alloc(&b.hist, 4ull * ((size_t)kRadix * tiles + 1), s);
+  if (e == cudaSuccess) e = graph_alloc(&b.key, 8ull * (cap + 2), s);    // + 2: radix_sort_u64's slack
+  if (e == cudaSuccess) e = graph_alloc(&b.key2, 8ull * (cap + 2), s);
+  if (e == cudaSuccess) e = graph_alloc(&key3, 8ull * (cap + 2), s);
+  if (e == cudaSuccess) e = graph_alloc(&bad, 4, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, 4, s);
   if (e != cudaSuccess) return fail(e);
   const int grid = grid_of(cap, c->sms);
@@ -711,8 +711,8 @@ int prx_graph_gen_batch(prx_context* c, prx_graph* gr, uint64_t nd_req, uint64_t
     const uint32_t count = (uint32_t)(del ? nd_req : ni_req);
     if (!count) continue;
     TidyBufs b;
-    cudaError_t e = cudaMalloc(&b.u, 4ull * count);
-    if (e == cudaSuccess) e = cudaMalloc(&b.v, 4ull * count);
+    cudaError_t e = graph_alloc(&b.u, 4ull * count, c->stream);
+    if (e == cudaSuccess) e = graph_alloc(&b.v, 4ull * count, c->stream);
     if (e == cudaSuccess) {
       const int grid = grid_of(count, c->sms);
       if (del) k_gen_deletions<<<grid, 256, 0, c->stream>>>(g.xoff, g.xedg, g.n, g.m, seed, count, b.u, b.v);
