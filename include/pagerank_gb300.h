@@ -99,6 +99,15 @@ typedef struct {
                                  of FP64 / 48 MB of FP32 contributions, >= n
                                  disables chunking.  Results do not depend
                                  on it [0]                                  */
+  int    refine_sweeps;       /* PRX_FP32_REFINE with DT / DF / DF-P, the
+                                 FP32 phase: 0 runs full sweeps from q when
+                                 the initial marking covers more than n/8
+                                 vertices (the frontier bookkeeping would
+                                 cost more than it skips), else the mode's
+                                 own frontier iterations; 1 always full
+                                 sweeps; 2 always the mode's iterations.
+                                 Either way the FP64 refinement returns the
+                                 ranks converged to the tolerance [0]       */
 } prx_options;
 
 /* PagerankResult<V> (inc/pagerank.hxx:64-113) minus the rank vector, which

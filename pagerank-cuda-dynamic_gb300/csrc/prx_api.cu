@@ -38,6 +38,7 @@ void prx_options_default(prx_options* o) {
   o->timing = 0;
   o->expansion = 0;
   o->chunk_vertices = 0;
+  o->refine_sweeps = 0;
 }
 
 const char* prx_status_string(int s) {
@@ -508,6 +509,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   const int repeat = o.repeat > 0 ? o.repeat : 1;
   float ti = 0, tm = 0, tc = 0, tt = 0;
   const bool timing = o.timing != 0;
+  bool full_sweeps = false;  // FP32-refined dynamic mode run as full sweeps (last repeat)
   for (int rep = 0; rep < repeat; ++rep) {
     c->launches = 0;
     c->tev_used = 0;
@@ -550,7 +552,12 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
         if (c->st_host[1].done) return PRX_OK;
       }
     };
-    if (refine && dyn) {
+    full_sweeps = refine && dyn && o.refine_sweeps == 1;
+    if (refine && dyn && o.refine_sweeps == 0) {  // the initial marking's size decides
+      TRY_CUDA_ST(cudaStreamSynchronize(s));
+      full_sweeps = c->st_host[0].affected > g.n / 8;
+    }
+    if (refine && dyn && !full_sweeps) {
       // DT / DF / DF-P with FP32 ranks, then the FP64 refinement of the result
       // (an FP64 residual sweep over all vertices decides convergence)
       if ((st = iterate(mode | MODE_F32, lay32))) return st;
@@ -558,6 +565,9 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
       c->launches += 1;
       if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity, false))) return st;
     } else if (refine) {
+      // Static / ND, or a dynamic mode whose marking covers most of the
+      // graph: FP32 sweeps over all vertices from the initial ranks (q for
+      // the dynamic modes), then the FP64 refinement
       if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity, true))) return st;
     } else if ((st = iterate(mode, lay64))) {
       return st;
@@ -578,7 +588,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
     res->marking_time_ms = tm / repeat;
     res->computation_time_ms = tc / repeat;
     res->affected_initial = dyn ? c->st_host[0].affected : g.n;
-    res->edges_processed = dyn ? h.edges : g.m * (uint64_t)h.iter;
+    res->edges_processed = dyn && !full_sweeps ? h.edges : g.m * (uint64_t)h.iter;
     res->last_delta = h.last_delta;
     res->refinements = refine ? h.rounds : 0;
     res->kernel_launches = c->launches;

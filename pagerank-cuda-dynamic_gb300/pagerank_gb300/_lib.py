@@ -22,7 +22,7 @@ class Options(C.Structure):
     _fields_ = [("repeat", C.c_int), ("tolerance", C.c_double), ("frontier_tolerance", C.c_double),
                 ("prune_tolerance", C.c_double), ("damping", C.c_double), ("max_iterations", C.c_int),
                 ("precision", C.c_int), ("loop", C.c_int), ("partition", C.c_int), ("timing", C.c_int),
-                ("expansion", C.c_int), ("chunk_vertices", C.c_uint32)]
+                ("expansion", C.c_int), ("chunk_vertices", C.c_uint32), ("refine_sweeps", C.c_int)]
 
 
 class Result(C.Structure):

@@ -105,11 +105,13 @@ def test_refine_dynamic_modes(pg, ctx, kind):
             want, _ = O.solve(mode, yoff, yedg, *yt, du, dv, iu, iv, q=q)
             own = np.abs(want - conv).max()
             _, r64 = pg.solve(ctx, g, pg.MODES[mode], (du, dv), (iu, iv), q)
-            for loop in (pg.LOOP_GRAPH, pg.LOOP_HOST):
-                o = pg.options(precision=pg.FP32_REFINE, loop=loop)
+            # the FP32 phase as the mode's own iterations (2), as full sweeps (1),
+            # and picked by the size of the initial marking (0)
+            for loop, sweeps in ((pg.LOOP_GRAPH, 2), (pg.LOOP_HOST, 2), (pg.LOOP_GRAPH, 1), (pg.LOOP_GRAPH, 0)):
+                o = pg.options(precision=pg.FP32_REFINE, loop=loop, refine_sweeps=sweeps)
                 got, res = pg.solve(ctx, g, pg.MODES[mode], (du, dv), (iu, iv), q, o)
-                assert np.abs(got - conv).max() <= bound(conv), (kind, mode, loop)
-                assert np.abs(got - want).max() <= own + bound(want), (kind, mode, loop)
+                assert np.abs(got - conv).max() <= bound(conv), (kind, mode, loop, sweeps)
+                assert np.abs(got - want).max() <= own + bound(want), (kind, mode, loop, sweeps)
                 assert res["refinements"] >= 1 and res["last_delta"] < 1e-10
                 assert res["affected_initial"] == r64["affected_initial"]
     finally:
@@ -127,12 +129,13 @@ def test_refine_dynamic_caps_and_empty_batch(pg, ctx):
     yt = O.transpose(yoff, yedg)
     g = pg.Graph(ctx, *yt, yoff, yedg)
     try:
-        for L in (0, 1, 3):
-            got, res = pg.solve(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, (du, dv), (iu, iv), q,
-                                pg.options(precision=pg.FP32_REFINE, max_iterations=L))
-            assert res["iterations"] == L and np.all(np.isfinite(got))
-            if L == 0:
-                np.testing.assert_array_equal(got, q)
+        for sweeps in (1, 2):
+            for L in (0, 1, 3):
+                got, res = pg.solve(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, (du, dv), (iu, iv), q,
+                                    pg.options(precision=pg.FP32_REFINE, max_iterations=L, refine_sweeps=sweeps))
+                assert res["iterations"] == L and np.all(np.isfinite(got)), (sweeps, L)
+                if L == 0:
+                    np.testing.assert_array_equal(got, q)
         e = np.zeros(0, np.uint32)
         want, _ = O.solve("prune_dynamic_frontier", yoff, yedg, *yt, e, e, e, e, q=q)
         got, res = pg.solve(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, (e, e), (e, e), q,
