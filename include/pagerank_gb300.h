@@ -108,6 +108,14 @@ typedef struct {
                                  sweeps; 2 always the mode's iterations.
                                  Either way the FP64 refinement returns the
                                  ranks converged to the tolerance [0]       */
+  int    l2_fetch_bytes;      /* L2 fetch granularity hint for the solve
+                                 (cudaLimitMaxL2FetchGranularity, how many
+                                 bytes a missed load brings into L2): 0 the
+                                 autotuner's pick for the graph (none when
+                                 untuned), 32 / 64 / 128 that many, -1 none.
+                                 The process's setting is put back before
+                                 the call returns; results do not depend on
+                                 it [0]                                     */
 } prx_options;
 
 /* PagerankResult<V> (inc/pagerank.hxx:64-113) minus the rank vector, which
@@ -181,6 +189,11 @@ int prx_graph_download64(prx_graph* g, uint64_t* xoff, uint32_t* xedg,
  * prx_release_cached_memory gives that memory back to the driver. */
 int prx_graph_destroy(prx_graph* g);
 int prx_release_cached_memory(int device);
+/* The L2 fetch granularity hint of this process's context on `device`
+ * (cudaLimitMaxL2FetchGranularity: how many bytes a missed load brings into
+ * L2).  *previous (may be NULL) receives the current value; bytes in 0..128
+ * sets it, bytes < 0 only reads it.  A context limit, gone with the process. */
+int prx_l2_fetch_granularity(int device, int bytes, int* previous);
 /* Current vertex / edge counts (m changes with prx_graph_apply_batch). */
 int prx_graph_size(const prx_graph* g, uint32_t* n, uint64_t* m);
 /* Vertices and in-edges in each in-degree class of the rank update:
@@ -341,16 +354,19 @@ typedef struct {
   float    ms_per_iteration32;
   int      trials;            /* trial solves run (0 when taken from the cache)         */
   int      cached;            /* 1: picks reused for a graph of the same signature      */
+  int      l2_fetch_bytes;    /* L2 fetch granularity of the solves (32, 64 or 128)     */
 } prx_tune_result;
 
 /* Times short Static solves on g (FP64 and FP32 refinement, 3 iterations
  * each, best of two) over the MID / HIGH in-degree boundary (1024, 4096,
- * 16384) and the source-chunk widths (none, 200/128/64 MB of FP64
- * contributions, 96/48/24 MB of FP32 ones), and keeps the fastest on g: later
- * solves with chunk_vertices = 0 use them.  Results do not depend on these
- * parameters.  Picks are cached per graph signature (n, m, in-degree class
+ * 16384), the source-chunk widths (none, 200/128/64 MB of FP64
+ * contributions, 96/48/24 MB of FP32 ones) and the L2 fetch granularity (32,
+ * 64, 128 bytes; FP64 plus FP32 time), and keeps the fastest on g: later
+ * solves with chunk_vertices = 0 and l2_fetch_bytes = 0 use them.  Results
+ * do not depend on these parameters.  Picks are cached per graph signature (n, m, in-degree class
  * sizes) in the process and, when cache_path is not NULL, in that text file
- * (read before, rewritten after). */
+ * (read before, rewritten after).  A graph created later in the process with
+ * the same signature takes the cached picks when it is built. */
 int prx_autotune(prx_context* ctx, prx_graph* g, const char* cache_path, prx_tune_result* out);
 
 /* Diagnostic with no counterpart in the reference: counts, on the context's

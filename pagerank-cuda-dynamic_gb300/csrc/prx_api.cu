@@ -39,6 +39,7 @@ void prx_options_default(prx_options* o) {
   o->expansion = 0;
   o->chunk_vertices = 0;
   o->refine_sweeps = 0;
+  o->l2_fetch_bytes = 0;
 }
 
 const char* prx_status_string(int s) {
@@ -702,6 +703,7 @@ int prx_graph_create(prx_context* c, uint32_t n, uint64_t m, const uint32_t* xof
   if (e == cudaSuccess && xoff) e = upload(&g.xedg, xedg, m);
   if (e == cudaSuccess) e = build_classes(g, c->sms, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = tune_apply_cached(g, c->sms, s);
   if (e != cudaSuccess) {
     set_error(std::string("prx_graph_create: ") + cudaGetErrorString(e));
     prx_graph_destroy(gr);
@@ -715,6 +717,16 @@ int prx_release_cached_memory(int device) {
   TRY_CUDA_ST(cudaSetDevice(device));
   TRY_CUDA_ST(cudaDeviceSynchronize());
   TRY_CUDA_ST(graph_pool_trim(device));
+  return PRX_OK;
+}
+
+int prx_l2_fetch_granularity(int device, int bytes, int* previous) {
+  if (bytes > 128) FAIL(PRX_EINVAL, "prx_l2_fetch_granularity: at most 128 bytes");
+  TRY_CUDA_ST(cudaSetDevice(device));
+  size_t cur = 0;
+  TRY_CUDA_ST(cudaDeviceGetLimit(&cur, cudaLimitMaxL2FetchGranularity));
+  if (previous) *previous = (int)cur;
+  if (bytes >= 0) TRY_CUDA_ST(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)bytes));
   return PRX_OK;
 }
 
@@ -795,6 +807,7 @@ int prx_graph_create64(prx_context* c, uint32_t n, uint64_t m, const uint64_t* x
   if (e == cudaSuccess && n) e = cudaMemcpyAsync(g.xtdat, xtdat, 4 * (uint64_t)n, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = build_classes(g, c->sms, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = tune_apply_cached(g, c->sms, s);
   cudaFree(tmp);
   if (e != cudaSuccess) {
     set_error(std::string("prx_graph_create64: ") + cudaGetErrorString(e));
@@ -948,6 +961,20 @@ int prx_graph_apply_batch(prx_graph* gr, const uint32_t* du, const uint32_t* dv,
   return PRX_OK;
 }
 
+// Sets the L2 fetch granularity hint for the life of a solve and puts the
+// process's previous setting back afterwards (bytes <= 0: leaves it).
+struct FetchGuard {
+  size_t prev = 0;
+  bool set = false;
+  explicit FetchGuard(int bytes) {
+    if (bytes <= 0 || cudaDeviceGetLimit(&prev, cudaLimitMaxL2FetchGranularity) != cudaSuccess) return;
+    if (prev != (size_t)bytes) set = cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)bytes) == cudaSuccess;
+  }
+  ~FetchGuard() {
+    if (set) cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, prev);
+  }
+};
+
 static int solve_common(prx_context* c, prx_graph* gr, int mode, const uint32_t* du, const uint32_t* dv,
                         uint64_t nd, const uint32_t* iu, const uint32_t* iv, uint64_t ni, const double* q,
                         const prx_options* o, double* ranks_out, prx_result* res, bool host) {
@@ -957,6 +984,8 @@ static int solve_common(prx_context* c, prx_graph* gr, int mode, const uint32_t*
   prx_options_default(&opt);
   if (o) opt = *o;
   if (!(opt.damping > 0 && opt.damping < 1)) FAIL(PRX_EINVAL, "prx_solve: damping must be in (0, 1)");
+  if (opt.l2_fetch_bytes < -1 || opt.l2_fetch_bytes > 128)
+    FAIL(PRX_EINVAL, "prx_solve: l2_fetch_bytes must be in -1 .. 128");
   if (!ranks_out && gr->g.n) FAIL(PRX_EINVAL, "prx_solve: ranks_out is NULL");
   if (res) std::memset(res, 0, sizeof(*res));
   const GraphDev& g = gr->g;
@@ -991,8 +1020,13 @@ static int solve_common(prx_context* c, prx_graph* gr, int mode, const uint32_t*
     }
   }
   const double* fr = nullptr;
+  // held until the stream is drained below (the destructor runs after it)
+  FetchGuard fetch(opt.l2_fetch_bytes == 0 ? g.tuned_fetch : opt.l2_fetch_bytes);
   st = solve_core(c, gr, mode, ddu, ddv, nd, diu, ni, dq, opt, res, &fr);
-  if (st) return st;
+  if (st) {
+    cudaStreamSynchronize(c->stream);
+    return st;
+  }
   TRY_CUDA_ST(cudaMemcpyAsync(ranks_out, fr, sizeof(double) * g.n,
                               host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, c->stream));
   TRY_CUDA_ST(cudaStreamSynchronize(c->stream));

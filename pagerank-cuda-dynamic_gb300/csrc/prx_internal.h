@@ -112,6 +112,7 @@ struct GraphDev {
   uint32_t mid_max = kDefaultMidMax;
   uint32_t tuned_w64 = 0;         // source-chunk widths picked by prx_autotune (0: library default)
   uint32_t tuned_w32 = 0;
+  int tuned_fetch = 0;            // L2 fetch granularity picked by prx_autotune (0: none)
   uint32_t* low_bm = nullptr;     // bitmap of the LOW class
   double* rcp = nullptr;          // RN(1 / outdeg) per vertex, for div_count
   float* rcp32 = nullptr;         // the same in FP32 (personalized PageRank sweeps)
@@ -224,6 +225,9 @@ void launch_state_reset(State* st, int max_iter, double tol, cudaStream_t s);
 
 // ---- graph construction (prx_graph.cu) ----------------------------------
 cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s);
+// A new graph takes the picks prx_autotune made earlier in this process for a
+// graph of the same signature, if any (prx_tune.cu).
+cudaError_t tune_apply_cached(GraphDev& g, int sms, cudaStream_t s);
 // Ids of the rows of `off` by length class (LOW, MID, HIGH; each ascending)
 // into list (n), their bounds and the edges of each class.
 cudaError_t build_class_lists(const uint32_t* off, uint32_t shift, uint32_t n, uint32_t mid_max, uint32_t* list,

@@ -657,6 +657,7 @@ static int create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, cons
   release();
   if (e == cudaSuccess) e = build_classes(g, c->sms, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess) e = tune_apply_cached(g, c->sms, s);
   if (e != cudaSuccess) return fail(e);
   *out = gr;
   return PRX_OK;

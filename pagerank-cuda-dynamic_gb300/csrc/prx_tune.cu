@@ -1,7 +1,9 @@
 // prx_tune.cu -- autotuner for the execution parameters that do not change
 // results: the MID / HIGH in-degree boundary (warp or block per vertex, both
-// in the reference's 256-way order) and the source-chunk widths of the FP64
-// and FP32 sweeps of the in-degree <= 64 rows.  No counterpart in the
+// in the reference's 256-way order), the source-chunk widths of the FP64
+// and FP32 sweeps of the in-degree <= 64 rows, and the L2 fetch granularity
+// (how much of a line a missed gather brings in: more helps when nearby
+// contributions are read soon after, less when gathers are scattered).  No counterpart in the
 // reference, which uses fixed thresholds (inc/pagerankCuda.hxx:625-638).
 //
 // Each candidate is timed by short solves on the graph itself (Static, 3
@@ -22,6 +24,7 @@ namespace {
 struct Pick {
   uint32_t mid_max, w64, w32;
   float ms64, ms32;
+  int fetch;
 };
 
 std::mutex g_tune_mu;
@@ -38,10 +41,12 @@ void load_file(const char* path) {
   if (!path) return;
   FILE* f = fopen(path, "r");
   if (!f) return;
-  char key[160];
-  Pick p{};
-  while (fscanf(f, "%159s %u %u %u %f %f", key, &p.mid_max, &p.w64, &p.w32, &p.ms64, &p.ms32) == 6)
-    g_tune_cache[key] = p;
+  char line[320], key[160];
+  while (fgets(line, sizeof line, f)) {
+    Pick p{};
+    if (sscanf(line, "%159s %u %u %u %f %f %d", key, &p.mid_max, &p.w64, &p.w32, &p.ms64, &p.ms32, &p.fetch) >= 6)
+      g_tune_cache[key] = p;
+  }
   fclose(f);
 }
 
@@ -50,18 +55,20 @@ void save_file(const char* path) {
   FILE* f = fopen(path, "w");
   if (!f) return;
   for (const auto& kv : g_tune_cache)
-    fprintf(f, "%s %u %u %u %.4f %.4f\n", kv.first.c_str(), kv.second.mid_max, kv.second.w64, kv.second.w32,
-            kv.second.ms64, kv.second.ms32);
+    fprintf(f, "%s %u %u %u %.4f %.4f %d\n", kv.first.c_str(), kv.second.mid_max, kv.second.w64, kv.second.w32,
+            kv.second.ms64, kv.second.ms32, kv.second.fetch);
   fclose(f);
 }
 
 // ms per iteration of a short Static solve (best of two), or < 0 on error.
-float trial(prx_context* c, prx_graph* gr, double* ranks, int precision, uint32_t width, int* status) {
+float trial(prx_context* c, prx_graph* gr, double* ranks, int precision, uint32_t width, int* status,
+            int fetch = -1) {
   prx_options o;
   prx_options_default(&o);
   o.max_iterations = 3;
   o.precision = precision;
   o.chunk_vertices = width;
+  o.l2_fetch_bytes = fetch;
   o.tolerance = 0.0;  // run all three iterations
   float best = -1.f;
   for (int rep = 0; rep < 2; ++rep) {
@@ -78,6 +85,25 @@ float trial(prx_context* c, prx_graph* gr, double* ranks, int precision, uint32_
 }
 
 }  // namespace
+
+cudaError_t prx::tune_apply_cached(GraphDev& g, int sms, cudaStream_t s) {
+  if (g.n == 0) return cudaSuccess;
+  Pick p;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    const auto it = g_tune_cache.find(signature(g));
+    if (it == g_tune_cache.end()) return cudaSuccess;
+    p = it->second;
+  }
+  g.tuned_w64 = p.w64;
+  g.tuned_w32 = p.w32;
+  g.tuned_fetch = p.fetch;
+  if (p.mid_max == g.mid_max) return cudaSuccess;
+  g.mid_max = p.mid_max;
+  cudaError_t e = build_classes(g, sms, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e;
+}
 
 extern "C" {
 
@@ -104,7 +130,8 @@ int prx_autotune(prx_context* c, prx_graph* gr, const char* cache_path, prx_tune
     }
     g.tuned_w64 = p.w64;
     g.tuned_w32 = p.w32;
-    res = {p.mid_max, p.w64, p.w32, p.ms64, p.ms32, 0, 1};
+    g.tuned_fetch = p.fetch;
+    res = {p.mid_max, p.w64, p.w32, p.ms64, p.ms32, 0, 1, p.fetch};
     if (out) *out = res;
     return PRX_OK;
   }
@@ -161,13 +188,34 @@ int prx_autotune(prx_context* c, prx_graph* gr, const char* cache_path, prx_tune
       }
     }
   }
+  // 3. L2 fetch granularity with those picks, by FP64 plus FP32 time
+  int fetch = 0;
+  if (!st) {
+    g.tuned_w64 = w64;
+    g.tuned_w32 = w32;
+    g.tuned_fetch = 0;
+    float bsum = -1.f;
+    for (int f : {32, 64, 128}) {
+      const float a = trial(c, gr, ranks, PRX_FP64, 0, &st, f);
+      const float b = st ? 0.f : trial(c, gr, ranks, PRX_FP32_REFINE, 0, &st, f);
+      trials += 2;
+      if (st) break;
+      if (bsum < 0 || a + b < bsum) {
+        bsum = a + b;
+        fetch = f;
+        ms64 = a;
+        ms32 = b;
+      }
+    }
+  }
   cudaFree(ranks);
   if (st) return st;
   g.tuned_w64 = w64;
   g.tuned_w32 = w32;
-  g_tune_cache[key] = {g.mid_max, w64, w32, ms64, ms32};
+  g.tuned_fetch = fetch;
+  g_tune_cache[key] = {g.mid_max, w64, w32, ms64, ms32, fetch};
   save_file(cache_path);
-  res = {g.mid_max, w64, w32, ms64, ms32, trials, 0};
+  res = {g.mid_max, w64, w32, ms64, ms32, trials, 0, fetch};
   if (out) *out = res;
   return PRX_OK;
 }

@@ -22,7 +22,8 @@ class Options(C.Structure):
     _fields_ = [("repeat", C.c_int), ("tolerance", C.c_double), ("frontier_tolerance", C.c_double),
                 ("prune_tolerance", C.c_double), ("damping", C.c_double), ("max_iterations", C.c_int),
                 ("precision", C.c_int), ("loop", C.c_int), ("partition", C.c_int), ("timing", C.c_int),
-                ("expansion", C.c_int), ("chunk_vertices", C.c_uint32), ("refine_sweeps", C.c_int)]
+                ("expansion", C.c_int), ("chunk_vertices", C.c_uint32), ("refine_sweeps", C.c_int),
+                ("l2_fetch_bytes", C.c_int)]
 
 
 class Result(C.Structure):
@@ -55,7 +56,7 @@ class TuneResult(C.Structure):
     """prx_tune_result (autotuner picks; no counterpart in the reference)."""
     _fields_ = [("mid_max", C.c_uint32), ("chunk_vertices64", C.c_uint32), ("chunk_vertices32", C.c_uint32),
                 ("ms_per_iteration64", C.c_float), ("ms_per_iteration32", C.c_float), ("trials", C.c_int),
-                ("cached", C.c_int)]
+                ("cached", C.c_int), ("l2_fetch_bytes", C.c_int)]
 
     as_dict = Result.as_dict
 
@@ -75,7 +76,7 @@ _lib = None
 EXPORTS = (
     "prx_options_default", "prx_status_string", "prx_last_error", "prx_context_create", "prx_context_destroy",
     "prx_context_stream", "prx_graph_create", "prx_graph_create64", "prx_graph_download64", "prx_graph_destroy",
-    "prx_release_cached_memory", "prx_graph_size", "prx_graph_class_stats",
+    "prx_release_cached_memory", "prx_l2_fetch_granularity", "prx_graph_size", "prx_graph_class_stats",
     "prx_graph_download",
     "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_selftest_division",
     "prx_solve_ppr_batched", "prx_solve_ppr_batched_device", "prx_graph_set_weights", "prx_solve_weighted",
@@ -117,6 +118,7 @@ def load(build_if_missing=True):
         "prx_graph_download64": (i32, [vp, vp, vp, vp, vp, vp]),
         "prx_graph_destroy": (i32, [vp]),
         "prx_release_cached_memory": (i32, [i32]),
+        "prx_l2_fetch_granularity": (i32, [i32, i32, C.POINTER(i32)]),
         "prx_graph_size": (i32, [vp, C.POINTER(C.c_uint32), C.POINTER(u64)]),
         "prx_graph_class_stats": (i32, [vp, C.POINTER(C.c_uint32), C.POINTER(u64)]),
         "prx_graph_download": (i32, [vp, vp, vp, vp, vp, vp]),

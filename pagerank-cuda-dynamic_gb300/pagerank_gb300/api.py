@@ -294,6 +294,15 @@ def release_cached_memory(device=0):
     check(load().prx_release_cached_memory(int(device)), "prx_release_cached_memory")
 
 
+def l2_fetch_granularity(bytes_=None, device=0):
+    """prx_l2_fetch_granularity: the previous L2 fetch granularity hint of this
+    process on `device`; sets it to bytes_ (0..128) when given."""
+    prev = C.c_int32()
+    check(load().prx_l2_fetch_granularity(int(device), -1 if bytes_ is None else int(bytes_), C.byref(prev)),
+          "prx_l2_fetch_granularity")
+    return prev.value
+
+
 def mark_affected(ctx, g, mode, deletions, insertions):
     """Initial affected flags of a dynamic mode -> uint8[n]."""
     n, _ = g.size()

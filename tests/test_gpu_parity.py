@@ -282,11 +282,39 @@ def test_autotune_keeps_results_and_caches(pg, ctx, tmp_path):
         assert res["iterations"] == it_w, mode
         np.testing.assert_array_equal(got, want, err_msg=mode)
     g2, _ = _graph(pg, ctx, yoff, yedg, yt)
+    # built after the tuning: the picks (here the MID / HIGH split) are taken at creation
+    assert g2.class_stats() == g.class_stats()
     t2 = pg.autotune(ctx, g2)
     assert t2["cached"] == 1 and t2["trials"] == 0 and t2["mid_max"] == t["mid_max"]
+    assert t["l2_fetch_bytes"] in (32, 64, 128) and t2["l2_fetch_bytes"] == t["l2_fetch_bytes"]
     lines = path.read_text().split()
-    assert len(lines) >= 6 and int(lines[1]) == t["mid_max"]
+    assert len(lines) >= 7 and int(lines[1]) == t["mid_max"] and int(lines[6]) == t["l2_fetch_bytes"]
     g2.close()
+    g.close()
+
+
+def test_l2_fetch_granularity_is_restored_and_changes_nothing(pg, ctx):
+    # the solve sets the hint for its own duration only; every granularity
+    # gives the oracle's ranks bit for bit
+    xoff, xedg = _synthetic(pg, "hubs")
+    xt = O.transpose(xoff, xedg)
+    g, _ = _graph(pg, ctx, xoff, xedg, xt)
+    want, it_w = O.solve("static", None, None, *xt)
+    prev = pg.l2_fetch_granularity()
+    assert pg.l2_fetch_granularity(128) == prev and pg.l2_fetch_granularity() == 128
+    pg.l2_fetch_granularity(prev)
+    for f in (-1, 0, 32, 64, 128):
+        got, res = pg.pagerank_static(ctx, g, opts=pg.options(l2_fetch_bytes=f))
+        assert res["iterations"] == it_w
+        np.testing.assert_array_equal(got, want)
+        assert pg.l2_fetch_granularity() == prev, f
+    for bad in (-2, 129):
+        with pytest.raises(pg.PrxError) as e:
+            pg.pagerank_static(ctx, g, opts=pg.options(l2_fetch_bytes=bad))
+        assert e.value.status == 1
+    with pytest.raises(pg.PrxError):
+        pg.l2_fetch_granularity(129)
+    assert pg.l2_fetch_granularity() == prev
     g.close()
 
 
