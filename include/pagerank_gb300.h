@@ -189,6 +189,10 @@ int prx_graph_download64(prx_graph* g, uint64_t* xoff, uint32_t* xedg,
  * prx_release_cached_memory gives that memory back to the driver. */
 int prx_graph_destroy(prx_graph* g);
 int prx_release_cached_memory(int device);
+/* That pool on `device`: bytes held from the driver and bytes in use, now and
+ * at their peak (each output may be NULL; all 0 before the first graph). */
+int prx_graph_pool_stats(int device, uint64_t* reserved, uint64_t* reserved_peak, uint64_t* used,
+                         uint64_t* used_peak);
 /* The L2 fetch granularity hint of this process's context on `device`
  * (cudaLimitMaxL2FetchGranularity: how many bytes a missed load brings into
  * L2).  *previous (may be NULL) receives the current value; bytes in 0..128

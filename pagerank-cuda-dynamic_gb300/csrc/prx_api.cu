@@ -720,6 +720,18 @@ int prx_release_cached_memory(int device) {
   return PRX_OK;
 }
 
+int prx_graph_pool_stats(int device, uint64_t* reserved, uint64_t* reserved_peak, uint64_t* used,
+                         uint64_t* used_peak) {
+  TRY_CUDA_ST(cudaSetDevice(device));
+  uint64_t v[4];
+  TRY_CUDA_ST(graph_pool_stats(device, v));
+  if (reserved) *reserved = v[0];
+  if (reserved_peak) *reserved_peak = v[1];
+  if (used) *used = v[2];
+  if (used_peak) *used_peak = v[3];
+  return PRX_OK;
+}
+
 int prx_l2_fetch_granularity(int device, int bytes, int* previous) {
   if (bytes > 128) FAIL(PRX_EINVAL, "prx_l2_fetch_granularity: at most 128 bytes");
   TRY_CUDA_ST(cudaSetDevice(device));

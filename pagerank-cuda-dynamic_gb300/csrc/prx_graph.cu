@@ -62,6 +62,23 @@ cudaError_t graph_pool_trim(int dev) {
   return cudaMemPoolTrimTo(pool, 0);
 }
 
+cudaError_t graph_pool_stats(int dev, uint64_t out[4]) {
+  for (int k = 0; k < 4; ++k) out[k] = 0;
+  cudaMemPool_t pool = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    if (dev < 0 || dev >= kMaxDevices || !g_pool[dev]) return cudaSuccess;
+    pool = g_pool[dev];
+  }
+  const cudaMemPoolAttr attrs[4] = {cudaMemPoolAttrReservedMemCurrent, cudaMemPoolAttrReservedMemHigh,
+                                    cudaMemPoolAttrUsedMemCurrent, cudaMemPoolAttrUsedMemHigh};
+  for (int k = 0; k < 4; ++k) {
+    const cudaError_t e = cudaMemPoolGetAttribute(pool, attrs[k], &out[k]);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 constexpr uint32_t kTileV = 2048;            // vertices per tile (256 threads x 8)
 constexpr int kFieldBits = 21;               // per-class count within a tile, packed into a u64
 constexpr unsigned long long kFieldMask = (1ull << kFieldBits) - 1;

@@ -259,6 +259,8 @@ cudaError_t graph_alloc(T** p, size_t bytes, cudaStream_t s) {
 }
 // Give the pool's free memory on device dev back to the driver.
 cudaError_t graph_pool_trim(int dev);
+// Bytes the pool holds from the driver and bytes handed out, now and at peak.
+cudaError_t graph_pool_stats(int dev, uint64_t out[4]);
 // Mismatches of div_count against the IEEE division (prx_selftest_division).
 cudaError_t selftest_division(uint32_t dmax, uint32_t per, unsigned long long* bad_host, int sms, cudaStream_t s);
 

@@ -76,7 +76,7 @@ _lib = None
 EXPORTS = (
     "prx_options_default", "prx_status_string", "prx_last_error", "prx_context_create", "prx_context_destroy",
     "prx_context_stream", "prx_graph_create", "prx_graph_create64", "prx_graph_download64", "prx_graph_destroy",
-    "prx_release_cached_memory", "prx_l2_fetch_granularity", "prx_graph_size", "prx_graph_class_stats",
+    "prx_release_cached_memory", "prx_graph_pool_stats", "prx_l2_fetch_granularity", "prx_graph_size", "prx_graph_class_stats",
     "prx_graph_download",
     "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_selftest_division",
     "prx_solve_ppr_batched", "prx_solve_ppr_batched_device", "prx_graph_set_weights", "prx_solve_weighted",
@@ -119,6 +119,7 @@ def load(build_if_missing=True):
         "prx_graph_destroy": (i32, [vp]),
         "prx_release_cached_memory": (i32, [i32]),
         "prx_l2_fetch_granularity": (i32, [i32, i32, C.POINTER(i32)]),
+        "prx_graph_pool_stats": (i32, [i32, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
         "prx_graph_size": (i32, [vp, C.POINTER(C.c_uint32), C.POINTER(u64)]),
         "prx_graph_class_stats": (i32, [vp, C.POINTER(C.c_uint32), C.POINTER(u64)]),
         "prx_graph_download": (i32, [vp, vp, vp, vp, vp, vp]),

@@ -294,6 +294,13 @@ def release_cached_memory(device=0):
     check(load().prx_release_cached_memory(int(device)), "prx_release_cached_memory")
 
 
+def graph_pool_stats(device=0):
+    """prx_graph_pool_stats -> dict of the graph pool's reserved / used bytes (now and peak)."""
+    v = [C.c_uint64() for _ in range(4)]
+    check(load().prx_graph_pool_stats(int(device), *(C.byref(x) for x in v)), "prx_graph_pool_stats")
+    return dict(zip(("reserved", "reserved_peak", "used", "used_peak"), (x.value for x in v)))
+
+
 def l2_fetch_granularity(bytes_=None, device=0):
     """prx_l2_fetch_granularity: the previous L2 fetch granularity hint of this
     process on `device`; sets it to bytes_ (0..128) when given."""

@@ -384,9 +384,15 @@ def test_graph_pool_reuse_and_release(pg, ctx):
     xt = O.transpose(xoff, xedg)
     want, it = O.solve("static", None, None, *xt)
     for k in range(3):
+        s0 = pg.graph_pool_stats()
         g = pg.Graph(ctx, *xt, xoff, xedg)
+        s1 = pg.graph_pool_stats()
+        assert s1["used"] >= s0["used"] + 8 * len(xedg) and s1["reserved"] >= s1["used"]
+        assert s1["reserved_peak"] >= s1["reserved"] and s1["used_peak"] >= s1["used"]
         r, res = pg.pagerank_static(ctx, g, pg.options(chunk_vertices=4096))
         assert res["iterations"] == it and np.array_equal(r, want)
         g.close()
+        assert pg.graph_pool_stats()["used"] <= s1["used"] - 8 * len(xedg)
         if k == 1:
             pg.release_cached_memory(0)
+            assert pg.graph_pool_stats()["reserved"] <= s1["reserved"]
