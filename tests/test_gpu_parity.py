@@ -392,7 +392,8 @@ def test_graph_pool_reuse_and_release(pg, ctx):
         r, res = pg.pagerank_static(ctx, g, pg.options(chunk_vertices=4096))
         assert res["iterations"] == it and np.array_equal(r, want)
         g.close()
-        assert pg.graph_pool_stats()["used"] <= s1["used"] - 8 * len(xedg)
+        if k:  # (the first solve may add the context's own pool buffers)
+            assert pg.graph_pool_stats()["used"] == s0["used"]
         if k == 1:
             pg.release_cached_memory(0)
             assert pg.graph_pool_stats()["reserved"] <= s1["reserved"]
