@@ -879,11 +879,7 @@ int prx_graph_destroy(prx_graph* gr) {
   if (!gr) return PRX_OK;
   cudaSetDevice(gr->g.device);
   GraphDev& g = gr->g;
-  cudaFree(g.xoff); cudaFree(g.xedg); cudaFree(g.xtoff); cudaFree(g.xtedg); cudaFree(g.xtdat); cudaFree(g.cls_list);
-  cudaFree(g.xbase); cudaFree(g.xtbase);
-  cudaFree(g.low_bm);
-  cudaFree(g.rcp);
-  cudaFree(g.rcp32);
+  graph_free({g.xoff, g.xedg, g.xtoff, g.xtedg, g.xtdat, g.cls_list, g.xbase, g.xtbase, g.low_bm, g.rcp, g.rcp32});
   drop_weights(g);
   cudaFree(g.ocls_list);
   free_chunks(g);

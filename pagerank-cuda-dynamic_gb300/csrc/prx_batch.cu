@@ -267,7 +267,7 @@ cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd64, ui
   k_out_degree<<<grid, kThreads, 0, s>>>(noff, n, ndat);
   PRX_CU(cudaGetLastError());
   PRX_CU(cudaStreamSynchronize(s));
-  cudaFree(g.xoff); cudaFree(g.xedg); cudaFree(g.xtoff); cudaFree(g.xtedg); cudaFree(g.xtdat);
+  graph_free({g.xoff, g.xedg, g.xtoff, g.xtedg, g.xtdat});
   g.xoff = noff; g.xedg = nedg; g.xtoff = ntoff; g.xtedg = ntedg; g.xtdat = ndat;
   noff = nedg = ntoff = ntedg = ndat = nullptr;
   g.m = m2;
@@ -276,11 +276,7 @@ cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd64, ui
 done:
   if (scratch) cudaFreeAsync(scratch, s);
   if (ranges) cudaFreeAsync(ranges, s);
-  if (noff) cudaFree(noff);
-  if (ntoff) cudaFree(ntoff);
-  if (nedg) cudaFree(nedg);
-  if (ntedg) cudaFree(ntedg);
-  if (ndat) cudaFree(ndat);
+  graph_free({noff, ntoff, nedg, ntedg, ndat});
   return err;
 }
 

@@ -52,6 +52,17 @@ cudaError_t graph_alloc(void** p, size_t bytes, cudaStream_t s) {
   return e;
 }
 
+void graph_free(std::initializer_list<void*> ps) {
+  bool any = false;
+  for (void* p : ps) any = any || p;
+  if (!any) return;
+  cudaDeviceSynchronize();
+  for (void* p : ps)
+    if (p) cudaFreeAsync(p, cudaStreamLegacy);
+  // the blocks are free before the next allocation on any stream looks
+  cudaStreamSynchronize(cudaStreamLegacy);
+}
+
 cudaError_t graph_pool_trim(int dev) {
   cudaMemPool_t pool = nullptr;
   {
@@ -235,7 +246,7 @@ cudaError_t selftest_division(uint32_t dmax, uint32_t per, unsigned long long* b
     e = cudaMemcpyAsync(bad_host, bad, sizeof(*bad), cudaMemcpyDeviceToHost, s);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  cudaFree(bad);
+  graph_free({bad});
   return e;
 }
 
@@ -358,10 +369,9 @@ __global__ void __launch_bounds__(256) k_chunk_scatter_w(const uint32_t* __restr
 }
 
 static void free_layout(ChunkLayout& l) {
-  cudaFree(l.off);
-  cudaFree(l.edg);
-  for (auto p : l.seg_off) cudaFree(p);
-  for (auto p : l.seg_edg) cudaFree(p);
+  graph_free({l.off, l.edg});
+  for (auto p : l.seg_off) graph_free({p});
+  for (auto p : l.seg_edg) graph_free({p});
   l = ChunkLayout();
 }
 

@@ -3,6 +3,7 @@
 #pragma once
 #include <cstdint>
 #include <cstddef>
+#include <initializer_list>
 #include <string>
 #include <vector>
 #include <cuda_runtime.h>
@@ -251,12 +252,17 @@ cudaError_t batch_by_target(const uint32_t* u, const uint32_t* v, uint32_t count
 // Graph arrays come from a stream-ordered pool of this library that keeps
 // freed memory (release threshold: unlimited), so a graph built after another
 // one was destroyed reuses its pages instead of mapping new ones.  Allocated
-// on stream s and usable there at once; cudaFree returns them to the pool.
+// on stream s and usable there at once; returned by cudaFreeAsync on a
+// stream or by graph_free.
 cudaError_t graph_alloc(void** p, size_t bytes, cudaStream_t s);
 template <class T>
 cudaError_t graph_alloc(T** p, size_t bytes, cudaStream_t s) {
   return graph_alloc(reinterpret_cast<void**>(p), bytes, s);
 }
+// Returns pool blocks (NULLs skipped) once all work queued on the device has
+// finished, like cudaFree; cudaFree itself would leave the pool counting the
+// blocks as in use.
+void graph_free(std::initializer_list<void*> ps);
 // Give the pool's free memory on device dev back to the driver.
 cudaError_t graph_pool_trim(int dev);
 // Bytes the pool holds from the driver and bytes handed out, now and at peak.

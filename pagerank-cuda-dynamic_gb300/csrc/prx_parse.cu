@@ -228,20 +228,17 @@ struct DevEdges {
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(nv, v, 4 * n, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
-      cudaFree(nu);
-      cudaFree(nv);
+      graph_free({nu, nv});
       return e;
     }
-    cudaFree(u);
-    cudaFree(v);
+    graph_free({u, v});
     u = nu;
     v = nv;
     cap = nc;
     return cudaSuccess;
   }
   void release() {
-    cudaFree(u);
-    cudaFree(v);
+    graph_free({u, v});
     u = v = nullptr;
     n = cap = 0;
   }
@@ -254,11 +251,7 @@ struct ParseBufs {
   uint32_t* nl = nullptr;
   uint64_t nl_cap = 0;
   unsigned long long* word = nullptr;  // [0] fail, [1] bad, [2] newline position
-  ~ParseBufs() {
-    cudaFree(text);
-    cudaFree(nl);
-    cudaFree(word);
-  }
+  ~ParseBufs() { graph_free({text, nl, word}); }
 };
 
 int parse_fail(cudaError_t e) {
@@ -285,7 +278,7 @@ int parse_chunk(prx_context* c, ParseBufs& B, const char* chunk, uint64_t bytes,
   const uint64_t padded = blocks64 * kParseBlock;
   cudaError_t e = cudaSuccess;
   if (B.text_cap < padded) {
-    cudaFree(B.text);
+    graph_free({B.text});
     B.text = nullptr;
     B.text_cap = 0;
     e = graph_alloc(&B.text, padded, s);
@@ -293,7 +286,7 @@ int parse_chunk(prx_context* c, ParseBufs& B, const char* chunk, uint64_t bytes,
     B.text_cap = padded;
   }
   if (B.nl_cap < blocks64 + 1) {
-    cudaFree(B.nl);
+    graph_free({B.nl});
     B.nl = nullptr;
     B.nl_cap = 0;
     e = graph_alloc(&B.nl, 4 * (blocks64 + 1), s);

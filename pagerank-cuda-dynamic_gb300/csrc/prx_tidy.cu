@@ -464,9 +464,7 @@ __global__ void k_gen_insertions(uint32_t n, uint64_t seed, uint32_t count, uint
 struct TidyBufs {
   uint32_t *u = nullptr, *v = nullptr, *flag = nullptr, *pos = nullptr, *hist = nullptr;
   unsigned long long *key = nullptr, *key2 = nullptr;
-  void release() {
-    cudaFree(u); cudaFree(v); cudaFree(flag); cudaFree(pos); cudaFree(hist); cudaFree(key); cudaFree(key2);
-  }
+  void release() { graph_free({u, v, flag, pos, hist, key, key2}); }
 };
 
 // Tidy one list (deletions or insertions) of `count` edges already in b.u /
@@ -580,8 +578,7 @@ static int create_from_edges(prx_context* c, uint32_t n, const uint32_t* u, cons
   auto release = [&]() {
     b.release();
     b = TidyBufs();
-    cudaFree(key3);
-    cudaFree(bad);
+    graph_free({key3, bad});
     key3 = nullptr;
     bad = nullptr;
   };
