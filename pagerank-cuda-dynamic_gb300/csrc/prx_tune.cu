@@ -99,10 +99,10 @@ cudaError_t prx::tune_apply_cached(GraphDev& g, int sms, cudaStream_t s) {
   g.tuned_w32 = p.w32;
   g.tuned_fetch = p.fetch;
   if (p.mid_max == g.mid_max) return cudaSuccess;
+  // only the MID / HIGH lists depend on the boundary (not the LOW bitmap,
+  // the reciprocals or source chunks, which a new graph does not have yet)
   g.mid_max = p.mid_max;
-  cudaError_t e = build_classes(g, sms, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  return e;
+  return build_class_lists(g.xtoff, g.seg_shift, g.n, g.mid_max, g.cls_list, g.cls_begin, g.cls_edges, sms, s);
 }
 
 extern "C" {
