@@ -793,7 +793,8 @@ def run_ours(args):
                        "ms_per_step": e2e_ms_max, "steps_ms": e2e_ms, "parts": e2e_parts,
                        "h2d_only_ms": h2d_only_ms},
                "roofline": roofline, "clocks": clk.summary(), "fp32_refine": fp32, "dfp": dfp,
-               "dynamic": dynamic, "autotune": tune, "offsets64": big, "ingest": ingest, "grid": grid, "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
+               "dynamic": dynamic, "autotune": tune, "offsets64": big, "ingest": ingest, "grid": grid, "ppr": ppr,
+               "adjoint": adj, "cpu_baseline": cpu}
         print(json.dumps(out), flush=True)
     g.close()
     ctx.close()

@@ -41,7 +41,10 @@ typedef enum {
   PRX_ECUDA = 3,     /* a CUDA call failed (see prx_last_error())         */
   PRX_ETIMEOUT = 4,  /* a bounded device-side wait gave up               */
   PRX_ERANGE = 5,    /* size beyond a documented limit                   */
-  PRX_ESTATE = 6     /* call not valid for this object (e.g. no out-CSR) */
+  PRX_ESTATE = 6,    /* call not valid for this object (e.g. no out-CSR) */
+  PRX_ENOCONV = 7    /* iteration cap reached before the L-inf test passed,
+                        reported only with prx_options.require_convergence;
+                        ranks and result are still written              */
 } prx_status;
 
 /* The reference's five solvers (inc/pagerankCuda.hxx:864-988). */
@@ -116,6 +119,12 @@ typedef struct {
                                  The process's setting is put back before
                                  the call returns; results do not depend on
                                  it [0]                                     */
+  int    require_convergence; /* 1: a solve that stops at max_iterations
+                                 with its last L-inf change not below the
+                                 tolerance returns PRX_ENOCONV (after
+                                 writing ranks and result); 0: PRX_OK, as
+                                 the reference returns its ranks either
+                                 way [0]                                    */
 } prx_options;
 
 /* PagerankResult<V> (inc/pagerank.hxx:64-113) minus the rank vector, which

@@ -40,6 +40,7 @@ void prx_options_default(prx_options* o) {
   o->chunk_vertices = 0;
   o->refine_sweeps = 0;
   o->l2_fetch_bytes = 0;
+  o->require_convergence = 0;
 }
 
 const char* prx_status_string(int s) {
@@ -51,6 +52,7 @@ const char* prx_status_string(int s) {
     case PRX_ETIMEOUT: return "device wait timed out";
     case PRX_ERANGE: return "size out of range";
     case PRX_ESTATE: return "invalid state";
+    case PRX_ENOCONV: return "did not converge";
     default: return "unknown status";
   }
 }
@@ -995,7 +997,9 @@ static int solve_common(prx_context* c, prx_graph* gr, int mode, const uint32_t*
   if (opt.l2_fetch_bytes < -1 || opt.l2_fetch_bytes > 128)
     FAIL(PRX_EINVAL, "prx_solve: l2_fetch_bytes must be in -1 .. 128");
   if (!ranks_out && gr->g.n) FAIL(PRX_EINVAL, "prx_solve: ranks_out is NULL");
-  if (res) std::memset(res, 0, sizeof(*res));
+  prx_result own;
+  if (!res) res = &own;  // the convergence check reads it
+  std::memset(res, 0, sizeof(*res));
   const GraphDev& g = gr->g;
   if (g.n == 0) return PRX_OK;  // empty graph: the reference returns {} (:869)
   const bool dyn = mode >= PRX_DYNAMIC_TRAVERSAL;
@@ -1038,6 +1042,8 @@ static int solve_common(prx_context* c, prx_graph* gr, int mode, const uint32_t*
   TRY_CUDA_ST(cudaMemcpyAsync(ranks_out, fr, sizeof(double) * g.n,
                               host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, c->stream));
   TRY_CUDA_ST(cudaStreamSynchronize(c->stream));
+  if (opt.require_convergence && !(res->last_delta < opt.tolerance))
+    FAIL(PRX_ENOCONV, "prx_solve: the iteration cap was reached before the L-inf test passed");
   return PRX_OK;
 }
 

@@ -14,7 +14,7 @@ FP64, FP32_REFINE = 0, 1
 LOOP_AUTO, LOOP_HOST, LOOP_GRAPH = 0, 1, 2
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "device wait timed out",
-          5: "size out of range", 6: "invalid state"}
+          5: "size out of range", 6: "invalid state", 7: "did not converge"}
 
 
 class Options(C.Structure):
@@ -23,7 +23,7 @@ class Options(C.Structure):
                 ("prune_tolerance", C.c_double), ("damping", C.c_double), ("max_iterations", C.c_int),
                 ("precision", C.c_int), ("loop", C.c_int), ("partition", C.c_int), ("timing", C.c_int),
                 ("expansion", C.c_int), ("chunk_vertices", C.c_uint32), ("refine_sweeps", C.c_int),
-                ("l2_fetch_bytes", C.c_int)]
+                ("l2_fetch_bytes", C.c_int), ("require_convergence", C.c_int)]
 
 
 class Result(C.Structure):
@@ -76,7 +76,8 @@ _lib = None
 EXPORTS = (
     "prx_options_default", "prx_status_string", "prx_last_error", "prx_context_create", "prx_context_destroy",
     "prx_context_stream", "prx_graph_create", "prx_graph_create64", "prx_graph_download64", "prx_graph_destroy",
-    "prx_release_cached_memory", "prx_graph_pool_stats", "prx_l2_fetch_granularity", "prx_graph_size", "prx_graph_class_stats",
+    "prx_release_cached_memory", "prx_graph_pool_stats", "prx_l2_fetch_granularity", "prx_graph_size",
+    "prx_graph_class_stats",
     "prx_graph_download",
     "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_selftest_division",
     "prx_solve_ppr_batched", "prx_solve_ppr_batched_device", "prx_graph_set_weights", "prx_solve_weighted",

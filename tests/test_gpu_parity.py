@@ -293,6 +293,24 @@ def test_autotune_keeps_results_and_caches(pg, ctx, tmp_path):
     g.close()
 
 
+def test_require_convergence_reports_the_cap(pg, ctx):
+    # opt-in PRX_ENOCONV: a solve cut by the iteration cap says so; one that
+    # converges returns as without the flag
+    xoff, xedg = _synthetic(pg, "hubs")
+    xt = O.transpose(xoff, xedg)
+    g, _ = _graph(pg, ctx, xoff, xedg, xt)
+    want, it = O.solve("static", None, None, *xt)
+    assert it > 3
+    got, res = pg.pagerank_static(ctx, g, opts=pg.options(require_convergence=1))
+    assert res["iterations"] == it and np.array_equal(got, want) and res["last_delta"] < 1e-10
+    with pytest.raises(pg.PrxError) as e:
+        pg.pagerank_static(ctx, g, opts=pg.options(require_convergence=1, max_iterations=3))
+    assert e.value.status == 7
+    _, res3 = pg.pagerank_static(ctx, g, opts=pg.options(max_iterations=3))
+    assert res3["iterations"] == 3 and res3["last_delta"] >= 1e-10
+    g.close()
+
+
 def test_l2_fetch_granularity_is_restored_and_changes_nothing(pg, ctx):
     # the solve sets the hint for its own duration only; every granularity
     # gives the oracle's ranks bit for bit

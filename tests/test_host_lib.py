@@ -103,3 +103,11 @@ def test_random_batch_is_tidy(pg):
     y2 = O.apply_batch(off, edg, du, dv, iu, iv)
     np.testing.assert_array_equal(yoff, y2[0])
     np.testing.assert_array_equal(yedg, y2[1])
+
+
+def test_status_strings(pg):
+    from pagerank_gb300 import _lib
+    lib = pg.load()
+    for code, text in _lib.STATUS.items():
+        assert lib.prx_status_string(code).decode() == text
+    assert lib.prx_status_string(99).decode() == "unknown status"
