@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-dfp", action="store_true")
     p.add_argument("--no-fp32", action="store_true")
-    p.add_argument("--e2e-steps", type=int, default=7)
+    p.add_argument("--e2e-steps", type=int, default=9)
     p.add_argument("--static-only", action="store_true", help="upload only the in-CSR; skip DF-P and the CPU leg")
     p.add_argument("--chunk", type=int, default=0, help="source-chunk width of the gathers (0: library default)")
     p.add_argument("--loop", default="auto", choices=("auto", "host"),
