@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--seed", type=int, default=42)
     p.add_argument("--cpu-sweeps", type=int, default=3, help="sweeps in the bounded CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-cpu-dfp", dest="cpu_dfp", action="store_false",
+                   help="skip the reference's CPU DF-P timed beside the GPU DF-P")
     p.add_argument("--no-dfp", action="store_true")
     p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--e2e-steps", type=int, default=9)
@@ -74,9 +76,13 @@ def parse():
     p.add_argument("--no-offsets64", action="store_true",
                    help="skip the 64-bit-offset graph (four copies of the bench graph, 4x its edges)")
     p.add_argument("--ingest-steps", type=int, default=2)
+    p.add_argument("--detail-out", default=None,
+                   help="also write the detail record (every section) to this file; it always goes to stderr")
     a = p.parse_args()
     if a.static_only:
         a.no_dfp = a.no_cpu = True
+    if a.no_cpu:
+        a.cpu_dfp = False
     return a
 
 
@@ -233,16 +239,99 @@ def cpu_baseline(args, xt, m):
                       f"same graph, {ms / 1e3:.1f}s"}
 
 
+def product_library_mapped():
+    """True when the product's shared library is mapped into this process."""
+    try:
+        with open("/proc/self/maps") as f:
+            return "libpagerank_gb300" in f.read()
+    except OSError:
+        return False
+
+
+def compact(x, digits=5):
+    """x with every float rounded to `digits` significant digits (keeps the
+    stdout line short)."""
+    if isinstance(x, float):
+        return float(f"{x:.{digits}g}")
+    if isinstance(x, dict):
+        return {k: compact(v, digits) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [compact(v, digits) for v in x]
+    return x
+
+
+def summarize(fp32, dfp, dynamic, grid, ppr, adj, big, ingest, tune):
+    """A few scalars per section for the stdout line (the full sections go to
+    the detail record)."""
+    def pick(d, *keys):
+        return None if d is None else {k: d.get(k) for k in keys if k in d}
+    out = {}
+    if fp32:
+        out["fp32_refine"] = pick(fp32, "ms_per_solve", "speedup_vs_fp64", "linf_vs_fp64", "fp32_sweep_ms",
+                                  "fp32_low_gbs", "fp32_low_frac")
+    if dfp:
+        out["dfp_after_1e-4"] = pick(dfp, "dfp_ms", "df_ms", "static_ms", "dfp_speedup_vs_static",
+                                     "df_speedup_vs_static", "dfp_fp32_refine_ms",
+                                     "dfp_fp32_refine_speedup_vs_dfp_fp64", "dfp_fp32_refine_speedup_vs_static",
+                                     "dfp_fp32_refine_linf_vs_dfp_fp64", "cpu_dfp_ms", "cpu_dfp_iterations",
+                                     "cpu_dfp_threads", "gpu_dfp_vs_cpu_dfp")
+    if dynamic:
+        out["dynamic_median_speedup_vs_static"] = dynamic["median_speedup_vs_static"]
+        out["tidy_1e-3_call_ms"] = dynamic["tidy"]["call_ms"]
+    if grid:
+        out["grid4096"] = {"static_ms": grid["static_ms"], "static_ge_s": grid["static_ge_s"],
+                           **{f"{k}_speedup_vs_static": grid[k]["speedup_vs_static"] for k in ("dt", "df", "dfp")
+                              if k in grid}}
+    if ppr:
+        out["ppr_rmat22_x64"] = {"fp64_ms": ppr["fp64"]["time_ms"], "fp32_refine_ms": ppr["fp32_refine"]["time_ms"],
+                                 "speedup": ppr["speedup_fp32_refine_vs_fp64"],
+                                 "graph_launches": ppr["fp32_refine"].get("graph_launches"),
+                                 "linf_fp32_refine_vs_fp64": ppr["linf_fp32_refine_vs_fp64"]}
+    if adj:
+        out["adjoint_rmat20"] = {"fd_max_rel_err": adj["fd_max_rel_err"], "fd_edges": sum(r["fd_edges"] for r in
+                                                                                      adj["rounds"]),
+                                 "batches": len(adj["rounds"]) - 1,
+                                 "adjoint_ms": adj["rounds"][0]["adjoint_ms"]}
+    if big:
+        out["offsets64_7.6B"] = pick(big, "ge_s", "copy_ranks_exactly_quarter_of_single")
+    if ingest:
+        out["ingest_1.9B_ms"] = statistics.median(ingest["device_ms"])
+    if tune:
+        out["autotune_s"] = tune.get("seconds")
+    return out
+
+
+def cpu_dfp_baseline(before, after, batch, q):
+    """The reference's CPU DF-P (asynchronous, OpenMP: the port of
+    pagerankPruneDynamicFrontierOmp, inc/pagerankPrune.hxx:306, as main.cu:123
+    runs it) on one batch: `before` = (xoff, xedg) of the graph before it,
+    `after` = the downloaded graph after it (out-CSR, in-CSR, out-degrees),
+    q = the ranks before it.  Timed on the host with all its threads."""
+    from oracle import pyoracle as O
+    threads = os.cpu_count() or 1
+    (r, it), ms = host_ms(lambda: O.cpu_prune_dynamic_frontier(*before, *after, batch[0], batch[2], q,
+                                                               threads=threads))
+    return {"ms": ms, "iterations": it, "threads": threads,
+            "sample": "one 1e-4|E| batch, the same graph and ranks as the GPU DF-P beside it"}
+
+
 def run_reference(args):
     """Reference arm: the reference's CPU Static PageRank (OpenMP port of
     pagerankStaticOmp; the reference's own binary cannot be built on this
-    aarch64 host) on the same graph, bounded sweeps per step."""
+    aarch64 host) on the same graph, bounded sweeps per step.  The graph comes
+    from the oracle's generator (the same arrays as the product generator),
+    so this arm never loads the product library."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if int(os.environ.get("RANK", "0")) != 0:
         return
-    import pagerank_gb300 as pg
     from oracle import pyoracle as O
-    xoff, xedg, xt = make_graph(args, pg)
+    t = time.perf_counter()
+    xoff, xedg = O.gen_weblike(args.vertices, alpha=2.1, dmin=args.dmin, dmax=100000, local=0.7, window=4096,
+                               seed=args.seed)
+    t1 = time.perf_counter()
+    xt = O.transpose(xoff, xedg, threads=True)
+    log(f"graph (oracle generator): n={len(xoff) - 1} m={len(xedg)} generated in {t1 - t:.1f}s, transposed in "
+        f"{time.perf_counter() - t1:.1f}s")
     m = len(xedg)
     threads = os.cpu_count() or 1
     per_step = 1
@@ -262,6 +351,8 @@ def run_reference(args):
                             "sample": f"{per_step} synchronous sweep of pagerankStaticOmp per step, "
                                       f"{threads} OpenMP threads"},
            "e2e": {"value": v, "unit": "GE/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if product_library_mapped():
+        raise RuntimeError("the reference arm mapped the product library")
     print(json.dumps(out), flush=True)
 
 
@@ -295,12 +386,17 @@ def run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m):
     out = torch.empty_like(q)
     rows = []
     od = oi = 0
+    cpu_dfp = None
     for sz, cnt in parts:
         kd = np.sort(pd[od:od + cnt // 5])
         ki = np.sort(pi[oi:oi + cnt - cnt // 5])
         od += cnt // 5
         oi += cnt - cnt // 5
         b = (du[kd], dv[kd], iu[ki], iv[ki])
+        # the reference's CPU DF-P (OpenMP port of pagerankPruneDynamicFrontierOmp)
+        # on the first 1e-4 batch: the graph before and after it, downloaded
+        cpu_leg = args.cpu_dfp and sz == 1e-4 and cpu_dfp is None
+        before = g.download()[:2] if cpu_leg else None
         _, apply_ms = host_ms(lambda: g.apply_batch(*b))
         bt = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint32).view(np.int32)).to(dev) for a in b]
         bp = (bt[0].data_ptr(), bt[1].data_ptr(), len(kd), bt[2].data_ptr(), bt[3].data_ptr(), len(ki))
@@ -325,6 +421,11 @@ def run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m):
             if name == "dfp_fp32_refine":
                 row[name]["linf_vs_dfp_fp64"] = float((out - out64).abs().max())
                 row[name]["speedup_vs_dfp_fp64"] = row["dfp"]["ms"] / r["time_ms"]
+        if cpu_leg:
+            cpu_dfp = cpu_dfp_baseline(before, g.download(), b, q.cpu().numpy())
+            cpu_dfp["gpu_dfp_ms"] = row["dfp"]["ms"]
+            del before
+            log(f"cpu dfp: {cpu_dfp}")
         rows.append(row)
         log(f"batch {sz:g}: " + ", ".join(f"{k} {row[k]['ms']:.1f} ms" for k in
                                           ("static", "nd", "dt", "df", "dfp", "dfp_fp32_refine")))
@@ -346,7 +447,10 @@ def run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m):
            "dfp_fp32_refine_speedup_vs_dfp_fp64": d32["speedup_vs_dfp_fp64"],
            "dfp_fp32_refine_speedup_vs_static": d32["speedup_vs_static"],
            "dfp_fp32_refine_linf_vs_dfp_fp64": d32["linf_vs_dfp_fp64"]}
-    return {"batches": rows, "median_speedup_vs_static": summary, "tidy": tidy}, dfp
+    if cpu_dfp:
+        dfp.update({"cpu_dfp_ms": cpu_dfp["ms"], "cpu_dfp_iterations": cpu_dfp["iterations"],
+                    "cpu_dfp_threads": cpu_dfp["threads"], "gpu_dfp_vs_cpu_dfp": cpu_dfp["ms"] / d["ms"]})
+    return {"batches": rows, "median_speedup_vs_static": summary, "tidy": tidy, "cpu_dfp": cpu_dfp}, dfp
 
 
 def run_grid(args, pg, ctx, local):
@@ -712,6 +816,8 @@ def run_ours(args):
                 "fp64_sweeps_ms": sum(u64), "fp32_sweep_ms": sum(u32) / max(n_fp32_sweeps, 1),
                 "fp32_low_gbs": (12 * cls_v[0] + 8 * cls_e[0]) * n_fp32_sweeps / (u32[0] / 1e3) / 1e9
                 if u32[0] else None}
+        if fp32["fp32_low_gbs"]:
+            fp32["fp32_low_frac"] = fp32["fp32_low_gbs"] / measured_peak()[0]
         log(f"fp32-refine: {fp32}")
 
     # ---- end to end through the C ABI from pinned host buffers ----------------
@@ -782,20 +888,34 @@ def run_ours(args):
         cpu = cpu_baseline(args, xt, m)
         log(f"cpu: {cpu}")
     if rank == 0:
+        detail = {"iterations": iters, "roofline": roofline, "e2e_steps_ms": e2e_ms, "e2e_parts": e2e_parts,
+                  "h2d_only_ms": h2d_only_ms, "fp32_refine": fp32, "dfp": dfp, "dynamic": dynamic, "autotune": tune,
+                  "offsets64": big, "ingest": ingest, "grid": grid, "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
+        text = json.dumps(detail)
+        log("detail: " + text)
+        if args.detail_out:
+            os.makedirs(os.path.dirname(os.path.abspath(args.detail_out)), exist_ok=True)
+            with open(args.detail_out, "w") as f:
+                f.write(text + "\n")
+        keep = ("bound", "kernel", "achieved", "peak", "unit", "frac", "traffic", "peak_source",
+                "alg_bytes_per_sweep", "sweep_ms", "launches_per_sweep", "share_of_step")
         out = {"metric": METRIC, "value": value, "unit": "GE/s", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator, host)",
                "config": {"workload": WORKLOAD, "vertices": n, "edges": m, "alpha": 0.85, "tolerance": 1e-10,
                           "max_iterations": 500, "parallelism": f"replicas{ws}",
                           "l2": "inputs larger than L2 (7.6 GB in-CSR per sweep)"},
-               "iterations": iters, "gpu_launches": launches,
+               "iterations_per_step": statistics.median(iters), "gpu_launches": launches,
                "e2e": {"value": e2e_value, "unit": "GE/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                       "ms_per_step": e2e_ms_max, "steps_ms": e2e_ms, "parts": e2e_parts,
-                       "h2d_only_ms": h2d_only_ms},
-               "roofline": roofline, "clocks": clk.summary(), "fp32_refine": fp32, "dfp": dfp,
-               "dynamic": dynamic, "autotune": tune, "offsets64": big, "ingest": ingest, "grid": grid, "ppr": ppr,
-               "adjoint": adj, "cpu_baseline": cpu}
-        print(json.dumps(out), flush=True)
+                       "ms_per_step": e2e_ms_max, "steps": len(e2e_ms), "statistic": "median step"},
+               "roofline": {k: roofline[k] for k in keep if k in roofline},
+               "clocks": clk.summary(), "cpu_baseline": cpu,
+               "summary": summarize(fp32, dfp, dynamic, grid, ppr, adj, big, ingest, tune),
+               "detail": args.detail_out or "stderr"}
+        line = json.dumps(compact(out))
+        if len(line) > 4096:
+            log(f"bench line is {len(line)} bytes")
+        print(line, flush=True)
     g.close()
     ctx.close()
     if ws > 1:
@@ -805,11 +925,13 @@ def run_ours(args):
 
 def main():
     args = parse()
-    import __graft_entry__
-    __graft_entry__.build()
     if args.impl == "reference":
+        from oracle import pyoracle as O
+        O.build()
         run_reference(args)
     else:
+        import __graft_entry__
+        __graft_entry__.build()
         run_ours(args)
 
 

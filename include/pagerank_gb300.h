@@ -402,8 +402,15 @@ int prx_selftest_division(prx_context* ctx, uint32_t dmax, uint32_t per, unsigne
  * sized for PRX_NOALLOC_MAX_VERTICES vertices (24 MiB per GPU that uses the
  * call, held until the process exits); larger n returns PRX_ERANGE.  All
  * calls share that array, so calls that overlap on the GPU race and must be
- * ordered by the caller.  The first call on a device looks up the array's
- * device address with that device current.  Returns after the solve
+ * ordered by the caller.  Every call looks the array's device address up
+ * in the calling thread's current context (no allocation); the first call in
+ * a context is where the CUDA loader places the array, so make it before any
+ * stream capture.  Preconditions, as prx_graph_create checks them for the
+ * regular path: xtoff[0] = 0, xtoff non-decreasing, xtoff[n] = m, every
+ * xtedg id < n, every xtdat >= 1 (each vertex's out-degree, its self-loop
+ * included).  A first or last offset that breaks them is caught on the
+ * device before any sweep and returns PRX_EINVAL; the rest is the caller's
+ * promise (a bad id reads out of bounds).  Returns after the solve
  * finished. */
 #define PRX_NOALLOC_MAX_VERTICES 1048576u
 int prx_static_solve_noalloc(uint32_t n, uint64_t m,

@@ -72,9 +72,14 @@ static double contrib_sum_gpu(const uint32_t* xtoff, const uint32_t* xtedg,
  * pagerankMarkNeighborsCudU :55-63). */
 static void expand_marks(uint32_t n, const uint32_t* xoff, const uint32_t* xedg,
                          const uint8_t* naff, uint8_t* vaff) {
-  for (uint32_t u = 0; u < n; ++u) {
+  /* threads only store 1s, so the result is independent of their order */
+  #pragma omp parallel for schedule(dynamic, 4096)
+  for (int64_t u = 0; u < (int64_t)n; ++u) {
     if (!naff[u]) continue;
-    for (uint64_t i = xoff[u]; i < xoff[u + 1]; ++i) vaff[xedg[i]] = 1;
+    for (uint64_t i = xoff[u]; i < xoff[u + 1]; ++i) {
+      #pragma omp atomic write
+      vaff[xedg[i]] = 1;
+    }
   }
 }
 
@@ -103,24 +108,25 @@ void orc_mark_traversal(uint32_t n, const uint32_t* xoff, const uint32_t* xedg,
                         const uint32_t* insu, uint64_t ni, uint8_t* vaff) {
   /* pagerankAffectedTraversalCuW, inc/pagerankCuda.hxx:438-456: start from the
    * DF marking, then repeatedly expand the whole last expansion (naff <- buff)
-   * and OR it into vaff until the count of vaff stops changing. */
-  uint8_t* naff = (uint8_t*)calloc(n ? n : 1, 1);
-  uint8_t* buff = (uint8_t*)calloc(n ? n : 1, 1);
+   * and OR it into vaff until the count of vaff stops changing.  Level k's
+   * expansion is the set of vertices k out-steps from the DF marking, and once
+   * a level adds nothing every later level lies inside vaff too, so the loop
+   * ends with every vertex reachable from the DF marking.  That set is formed
+   * here by one breadth-first search (O(n + m) instead of a scan of all n
+   * flags per level, which on a 4096 x 4096 grid means thousands of levels). */
   orc_mark_frontier(n, xoff, xedg, delu, delv, nd, insu, ni, vaff);
-  memcpy(naff, vaff, n);
-  uint64_t count = 0;
-  for (uint32_t v = 0; v < n; ++v) count += vaff[v];
-  for (;;) {
-    memset(buff, 0, n);
-    expand_marks(n, xoff, xedg, naff, buff);
-    uint64_t c2 = 0;
-    for (uint32_t v = 0; v < n; ++v) { vaff[v] |= buff[v]; c2 += vaff[v]; }
-    uint8_t* t = naff; naff = buff; buff = t;
-    if (c2 == count) break;
-    count = c2;
+  uint32_t* queue = (uint32_t*)malloc(sizeof(uint32_t) * (n ? n : 1));
+  uint64_t head = 0, tail = 0;
+  for (uint32_t v = 0; v < n; ++v)
+    if (vaff[v]) queue[tail++] = v;
+  while (head < tail) {
+    const uint32_t u = queue[head++];
+    for (uint64_t i = xoff[u]; i < xoff[u + 1]; ++i) {
+      const uint32_t w = xedg[i];
+      if (!vaff[w]) { vaff[w] = 1; queue[tail++] = w; }
+    }
   }
-  free(naff);
-  free(buff);
+  free(queue);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -150,7 +156,8 @@ int orc_solve(int mode, uint32_t n, uint64_t m,
   /* Initial ranks: previous ranks if given, else 1/N
    * (inc/pagerankCuda.hxx:810,817-818, pagerankInitializeRanksCukW :232-239). */
   const int use_q = q && mode != ORC_STATIC;
-  for (uint32_t v = 0; v < n; ++v) r[v] = a[v] = use_q ? q[v] : 1.0 / (double)n;
+  #pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v < (int64_t)n; ++v) r[v] = a[v] = use_q ? q[v] : 1.0 / (double)n;
   /* Initial marking, only when the batch is non-empty (:927,956,985).  With an
    * empty batch the reference leaves vaff uninitialised; here it is all-zero. */
   if (DYNAMIC && (nd > 0 || ni > 0)) {
@@ -163,7 +170,10 @@ int orc_solve(int mode, uint32_t n, uint64_t m,
   int l = 0;
   while (l < L) {
     if (FRONTIER) memset(naff, 0, n);
-    for (uint32_t v = 0; v < n; ++v) {
+    /* vertices are independent within a sweep (each writes only its own
+     * a[v], vaff[v], naff[v]), so threads do not change any result */
+    #pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t v = 0; v < (int64_t)n; ++v) {
       if (DYNAMIC && !vaff[v]) { a[v] = r[v]; continue; }
       const uint32_t d = xtdat[v];
       const double rv = r[v];
@@ -178,7 +188,8 @@ int orc_solve(int mode, uint32_t n, uint64_t m,
     }
     ++l;
     double el = 0.0;  /* liNormDeltaInplaceCuW, inc/_cuda.hxx:926-934 */
-    for (uint32_t v = 0; v < n; ++v) el = fmax(el, fabs(a[v] - r[v]));
+    #pragma omp parallel for schedule(static) reduction(max:el)
+    for (int64_t v = 0; v < (int64_t)n; ++v) el = fmax(el, fabs(a[v] - r[v]));
     if (FRONTIER) expand_marks(n, xoff, xedg, naff, vaff);
     double* t = a; a = r; r = t;
     if (el < E) break;
@@ -311,38 +322,80 @@ int orc_cpu_prune_dynamic_frontier(uint32_t n,
 /* Graph helpers.                                                             */
 /* ------------------------------------------------------------------------- */
 
+/* first index i in [0, cnt) with key[i] >= u (key ascending) */
+static uint64_t lower_u32(const uint32_t* key, uint64_t cnt, uint32_t u) {
+  uint64_t lo = 0, hi = cnt;
+  while (lo < hi) {
+    const uint64_t mid = lo + (hi - lo) / 2;
+    if (key[mid] < u) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+/* Row u of the updated graph: the old row minus deleted targets, merged with
+ * the inserted targets; writes it to out (when non-NULL), returns its length. */
+static uint64_t apply_row(const uint32_t* xedg, uint64_t i, uint64_t e,
+                          const uint32_t* delv, uint64_t id, uint64_t id_end,
+                          const uint32_t* insv, uint64_t ii, uint64_t ii_end, uint32_t* out) {
+  uint64_t k = 0;
+  for (;;) {
+    const int has_old = i < e;
+    const int has_ins = ii < ii_end;
+    if (!has_old && !has_ins) break;
+    uint32_t w;
+    if (has_old && (!has_ins || xedg[i] < insv[ii])) {
+      w = xedg[i++];
+      while (id < id_end && delv[id] < w) ++id;
+      if (id < id_end && delv[id] == w) { ++id; continue; }
+    } else if (has_old && has_ins && xedg[i] == insv[ii]) {
+      w = xedg[i++]; ++ii;  /* insertion of an existing edge: kept once */
+    } else {
+      w = insv[ii++];
+    }
+    if (out) out[k] = w;
+    ++k;
+  }
+  return k;
+}
+
 uint64_t orc_apply_batch(uint32_t n, const uint32_t* xoff, const uint32_t* xedg,
                          const uint32_t* delu, const uint32_t* delv, uint64_t nd,
                          const uint32_t* insu, const uint32_t* insv, uint64_t ni,
                          uint32_t* yoff, uint32_t* yedg, uint64_t m_cap) {
   /* applyBatchUpdateOmpU (inc/batch.hxx:239-247) on sorted adjacency
    * (LazyBitset keeps keys ascending): each row becomes
-   * (old row minus deleted targets) merged with inserted targets. */
-  uint64_t id = 0, ii = 0, k = 0;
+   * (old row minus deleted targets) merged with inserted targets.  The batch
+   * is sorted by source, so each row finds its deletions and insertions by
+   * binary search and rows are built independently: lengths, a scan, then
+   * the rows themselves. */
+  uint64_t* len = (uint64_t*)malloc(sizeof(uint64_t) * ((size_t)n + 1));
+  if (!len) return UINT64_MAX;
+  #pragma omp parallel for schedule(dynamic, 4096)
+  for (int64_t u = 0; u < (int64_t)n; ++u) {
+    const uint64_t d0 = lower_u32(delu, nd, (uint32_t)u), d1 = lower_u32(delu, nd, (uint32_t)u + 1);
+    const uint64_t i0 = lower_u32(insu, ni, (uint32_t)u), i1 = lower_u32(insu, ni, (uint32_t)u + 1);
+    len[u] = (d0 == d1 && i0 == i1) ? (uint64_t)xoff[u + 1] - xoff[u]
+                                     : apply_row(xedg, xoff[u], xoff[u + 1], delv, d0, d1, insv, i0, i1, NULL);
+  }
+  uint64_t k = 0;
   for (uint32_t u = 0; u < n; ++u) {
-    yoff[u] = (uint32_t)k;
-    uint64_t i = xoff[u], e = xoff[u + 1];
-    for (;;) {
-      while (id < nd && (delu[id] < u)) ++id;
-      while (ii < ni && (insu[ii] < u)) ++ii;
-      int has_old = i < e;
-      int has_ins = ii < ni && insu[ii] == u;
-      if (!has_old && !has_ins) break;
-      uint32_t w;
-      if (has_old && (!has_ins || xedg[i] < insv[ii])) {
-        w = xedg[i++];
-        while (id < nd && delu[id] == u && delv[id] < w) ++id;
-        if (id < nd && delu[id] == u && delv[id] == w) { ++id; continue; }
-      } else if (has_old && has_ins && xedg[i] == insv[ii]) {
-        w = xedg[i++]; ++ii;  /* insertion of an existing edge: kept once */
-      } else {
-        w = insv[ii++];
-      }
-      if (k >= m_cap) return UINT64_MAX;
-      yedg[k++] = w;
-    }
+    const uint64_t l = len[u];
+    len[u] = k;
+    k += l;
+  }
+  if (k > m_cap || k > 0xffffffffull) { free(len); return UINT64_MAX; }
+  #pragma omp parallel for schedule(dynamic, 4096)
+  for (int64_t u = 0; u < (int64_t)n; ++u) {
+    const uint64_t d0 = lower_u32(delu, nd, (uint32_t)u), d1 = lower_u32(delu, nd, (uint32_t)u + 1);
+    const uint64_t i0 = lower_u32(insu, ni, (uint32_t)u), i1 = lower_u32(insu, ni, (uint32_t)u + 1);
+    yoff[u] = (uint32_t)len[u];
+    if (d0 == d1 && i0 == i1)
+      memcpy(yedg + len[u], xedg + xoff[u], sizeof(uint32_t) * ((uint64_t)xoff[u + 1] - xoff[u]));
+    else
+      apply_row(xedg, xoff[u], xoff[u + 1], delv, d0, d1, insv, i0, i1, yedg + len[u]);
   }
   yoff[n] = (uint32_t)k;
+  free(len);
   return k;
 }
 

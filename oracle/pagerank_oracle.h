@@ -100,6 +100,18 @@ uint64_t orc_apply_batch(uint32_t n, const uint32_t* xoff, const uint32_t* xedg,
 void orc_transpose(uint32_t n, const uint32_t* xoff, const uint32_t* xedg,
                    uint32_t* xtoff, uint32_t* xtedg, uint32_t* xtdat);
 
+/* Seeded synthetic inputs (oracle_gen.c): the product generators' graphs,
+ * built without the product library.  orc_gen_weblike returns 0 and
+ * malloc'd *xoff_out[n+1], *xedg_out[*m_out] (free with orc_free); -1 bad
+ * arguments, -2 out of memory, -3 more than 2^32 - 1 edges. */
+int orc_gen_weblike(uint32_t n, double alpha, double dmin, uint32_t dmax, double local,
+                    uint32_t window, uint64_t seed, uint32_t** xoff_out, uint32_t** xedg_out,
+                    uint64_t* m_out);
+/* orc_transpose with OpenMP threads (same output). */
+void orc_transpose_omp(uint32_t n, const uint32_t* xoff, const uint32_t* xedg,
+                       uint32_t* xtoff, uint32_t* xtedg, uint32_t* xtdat);
+void orc_free(void* p);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,8 +27,9 @@ class Options(C.Structure):
 
 
 def build(force=False):
+    srcs = ("pagerank_oracle.c", "oracle_gen.c", "pagerank_oracle.h")
     if force or not os.path.exists(LIB_PATH) or \
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "pagerank_oracle.c")):
+            os.path.getmtime(LIB_PATH) < max(os.path.getmtime(os.path.join(HERE, f)) for f in srcs):
         subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     return LIB_PATH
 
@@ -62,6 +63,14 @@ def lib():
                                       C.c_void_p, C.c_void_p, u64, u32p, u32p, u64]
         L.orc_transpose.restype = None
         L.orc_transpose.argtypes = [C.c_uint32, u32p, u32p, u32p, u32p, u32p]
+        L.orc_transpose_omp.restype = None
+        L.orc_transpose_omp.argtypes = [C.c_uint32, u32p, u32p, u32p, u32p, u32p]
+        L.orc_gen_weblike.restype = C.c_int
+        L.orc_gen_weblike.argtypes = [C.c_uint32, C.c_double, C.c_double, C.c_uint32, C.c_double, C.c_uint32,
+                                      C.c_uint64, C.POINTER(C.POINTER(C.c_uint32)),
+                                      C.POINTER(C.POINTER(C.c_uint32)), C.POINTER(C.c_uint64)]
+        L.orc_free.restype = None
+        L.orc_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -139,19 +148,40 @@ def apply_batch(xoff, xedg, delu, delv, insu, insv):
     n = len(xoff) - 1
     cap = len(xedg) + len(insu)
     yoff = np.zeros(n + 1, np.uint32)
-    yedg = np.zeros(max(cap, 1), np.uint32)
+    yedg = np.empty(max(cap, 1), np.uint32)
     k = lib().orc_apply_batch(n, xoff, xedg, _ptr(delu), _ptr(delv), len(delu), _ptr(insu), _ptr(insv),
                               len(insu), yoff, yedg, cap)
     if k == 2 ** 64 - 1:
         raise ValueError("capacity exceeded")
-    return yoff, yedg[:k].copy()
+    return yoff, yedg[:k]
 
 
-def transpose(xoff, xedg):
+def transpose(xoff, xedg, threads=False):
+    """(xtoff, xtedg, xtdat) of an out-CSR; threads=True runs the OpenMP
+    version (same output)."""
     xoff, xedg = _u32(xoff), _u32(xedg)
     n = len(xoff) - 1
     xtoff = np.zeros(n + 1, np.uint32)
-    xtedg = np.zeros(max(len(xedg), 1), np.uint32)
+    xtedg = np.empty(max(len(xedg), 1), np.uint32)
     xtdat = np.zeros(max(n, 1), np.uint32)
-    lib().orc_transpose(n, xoff, xedg, xtoff, xtedg, xtdat)
-    return xtoff, xtedg[:len(xedg)].copy(), xtdat[:n].copy()
+    (lib().orc_transpose_omp if threads else lib().orc_transpose)(n, xoff, xedg, xtoff, xtedg, xtdat)
+    return xtoff, xtedg[:len(xedg)], xtdat[:n]
+
+
+def _take(ptr, count):
+    """Copy `count` uint32 from a malloc'd oracle array into numpy and free it."""
+    try:
+        return np.ctypeslib.as_array(ptr, shape=(count,)).copy() if count else np.zeros(0, np.uint32)
+    finally:
+        lib().orc_free(ptr)
+
+
+def gen_weblike(n, alpha=2.1, dmin=5.9, dmax=100000, local=0.7, window=4096, seed=42):
+    """The web-like generator's graph (the product's host generator gives
+    the same arrays) -> (xoff, xedg)."""
+    po, pe = C.POINTER(C.c_uint32)(), C.POINTER(C.c_uint32)()
+    m = C.c_uint64()
+    st = lib().orc_gen_weblike(n, alpha, dmin, dmax, local, window, seed, C.byref(po), C.byref(pe), C.byref(m))
+    if st != 0:
+        raise ValueError(f"orc_gen_weblike failed ({st})")
+    return _take(po, n + 1), _take(pe, m.value)

@@ -17,14 +17,22 @@
 //    them on one stream or with events;
 //  - the array keeps whatever the last call left; each call re-initialises
 //    everything it reads (control block, ranks, contributions) before use.
-//  - The first call on a device looks the array's device address up
-//    (cudaGetSymbolAddress) with that device current.
+//  - Every call looks the array's device address up (cudaGetSymbolAddress,
+//    which allocates nothing) in the context current on the calling thread,
+//    so a device reset or another context on the same device never leaves a
+//    stale address behind.  The first call in a context is also where the
+//    CUDA loader places the array, so make it before any stream capture.
+//
+// Preconditions (as prx_graph_create checks them for the regular path):
+// xtoff[0] = 0, xtoff non-decreasing, xtoff[n] = m, every xtedg id below n,
+// every xtdat (out-degree, self-loop included) at least 1.  The first and
+// last offsets are checked on the device before any sweep (PRX_EINVAL); the
+// rest is the caller's promise.
 //
 // Results are bit-identical to prx_solve(PRX_STATIC): the same sums in the
 // same order (front to back for in-degree <= 64, 256 strided partial sums
 // and a halving tree above that, inc/pagerankCuda.hxx:87-109, 162-188 and
 // inc/_cuda.hxx:541-551), the same fma epilogue and stopping rule.
-#include <mutex>
 #include <string>
 #include "prx_device.cuh"
 
@@ -32,7 +40,6 @@ namespace {
 
 constexpr int kHeadDoubles = 32;  // 256-byte control block before the vectors
 constexpr size_t kScratchDoubles = kHeadDoubles + 3 * (size_t)PRX_NOALLOC_MAX_VERTICES;
-constexpr int kMaxDevices = 64;
 
 // The device scratch.  In host code this name is only a stand-in for the
 // symbol; kernels get the address cudaGetSymbolAddress returned.
@@ -43,7 +50,7 @@ struct NaState {
   int iter;
   int done;
   int max_iter;
-  int pad;
+  int bad;      // the offsets failed the first / last check
   double tol;
 };
 static_assert(sizeof(NaState) <= kHeadDoubles * sizeof(double), "control block too large");
@@ -63,11 +70,12 @@ struct NaArgs {
   }
 };
 
-__global__ void k_na_reset(NaArgs a, int max_iter, double tol) {
+__global__ void k_na_reset(NaArgs a, uint32_t m, int max_iter, double tol) {
   NaState* s = a.st();
   s->el_bits[0] = s->el_bits[1] = 0;
   s->iter = 0;
-  s->done = max_iter <= 0;
+  s->bad = a.xtoff[0] != 0u || a.xtoff[a.n] != m;
+  s->done = max_iter <= 0 || s->bad;   // no sweep reads a bad CSR
   s->max_iter = max_iter;
   s->tol = tol;
 }
@@ -156,33 +164,17 @@ __global__ void k_na_finalize(NaArgs a) {
   s->el_bits[p ^ 1] = 0;
 }
 
-std::mutex g_setup_mu;
-double* g_scratch_addr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device, looked up once
-// per device.
+// Device address of the scratch array in the current context.  Looked up on
+// every call: the lookup allocates nothing, and an address cached per device
+// would go stale after a device reset or under another context.
 int scratch_address(double** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    prx::set_error(std::string("prx_static_solve_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    prx::set_error(std::string("prx_static_solve_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     return PRX_ECUDA;
   }
-  if (dev < 0 || dev >= kMaxDevices) {
-    prx::set_error("prx_static_solve_noalloc: device index beyond the supported 64");
-    return PRX_EINVAL;
-  }
-  std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      prx::set_error(std::string("prx_static_solve_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-      return PRX_ECUDA;
-    }
-    g_scratch_addr[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch_addr[dev];
+  *out = static_cast<double*>(p);
   return PRX_OK;
 }
 
@@ -227,7 +219,7 @@ extern "C" int prx_static_solve_noalloc(uint32_t n, uint64_t m, const uint32_t* 
   a.P = damping;
   a.C0 = (1 - damping) / (double)n;
   const uint32_t tgrid = (n + 255) / 256 < (uint32_t)sms * 8 ? (n + 255) / 256 : (uint32_t)sms * 8;
-  k_na_reset<<<1, 1, 0, s>>>(a, max_iterations, tolerance);
+  k_na_reset<<<1, 1, 0, s>>>(a, (uint32_t)m, max_iterations, tolerance);
   k_na_init<<<tgrid, 256, 0, s>>>(a);
   NaState h;  // read back on the host stack; no allocation
   for (int k = 1;; k = k < 16 ? 2 * k : 16) {
@@ -243,6 +235,10 @@ extern "C" int prx_static_solve_noalloc(uint32_t n, uint64_t m, const uint32_t* 
       return PRX_ECUDA;
     }
     if (h.done) break;
+  }
+  if (h.bad) {
+    prx::set_error("prx_static_solve_noalloc: xtoff[0] must be 0 and xtoff[n] must equal m");
+    return PRX_EINVAL;
   }
   if (h.iter & 1) {  // the last sweep wrote the scratch rank buffer
     cudaError_t e = cudaMemcpyAsync(ranks, scratch + kHeadDoubles, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);

@@ -14,7 +14,7 @@ fixture stores the inputs and what the reference produced:
   exact_y_ranks                         pagerankStaticOmp with tol 1e-100
 
 Run from the repository root where the reference headers exist:
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref REF_INC=<reference>/inc && python tests/golden/make_golden.py
 """
 import os
 import subprocess
@@ -150,7 +150,7 @@ def make_case(name, n, u, v, batch, tol=1e-10):
 
 def main():
     if not os.path.exists(HARNESS):
-        sys.exit("build the reference harness first: make -C oracle ref")
+        sys.exit("build the reference harness first: make -C oracle ref REF_INC=<reference>/inc")
     rng = np.random.default_rng(42)
     frac = lambda f: (lambda n, u, v: random_batch(n, u, v, max(1, int(f * len(u))), rng))
     n, u, v = rmat_edges(8, 16, rng)

@@ -13,7 +13,7 @@ compiled against the headers of puzzlef/pagerank-cuda-dynamic by
                               the next batch's x), 0-based CSRs
 
 Run from the repository root where the reference headers exist:
-    make -C oracle ref && python tests/golden/make_readers_golden.py
+    make -C oracle ref REF_INC=<reference>/inc && python tests/golden/make_readers_golden.py
 """
 import os
 import subprocess

@@ -32,15 +32,21 @@ def _reference_solution(pg, xt, **kw):
     return ranks, res["iterations"]
 
 
-def _noalloc(f, xt, damping=0.85, tol=1e-10, max_iter=500):
+def _noalloc(f, xt, damping=0.85, tol=1e-10, max_iter=500, stream=None, m=None):
+    """One call; with `stream` (a torch.cuda.Stream) the inputs are made and
+    the call is issued on that stream."""
     import torch
-    xtoff, xtedg, xtdat = (torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).cuda() for a in xt)
-    n, m = len(xt[0]) - 1, len(xt[1])
-    ranks = torch.full((max(n, 1),), float("nan"), dtype=torch.float64, device="cuda")
+    with torch.cuda.stream(stream) if stream is not None else torch.cuda.device(0):
+        xtoff, xtedg, xtdat = (torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).cuda()
+                               for a in xt)
+        n = len(xt[0]) - 1
+        m = len(xt[1]) if m is None else m
+        ranks = torch.full((max(n, 1),), float("nan"), dtype=torch.float64, device="cuda")
     it = C.c_int(-1)
-    torch.cuda.synchronize()
+    if stream is None:
+        torch.cuda.synchronize()
     st = f(n, m, xtoff.data_ptr(), xtedg.data_ptr(), xtdat.data_ptr(), damping, tol, max_iter, ranks.data_ptr(),
-           C.byref(it), None)
+           C.byref(it), None if stream is None else stream.cuda_stream)
     torch.cuda.synchronize()
     return st, ranks[:n].cpu().numpy(), it.value
 
@@ -73,3 +79,35 @@ def test_noalloc_options_and_limits():
     it = C.c_int(-1)
     assert f(LIMIT + 1, 0, None, None, None, 0.85, 1e-10, 500, None, C.byref(it), None) == 5
     assert "exceeds" in pg.load().prx_last_error().decode()
+
+
+def test_noalloc_on_a_non_default_stream():
+    # inputs made on a torch stream and two calls issued on it back to back:
+    # the stream argument is honoured and the second call re-initialises the
+    # shared scratch the first one left behind
+    import torch
+    pg, f = _lib()
+    off, edg = pg.graphs.rmat(15, 16, seed=9)
+    xt = pg.graphs.transpose(off, edg)
+    want, want_it = _reference_solution(pg, xt)
+    s = torch.cuda.Stream()
+    for _ in range(2):
+        st, got, it = _noalloc(f, xt, stream=s)
+        assert st == 0, pg.load().prx_last_error()
+        assert it == want_it
+        np.testing.assert_array_equal(got, want)
+
+
+def test_noalloc_rejects_offsets_that_do_not_end_at_m():
+    # xtoff[n] != m is caught on the device before any sweep; the next call
+    # with the right m still gives the regular entry point's answer
+    pg, f = _lib()
+    off, edg = pg.graphs.rmat(10, 8, seed=5)
+    xt = pg.graphs.transpose(off, edg)
+    st, _, it = _noalloc(f, xt, m=len(xt[1]) - 1)
+    assert st == 1 and it == 0
+    assert "xtoff" in pg.load().prx_last_error().decode()
+    want, want_it = _reference_solution(pg, xt)
+    st, got, it = _noalloc(f, xt)
+    assert st == 0 and it == want_it
+    np.testing.assert_array_equal(got, want)
