@@ -58,6 +58,11 @@ struct PagerankResult {
   float markingTime;
   float computationTime;
   PagerankResult() : ranks(), iterations(0), time(0), initializationTime(0), markingTime(0), computationTime(0) {}
+  // inc/pagerank.hxx:98 (an rvalue vector) and :111 (an lvalue vector, moved from)
+  PagerankResult(std::vector<V>&& ranks, int iterations = 0, float time = 0, float initializationTime = 0,
+                 float markingTime = 0, float computationTime = 0)
+      : ranks(std::move(ranks)), iterations(iterations), time(time), initializationTime(initializationTime),
+        markingTime(markingTime), computationTime(computationTime) {}
   PagerankResult(std::vector<V>& ranks, int iterations = 0, float time = 0, float initializationTime = 0,
                  float markingTime = 0, float computationTime = 0)
       : ranks(std::move(ranks)), iterations(iterations), time(time), initializationTime(initializationTime),

@@ -12,6 +12,10 @@ for p in (ROOT, PKG):
         sys.path.insert(0, p)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
+# The reference's checkout, for the CPU tests that compile against its
+# headers (PRX_REFERENCE_DIR, else where it is mounted beside this checkout
+# for tests); those tests skip where it is absent.
+REFERENCE_DIR = os.environ.get("PRX_REFERENCE_DIR") or "/root/reference"
 
 
 def pytest_configure(config):
