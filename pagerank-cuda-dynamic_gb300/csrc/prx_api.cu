@@ -41,6 +41,8 @@ void prx_options_default(prx_options* o) {
   o->refine_sweeps = 0;
   o->l2_fetch_bytes = 0;
   o->require_convergence = 0;
+  o->low_sweep = 0;
+  o->hot_sources = 0;
 }
 
 const char* prx_status_string(int s) {
@@ -91,6 +93,8 @@ static void free_ws(prx_context* c) {
   for (auto& f : c->fr) { cudaFree(f); f = nullptr; }
   cudaFree(c->acc64); c->acc64 = nullptr;
   cudaFree(c->acc32); c->acc32 = nullptr;
+  for (auto& h : c->ch) { cudaFree(h); h = nullptr; }
+  c->ch_n = 0;
   cudaFree(c->flags); c->flags = nullptr;
   for (auto& b : c->bm) { cudaFree(b); b = nullptr; }
   for (auto& b : c->nf) { cudaFree(b); b = nullptr; }
@@ -158,6 +162,15 @@ static int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
   return PRX_OK;
 }
 
+static int ensure_ch(prx_context* c, uint32_t hot_n) {
+  if (c->ch_n >= hot_n) return PRX_OK;
+  for (auto& h : c->ch) { cudaFree(h); h = nullptr; }
+  c->ch_n = 0;
+  for (auto& h : c->ch) TRY_CUDA_ST(cudaMalloc(&h, sizeof(double) * hot_n));
+  c->ch_n = hot_n;
+  return PRX_OK;
+}
+
 static int ensure_ws32(prx_context* c, uint32_t n) {
   if (c->ws32_n >= n) return PRX_OK;
   cudaFree(c->rho);
@@ -197,6 +210,7 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
   for (int p = 0; p < 2; ++p) {
     a.r[p] = c->r[p];
     a.c[p] = c->c[p];
+    a.ch[p] = c->ch[p];
     for (int k = 0; k < NCLS; ++k) a.list[p][k] = c->lists[p][k];
   }
   for (int k = 0; k < 3; ++k) a.bm[k] = c->bm[k];
@@ -215,6 +229,7 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
   a.st = c->st;
   a.n = g.n;
   a.mid_max = g.mid_max;
+  a.low_sweep = o.low_sweep;
   a.P = o.damping;
   a.C0 = (1 - o.damping) / (double)g.n;  // pagerankLoopCuU :679, N = order
   a.D = o.frontier_tolerance;
@@ -336,6 +351,8 @@ static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArg
                                        [&] { return launch_update_class(a, gr->g, mode, cls, lay, c->sms, s); });
     if (st) return st;
   }
+  if (!(mode & MODE_F32) && mode < PRX_DYNAMIC_TRAVERSAL)  // the contributions this sweep wrote
+    c->launches += launch_hot_copy(a, -1, c->sms, s);
   if ((mode & ~MODE_F32) >= PRX_DYNAMIC_FRONTIER) {
     launch_expand_iteration(a, c->sms, s);  // push or pull, chosen on the device
     c->launches += 3;
@@ -430,7 +447,7 @@ static int run_refine_loop(prx_context* c, const prx_graph* gr, const SolveArgs&
       if (c->st_host[1].inner_done) break;
     }
     launch_refine_commit(a, c->sms, s);
-    c->launches += 1;
+    c->launches += 1 + launch_hot_copy(a, 0, c->sms, s);
     return PRX_OK;
   };
   if (max_iter <= 0) {
@@ -504,11 +521,22 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   const uint32_t w32 = o.chunk_vertices ? o.chunk_vertices
                       : g.tuned_w32          ? g.tuned_w32
                                              : (48u << 20) / sizeof(float);
+  // Hot sources (the FP64 sweeps of Static / ND and of the refinement): a
+  // layout whose edges from the highest out-degree vertices gather from a
+  // dense copy of their contributions
+  const bool hot_ok = o.hot_sources >= 0 && o.low_sweep < 2 && (!dyn || refine);
+  if (hot_ok) {
+    TRY_CUDA_ST(ensure_hot(gr->g, o.hot_sources > 0 ? (uint32_t)o.hot_sources : kDefaultHotCap, c->sms,
+                           c->stream));
+    if (g.hot_n && (st = ensure_ch(c, g.hot_n))) return st;
+  }
   const ChunkLayout *lay64 = nullptr, *lay32 = nullptr;
-  TRY_CUDA_ST(ensure_chunks(gr->g, w64, refine ? w32 : w64, c->sms, c->stream, &lay64));
-  if (refine) TRY_CUDA_ST(ensure_chunks(gr->g, w32, w64, c->sms, c->stream, &lay32));
+  TRY_CUDA_ST(ensure_chunks(gr->g, w64, c->sms, c->stream, &lay64, o.low_sweep >= 2, hot_ok && g.hot_n > 0));
+  if (refine) TRY_CUDA_ST(ensure_chunks(gr->g, w32, c->sms, c->stream, &lay32));
   cudaStream_t s = c->stream;
-  const SolveArgs a = make_args(c, g, o);
+  SolveArgs a = make_args(c, g, o);
+  a.hot_list = g.hot_list;
+  a.hot_n = (lay64 && lay64->hot) ? g.hot_n : 0;
   const int repeat = o.repeat > 0 ? o.repeat : 1;
   float ti = 0, tm = 0, tc = 0, tt = 0;
   const bool timing = o.timing != 0;
@@ -520,7 +548,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
     TRY_CUDA_ST(cudaEventRecord(c->ev[0], s));
     launch_state_reset(c->st, o.max_iterations, o.tolerance, s);
     launch_init_ranks(a, (mode == PRX_STATIC) ? nullptr : q_dev, dyn, s);
-    c->launches += 2;
+    c->launches += 2 + launch_hot_copy(a, 0, c->sms, s);
     if (mode == PRX_PRUNE_DYNAMIC_FRONTIER && !refine) {
       launch_prune_factor(a, s);
       c->launches += 1;
@@ -565,7 +593,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
       // (an FP64 residual sweep over all vertices decides convergence)
       if ((st = iterate(mode | MODE_F32, lay32))) return st;
       launch_commit_dyn32(a, c->st_host[1].iter & 1, s);
-      c->launches += 1;
+      c->launches += 1 + launch_hot_copy(a, 0, c->sms, s);
       if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity, false))) return st;
     } else if (refine) {
       // Static / ND, or a dynamic mode whose marking covers most of the
@@ -885,6 +913,7 @@ int prx_graph_destroy(prx_graph* gr) {
   drop_weights(g);
   cudaFree(g.ocls_list);
   free_chunks(g);
+  free_hot(g);
   delete gr;
   return PRX_OK;
 }
@@ -996,6 +1025,8 @@ static int solve_common(prx_context* c, prx_graph* gr, int mode, const uint32_t*
   if (!(opt.damping > 0 && opt.damping < 1)) FAIL(PRX_EINVAL, "prx_solve: damping must be in (0, 1)");
   if (opt.l2_fetch_bytes < -1 || opt.l2_fetch_bytes > 128)
     FAIL(PRX_EINVAL, "prx_solve: l2_fetch_bytes must be in -1 .. 128");
+  if (opt.low_sweep < 0 || opt.low_sweep > 5) FAIL(PRX_EINVAL, "prx_solve: low_sweep must be in 0 .. 5");
+  if (opt.hot_sources < -1) FAIL(PRX_EINVAL, "prx_solve: hot_sources must be -1, 0 or a vertex count");
   if (!ranks_out && gr->g.n) FAIL(PRX_EINVAL, "prx_solve: ranks_out is NULL");
   prx_result own;
   if (!res) res = &own;  // the convergence check reads it

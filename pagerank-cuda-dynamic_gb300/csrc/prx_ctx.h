@@ -25,6 +25,8 @@ struct prx_context {
   double* r[2] = {nullptr, nullptr};
   double* c[2] = {nullptr, nullptr};
   double* acc64 = nullptr;    // partial sums between chunk passes
+  double* ch[2] = {nullptr, nullptr};  // dense copies of the hot sources' contributions
+  uint32_t ch_n = 0;
   float* acc32 = nullptr;
   uint8_t* flags = nullptr;   // byte flags for prx_mark_affected
   uint32_t* bm[3] = {nullptr, nullptr, nullptr};

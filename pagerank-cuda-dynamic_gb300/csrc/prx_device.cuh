@@ -146,20 +146,28 @@ __device__ __forceinline__ bool quot_gt(double x, double m, double c) {
   return x / m > c;
 }
 
+// The contribution of edge id u: with `hot` (a layout whose hot sources are
+// encoded, kHotFlag | number) from the dense hot copy ch, else c[u].
+template <class T>
+__device__ __forceinline__ T gather(const T* __restrict__ c, const T* __restrict__ ch, bool hot, uint32_t u) {
+  return __ldg((hot && (u & kHotFlag)) ? ch + (u ^ kHotFlag) : c + u);
+}
+
 // Sum of c[edg[j]] for j in [s, e) added front to back onto acc.  The edge
 // ids are read as aligned 16-byte groups of four (edg must be 16-byte
 // aligned and allocated per edge_slots); ids outside [s, e) in the first and
 // last group are loaded but neither gathered nor added.  Four gathers are in
-// flight per group.
+// flight per group.  hot / ch: see gather().
 template <class T>
 __device__ __forceinline__ T lane_row_sum(const T* __restrict__ c, const uint32_t* __restrict__ edg, uint32_t s,
-                                          uint32_t e, T acc) {
+                                          uint32_t e, T acc, const T* __restrict__ ch = nullptr, bool hot = false) {
   if (s >= e) return acc;
   uint32_t j = s & ~3u;
   if (j < s) {  // head group: ids j+1 .. j+3 from s on
     const uint4 u = __ldg(reinterpret_cast<const uint4*>(edg + j));
     const bool b1 = s <= j + 1 && j + 1 < e, b2 = s <= j + 2 && j + 2 < e, b3 = j + 3 < e;
-    const T c1 = b1 ? __ldg(c + u.y) : T(0), c2 = b2 ? __ldg(c + u.z) : T(0), c3 = b3 ? __ldg(c + u.w) : T(0);
+    const T c1 = b1 ? gather(c, ch, hot, u.y) : T(0), c2 = b2 ? gather(c, ch, hot, u.z) : T(0),
+            c3 = b3 ? gather(c, ch, hot, u.w) : T(0);
     if (b1) acc += c1;
     if (b2) acc += c2;
     if (b3) acc += c3;
@@ -167,13 +175,15 @@ __device__ __forceinline__ T lane_row_sum(const T* __restrict__ c, const uint32_
   }
   for (; j + 4 <= e; j += 4) {
     const uint4 u = __ldg(reinterpret_cast<const uint4*>(edg + j));
-    const T c0 = __ldg(c + u.x), c1 = __ldg(c + u.y), c2 = __ldg(c + u.z), c3 = __ldg(c + u.w);
+    const T c0 = gather(c, ch, hot, u.x), c1 = gather(c, ch, hot, u.y), c2 = gather(c, ch, hot, u.z),
+            c3 = gather(c, ch, hot, u.w);
     acc += c0; acc += c1; acc += c2; acc += c3;
   }
   if (j < e) {  // tail group: ids j .. e-1 (at most 3)
     const uint4 u = __ldg(reinterpret_cast<const uint4*>(edg + j));
     const bool b1 = j + 1 < e, b2 = j + 2 < e;
-    const T c0 = __ldg(c + u.x), c1 = b1 ? __ldg(c + u.y) : T(0), c2 = b2 ? __ldg(c + u.z) : T(0);
+    const T c0 = gather(c, ch, hot, u.x), c1 = b1 ? gather(c, ch, hot, u.y) : T(0),
+            c2 = b2 ? gather(c, ch, hot, u.z) : T(0);
     acc += c0;
     if (b1) acc += c1;
     if (b2) acc += c2;

@@ -280,9 +280,18 @@ __global__ void k_chunk_count(const uint32_t* __restrict__ xtoff, const uint32_t
   }
 }
 
+// Edge id as stored in a layout: a hot source's number with the flag, else
+// the id itself (hot_idx null: plain ids).
+__device__ __forceinline__ uint32_t layout_id(const uint32_t* __restrict__ hot_idx, uint32_t u) {
+  if (!hot_idx) return u;
+  const uint32_t h = hot_idx[u];
+  return h == kNotHot ? u : (kHotFlag | h);
+}
+
 __global__ void k_chunk_scatter(const uint32_t* __restrict__ xtoff, const uint32_t* __restrict__ xtedg,
                                 const uint32_t* __restrict__ low_bm, uint32_t n, uint32_t width, int K,
-                                const uint32_t* __restrict__ off, uint32_t* __restrict__ edg) {
+                                const uint32_t* __restrict__ off, uint32_t* __restrict__ edg,
+                                const uint32_t* __restrict__ hot_idx) {
   const size_t row = (size_t)n + 1;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     if (!((low_bm[v >> 5] >> (v & 31u)) & 1u)) continue;
@@ -291,7 +300,7 @@ __global__ void k_chunk_scatter(const uint32_t* __restrict__ xtoff, const uint32
     for (int k = 0; k < K; ++k) {
       const uint64_t hi = (uint64_t)(k + 1) * width;
       uint32_t pos = off[k * row + v];
-      while (j < e && xtedg[j] < hi) edg[pos++] = xtedg[j++];
+      while (j < e && xtedg[j] < hi) edg[pos++] = layout_id(hot_idx, xtedg[j++]);
     }
   }
 }
@@ -308,7 +317,8 @@ __global__ void __launch_bounds__(256) k_chunk_scatter_w(const uint32_t* __restr
                                                          const uint32_t* __restrict__ xtedg,
                                                          const uint32_t* __restrict__ low_bm, uint32_t n,
                                                          uint32_t width, int K, const uint32_t* __restrict__ off,
-                                                         uint32_t* __restrict__ edg) {
+                                                         uint32_t* __restrict__ edg,
+                                                         const uint32_t* __restrict__ hot_idx) {
   const size_t row = (size_t)n + 1;
   const uint32_t lane = lane_id();
   const uint32_t groups = (n + 31) >> 5;
@@ -362,7 +372,7 @@ __global__ void __launch_bounds__(256) k_chunk_scatter_w(const uint32_t* __restr
             rr = rk;
           }
         }
-        if (act) edg[d + (j - sr - rr)] = u;
+        if (act) edg[d + (j - sr - rr)] = layout_id(hot_idx, u);
       }
     }
   }
@@ -383,7 +393,7 @@ void free_chunks(GraphDev& g) {
 // edg, LOW bitmap from its first row): counts, scan, scatter.
 static cudaError_t build_layout(const uint32_t* off, const uint32_t* edg, const uint32_t* low_bm, uint32_t rows,
                                 uint64_t low_edges, uint32_t width, int K, int sms, cudaStream_t s,
-                                uint32_t** lay_off, uint32_t** lay_edg) {
+                                uint32_t** lay_off, uint32_t** lay_edg, const uint32_t* hot_idx) {
   const size_t len = (size_t)K * ((size_t)rows + 1);
   if (len > 0xffffffffull) return cudaErrorInvalidValue;
   cudaError_t e = graph_alloc(lay_off, sizeof(uint32_t) * len, s);
@@ -393,29 +403,45 @@ static cudaError_t build_layout(const uint32_t* off, const uint32_t* edg, const 
   k_chunk_count<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, *lay_off);
   e = exclusive_scan_u32(*lay_off, (uint32_t)len, s);
   if (e == cudaSuccess) {
-    if (K <= kScatterK) k_chunk_scatter_w<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, *lay_off, *lay_edg);
-    else k_chunk_scatter<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, *lay_off, *lay_edg);
+    if (K <= kScatterK)
+      k_chunk_scatter_w<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, *lay_off, *lay_edg, hot_idx);
+    else
+      k_chunk_scatter<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, *lay_off, *lay_edg, hot_idx);
     e = cudaGetLastError();
   }
   return e;
 }
 
-cudaError_t ensure_chunks(GraphDev& g, uint32_t width, uint32_t keep, int sms, cudaStream_t s,
-                          const ChunkLayout** out) {
+cudaError_t ensure_chunks(GraphDev& g, uint32_t width, int sms, cudaStream_t s, const ChunkLayout** out,
+                          bool single, bool hot) {
+  static uint64_t clock = 0;
   *out = nullptr;
-  if (width == 0 || width >= g.n) return cudaSuccess;  // one chunk: the row-major CSR is the layout
+  if (width == 0 || g.n == 0) return cudaSuccess;
+  if (hot && !g.hot_n) hot = false;
+  if (width >= g.n) {  // one chunk: the row-major CSR is the layout, or its LOW rows alone
+    const bool all_low = g.cls_begin[1] == g.n;
+    if (g.cls_begin[1] == g.cls_begin[0] || (!hot && (!single || all_low))) return cudaSuccess;
+    width = g.n;
+  }
   if (g.nseg > 1 && g.seg_shift < 5) return cudaSuccess;  // segments must start on a LOW-bitmap word
   for (auto& l : g.lay)
-    if (l.width == width) { *out = &l; return cudaSuccess; }
-  // an empty slot, else the one not holding `keep` (still in use by the caller)
-  ChunkLayout& l = g.lay[0].width == 0 ? g.lay[0]
-                   : g.lay[1].width == 0 ? g.lay[1]
-                   : (g.lay[0].width == keep ? g.lay[1] : g.lay[0]);
+    if (l.width == width && l.hot == hot) {
+      l.stamp = ++clock;
+      *out = &l;
+      return cudaSuccess;
+    }
+  // an empty slot, else the least recently used one (never one handed out
+  // for the current solve: those were used last)
+  ChunkLayout* pick = &g.lay[0];
+  for (auto& l : g.lay)
+    if (l.width == 0 || (pick->width != 0 && l.stamp < pick->stamp)) pick = &l;
+  ChunkLayout& l = *pick;
   free_layout(l);
+  const uint32_t* hot_idx = hot ? g.hot_idx : nullptr;
   const int K = (int)((g.n + (uint64_t)width - 1) / width);
   cudaError_t e = cudaSuccess;
   if (g.nseg <= 1) {
-    e = build_layout(g.xtoff, g.xtedg, g.low_bm, g.n, g.cls_edges[LOW], width, K, sms, s, &l.off, &l.edg);
+    e = build_layout(g.xtoff, g.xtedg, g.low_bm, g.n, g.cls_edges[LOW], width, K, sms, s, &l.off, &l.edg, hot_idx);
   } else {
     // one layout per row segment: its rows' offsets are a plain CSR of the
     // segment's edges; sources keep their global ids, so the chunks are global
@@ -426,7 +452,7 @@ cudaError_t ensure_chunks(GraphDev& g, uint32_t width, uint32_t keep, int sms, c
           (q + 1 < g.nseg ? g.xtseg0[q + 1] : g.m) - g.xtseg0[q];  // every edge of the segment
       uint32_t *lo = nullptr, *le = nullptr;
       e = build_layout(g.xtoff + v0 + q, g.xtedg + g.xtpos[q], g.low_bm + (v0 >> 5), rows, seg_edges_bound, width,
-                       K, sms, s, &lo, &le);
+                       K, sms, s, &lo, &le, hot_idx);
       l.seg_off.push_back(lo);
       l.seg_edg.push_back(le);
     }
@@ -437,13 +463,108 @@ cudaError_t ensure_chunks(GraphDev& g, uint32_t width, uint32_t keep, int sms, c
   }
   l.width = width;
   l.K = K;
+  l.hot = hot;
+  l.stamp = ++clock;
   *out = &l;
+  return cudaSuccess;
+}
+
+// ---- hot sources --------------------------------------------------------------
+constexpr uint32_t kDegBins = 1u << 16;  // out-degree histogram (the last bin holds every larger degree)
+
+__global__ void k_degree_hist(const uint32_t* __restrict__ xtdat, uint32_t n, uint32_t* __restrict__ hist) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    atomicAdd(&hist[min(xtdat[v], kDegBins - 1)], 1u);
+}
+
+__global__ void k_hot_flags(const uint32_t* __restrict__ xtdat, uint32_t n, uint32_t t, uint32_t* __restrict__ flag) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += gridDim.x * blockDim.x)
+    flag[v] = v < n && xtdat[v] >= t ? 1u : 0u;
+}
+
+// flag holds the exclusive scan of the hot flags: v's number if hot
+__global__ void k_hot_index(const uint32_t* __restrict__ xtdat, uint32_t n, uint32_t t,
+                            const uint32_t* __restrict__ scan, uint32_t* __restrict__ hot_idx,
+                            uint32_t* __restrict__ hot_list) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const bool hot = xtdat[v] >= t;
+    hot_idx[v] = hot ? scan[v] : kNotHot;
+    if (hot) hot_list[scan[v]] = v;
+  }
+}
+
+void free_hot(GraphDev& g) {
+  graph_free({g.hot_idx, g.hot_list});
+  g.hot_idx = g.hot_list = nullptr;
+  g.hot_n = 0;
+  g.hot_cap = 0;
+  g.hot_built = false;
+}
+
+cudaError_t ensure_hot(GraphDev& g, uint32_t cap, int sms, cudaStream_t s) {
+  if (g.hot_built && g.hot_cap == cap) return cudaSuccess;
+  // layouts built with the old numbering must not be used again
+  for (auto& l : g.lay)
+    if (l.hot) free_layout(l);
+  free_hot(g);
+  g.hot_built = true;
+  g.hot_cap = cap;
+  const uint32_t n = g.n;
+  if (cap == 0 || n == 0 || n >= kHotFlag) return cudaSuccess;
+  uint32_t* hist = nullptr;
+  cudaError_t e = graph_alloc(&hist, sizeof(uint32_t) * kDegBins, s);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(hist, 0, sizeof(uint32_t) * kDegBins, s);
+  if (e == cudaSuccess) {
+    k_degree_hist<<<sms * 4, 256, 0, s>>>(g.xtdat, n, hist);
+    e = cudaGetLastError();
+  }
+  std::vector<uint32_t> h(kDegBins);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), hist, sizeof(uint32_t) * kDegBins, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  graph_free({hist});
+  if (e != cudaSuccess) return e;
+  // threshold t: the smallest degree with count(d >= t) <= cap, and at least
+  // twice the average out-degree (a graph without skew gains nothing)
+  uint64_t above = 0;
+  uint32_t t = kDegBins;
+  for (uint32_t b = kDegBins; b-- > 1;) {
+    if (above + h[b] > cap) break;
+    above += h[b];
+    t = b;
+  }
+  const uint32_t floor_t = (uint32_t)std::min<uint64_t>(kDegBins - 1, (2 * g.m + n - 1) / n);
+  t = std::max(t, std::max(floor_t, 2u));
+  uint64_t count = 0;
+  for (uint32_t b = t; b < kDegBins; ++b) count += h[b];
+  if (count == 0 || t >= kDegBins) return cudaSuccess;
+  uint32_t* scan = nullptr;
+  e = graph_alloc(&scan, sizeof(uint32_t) * ((size_t)n + 1), s);
+  if (e == cudaSuccess) e = graph_alloc(&g.hot_idx, sizeof(uint32_t) * (size_t)n, s);
+  if (e == cudaSuccess) e = graph_alloc(&g.hot_list, sizeof(uint32_t) * count, s);
+  if (e == cudaSuccess) {
+    k_hot_flags<<<sms * 4, 256, 0, s>>>(g.xtdat, n, t, scan);
+    e = exclusive_scan_u32(scan, n + 1, s);
+  }
+  if (e == cudaSuccess) {
+    k_hot_index<<<sms * 4, 256, 0, s>>>(g.xtdat, n, t, scan, g.hot_idx, g.hot_list);
+    e = cudaGetLastError();
+  }
+  graph_free({scan});
+  if (e != cudaSuccess) {
+    free_hot(g);
+    return e;
+  }
+  g.hot_built = true;
+  g.hot_cap = cap;
+  g.hot_n = (uint32_t)count;
   return cudaSuccess;
 }
 
 cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
   const uint32_t n = g.n;
   free_chunks(g);
+  free_hot(g);
   if (!g.low_bm) {
     cudaError_t e = graph_alloc(&g.low_bm, sizeof(uint32_t) * (((size_t)n + 31) / 32 + 1), s);
     if (e != cudaSuccess) return e;

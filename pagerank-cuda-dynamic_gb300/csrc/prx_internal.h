@@ -78,6 +78,11 @@ constexpr int MODE_F32 = 0x20;
 struct ChunkLayout {
   uint32_t width = 0;             // vertices per source chunk, 0 = slot unused
   int K = 0;                      // number of chunks
+  // Edge ids of hot sources (see GraphDev::hot_idx) are stored as
+  // kHotFlag | (their index in the hot list): the sweep gathers those from
+  // the dense hot copy of the contributions instead of c[].
+  bool hot = false;
+  uint64_t stamp = 0;             // last use (the least recently used slot is rebuilt)
   uint32_t* off = nullptr;        // K x (n + 1) offsets into edg
   uint32_t* edg = nullptr;
   // graphs with row segments: one layout per segment (rows [k * 2^S, ...),
@@ -117,7 +122,18 @@ struct GraphDev {
   uint32_t* low_bm = nullptr;     // bitmap of the LOW class
   double* rcp = nullptr;          // RN(1 / outdeg) per vertex, for div_count
   float* rcp32 = nullptr;         // the same in FP32 (personalized PageRank sweeps)
-  ChunkLayout lay[2];             // cached chunk layouts (rebuilt after a batch)
+  ChunkLayout lay[3];             // cached chunk layouts (rebuilt after a batch)
+  // Hot sources: the vertices of largest out-degree (at most hot_cap of
+  // them, out-degree at least twice the average), numbered 0 .. hot_n-1 in
+  // id order.  Their contributions are copied after every sweep into a dense
+  // array of hot_n values that stays in L2; edges from them are gathered
+  // there (their values are the same, so sums are unchanged).  hot_idx[v] is
+  // v's number or kNotHot; built on first use per graph version.
+  uint32_t* hot_idx = nullptr;
+  uint32_t* hot_list = nullptr;
+  uint32_t hot_n = 0;
+  uint32_t hot_cap = 0;
+  bool hot_built = false;
   // edge weights (prx_graph_set_weights; dropped when a batch changes the edges)
   double* px = nullptr;           // P_uv = w_uv / W_u in out-CSR (xedg) order
   double* pt = nullptr;           // the same in in-CSR (xtedg) order
@@ -130,11 +146,21 @@ struct GraphDev {
 // Frees the edge weights of g (after a batch, or with the graph).
 void drop_weights(GraphDev& g);
 
+constexpr uint32_t kHotFlag = 0x80000000u;
+constexpr uint32_t kNotHot = 0xffffffffu;
+// The hot sources of g for a cap of `cap` vertices (0: none); graphs of 2^31
+// vertices or more get none (their ids use the flag bit).
+cudaError_t ensure_hot(GraphDev& g, uint32_t cap, int sms, cudaStream_t s);
+void free_hot(GraphDev& g);
+
 // Chunk layout of `width` vertices per chunk (built on first use, cached in
-// two slots; the layout of width `keep` is not evicted); width >= n means no
-// chunking (K = 1, *out = nullptr).
-cudaError_t ensure_chunks(GraphDev& g, uint32_t width, uint32_t keep, int sms, cudaStream_t s,
-                          const ChunkLayout** out);
+// three slots, the least recently used one rebuilt); width >= n means no
+// chunking: *out = nullptr, or with `single` a one-chunk layout of the LOW
+// rows' edges (non-LOW rows empty) when the graph has non-LOW rows.  `hot`:
+// ids of hot sources encoded (ensure_hot first; always a layout, even of
+// one chunk).
+cudaError_t ensure_chunks(GraphDev& g, uint32_t width, int sms, cudaStream_t s, const ChunkLayout** out,
+                          bool single = false, bool hot = false);
 void free_chunks(GraphDev& g);
 
 // Pointers a solve kernel needs.  Passed by value.
@@ -150,6 +176,9 @@ struct SolveArgs {
   const uint32_t* cls_list;       // static classes (see GraphDev)
   double* r[2];                   // FP64 ranks, ping-pong by iteration parity
   double* c[2];                   // FP64 contributions r/outdeg, ping-pong
+  double* ch[2];                  // dense copies of the hot sources' c[p] (GraphDev::hot_idx)
+  const uint32_t* hot_list;
+  uint32_t hot_n;
   uint32_t* bm[3];                // affected bitmaps: iteration k uses bm[k%3] (cur), bm[(k+1)%3] (next)
   uint32_t* naff;                 // bitmap of seeded sources (marking)
   uint32_t* list[2][NCLS];        // dynamic: affected MID / HIGH vertices queued per iteration (list[0])
@@ -170,6 +199,7 @@ struct SolveArgs {
   uint32_t n;
   uint32_t mid_max;
   uint32_t pull_threshold;        // expand by pulling when more than this many vertices changed by > D
+  int low_sweep;                  // LOW-class sweep of Static / ND / refinement (prx_options.low_sweep)
   double C0, P, D, C;
 };
 
@@ -189,6 +219,11 @@ void launch_commit_dyn32(const SolveArgs& a, int parity, cudaStream_t s);
 bool launch_update_class(const SolveArgs& a, const GraphDev& g, int mode, int cls, const ChunkLayout* lay, int sms,
                          cudaStream_t s);
 void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s);
+// ch[p] <- the hot sources' c[p] (parity < 0: the parity the running
+// iteration wrote); false when the solve uses no hot copy.
+bool launch_hot_copy(const SolveArgs& a, int parity, int sms, cudaStream_t s);
+// Hot-source cap when prx_options.hot_sources is 0: 32 MB of FP64 values.
+constexpr uint32_t kDefaultHotCap = 4u << 20;
 
 // ---- FP32 refinement (prx_refine.cu) --------------------------------------
 // FP64 residual sweep of one in-degree class (update kernels in MODE_REFINE64).
