@@ -287,7 +287,9 @@ def summarize(fp32, dfp, dynamic, grid, ppr, adj, big, ingest, tune):
     if ppr:
         out["ppr_rmat22_x64"] = {"fp64_ms": ppr["fp64"]["time_ms"], "fp32_refine_ms": ppr["fp32_refine"]["time_ms"],
                                  "speedup": ppr["speedup_fp32_refine_vs_fp64"],
-                                 "graph_launches": ppr["fp32_refine"].get("graph_launches"),
+                                 "graph_launches_per_solve": ppr["fp32_refine"].get("graph_launches"),
+                                 "fp32_refine_host_loop_ms": ppr.get("fp32_refine_host_loop_ms"),
+                                 "fp32_sweep_frac": ppr.get("fp32_sweep_frac"),
                                  "linf_fp32_refine_vs_fp64": ppr["linf_fp32_refine_vs_fp64"]}
     if adj:
         out["adjoint_rmat20"] = {"fd_max_rel_err": adj["fd_max_rel_err"], "fd_edges": sum(r["fd_edges"] for r in
@@ -506,6 +508,10 @@ def run_ppr(args, pg, ctx, local):
     n, m = len(xoff) - 1, len(xedg)
     g = pg.Graph(ctx, *xt)
     log(f"ppr graph: rmat{args.ppr_scale} n={n} m={m} in {time.perf_counter() - t:.1f}s")
+    t = time.perf_counter()
+    tune = pg.autotune_ppr(ctx, g)    # row split of the sweeps (untimed, like the upload)
+    tune["seconds"] = time.perf_counter() - t
+    log(f"ppr autotune: {tune}")
     rng = np.random.default_rng(args.seed)
     sizes = np.clip(np.exp(rng.uniform(0, np.log(1000), 64)).astype(np.int64), 1, 1000)
     seeds = [rng.integers(0, n, s) for s in sizes]
@@ -517,8 +523,18 @@ def run_ppr(args, pg, ctx, local):
         res = [pg.solve_ppr_batched_device(ctx, g, seeds, out.data_ptr(), o) for _ in range(2)]
         outs[name], runs[name] = out, res[-1]
     f64, f32 = runs["fp64"], runs["fp32_refine"]
+    # the same FP32-refined solve with the host-driven loop (no CUDA graph)
+    oh = pg.options(tolerance=1e-9, precision=pg.FP32_REFINE, loop=pg.LOOP_HOST)
+    host = [pg.solve_ppr_batched_device(ctx, g, seeds, outs["fp32_refine"].data_ptr(), oh) for _ in range(2)][-1]
     sweep64 = f64["time_ms"] / max(f64["fp64_sweeps"], 1)
-    est32 = (f32["time_ms"] - f32["fp64_sweeps"] * sweep64) / max(f32["fp32_sweeps"], 1)
+    # one FP32 correction sweep, timed: solves capped at 1 sweep (the FP64
+    # residual sweep) and at 21 (plus 20 FP32 sweeps), tolerance 0
+    out = torch.empty(n * 64, dtype=torch.float64, device=f"cuda:{local}")
+    def capped(k):
+        o = pg.options(tolerance=0.0, max_iterations=k, precision=pg.FP32_REFINE)
+        pg.solve_ppr_batched_device(ctx, g, seeds, out.data_ptr(), o)
+        return min(pg.solve_ppr_batched_device(ctx, g, seeds, out.data_ptr(), o)["time_ms"] for _ in range(3))
+    sweep32 = (capped(21) - capped(1)) / 20
     # FP32 correction sweep bytes: per edge index 4 + 256-byte row + rcp 4; per
     # vertex offsets 4 + rho, old and new correction rows 3 * 256
     b32 = m * (4 + 256 + 4) + n * (4 + 3 * 256)
@@ -526,12 +542,13 @@ def run_ppr(args, pg, ctx, local):
     res = {"workload": f"rmat{args.ppr_scale}: {n} vertices, {m} edges, 64 teleport vectors, seed sets "
                        "log-uniform in [1, 1000], tolerance 1e-9",
            "fp64": f64, "fp32_refine": f32, "speedup_fp32_refine_vs_fp64": f64["time_ms"] / f32["time_ms"],
+           "fp32_refine_host_loop_ms": host["time_ms"],
            "linf_fp32_refine_vs_fp64": float((outs["fp64"] - outs["fp32_refine"]).abs().max()),
            "vector_ge_s_fp64": 64 * m * f64["fp64_sweeps"] / (f64["time_ms"] / 1e3) / 1e9,
-           "fp64_sweep_ms": sweep64, "fp32_sweep_ms_est": est32,
-           "fp32_sweep_gbs_est": b32 / (est32 / 1e3) / 1e9 if est32 > 0 else None,
-           "fp32_sweep_frac_est": (b32 / (est32 / 1e3) / 1e9) / peak if est32 > 0 else None,
-           "peak_gbs": peak, "peak_source": peak_kind}
+           "fp64_sweep_ms": sweep64, "fp32_sweep_ms": sweep32,
+           "fp32_sweep_gbs": b32 / (sweep32 / 1e3) / 1e9 if sweep32 > 0 else None,
+           "fp32_sweep_frac": (b32 / (sweep32 / 1e3) / 1e9) / peak if sweep32 > 0 else None,
+           "peak_gbs": peak, "peak_source": peak_kind, "autotune": tune}
     g.close()
     return res
 

@@ -321,7 +321,12 @@ typedef struct {
   int      refinements;       /* FP64 residual sweeps (FP32_REFINE)         */
   float    time_ms;           /* device time of the solve (CUDA events)     */
   double   last_delta;        /* largest final L-inf change of a block      */
-  uint64_t kernel_launches;
+  uint64_t kernel_launches;   /* kernels run, inside the graphs included    */
+  uint64_t graph_launches;    /* CUDA graph launches: one per column block
+                                 with the default loop, 0 with PRX_LOOP_HOST */
+  uint32_t low_max;           /* rows of in-degree above this were cut ...  */
+  uint32_t seg_edges;         /* ... into segments of this many in-edges
+                                 (64 / 512, or prx_autotune_ppr's picks)    */
 } prx_ppr_result;
 
 /* Personalized PageRank of nvec teleport vectors on graph g.  Vector k
@@ -333,11 +338,31 @@ typedef struct {
  * o->tolerance, or o->max_iterations sweeps.  o->precision PRX_FP64 stores
  * and sums in FP64; PRX_FP32_REFINE runs the correction sweeps in FP32 with
  * FP64 residuals (the FP64 residual decides convergence).  Vectors are
- * solved 64 at a time.  ranks_out: n * nvec doubles in host memory,
- * vertex-major (ranks_out[v * nvec + k]).  Other options are ignored. */
+ * solved 64 at a time; each block's iteration loop is one CUDA graph launch
+ * (a conditional WHILE node, and for the refinement a nested one over each
+ * round's FP32 sweeps), or with o->loop = PRX_LOOP_HOST a host loop over the
+ * same kernels (the same results).  ranks_out: n * nvec doubles in host
+ * memory, vertex-major (ranks_out[v * nvec + k]).  Other options are
+ * ignored. */
 int prx_solve_ppr_batched(prx_context* ctx, prx_graph* g, uint32_t nvec,
                           const uint32_t* seed_off, const uint32_t* seeds,
                           const prx_options* o, double* ranks_out, prx_ppr_result* res);
+
+/* Picks of prx_autotune_ppr (no counterpart in the reference). */
+typedef struct {
+  uint32_t low_max;           /* rows up to this in-degree: one warp per vertex */
+  uint32_t seg_edges;         /* longer rows: segments of this many in-edges     */
+  float    ms_per_solve;      /* the winner's time for the trial solve           */
+  int      trials;            /* candidate pairs timed                           */
+} prx_ppr_tune_result;
+
+/* Times short FP32-refined batched solves on g (64 vectors; 1 FP64 and 5
+ * FP32 sweeps, best of two) over the warp-per-vertex bound (64, 256, 1024)
+ * and the segment width of longer rows (256, 512, 1024, 2048 in-edges), and
+ * keeps the fastest pair on g: later prx_solve_ppr_batched calls on g use it
+ * (results change only by rounding: the sums' grouping follows the split).
+ * Not for graphs with row segments (PRX_ERANGE). */
+int prx_autotune_ppr(prx_context* ctx, prx_graph* g, prx_ppr_tune_result* out);
 
 /* The same with ranks_out in device memory (seeds stay host arrays). */
 int prx_solve_ppr_batched_device(prx_context* ctx, prx_graph* g, uint32_t nvec,

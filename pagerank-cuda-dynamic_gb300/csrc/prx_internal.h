@@ -58,6 +58,7 @@ struct State {
   unsigned int el32_bits[2];      // L-inf change of the FP32 sweep with parity k32 & 1 (bits of a float >= 0)
   unsigned int e32max_bits[2];    // L-inf of the correction it produced (personalized PageRank)
   int graph_rounds;               // bodies run by the CUDA-graph loop (its own bound)
+  int graph_inner;                // bodies of a nested graph loop in the current outer body
 };
 
 // Internal mode of the update kernels: the FP64 residual sweep of the FP32
@@ -134,6 +135,10 @@ struct GraphDev {
   uint32_t hot_n = 0;
   uint32_t hot_cap = 0;
   bool hot_built = false;
+  // batched personalized PageRank picks of prx_autotune_ppr (0: defaults):
+  // rows of in-degree above ppr_low_max are cut into ppr_seg-edge segments
+  uint32_t ppr_low_max = 0;
+  uint32_t ppr_seg = 0;
   // edge weights (prx_graph_set_weights; dropped when a batch changes the edges)
   double* px = nullptr;           // P_uv = w_uv / W_u in out-CSR (xedg) order
   double* pt = nullptr;           // the same in in-CSR (xtedg) order

@@ -172,6 +172,7 @@ __global__ void k_state_reset(State* st, int max_iter, double tol) {
   st->el32_bits[0] = st->el32_bits[1] = 0;
   st->e32max_bits[0] = st->e32max_bits[1] = 0;
   st->graph_rounds = 0;
+  st->graph_inner = 0;
 }
 
 // ---- launchers ------------------------------------------------------------------

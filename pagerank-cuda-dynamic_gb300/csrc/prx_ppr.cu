@@ -23,11 +23,20 @@
 //    below 2^-18 of the correction's size (FP32 cannot resolve more), or at
 //    the iteration cap.
 //
-// In-degree <= 64 rows: one warp per vertex.  Longer rows are cut into
-// segments of kSeg in-edges; a block sums a segment (warp w a contiguous
-// eighth of it) into a partial row, and a warp per long vertex adds its
-// segments' partials in order and finishes the vertex.  Every sum has a fixed
-// order, so results are deterministic.
+// Rows of in-degree up to low_max (64 by default): one warp per vertex.
+// Longer rows are cut into segments of `seg` in-edges (512 by default); a
+// block sums a segment (warp w a contiguous eighth of it) into a partial
+// row, and a warp per long vertex adds its segments' partials in order and
+// finishes the vertex.  Every sum has a fixed order for given low_max / seg,
+// so results are deterministic; prx_autotune_ppr picks both per graph.
+//
+// Loop: by default the whole iteration loop of a column block is one CUDA
+// graph launch -- a conditional WHILE node over FP64 sweeps, and for the
+// refinement a nested WHILE node over the FP32 correction sweeps of each
+// round -- whose condition kernels read the device control block, so the
+// host waits once per block; prx_options.loop = PRX_LOOP_HOST runs the same
+// kernels from a host loop that reads the control block back between batches
+// of sweeps.  Both run the same kernels in the same order (same results).
 #include <algorithm>
 #include <vector>
 #include "prx_ctx.h"
@@ -36,7 +45,7 @@
 namespace prx {
 
 constexpr int kCols = 64;         // vectors per column block
-constexpr uint32_t kSeg = 512;    // in-edges per segment of a long row
+constexpr uint32_t kSeg = 512;    // default in-edges per segment of a long row
 constexpr int kSegWarps = 8;      // warps per segment block
 
 enum PprMode { PPR_J64 = 0, PPR_R64 = 1, PPR_S32 = 2 };
@@ -54,6 +63,8 @@ struct PprWs {
   size_t seg_cap = 0;
   uint32_t* segstart = nullptr;        // first segment of each long vertex (+ total)
   size_t segstart_cap = 0;
+  uint32_t* big = nullptr;             // vertices above a low_max other than 64, and their scan
+  size_t big_cap = 0;
   uint32_t* toff = nullptr;            // teleport entries by vertex: offsets (n+1)
   uint32_t* tent = nullptr;            // entries: vertex, column (sorted)
   double* tmass = nullptr;             // entry mass 1/|S_k|
@@ -73,6 +84,7 @@ void ppr_free(PprWs* w) {
   cudaFree(w->part);
   cudaFree(w->seg);
   cudaFree(w->segstart);
+  cudaFree(w->big);
   cudaFree(w->toff);
   cudaFree(w->tent);
   cudaFree(w->tmass);
@@ -91,8 +103,10 @@ struct PprArgs {
   double* x[2];
   float* rho;
   float* e[2];
-  const uint32_t* big;            // vertices with in-degree > 64, ascending within class
+  const uint32_t* big;            // vertices with in-degree > low_max
   uint32_t nbig;
+  uint32_t low_max;               // rows up to this in-degree: one warp per vertex
+  uint32_t seg;                   // in-edges per segment of a longer row (a multiple of kSegWarps)
   const uint32_t* segstart;       // [nbig + 1]
   const uint32_t* seg_v;
   const uint32_t* seg_e;
@@ -219,7 +233,7 @@ __global__ void __launch_bounds__(256) k_ppr_low(PprArgs a) {
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < a.n; v += warps) {
     const uint32_t s = __ldg(a.xtoff + v), e = __ldg(a.xtoff + v + 1);
-    if (e - s > kLowMax) continue;
+    if (e - s > a.low_max) continue;
     V2 acc;
     acc.x = 0;
     acc.y = 0;
@@ -245,8 +259,8 @@ __global__ void __launch_bounds__(kSegWarps * 32) k_ppr_seg(PprArgs a) {
   V2* part = reinterpret_cast<V2*>(a.part);
   for (uint32_t g = blockIdx.x; g < a.nseg; g += gridDim.x) {
     const uint32_t v = a.seg_v[g], s0 = a.seg_e[g];
-    const uint32_t end = min(s0 + kSeg, a.xtoff[v + 1]);
-    const uint32_t per = kSeg / kSegWarps;
+    const uint32_t end = min(s0 + a.seg, a.xtoff[v + 1]);
+    const uint32_t per = a.seg / kSegWarps;
     const uint32_t s = min(s0 + w * per, end), e = min(s + per, end);
     V2 acc;
     acc.x = 0;
@@ -336,12 +350,31 @@ __global__ void k_ppr_fin32(State* st) {  // refinement: FP32 correction sweep
   if (dl < (float)st->tol || dl < em * 0x1p-18f || st->iter >= st->max_iter) st->inner_done = 1;
 }
 
-// x_b += e (the correction of the last FP32 sweep).
+// x_b += e (the correction of the last FP32 sweep); nothing once the solve
+// is done (the graph loop reaches it after a converged FP64 sweep).
 __global__ void k_ppr_commit(PprArgs a) {
+  if (a.st->done) return;
   const float* __restrict__ e = a.e[a.st->k32 & 1];
   const size_t total = (size_t)a.n * kCols;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
     a.x[0][i] += (double)e[i];
+}
+
+// Conditions of the graph-launched loops.  Each counts its own bodies and
+// stops after `cap` of them whatever the other kernels did, so the loops end
+// even if a finalize kernel never ran.
+__global__ void k_ppr_cond(cudaGraphConditionalHandle h, State* st, int cap, int refine) {
+  const int rounds = ++st->graph_rounds;
+  const bool more = !st->done && (!refine || st->iter < st->max_iter) && rounds < cap;
+  cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+__global__ void k_ppr_arm_inner(cudaGraphConditionalHandle h, State* st) {
+  st->graph_inner = 0;
+  cudaGraphSetConditional(h, (!st->done && !st->inner_done) ? 1u : 0u);
+}
+__global__ void k_ppr_cond_inner(cudaGraphConditionalHandle h, State* st, int cap) {
+  const int rounds = ++st->graph_inner;
+  cudaGraphSetConditional(h, (!st->done && !st->inner_done && rounds < cap) ? 1u : 0u);
 }
 
 // ---- setup ---------------------------------------------------------------------
@@ -364,23 +397,35 @@ __global__ void k_ppr_init(PprArgs a) {
     for (uint32_t i = a.toff[v]; i < a.toff[v + 1]; ++i) a.x[0][(size_t)v * kCols + a.tcol[i]] += a.tmass[i];
 }
 
-// Segment counts of the long vertices (ceil(indeg / kSeg)), then the segments.
+// Segment counts of the long vertices (ceil(indeg / seg)), then the segments.
 __global__ void k_ppr_segcount(const uint32_t* __restrict__ xtoff, const uint32_t* __restrict__ big, uint32_t nbig,
-                               uint32_t* __restrict__ cnt) {
+                               uint32_t seg, uint32_t* __restrict__ cnt) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nbig; i += gridDim.x * blockDim.x) {
     const uint32_t v = big[i];
-    cnt[i] = (xtoff[v + 1] - xtoff[v] + kSeg - 1) / kSeg;
+    cnt[i] = (xtoff[v + 1] - xtoff[v] + seg - 1) / seg;
   }
 }
 
+// Vertices of in-degree above t: flags (n + 1 entries, the last 0) for the
+// scan, then the ascending list.
+__global__ void k_ppr_bigflags(const uint32_t* __restrict__ xtoff, uint32_t n, uint32_t t, uint32_t* __restrict__ f) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += gridDim.x * blockDim.x)
+    f[v] = v < n && xtoff[v + 1] - xtoff[v] > t ? 1u : 0u;
+}
+__global__ void k_ppr_biglist(const uint32_t* __restrict__ xtoff, uint32_t n, uint32_t t,
+                              const uint32_t* __restrict__ pos, uint32_t* __restrict__ big) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    if (xtoff[v + 1] - xtoff[v] > t) big[pos[v]] = v;
+}
+
 __global__ void k_ppr_segfill(const uint32_t* __restrict__ xtoff, const uint32_t* __restrict__ big, uint32_t nbig,
-                              const uint32_t* __restrict__ start, uint32_t* __restrict__ seg_v,
+                              uint32_t seg, const uint32_t* __restrict__ start, uint32_t* __restrict__ seg_v,
                               uint32_t* __restrict__ seg_e) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nbig; i += gridDim.x * blockDim.x) {
     const uint32_t v = big[i];
     for (uint32_t g = start[i], k = 0; g < start[i + 1]; ++g, ++k) {
       seg_v[g] = v;
-      seg_e[g] = xtoff[v] + k * kSeg;
+      seg_e[g] = xtoff[v] + k * seg;
     }
   }
 }
@@ -454,25 +499,38 @@ static int ppr_ws(prx_context* c, uint32_t n, bool fp32) {
   return PRX_OK;
 }
 
-// Segments of the long rows of graph g into the workspace; returns the counts.
+// The long rows of graph g (in-degree above a.low_max) and their segments of
+// a.seg edges into the workspace; returns the counts.
 static int ppr_segments(prx_context* c, const GraphDev& g, PprArgs& a) {
   PprWs& w = *c->ppr;
   cudaStream_t s = c->stream;
-  const uint32_t nbig = g.cls_begin[NCLS] - g.cls_begin[MID];
-  a.big = g.cls_list + g.cls_begin[MID];
+  uint32_t nbig = 0;
+  if (a.low_max == kLowMax) {  // the graph's MID and HIGH classes
+    nbig = g.cls_begin[NCLS] - g.cls_begin[MID];
+    a.big = g.cls_list + g.cls_begin[MID];
+  } else {
+    TRY_CUDA_ST(grow(&w.big, w.big_cap, 2 * ((size_t)g.n + 1)));
+    uint32_t* pos = w.big + g.n + 1;
+    k_ppr_bigflags<<<grid_for((uint64_t)g.n + 1, 256, c->sms * 16), 256, 0, s>>>(g.xtoff, g.n, a.low_max, pos);
+    TRY_CUDA_ST(exclusive_scan_u32(pos, g.n + 1, s));
+    k_ppr_biglist<<<grid_for(g.n, 256, c->sms * 16), 256, 0, s>>>(g.xtoff, g.n, a.low_max, pos, w.big);
+    TRY_CUDA_ST(cudaMemcpyAsync(&nbig, pos + g.n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    TRY_CUDA_ST(cudaStreamSynchronize(s));
+    a.big = w.big;
+  }
   a.nbig = nbig;
   a.nseg = 0;
   if (!nbig) return PRX_OK;
   TRY_CUDA_ST(grow(&w.segstart, w.segstart_cap, (size_t)nbig + 1));
   const int grid = grid_for(nbig, 256, c->sms * 4);
-  k_ppr_segcount<<<grid, 256, 0, s>>>(g.xtoff, a.big, nbig, w.segstart);
+  k_ppr_segcount<<<grid, 256, 0, s>>>(g.xtoff, a.big, nbig, a.seg, w.segstart);
   TRY_CUDA_ST(exclusive_scan_u32(w.segstart, nbig + 1, s));
   uint32_t nseg = 0;
   TRY_CUDA_ST(cudaMemcpyAsync(&nseg, w.segstart + nbig, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   TRY_CUDA_ST(cudaStreamSynchronize(s));
   TRY_CUDA_ST(grow(&w.seg, w.seg_cap, 2 * (size_t)nseg));
   TRY_CUDA_ST(grow(&w.part, w.part_cap, (size_t)nseg * kCols));
-  k_ppr_segfill<<<grid, 256, 0, s>>>(g.xtoff, a.big, nbig, w.segstart, w.seg, w.seg + nseg);
+  k_ppr_segfill<<<grid, 256, 0, s>>>(g.xtoff, a.big, nbig, a.seg, w.segstart, w.seg, w.seg + nseg);
   a.segstart = w.segstart;
   a.seg_v = w.seg;
   a.seg_e = w.seg + nseg;
@@ -525,6 +583,106 @@ static int ppr_check(prx_context* c) {
   return PRX_OK;
 }
 
+// The iteration loop of one column block as one CUDA graph launch (see the
+// file comment); on return st_host[1] holds the control block.  Kernel
+// launches inside the graph are counted into *body_launches from the
+// control block (FP64 sweeps, FP32 sweeps).
+static int ppr_block_graph(prx_context* c, PprArgs& a, const prx_options& o, bool fp32, uint64_t* body_launches) {
+  cudaStream_t s = c->stream, s2 = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int st = PRX_OK;
+  const int cap = (o.max_iterations < (1 << 30) ? o.max_iterations : (1 << 30)) + 2;
+  uint64_t sweep_l = 0, sweep32_l = 0;
+  cudaError_t e = cudaGraphCreate(&graph, 0);
+  cudaGraphConditionalHandle ho{}, hi{};
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&ho, graph, 1, cudaGraphCondAssignDefault);
+  cudaGraphNodeParams p{};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = ho;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (e == cudaSuccess) e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &p);
+  if (e == cudaSuccess && fp32) e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(s, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                          cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t ec = cudaSuccess;
+    if (!fp32) {
+      ppr_sweep<PPR_J64>(a, c->sms, s, sweep_l);
+      k_ppr_fin64<<<1, 1, 0, s>>>(a.st);
+      k_ppr_cond<<<1, 1, 0, s>>>(ho, a.st, cap, 0);
+    } else {
+      // the inner handle belongs to the outer body, the graph being captured
+      cudaStreamCaptureStatus cs;
+      cudaGraph_t body = nullptr;
+      const cudaGraphNode_t* deps = nullptr;
+      const cudaGraphEdgeData* edata = nullptr;
+      size_t ndeps = 0;
+      ec = cudaStreamGetCaptureInfo(s, &cs, nullptr, &body, nullptr, nullptr, nullptr);
+      if (ec == cudaSuccess) ec = cudaGraphConditionalHandleCreate(&hi, body, 0, 0);
+      if (ec == cudaSuccess) {
+        ppr_sweep<PPR_R64>(a, c->sms, s, sweep_l);
+        k_ppr_fin_r64<<<1, 1, 0, s>>>(a.st);
+        k_ppr_arm_inner<<<1, 1, 0, s>>>(hi, a.st);
+        ec = cudaStreamGetCaptureInfo(s, &cs, nullptr, &body, &deps, &edata, &ndeps);
+      }
+      cudaGraphNodeParams pi{};
+      pi.type = cudaGraphNodeTypeConditional;
+      pi.conditional.handle = hi;
+      pi.conditional.type = cudaGraphCondTypeWhile;
+      pi.conditional.size = 1;
+      cudaGraphNode_t inode;
+      if (ec == cudaSuccess) ec = cudaGraphAddNode(&inode, body, deps, edata, ndeps, &pi);
+      if (ec == cudaSuccess) ec = cudaStreamUpdateCaptureDependencies(s, &inode, nullptr, 1,
+                                                                      cudaStreamSetCaptureDependencies);
+      // the FP32 sweeps of a round: the inner body, captured on a second stream
+      if (ec == cudaSuccess) ec = cudaStreamBeginCaptureToGraph(s2, pi.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                                cudaStreamCaptureModeThreadLocal);
+      if (ec == cudaSuccess) {
+        ppr_sweep<PPR_S32>(a, c->sms, s2, sweep32_l);
+        k_ppr_fin32<<<1, 1, 0, s2>>>(a.st);
+        k_ppr_cond_inner<<<1, 1, 0, s2>>>(hi, a.st, cap);
+        const cudaError_t el = cudaGetLastError();
+        cudaGraph_t inner = nullptr;
+        ec = cudaStreamEndCapture(s2, &inner);
+        if (ec == cudaSuccess) ec = el;
+      }
+      if (ec == cudaSuccess) {
+        k_ppr_commit<<<grid_for((size_t)a.n * kCols, 256, c->sms * 16), 256, 0, s>>>(a);
+        k_ppr_cond<<<1, 1, 0, s>>>(ho, a.st, cap, 1);
+      }
+    }
+    const cudaError_t el = cudaGetLastError();
+    cudaGraph_t captured = nullptr;
+    e = cudaStreamEndCapture(s, &captured);  // always leave capture mode
+    if (e == cudaSuccess) e = ec;
+    if (e == cudaSuccess) e = el;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    set_error(std::string("prx_solve_ppr_batched (graph loop): ") + cudaGetErrorString(e));
+    st = e == cudaErrorMemoryAllocation ? PRX_ENOMEM : PRX_ECUDA;
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (s2) cudaStreamDestroy(s2);
+  if (!st) {
+    const State& h = c->st_host[1];
+    if (!fp32) {
+      *body_launches = (uint64_t)h.iter * (sweep_l + 2);
+    } else {
+      const uint64_t n64 = (uint64_t)h.rounds, n32 = (uint64_t)(h.iter - h.rounds);
+      *body_launches = n64 * (sweep_l + 5) + n32 * (sweep32_l + 2);
+    }
+  }
+  return st;
+}
+
 // One column block; the answer's FP64 rows are left in *answer.
 static int ppr_block(prx_context* c, const GraphDev& g, PprArgs& a, const prx_options& o, bool fp32,
                      const double** answer, prx_ppr_result* res) {
@@ -536,6 +694,25 @@ static int ppr_block(prx_context* c, const GraphDev& g, PprArgs& a, const prx_op
   launch_state_reset(c->st, o.max_iterations, o.tolerance, s);
   L += 2;
   int st;
+  if (o.loop != PRX_LOOP_HOST && o.max_iterations > 0) {
+    uint64_t body = 0;
+    if ((st = ppr_block_graph(c, a, o, fp32, &body))) return st;
+    L += body;
+    res->graph_launches += 1;
+    const State& h = c->st_host[1];
+    if (!fp32) {
+      *answer = a.x[h.iter & 1];
+      res->fp64_sweeps += h.iter;
+    } else {
+      *answer = h.done ? a.x[1] : a.x[0];  // a converged (or capped) FP64 sweep, else the committed base
+      res->fp64_sweeps += h.rounds;
+      res->fp32_sweeps += h.iter - h.rounds;
+      res->refinements += h.rounds;
+    }
+    res->iterations = std::max(res->iterations, h.iter);
+    res->last_delta = std::max(res->last_delta, h.last_delta);
+    return PRX_OK;
+  }
   if (!fp32) {
     if (o.max_iterations > 0) {
       for (int k = 1;; k = std::min(2 * k, 16)) {
@@ -642,6 +819,10 @@ static int ppr_common(prx_context* c, prx_graph* gr, uint32_t nvec, const uint32
   a.n = g.n;
   a.P = o.damping;
   a.Q = 1.0 - o.damping;
+  a.low_max = g.ppr_low_max ? g.ppr_low_max : kLowMax;
+  a.seg = g.ppr_seg ? g.ppr_seg : kSeg;
+  r.low_max = a.low_max;
+  r.seg_edges = a.seg;
   if ((st = ppr_segments(c, g, a))) return st;
   double* out = ranks_out;
   const size_t total = (size_t)g.n * nvec;
@@ -682,6 +863,73 @@ int prx_solve_ppr_batched_device(prx_context* c, prx_graph* gr, uint32_t nvec, c
                                  const uint32_t* seeds, const prx_options* o, double* ranks_out,
                                  prx_ppr_result* res) {
   return ppr_common(c, gr, nvec, seed_off, seeds, o, ranks_out, res, true);
+}
+
+// Times short FP32-refined solves (64 teleport vectors of one seed each, 1
+// FP64 and 5 FP32 sweeps, best of two) over the warp-per-vertex bound
+// (64, 256, 1024) and the segment width (256, 512, 1024, 2048 in-edges), and
+// keeps the fastest pair on the graph for its later solves.
+int prx_autotune_ppr(prx_context* c, prx_graph* gr, prx_ppr_tune_result* out) {
+  if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_autotune_ppr: bad context or graph");
+  GraphDev& g = gr->g;
+  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_autotune_ppr: not for graphs with row segments (64-bit offsets)");
+  prx_ppr_tune_result best{};
+  if (g.n == 0) {
+    if (out) *out = best;
+    return PRX_OK;
+  }
+  TRY_CUDA_ST(cudaSetDevice(c->device));
+  const uint32_t nvec = kCols;
+  std::vector<uint32_t> off(nvec + 1), seeds(nvec);
+  for (uint32_t k = 0; k < nvec; ++k) {
+    off[k] = k;
+    seeds[k] = (uint32_t)((uint64_t)k * g.n / nvec);
+  }
+  off[nvec] = nvec;
+  double* ranks = nullptr;
+  TRY_CUDA_ST(cudaMalloc(&ranks, sizeof(double) * (size_t)g.n * nvec));
+  prx_options o;
+  prx_options_default(&o);
+  o.precision = PRX_FP32_REFINE;
+  o.tolerance = 0.0;
+  o.max_iterations = 6;
+  const uint32_t lows[] = {64, 256, 1024}, segs[] = {256, 512, 1024, 2048};
+  const uint32_t keep_low = g.ppr_low_max, keep_seg = g.ppr_seg;
+  float best_ms = 0;
+  int trials = 0, st = PRX_OK;
+  for (uint32_t lo : lows) {
+    for (uint32_t sg : segs) {
+      g.ppr_low_max = lo;
+      g.ppr_seg = sg;
+      float ms = 0;
+      for (int rep = 0; rep < 2 && !st; ++rep) {
+        prx_ppr_result r{};
+        st = ppr_common(c, gr, nvec, off.data(), seeds.data(), &o, ranks, &r, true);
+        if (!st && (rep == 0 || r.time_ms < ms)) ms = r.time_ms;
+      }
+      if (st) break;
+      ++trials;
+      if (!best.trials || ms < best_ms) {
+        best_ms = ms;
+        best.low_max = lo;
+        best.seg_edges = sg;
+        best.trials = 1;
+      }
+    }
+    if (st) break;
+  }
+  cudaFree(ranks);
+  if (st) {
+    g.ppr_low_max = keep_low;
+    g.ppr_seg = keep_seg;
+    return st;
+  }
+  g.ppr_low_max = best.low_max;
+  g.ppr_seg = best.seg_edges;
+  best.ms_per_solve = best_ms;
+  best.trials = trials;
+  if (out) *out = best;
+  return PRX_OK;
 }
 
 }  // extern "C"

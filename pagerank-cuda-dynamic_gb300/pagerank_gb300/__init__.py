@@ -7,7 +7,7 @@ from ._lib import (DYNAMIC_FRONTIER, DYNAMIC_TRAVERSAL, FP32_REFINE, FP64, LOOP_
                    NAIVE_DYNAMIC, PRUNE_DYNAMIC_FRONTIER, STATIC, PrxError, library_path, load)
 from .api import (Context, Graph, mark_affected, options, pagerank_dynamic_frontier, pagerank_dynamic_traversal,
                   pagerank_naive_dynamic, pagerank_prune_dynamic_frontier, pagerank_static, release_cached_memory,
-                  l2_fetch_granularity, graph_pool_stats, selftest_division, solve, autotune,
+                  l2_fetch_granularity, graph_pool_stats, selftest_division, solve, autotune, autotune_ppr,
                   solve_device, solve_ppr_batched, solve_ppr_batched_device)
 from . import graphs
 

@@ -48,7 +48,16 @@ class PprResult(C.Structure):
     """prx_ppr_result (batched personalized PageRank; no counterpart in the reference)."""
     _fields_ = [("iterations", C.c_int), ("fp64_sweeps", C.c_int), ("fp32_sweeps", C.c_int),
                 ("refinements", C.c_int), ("time_ms", C.c_float), ("last_delta", C.c_double),
-                ("kernel_launches", C.c_uint64)]
+                ("kernel_launches", C.c_uint64), ("graph_launches", C.c_uint64), ("low_max", C.c_uint32),
+                ("seg_edges", C.c_uint32)]
+
+    as_dict = Result.as_dict
+
+
+class PprTuneResult(C.Structure):
+    """prx_ppr_tune_result (personalized PageRank thresholds; no counterpart in the reference)."""
+    _fields_ = [("low_max", C.c_uint32), ("seg_edges", C.c_uint32), ("ms_per_solve", C.c_float),
+                ("trials", C.c_int)]
 
     as_dict = Result.as_dict
 
@@ -82,7 +91,7 @@ EXPORTS = (
     "prx_graph_download",
     "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_selftest_division",
     "prx_solve_ppr_batched", "prx_solve_ppr_batched_device", "prx_graph_set_weights", "prx_solve_weighted",
-    "prx_adjoint", "prx_autotune", "prx_graph_tidy_batch", "prx_graph_create_from_edges",
+    "prx_adjoint", "prx_autotune", "prx_autotune_ppr", "prx_graph_tidy_batch", "prx_graph_create_from_edges",
     "prx_graph_create_from_edges_device", "prx_graph_gen_batch",
     "prx_edge_reader_open", "prx_edge_reader_next", "prx_edge_reader_close", "prx_read_mtx", "prx_format_glog",
     "prx_graph_create_from_text", "prx_edge_reader_next_graph", "prx_graph_create_from_mtx", "prx_format_edges",
@@ -136,6 +145,7 @@ def load(build_if_missing=True):
                                                C.POINTER(PprResult)]),
         "prx_graph_set_weights": (i32, [vp, vp, vp]),
         "prx_autotune": (i32, [vp, vp, C.c_char_p, C.POINTER(TuneResult)]),
+        "prx_autotune_ppr": (i32, [vp, vp, C.POINTER(PprTuneResult)]),
         "prx_graph_tidy_batch": (i32, [vp, vp, vp, vp, u64, vp, vp, u64, vp, vp, C.POINTER(u64), vp, vp,
                                        C.POINTER(u64)]),
         "prx_graph_create_from_edges": (i32, [vp, C.c_uint32, vp, vp, u64, i32, C.POINTER(vp)]),

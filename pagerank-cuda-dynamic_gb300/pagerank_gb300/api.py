@@ -362,6 +362,15 @@ def autotune(ctx, g, cache_path=None):
     return res.as_dict()
 
 
+def autotune_ppr(ctx, g):
+    """Pick the batched personalized PageRank row split of g (warp-per-vertex
+    bound, segment width) by trial solves (prx_autotune_ppr) -> dict."""
+    from ._lib import PprTuneResult
+    res = PprTuneResult()
+    check(load().prx_autotune_ppr(ctx.handle, g.handle, C.byref(res)), "prx_autotune_ppr")
+    return res.as_dict()
+
+
 def selftest_division(ctx, dmax, per):
     """Mismatches of the solvers' reciprocal division against IEEE a / d."""
     bad = C.c_uint64(0)

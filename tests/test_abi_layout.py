@@ -11,7 +11,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 STRUCTS = {"prx_options": "Options", "prx_result": "Result", "prx_ppr_result": "PprResult",
-           "prx_tune_result": "TuneResult", "prx_host_csr": "HostCsr"}
+           "prx_tune_result": "TuneResult", "prx_ppr_tune_result": "PprTuneResult", "prx_host_csr": "HostCsr"}
 
 
 @pytest.fixture(scope="module")

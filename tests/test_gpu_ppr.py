@@ -113,3 +113,43 @@ def test_ppr_caps_and_errors(pg, ctx):
         pg.solve_ppr_batched(ctx, g, [])
     assert e.value.status == 1
     g.close()
+
+
+@pytest.mark.parametrize("kind,nvec", [("rmat12", 64), ("hubs", 70), ("web20k", 33)])
+def test_ppr_graph_loop_equals_host_loop(pg, ctx, kind, nvec):
+    # the iteration loop of a block as one CUDA graph launch (a WHILE node,
+    # and for the refinement a nested WHILE node over each round's FP32
+    # sweeps) runs the host loop's kernels in the same order: bit-identical
+    # ranks and equal sweep counts, also when the iteration cap stops a round
+    g, xt = _graph(pg, ctx, kind)
+    n = len(xt[0]) - 1
+    seeds = _seeds(n, nvec, 41)
+    blocks = (nvec + 63) // 64
+    for prec in (pg.FP64, pg.FP32_REFINE):
+        for cap in (500, 1, 2, 7):
+            kw = dict(tolerance=1e-10, precision=prec, max_iterations=cap)
+            host, rh = pg.solve_ppr_batched(ctx, g, seeds, pg.options(loop=pg.LOOP_HOST, **kw))
+            got, rg = pg.solve_ppr_batched(ctx, g, seeds, pg.options(**kw))
+            np.testing.assert_array_equal(got, host, err_msg=f"{kind} prec={prec} cap={cap}")
+            for k in ("iterations", "fp64_sweeps", "fp32_sweeps", "refinements"):
+                assert rg[k] == rh[k], (k, kind, prec, cap)
+            assert rg["graph_launches"] == blocks and rh["graph_launches"] == 0
+    g.close()
+
+
+@pytest.mark.parametrize("kind", ["hubs", "web20k"])
+def test_ppr_autotuned_split(pg, ctx, kind):
+    # prx_autotune_ppr keeps a (warp-per-vertex bound, segment width) pair on
+    # the graph; every split gives the oracle's answer to rounding
+    g, xt = _graph(pg, ctx, kind)
+    n = len(xt[0]) - 1
+    seeds = _seeds(n, 20, 43)
+    want, its = PO.jacobi(*xt, seeds, tol=1e-10)
+    pick = pg.autotune_ppr(ctx, g)
+    assert pick["low_max"] in (64, 256, 1024) and pick["seg_edges"] in (256, 512, 1024, 2048)
+    assert pick["trials"] == 12
+    got, res = pg.solve_ppr_batched(ctx, g, seeds, pg.options(tolerance=1e-10))
+    assert (res["low_max"], res["seg_edges"]) == (pick["low_max"], pick["seg_edges"])
+    assert res["iterations"] == max(its)
+    assert np.abs(got - want).max() <= 1e-12
+    g.close()
