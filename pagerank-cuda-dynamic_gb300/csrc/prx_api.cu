@@ -124,6 +124,7 @@ int prx_context_destroy(prx_context* c) {
     if (e) cudaEventDestroy(e);
   for (auto& e : c->tev) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   delete c;
   return PRX_OK;
 }
@@ -517,7 +518,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   // 48 MB chunks.
   const uint32_t w64 = o.chunk_vertices ? o.chunk_vertices
                       : g.tuned_w64          ? g.tuned_w64
-                                             : (200u << 20) / sizeof(double);
+                                             : kDefaultChunk64;
   const uint32_t w32 = o.chunk_vertices ? o.chunk_vertices
                       : g.tuned_w32          ? g.tuned_w32
                                              : (48u << 20) / sizeof(float);
@@ -721,19 +722,67 @@ int prx_graph_create(prx_context* c, uint32_t n, uint64_t m, const uint32_t* xof
   g.m = m;
   g.m_cap = m;
   cudaStream_t s = c->stream;
-  auto upload = [&](uint32_t** dst, const uint32_t* src, size_t cnt, size_t slots = 0) -> cudaError_t {
-    cudaError_t e = graph_alloc(dst, sizeof(uint32_t) * (slots > cnt ? slots : (cnt ? cnt : 1)), s);
-    if (e == cudaSuccess && cnt) e = cudaMemcpyAsync(*dst, src, sizeof(uint32_t) * cnt, cudaMemcpyHostToDevice, s);
-    return e;
+  // The in-edges go up on a copy stream in row-range pieces; meanwhile the
+  // degree classes, the hot sources and the default LOW layout are built on
+  // the context's stream, each piece's part of the layout as soon as that
+  // piece has landed.  The out-CSR (dynamic modes) follows the in-edges.
+  auto alloc = [&](uint32_t** dst, size_t cnt, size_t slots = 0) -> cudaError_t {
+    return graph_alloc(dst, sizeof(uint32_t) * (slots > cnt ? slots : (cnt ? cnt : 1)), s);
   };
-  cudaError_t e = upload(&g.xtoff, xtoff, (size_t)n + 1);
-  if (e == cudaSuccess) e = upload(&g.xtedg, xtedg, m, edge_slots(m));
-  if (e == cudaSuccess) e = upload(&g.xtdat, xtdat, n);
-  if (e == cudaSuccess && xoff) e = upload(&g.xoff, xoff, (size_t)n + 1);
-  if (e == cudaSuccess && xoff) e = upload(&g.xedg, xedg, m);
+  cudaError_t e = alloc(&g.xtoff, (size_t)n + 1);
+  if (e == cudaSuccess) e = alloc(&g.xtedg, m, edge_slots(m));
+  if (e == cudaSuccess) e = alloc(&g.xtdat, n);
+  if (e == cudaSuccess && xoff) e = alloc(&g.xoff, (size_t)n + 1);
+  if (e == cudaSuccess && xoff) e = alloc(&g.xedg, m);
+  if (e == cudaSuccess && !c->copy_stream) e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+  constexpr int kMaxPieces = 8;
+  const int pieces = (int)std::max<uint64_t>(1, std::min<uint64_t>(kMaxPieces, m >> 24));
+  uint32_t rows[kMaxPieces + 1];
+  rows[0] = 0;
+  for (int p = 1; p < pieces; ++p) {  // piece p starts at the first row whose edges reach p/pieces of m (32-row steps)
+    const uint64_t want = m * (uint64_t)p / pieces;
+    uint32_t lo = rows[p - 1], hi = n;
+    while (lo < hi) {
+      const uint32_t mid = lo + (hi - lo) / 2;
+      if (xtoff[mid] < want) lo = mid + 1; else hi = mid;
+    }
+    rows[p] = std::max(rows[p - 1], lo & ~31u);
+  }
+  rows[pieces] = n;
+  cudaEvent_t ev[kMaxPieces + 3] = {};
+  for (int i = 0; i < pieces + 3 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming);
+  cudaEvent_t ev_alloc = ev[pieces], ev_meta = ev[pieces + 1], ev_done = ev[pieces + 2];
+  cudaStream_t cs = c->copy_stream;
+  auto h2d = [&](uint32_t* dst, const uint32_t* src, size_t cnt) -> cudaError_t {
+    return cnt ? cudaMemcpyAsync(dst, src, sizeof(uint32_t) * cnt, cudaMemcpyHostToDevice, cs) : cudaSuccess;
+  };
+  if (e == cudaSuccess) e = cudaEventRecord(ev_alloc, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev_alloc, 0);
+  if (e == cudaSuccess) e = h2d(g.xtoff, xtoff, (size_t)n + 1);
+  if (e == cudaSuccess) e = h2d(g.xtdat, xtdat, n);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_meta, cs);
+  for (int p = 0; p < pieces && e == cudaSuccess; ++p) {
+    const uint32_t b = xtoff[rows[p]], en = xtoff[rows[p + 1]];
+    e = h2d(g.xtedg + b, xtedg + b, en - b);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[p], cs);
+  }
+  if (e == cudaSuccess && xoff) e = h2d(g.xoff, xoff, (size_t)n + 1);
+  if (e == cudaSuccess && xoff) e = h2d(g.xedg, xedg, m);
+  if (e == cudaSuccess) e = cudaEventRecord(ev_done, cs);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_meta, 0);
   if (e == cudaSuccess) e = build_classes(g, c->sms, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e == cudaSuccess) e = tune_apply_cached(g, c->sms, s);
+  if (e == cudaSuccess) e = ensure_hot(g, kDefaultHotCap, c->sms, s);
+  if (e == cudaSuccess) {
+    const uint32_t width = g.tuned_w64 ? g.tuned_w64 : kDefaultChunk64;
+    e = build_default_layout_pipelined(g, width, g.hot_n > 0, pieces, rows, ev, c->sms, s);
+  }
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev_done, 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) cudaStreamSynchronize(cs);  // no copy may still write into freed arrays
+  for (auto x : ev)
+    if (x) cudaEventDestroy(x);
   if (e != cudaSuccess) {
     set_error(std::string("prx_graph_create: ") + cudaGetErrorString(e));
     prx_graph_destroy(gr);

@@ -16,6 +16,7 @@ struct prx_context {
   int device = 0;
   int sms = 152;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // graph uploads overlapped with layout builds (created on first use)
   State* st = nullptr;        // device control block
   State* st_host = nullptr;   // pinned: [0] after marking, [1] loop checks
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};

@@ -318,11 +318,12 @@ __global__ void __launch_bounds__(256) k_chunk_scatter_w(const uint32_t* __restr
                                                          const uint32_t* __restrict__ low_bm, uint32_t n,
                                                          uint32_t width, int K, const uint32_t* __restrict__ off,
                                                          uint32_t* __restrict__ edg,
-                                                         const uint32_t* __restrict__ hot_idx) {
+                                                         const uint32_t* __restrict__ hot_idx, uint32_t g0 = 0,
+                                                         uint32_t g1 = 0xffffffffu, uint64_t cap = ~0ull) {
   const size_t row = (size_t)n + 1;
   const uint32_t lane = lane_id();
-  const uint32_t groups = (n + 31) >> 5;
-  for (uint32_t gi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; gi < groups;
+  const uint32_t groups = min((n + 31) >> 5, g1);
+  for (uint32_t gi = g0 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); gi < groups;
        gi += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t v = (gi << 5) + lane;
     const uint32_t s = xtoff[min(v, n)];
@@ -372,7 +373,8 @@ __global__ void __launch_bounds__(256) k_chunk_scatter_w(const uint32_t* __restr
             rr = rk;
           }
         }
-        if (act) edg[d + (j - sr - rr)] = layout_id(hot_idx, u);
+        const uint64_t at = (uint64_t)d + (j - sr - rr);
+        if (act && at < cap) edg[at] = layout_id(hot_idx, u);
       }
     }
   }
@@ -412,9 +414,149 @@ static cudaError_t build_layout(const uint32_t* off, const uint32_t* edg, const 
   return e;
 }
 
+static uint64_t g_layout_clock = 0;  // stamps of the layout slots (least recently used is rebuilt)
+
+// ---- the default layout, built while the in-edges upload ---------------------
+// Counts of rows [r0, r1) per chunk into cnt (chunk-major, K x (n+1)), and
+// the piece's total per chunk into tot[k] (one atomic per warp and chunk).
+__global__ void k_chunk_count_range(const uint32_t* __restrict__ xtoff, const uint32_t* __restrict__ xtedg,
+                                    const uint32_t* __restrict__ low_bm, uint32_t n, uint32_t r0, uint32_t r1,
+                                    uint32_t width, int K, uint32_t* __restrict__ cnt, uint32_t* __restrict__ tot) {
+  const size_t row = (size_t)n + 1;
+  const uint32_t span = r1 - r0;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  // every lane runs the same trip count (the warp sums below are collective)
+  for (uint32_t base = blockIdx.x * blockDim.x; base < span; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    const uint32_t v = r0 + i;
+    const bool low = i < span && ((low_bm[v >> 5] >> (v & 31u)) & 1u);
+    uint32_t j = low ? xtoff[v] : 0, e = low ? xtoff[v + 1] : 0;
+    for (int k = 0; k < K; ++k) {
+      const uint64_t hi = (uint64_t)(k + 1) * width;
+      const uint32_t b = j;
+      while (j < e && xtedg[j] < hi) ++j;
+      if (i < span) cnt[k * row + v] = j - b;
+      uint32_t c = j - b;
+      for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+      if (lane_id() == 0 && c) atomicAdd(tot + k, c);
+    }
+  }
+}
+
+// Out-edges of the sources of each chunk: a bound on the chunk's in-edges
+// in the layout, known before the in-edges themselves.
+__global__ void k_chunk_bounds(const uint32_t* __restrict__ xtdat, uint32_t n, uint32_t width, int K,
+                               unsigned long long* __restrict__ bound) {
+  for (int k = 0; k < K; ++k) {
+    const uint64_t lo = (uint64_t)k * width, hi = lo + width < n ? lo + width : n;
+    unsigned long long x = 0;
+    for (uint64_t u = lo + blockIdx.x * blockDim.x + threadIdx.x; u < hi; u += gridDim.x * blockDim.x) x += xtdat[u];
+    block_sum_u64(x, bound + k);
+  }
+}
+
+// After the piece's per-chunk exclusive scans: add the chunk's base in the
+// edge array (the bounds of the chunks before it) and the totals of the
+// pieces before this one (tot holds P x K totals), and write the offset of
+// row r1 (the next piece's first row, or the end of the chunk).
+__global__ void k_chunk_carry(uint32_t* __restrict__ off, uint32_t n, uint32_t r0, uint32_t r1, int K,
+                              const uint32_t* __restrict__ tot, int p, const unsigned long long* __restrict__ bound) {
+  const size_t row = (size_t)n + 1;
+  for (int k = 0; k < K; ++k) {
+    uint32_t carry = 0;
+    for (int q = 0; q < k; ++q) carry += (uint32_t)bound[q];
+    for (int q = 0; q < p; ++q) carry += tot[q * K + k];
+    for (uint32_t v = r0 + blockIdx.x * blockDim.x + threadIdx.x; v < r1; v += gridDim.x * blockDim.x)
+      off[k * row + v] += carry;
+    if (blockIdx.x == 0 && threadIdx.x == 0) off[k * row + r1] = carry + tot[p * K + k];
+  }
+}
+
+cudaError_t build_default_layout_pipelined(GraphDev& g, uint32_t width, bool hot, int pieces,
+                                           const uint32_t* piece_rows, const cudaEvent_t* piece_ready, int sms,
+                                           cudaStream_t s) {
+  if (width == 0 || g.n == 0 || g.nseg > 1) return cudaSuccess;
+  if (hot && !g.hot_n) hot = false;
+  const uint32_t n = g.n;
+  if (width >= n) {  // one chunk: a layout only to encode hot sources (the solve reads the CSR otherwise)
+    if (g.cls_begin[1] == g.cls_begin[0] || !hot) return cudaSuccess;
+    width = n;
+  }
+  const int K = (int)((n + (uint64_t)width - 1) / width);
+  if (K > kScatterK) return cudaSuccess;  // left to the first solve
+  const size_t len = (size_t)K * ((size_t)n + 1);
+  if (len > 0xffffffffull) return cudaSuccess;
+  ChunkLayout* l = &g.lay[0];
+  for (auto& x : g.lay)
+    if (x.width == 0 || (l->width != 0 && x.stamp < l->stamp)) l = &x;
+  free_layout(*l);
+  // chunk k's edges go to a region of its sources' out-edge count, placed
+  // after the regions of chunks 0 .. k-1 (the regions add up to m)
+  uint32_t* tot = nullptr;
+  unsigned long long* bound = nullptr;
+  cudaError_t e = graph_alloc(&l->off, sizeof(uint32_t) * len, s);
+  if (e == cudaSuccess) e = graph_alloc(&l->edg, sizeof(uint32_t) * edge_slots(g.m), s);
+  if (e == cudaSuccess) e = graph_alloc(&tot, sizeof(uint32_t) * (size_t)pieces * K, s);
+  if (e == cudaSuccess) e = graph_alloc(&bound, sizeof(unsigned long long) * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(tot, 0, sizeof(uint32_t) * (size_t)pieces * K, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(bound, 0, sizeof(unsigned long long) * K, s);
+  unsigned long long hb[kScatterK] = {};
+  if (e == cudaSuccess) {
+    k_chunk_bounds<<<sms * 4, 256, 0, s>>>(g.xtdat, n, width, K, bound);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hb, bound, sizeof(unsigned long long) * K, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  uint64_t sum_bound = 0;
+  for (int k = 0; k < K; ++k) sum_bound += hb[k];
+  const uint64_t cap = edge_slots(g.m);
+  if (e == cudaSuccess && sum_bound > g.m) {  // out-degrees inconsistent with m: leave it to the first solve
+    cudaFreeAsync(tot, s);
+    cudaFreeAsync(bound, s);
+    free_layout(*l);
+    return cudaSuccess;
+  }
+  const uint32_t* hot_idx = hot ? g.hot_idx : nullptr;
+  for (int p = 0; p < pieces && e == cudaSuccess; ++p) {
+    const uint32_t r0 = piece_rows[p], r1 = piece_rows[p + 1];
+    e = cudaStreamWaitEvent(s, piece_ready[p], 0);
+    if (e != cudaSuccess || r0 == r1) continue;
+    k_chunk_count_range<<<sms * 8, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, n, r0, r1, width, K, l->off,
+                                                tot + (size_t)p * K);
+    for (int k = 0; k < K && e == cudaSuccess; ++k)
+      e = exclusive_scan_u32(l->off + (size_t)k * (n + 1) + r0, r1 - r0, s);
+    if (e != cudaSuccess) break;
+    k_chunk_carry<<<sms * 4, 256, 0, s>>>(l->off, n, r0, r1, K, tot, p, bound);
+    k_chunk_scatter_w<<<sms * 8, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, n, width, K, l->off, l->edg, hot_idx,
+                                              r0 >> 5, (r1 + 31) >> 5, cap);
+    e = cudaGetLastError();
+  }
+  // every chunk must have stayed within its region (the out-degrees bound it)
+  std::vector<uint32_t> ht((size_t)pieces * K);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ht.data(), tot, sizeof(uint32_t) * ht.size(), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (tot) cudaFreeAsync(tot, s);
+  if (bound) cudaFreeAsync(bound, s);
+  bool fits = true;
+  for (int k = 0; k < K && e == cudaSuccess; ++k) {
+    uint64_t t = 0;
+    for (int p = 0; p < pieces; ++p) t += ht[(size_t)p * K + k];
+    fits = fits && t <= hb[k];
+  }
+  if (e != cudaSuccess || !fits) {
+    free_layout(*l);
+    return e;
+  }
+  l->width = width;
+  l->K = K;
+  l->hot = hot;
+  l->stamp = ++g_layout_clock;
+  return cudaSuccess;
+}
+
 cudaError_t ensure_chunks(GraphDev& g, uint32_t width, int sms, cudaStream_t s, const ChunkLayout** out,
                           bool single, bool hot) {
-  static uint64_t clock = 0;
+  uint64_t& clock = g_layout_clock;
   *out = nullptr;
   if (width == 0 || g.n == 0) return cudaSuccess;
   if (hot && !g.hot_n) hot = false;
@@ -522,7 +664,7 @@ cudaError_t ensure_hot(GraphDev& g, uint32_t cap, int sms, cudaStream_t s) {
   std::vector<uint32_t> h(kDegBins);
   if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), hist, sizeof(uint32_t) * kDegBins, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  graph_free({hist});
+  cudaFreeAsync(hist, s);  // stream-ordered: no device-wide wait (a graph upload may still run beside it)
   if (e != cudaSuccess) return e;
   // threshold t: the smallest degree with count(d >= t) <= cap, and at least
   // twice the average out-degree (a graph without skew gains nothing)
@@ -550,7 +692,7 @@ cudaError_t ensure_hot(GraphDev& g, uint32_t cap, int sms, cudaStream_t s) {
     k_hot_index<<<sms * 4, 256, 0, s>>>(g.xtdat, n, t, scan, g.hot_idx, g.hot_list);
     e = cudaGetLastError();
   }
-  graph_free({scan});
+  cudaFreeAsync(scan, s);
   if (e != cudaSuccess) {
     free_hot(g);
     return e;

@@ -151,6 +151,17 @@ struct GraphDev {
 // Frees the edge weights of g (after a batch, or with the graph).
 void drop_weights(GraphDev& g);
 
+// The default LOW layout of a new graph (chunk width `width`, hot sources
+// encoded when `hot`), built while its in-edges are still uploading: rows
+// [piece_rows[p], piece_rows[p+1]) become usable when piece_ready[p] has
+// fired; each piece is counted, scanned (with the totals of the pieces
+// before it carried in) and scattered on stream s as soon as it has landed.
+// Leaves the layout in the graph's cache; nothing for graphs of several row
+// segments, more than 8 chunks or no layout to build.  Synchronizes s.
+cudaError_t build_default_layout_pipelined(GraphDev& g, uint32_t width, bool hot, int pieces,
+                                           const uint32_t* piece_rows, const cudaEvent_t* piece_ready, int sms,
+                                           cudaStream_t s);
+
 constexpr uint32_t kHotFlag = 0x80000000u;
 constexpr uint32_t kNotHot = 0xffffffffu;
 // The hot sources of g for a cap of `cap` vertices (0: none); graphs of 2^31
@@ -229,6 +240,9 @@ void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s);
 bool launch_hot_copy(const SolveArgs& a, int parity, int sms, cudaStream_t s);
 // Hot-source cap when prx_options.hot_sources is 0: 32 MB of FP64 values.
 constexpr uint32_t kDefaultHotCap = 4u << 20;
+// Source-chunk width of the FP64 sweeps when prx_options.chunk_vertices is 0
+// and the graph is untuned: 200 MB of FP64 contributions per chunk.
+constexpr uint32_t kDefaultChunk64 = (200u << 20) / sizeof(double);
 
 // ---- FP32 refinement (prx_refine.cu) --------------------------------------
 // FP64 residual sweep of one in-degree class (update kernels in MODE_REFINE64).
