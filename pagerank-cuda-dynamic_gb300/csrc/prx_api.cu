@@ -255,35 +255,28 @@ static int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint3
   c->launches += 3;
   TRY_CUDA_ST(cudaMemsetAsync(&c->st->xbcnt, 0, sizeof(uint32_t), s));
   if (mode == PRX_DYNAMIC_TRAVERSAL) {
-    // Closure by BFS levels, all enqueued without a host round trip per
-    // level: a level whose frontier is empty returns at once, so levels go
-    // out in batches of 1, 2, 4, ..., 1024 and the host reads the frontier
-    // length once per batch (a graph of diameter 8k needs ~15 reads).
-    //
-    // Once a frontier holds more than pull_threshold vertices (n/16 by
-    // default; prx_options.expansion 1 never, 2 at once), the rest of the
-    // closure is done by pull rounds until one adds nothing: each vertex not
-    // yet reached scans its in-edges only until it finds a reached one, so a
-    // closure that covers most of the graph no longer walks every out-edge.
+    // The closure of the DF marking under out-edges.  A work queue of reached
+    // vertices (k_closure_queue) runs it without levels, so a high-diameter
+    // graph costs one launch instead of one per BFS level.  When the queue
+    // explodes (more than pull_threshold vertices, n/16 by default, and eight
+    // times those expanded), the closure is about to cover most of the graph:
+    // the rest is done by pull rounds until one adds nothing -- each vertex
+    // not yet reached scans its in-edges only until it finds a reached one,
+    // so it no longer walks every out-edge.  prx_options.expansion 1 never
+    // switches, 2 pulls from the start.  The set is the same either way.
+    const size_t qbytes = sizeof(uint32_t) * (size_t)a.n;
+    TRY_CUDA_ST(cudaMemsetAsync(c->fr[0], 0xff, qbytes, s));
     launch_frontier_from_bitmap(a, c->sms, s);
     c->launches += 1;
-    uint32_t level = 0;
     bool pull = a.pull_threshold == 0;
-    if (!pull && a.pull_threshold != 0xffffffffu) {
-      TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1].fcnt[0], &c->st->fcnt[0], sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                                  s));
+    if (!pull) {
+      launch_closure_queue(a, a.pull_threshold, c->sms, s);
+      c->launches += 1;
+      TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
       TRY_CUDA_ST(cudaStreamSynchronize(s));
-      pull = c->st_host[1].fcnt[0] > a.pull_threshold;
-    }
-    for (uint32_t k = 1; !pull; k = std::min<uint32_t>(2 * k, 1024)) {
-      for (uint32_t i = 0; i < k; ++i) launch_expand_level(a, level++, c->sms, s);
-      c->launches += k;
-      TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1].fcnt[level % 3], &c->st->fcnt[level % 3], sizeof(uint32_t),
-                                  cudaMemcpyDeviceToHost, s));
-      TRY_CUDA_ST(cudaStreamSynchronize(s));
-      const uint32_t next = c->st_host[1].fcnt[level % 3];
-      if (next == 0) break;
-      pull = next > a.pull_threshold;
+      const State& h = c->st_host[1];
+      if (h.err & kErrClosureWait) FAIL(PRX_ETIMEOUT, "DT closure: a bounded device wait ran out");
+      pull = h.q_done != h.fcnt[0];  // left to pull rounds
     }
     if (pull) {
       // rounds in batches of 1, 2, 4, ..., 64; done when a round of the batch
@@ -542,6 +535,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   float ti = 0, tm = 0, tc = 0, tt = 0;
   const bool timing = o.timing != 0;
   bool full_sweeps = false;  // FP32-refined dynamic mode run as full sweeps (last repeat)
+  bool dt_all = false;       // DT whose closure covers every vertex, run as ND (last repeat)
   for (int rep = 0; rep < repeat; ++rep) {
     c->launches = 0;
     c->tev_used = 0;
@@ -584,6 +578,14 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
         if (c->st_host[1].done) return PRX_OK;
       }
     };
+    // DT whose closure reached every vertex updates every vertex in every
+    // iteration with nothing to expand or prune: exactly ND's iterations,
+    // which the Static kernels run without the bitmaps
+    dt_all = false;
+    if (mode == PRX_DYNAMIC_TRAVERSAL && !refine && nd + ni > 0) {
+      TRY_CUDA_ST(cudaStreamSynchronize(s));
+      dt_all = c->st_host[0].affected == g.n;
+    }
     full_sweeps = refine && dyn && o.refine_sweeps == 1;
     if (refine && dyn && o.refine_sweeps == 0) {  // the initial marking's size decides
       TRY_CUDA_ST(cudaStreamSynchronize(s));
@@ -601,7 +603,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
       // graph: FP32 sweeps over all vertices from the initial ranks (q for
       // the dynamic modes), then the FP64 refinement
       if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity, true))) return st;
-    } else if ((st = iterate(mode, lay64))) {
+    } else if ((st = iterate(dt_all ? PRX_NAIVE_DYNAMIC : mode, lay64))) {
       return st;
     }
     TRY_CUDA_ST(cudaEventRecord(c->ev[3], s));
@@ -620,7 +622,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
     res->marking_time_ms = tm / repeat;
     res->computation_time_ms = tc / repeat;
     res->affected_initial = dyn ? c->st_host[0].affected : g.n;
-    res->edges_processed = dyn && !full_sweeps ? h.edges : g.m * (uint64_t)h.iter;
+    res->edges_processed = dyn && !full_sweeps && !dt_all ? h.edges : g.m * (uint64_t)h.iter;
     res->last_delta = h.last_delta;
     res->refinements = refine ? h.rounds : 0;
     res->kernel_launches = c->launches;

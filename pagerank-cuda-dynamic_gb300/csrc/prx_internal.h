@@ -59,7 +59,12 @@ struct State {
   unsigned int e32max_bits[2];    // L-inf of the correction it produced (personalized PageRank)
   int graph_rounds;               // bodies run by the CUDA-graph loop (its own bound)
   int graph_inner;                // bodies of a nested graph loop in the current outer body
+  uint32_t q_head;                // DT closure queue (fr[0], length fcnt[0]): items claimed
+  uint32_t q_done;                // ... and items whose out-neighbours are marked
 };
+
+// Device error codes (State::err bits).
+constexpr uint32_t kErrClosureWait = 1u << 4;  // the DT closure's bounded wait ran out
 
 // Internal mode of the update kernels: the FP64 residual sweep of the FP32
 // refinement (reads the base ranks r[0] / c[0], writes the next iterate to
@@ -269,8 +274,12 @@ void launch_mark_seed(const SolveArgs& a, const uint32_t* delu, const uint32_t* 
                       const uint32_t* insu, uint64_t ni, int sms, cudaStream_t s);
 void launch_expand_seeds(const SolveArgs& a, int sms, cudaStream_t s);
 void launch_frontier_from_bitmap(const SolveArgs& a, int sms, cudaStream_t s);
-// One DT closure level (no-op once the frontier is empty).
-void launch_expand_level(const SolveArgs& a, uint32_t level, int sms, cudaStream_t s);
+// DT closure by a work queue (frontier 0 holds the DF marking, its slots
+// past the count set to all ones): persistent warps take reached vertices
+// and mark their out-neighbours, until nothing is left, or until the queue
+// holds more than switch_at vertices and eight times those done (a closure
+// exploding in few steps, left to pull rounds).
+void launch_closure_queue(const SolveArgs& a, uint32_t switch_at, int sms, cudaStream_t s);
 // One DT closure round by pulling: every vertex not yet reached that has a
 // reached in-neighbour joins (no-op once a round added nothing).
 void launch_closure_pull(const SolveArgs& a, uint32_t round, int sms, cudaStream_t s);

@@ -65,24 +65,140 @@ __global__ void __launch_bounds__(kThreads) k_frontier_from_bitmap(SolveArgs a) 
   }
 }
 
-// Closure level L: the out-neighbours of frontier L % 3 not yet reached go to
-// bitmap 0 and frontier (L+1) % 3.  The counter of frontier (L+2) % 3 -- the
-// one level L+1 fills -- is zeroed here: level L-1 was its last reader.
-__global__ void __launch_bounds__(kThreads) k_expand_level(SolveArgs a, uint32_t level) {
+// DT closure without levels.  The closure is every vertex reachable from the
+// DF marking (the reference grows it level by level until the count stops
+// changing, :438-456; the order in which vertices are reached does not
+// change the set), so persistent warps take reached vertices from a queue
+// and mark their out-neighbours.
+//   queue: frontier 0; its length is fcnt[0] (the tail), q_head counts items
+//   taken, q_done items finished.  A slot is all ones until its producer has
+//   written it (a consumer may take a slot the moment the tail covers it).
+// A warp takes up to 32 items, one per lane.  A lane marks the out-neighbours
+// of a vertex of out-degree <= 32 itself and goes on from one of the newly
+// marked ones (up to kChain steps), so a long path -- the diameter of a road
+// or grid graph -- is walked at one thread's memory latency per step rather
+// than one queue round trip or one kernel launch per level.  The other new
+// vertices wait in shared memory and reach the queue with one atomic per
+// warp; vertices of larger out-degree are expanded by the whole warp.  Tail
+// increments precede the warp's q_done increment (fence), so a warp that
+// reads q_done and then the tail and finds them equal knows nothing is in
+// flight: the closure is done.  Idle warps back off exponentially; every
+// wait is bounded, and running out sets kErrClosureWait and returns.
+constexpr uint32_t kQueueEmpty = 0xffffffffu;
+constexpr int kClosureSpin = 1 << 20;
+constexpr int kChain = 64;
+constexpr int kQWarps = 4;           // warps per block of the queue kernel
+constexpr uint32_t kQBuf = 2048;     // buffered new vertices per warp (32 KB of shared memory a block)
+
+__global__ void __launch_bounds__(kQWarps * 32) k_closure_queue(SolveArgs a, uint32_t switch_at) {
+  __shared__ uint32_t buf[kQWarps][kQBuf];
+  __shared__ uint32_t nbuf[kQWarps];
   State* st = a.st;
-  const uint32_t cur = level % 3, nxt = (level + 1) % 3, clr = (level + 2) % 3;
-  const uint32_t count = st->fcnt[cur];
-  if (blockIdx.x == 0 && threadIdx.x == 0) st->fcnt[clr] = 0;
-  const uint32_t lane = lane_id();
-  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < count; i += (gridDim.x * blockDim.x) >> 5) {
-    const uint32_t u = a.fr[cur][i];
-    const uint64_t iu = seg_index(u, a.seg_shift);
-    const uint32_t e = a.xoff[iu + 1];
-    const uint32_t* ed = seg_edges(a.xedg, a.xbase, a.seg_shift, u);
-    for (uint32_t j = a.xoff[iu] + lane; j < e; j += 32) {
-      const uint32_t w = ed[j];
-      if (test_and_set(a.bm[0], w)) push(a.fr[nxt], &st->fcnt[nxt], w);
+  volatile uint32_t* vhead = &st->q_head;
+  volatile uint32_t* vtail = &st->fcnt[0];
+  volatile uint32_t* vdone = &st->q_done;
+  volatile uint32_t* verr = &st->err;
+  uint32_t* queue = a.fr[0];
+  volatile const uint32_t* vq = queue;
+  uint32_t* reached = a.bm[0];
+  const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
+  auto flush = [&]() {  // the warp's buffered vertices to the queue
+    __syncwarp();
+    const uint32_t k = nbuf[w];
+    uint32_t base = 0;
+    if (lane == 0 && k) base = atomicAdd(&st->fcnt[0], k);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    for (uint32_t i = lane; i < k; i += 32) queue[base + i] = buf[w][i];
+    __syncwarp();
+    if (lane == 0) nbuf[w] = 0;
+    __syncwarp();
+  };
+  if (lane == 0) nbuf[w] = 0;
+  __syncwarp();
+  for (;;) {
+    uint32_t h = 0, cnt = 0;
+    if (lane == 0) {
+      unsigned backoff = 64;
+      for (int spin = 0;;) {
+        if (*verr) break;
+        const uint32_t head = *vhead;
+        const uint32_t done = *vdone;
+        __threadfence();
+        const uint32_t tail = *vtail;
+        if (tail > switch_at && tail / 8u > done) break;  // exploding: pull rounds finish it
+        if (head < tail) {
+          const uint32_t take = min(32u, tail - head);
+          if (atomicCAS(&st->q_head, head, head + take) == head) {
+            h = head;
+            cnt = take;
+            break;
+          }
+          continue;
+        }
+        if (done == tail) break;  // closed
+        if (++spin > kClosureSpin) {
+          atomicOr(&st->err, kErrClosureWait);
+          break;
+        }
+        __nanosleep(backoff);
+        backoff = min(backoff * 2, 8192u);
+      }
     }
+    h = __shfl_sync(0xffffffffu, h, 0);
+    cnt = __shfl_sync(0xffffffffu, cnt, 0);
+    if (cnt == 0) break;
+    uint32_t u = kQueueEmpty;
+    if (lane < cnt) {
+      for (int spin = 0; (u = vq[h + lane]) == kQueueEmpty;) {
+        if (++spin > kClosureSpin || *verr) {
+          atomicOr(&st->err, kErrClosureWait);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    for (int step = 0; step < kChain; ++step) {
+      const bool valid = u != kQueueEmpty;
+      if (!__any_sync(0xffffffffu, valid)) break;
+      uint32_t b = 0, e = 0;
+      if (valid) {
+        const uint64_t iu = seg_index(u, a.seg_shift);
+        b = a.xoff[iu];
+        e = a.xoff[iu + 1];
+      }
+      const bool small = e - b <= 32u;
+      uint32_t next = kQueueEmpty;
+      if (valid && small) {
+        const uint32_t* ed = seg_edges(a.xedg, a.xbase, a.seg_shift, u);
+        for (uint32_t j = b; j < e; ++j) {
+          const uint32_t x = ed[j];
+          if (test_and_set(reached, x)) {
+            if (next == kQueueEmpty) next = x;  // this lane goes on from x
+            else buf[w][atomicAdd(&nbuf[w], 1u)] = x;
+          }
+        }
+      }
+      unsigned big = __ballot_sync(0xffffffffu, valid && !small);
+      while (big) {
+        const int src = __ffs(big) - 1;
+        big &= big - 1;
+        const uint32_t ub = __shfl_sync(0xffffffffu, u, src);
+        const uint32_t bb = __shfl_sync(0xffffffffu, b, src), eb = __shfl_sync(0xffffffffu, e, src);
+        const uint32_t* ed = seg_edges(a.xedg, a.xbase, a.seg_shift, ub);
+        for (uint32_t j = bb + lane; j < eb; j += 32) {
+          const uint32_t x = ed[j];
+          if (test_and_set(reached, x)) push(queue, &st->fcnt[0], x);
+        }
+      }
+      u = next;
+      __syncwarp();
+      if (nbuf[w] > kQBuf - 32u * 32u) flush();  // room for one more step of every lane
+    }
+    if (u != kQueueEmpty) buf[w][atomicAdd(&nbuf[w], 1u)] = u;  // chain cut: back to the queue
+    flush();
+    __threadfence();  // this warp's tail increments and slots before its q_done increment
+    __syncwarp();
+    if (lane == 0) atomicAdd(&st->q_done, cnt);
   }
 }
 
@@ -173,6 +289,8 @@ __global__ void k_state_reset(State* st, int max_iter, double tol) {
   st->e32max_bits[0] = st->e32max_bits[1] = 0;
   st->graph_rounds = 0;
   st->graph_inner = 0;
+  st->q_head = 0;
+  st->q_done = 0;
 }
 
 // ---- launchers ------------------------------------------------------------------
@@ -191,8 +309,8 @@ void launch_frontier_from_bitmap(const SolveArgs& a, int sms, cudaStream_t s) {
   k_frontier_from_bitmap<<<sms * 4, kThreads, 0, s>>>(a);
 }
 
-void launch_expand_level(const SolveArgs& a, uint32_t level, int sms, cudaStream_t s) {
-  k_expand_level<<<sms * 4, kThreads, 0, s>>>(a, level);
+void launch_closure_queue(const SolveArgs& a, uint32_t switch_at, int sms, cudaStream_t s) {
+  k_closure_queue<<<sms * 2, kQWarps * 32, 0, s>>>(a, switch_at);
 }
 
 void launch_closure_pull(const SolveArgs& a, uint32_t round, int sms, cudaStream_t s) {
