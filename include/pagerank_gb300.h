@@ -135,7 +135,7 @@ typedef struct {
                                  4 per SM); 0 the library's choice (1).  Each
                                  row is still added by one lane in source
                                  order: results do not depend on it [0]     */
-  int    hot_sources;         /* FP64 sweeps of Static / ND and of
+  int    hot_sources;         /* FP64 sweeps of every mode and of
                                  PRX_FP32_REFINE: the vertices of largest
                                  out-degree (at most this many, with
                                  out-degree at least twice the average) get

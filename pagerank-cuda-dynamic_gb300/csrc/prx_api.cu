@@ -345,8 +345,9 @@ static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArg
                                        [&] { return launch_update_class(a, gr->g, mode, cls, lay, c->sms, s); });
     if (st) return st;
   }
-  if (!(mode & MODE_F32) && mode < PRX_DYNAMIC_TRAVERSAL)  // the contributions this sweep wrote
-    c->launches += launch_hot_copy(a, -1, c->sms, s);
+  // the contributions this iteration wrote (the dynamic modes' stale copies
+  // included: after an iteration its parity holds every vertex's value)
+  if (!(mode & MODE_F32)) c->launches += launch_hot_copy(a, -1, c->sms, s);
   if ((mode & ~MODE_F32) >= PRX_DYNAMIC_FRONTIER) {
     launch_expand_iteration(a, c->sms, s);  // push or pull, chosen on the device
     c->launches += 3;
@@ -515,10 +516,10 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   const uint32_t w32 = o.chunk_vertices ? o.chunk_vertices
                       : g.tuned_w32          ? g.tuned_w32
                                              : (48u << 20) / sizeof(float);
-  // Hot sources (the FP64 sweeps of Static / ND and of the refinement): a
-  // layout whose edges from the highest out-degree vertices gather from a
-  // dense copy of their contributions
-  const bool hot_ok = o.hot_sources >= 0 && o.low_sweep < 2 && (!dyn || refine);
+  // Hot sources (the FP64 sweeps of every mode): a layout whose edges from
+  // the highest out-degree vertices gather from a dense copy of their
+  // contributions
+  const bool hot_ok = o.hot_sources >= 0 && o.low_sweep < 2;
   if (hot_ok) {
     TRY_CUDA_ST(ensure_hot(gr->g, o.hot_sources > 0 ? (uint32_t)o.hot_sources : kDefaultHotCap, c->sms,
                            c->stream));

@@ -147,8 +147,8 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
 // one finishes the vertex.
 enum Pass { PASS_ONLY = 0, PASS_FIRST = 1, PASS_INNER = 2, PASS_LAST = 3 };
 
-// hot: the layout encodes hot sources (FP64 Static / ND / refinement only);
-// their contributions are gathered from a.ch[p].
+// hot: the layout encodes hot sources (the FP64 modes); their contributions
+// are gathered from a.ch[p].
 template <int MODE, int PASS>
 __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, uint32_t vb, uint32_t ve,
                                                          const unsigned long long* __restrict__ base,
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, uint32_t v
   const int iter = st->iter, p = data_parity<MODE>(st);
   const V* __restrict__ c = contribs_of<MODE>(a, p);
   const V* __restrict__ ch = nullptr;
-  if constexpr (!T::F32 && !T::DYN) ch = a.ch[p];
+  if constexpr (!T::F32) ch = a.ch[p];
   uint32_t *cur = nullptr, *nxt = nullptr, *prev = nullptr;
   if (T::DYN) {
     cur = a.bm[iter % 3];
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, uint32_t v
     V acc = V(0);
     if (mine)
       acc = lane_row_sum(c, seg_edges(edg, base, shift, v), s, e, FIRST ? V(0) : carried_of<MODE>(a)[v], ch,
-                         (!T::F32 && !T::DYN) && hot);
+                         !T::F32 && hot);
     if (mine) {
       edges += e - s;
       if (LAST) {
