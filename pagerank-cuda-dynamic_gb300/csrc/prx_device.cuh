@@ -146,6 +146,21 @@ __device__ __forceinline__ bool quot_gt(double x, double m, double c) {
   return x / m > c;
 }
 
+// FP32 rounds of the refinement stop once the change they predict for their
+// next sweep -- this sweep's change times the larger of its last two ratios
+// to the sweep before (the observed rate of the Jacobi iteration) -- is below
+// kPredictSafety times the tolerance: the FP64 residual sweep that follows
+// measures about that next change, so it passes without the FP32 sweep that
+// would only confirm it.  The FP64 test still decides convergence; a wrong
+// prediction costs one more round, never accuracy.  prev / prev2: the
+// changes of the two sweeps before (0: none yet).
+constexpr float kPredictSafety = 0.8f;
+__device__ __forceinline__ bool fp32_round_done(float change, float prev, float prev2, double tol) {
+  if (!(prev > 0.f && prev2 > 0.f && change < prev && prev < prev2)) return false;
+  const float rate = fmaxf(change / prev, prev / prev2);
+  return change * rate < kPredictSafety * (float)tol;
+}
+
 // The contribution of edge id u: with `hot` (a layout whose hot sources are
 // encoded, kHotFlag | number) from the dense hot copy ch, else c[u].
 template <class T>

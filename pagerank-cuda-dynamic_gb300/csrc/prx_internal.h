@@ -59,6 +59,7 @@ struct State {
   unsigned int e32max_bits[2];    // L-inf of the correction it produced (personalized PageRank)
   int graph_rounds;               // bodies run by the CUDA-graph loop (its own bound)
   int graph_inner;                // bodies of a nested graph loop in the current outer body
+  unsigned int el32_prev[2];      // FP32 rounds: the changes of the round's two previous sweeps (bits, 0: none)
   uint32_t q_head;                // DT closure queue (fr[0], length fcnt[0]): items claimed
   uint32_t q_done;                // ... and items whose out-neighbours are marked
 };

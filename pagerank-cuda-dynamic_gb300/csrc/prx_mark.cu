@@ -291,6 +291,7 @@ __global__ void k_state_reset(State* st, int max_iter, double tol) {
   st->graph_inner = 0;
   st->q_head = 0;
   st->q_done = 0;
+  st->el32_prev[0] = st->el32_prev[1] = 0;
 }
 
 // ---- launchers ------------------------------------------------------------------

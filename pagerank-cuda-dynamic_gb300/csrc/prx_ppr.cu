@@ -336,6 +336,7 @@ __global__ void k_ppr_fin_r64(State* st) {  // refinement: FP64 residual sweep
   st->inner_done = 0;
   st->el32_bits[0] = st->el32_bits[1] = 0;
   st->e32max_bits[0] = st->e32max_bits[1] = 0;
+  st->el32_prev[0] = st->el32_prev[1] = 0;
 }
 
 __global__ void k_ppr_fin32(State* st) {  // refinement: FP32 correction sweep
@@ -347,7 +348,12 @@ __global__ void k_ppr_fin32(State* st) {  // refinement: FP32 correction sweep
   st->k32 += 1;
   st->el32_bits[q ^ 1] = 0;
   st->e32max_bits[q ^ 1] = 0;
-  if (dl < (float)st->tol || dl < em * 0x1p-18f || st->iter >= st->max_iter) st->inner_done = 1;
+  const float prev = __uint_as_float(st->el32_prev[0]), prev2 = __uint_as_float(st->el32_prev[1]);
+  st->el32_prev[1] = st->el32_prev[0];
+  st->el32_prev[0] = __float_as_uint(dl);
+  if (dl < (float)st->tol || dl < em * 0x1p-18f || st->iter >= st->max_iter ||
+      fp32_round_done(dl, prev, prev2, st->tol))
+    st->inner_done = 1;
 }
 
 // x_b += e (the correction of the last FP32 sweep); nothing once the solve

@@ -141,6 +141,7 @@ __global__ void k_refine_finalize64(State* st) {
   st->inner_done = 0;
   st->el32_bits[0] = st->el32_bits[1] = 0;
   st->e32max_bits[0] = st->e32max_bits[1] = 0;
+  st->el32_prev[0] = st->el32_prev[1] = 0;
 }
 
 __global__ void k_finalize32(State* st) {
@@ -152,7 +153,12 @@ __global__ void k_finalize32(State* st) {
   st->k32 += 1;
   st->el32_bits[q ^ 1] = 0;
   st->e32max_bits[q ^ 1] = 0;
-  if (dl < (float)st->tol || dl < em * 0x1p-18f || st->iter >= st->max_iter) st->inner_done = 1;
+  const float prev = __uint_as_float(st->el32_prev[0]), prev2 = __uint_as_float(st->el32_prev[1]);
+  st->el32_prev[1] = st->el32_prev[0];
+  st->el32_prev[0] = __float_as_uint(dl);
+  if (dl < (float)st->tol || dl < em * 0x1p-18f || st->iter >= st->max_iter ||
+      fp32_round_done(dl, prev, prev2, st->tol))
+    st->inner_done = 1;
 }
 
 // Round 0: x_b = 0, rho = C0, e_0 = the initial ranks (FP32), ce_0 = e_0 / d.
@@ -171,6 +177,7 @@ __global__ void k_refine_round0(SolveArgs a) {
     st->inner_done = st->done;
     st->el32_bits[0] = st->el32_bits[1] = 0;
     st->e32max_bits[0] = st->e32max_bits[1] = 0;
+    st->el32_prev[0] = st->el32_prev[1] = 0;
   }
 }
 

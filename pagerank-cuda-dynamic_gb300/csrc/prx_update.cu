@@ -577,8 +577,12 @@ __global__ void k_finalize(State* st) {
   st->last_delta = el;
   st->iter += 1;
   bool stop = el < st->tol || st->iter >= st->max_iter;  // pagerankLoopCuU :680,689
-  if (F32) {  // FP32 phase: also stop at what FP32 ranks can resolve
-    stop = stop || el < (double)__uint_as_float(st->e32max_bits[p]) * 0x1p-18;
+  if (F32) {  // FP32 phase: also stop at what FP32 ranks can resolve, or on the predicted next change
+    const float prev = __uint_as_float(st->el32_prev[0]), prev2 = __uint_as_float(st->el32_prev[1]);
+    st->el32_prev[1] = st->el32_prev[0];
+    st->el32_prev[0] = __float_as_uint((float)el);
+    stop = stop || el < (double)__uint_as_float(st->e32max_bits[p]) * 0x1p-18 ||
+           fp32_round_done((float)el, prev, prev2, st->tol);
     st->e32max_bits[p ^ 1] = 0;
   }
   if (stop) st->done = 1;
@@ -640,6 +644,7 @@ __global__ void k_commit_dyn32(SolveArgs a, int parity) {
     st->inner_done = 0;
     st->el32_bits[0] = st->el32_bits[1] = 0;
     st->e32max_bits[0] = st->e32max_bits[1] = 0;
+    st->el32_prev[0] = st->el32_prev[1] = 0;
     st->cnt[0][MID] = st->cnt[0][HIGH] = 0;
     st->nfcnt = 0;
     st->xbcnt = 0;
