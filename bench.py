@@ -59,8 +59,6 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=9)
     p.add_argument("--static-only", action="store_true", help="upload only the in-CSR; skip DF-P and the CPU leg")
     p.add_argument("--chunk", type=int, default=0, help="source-chunk width of the gathers (0: library default)")
-    p.add_argument("--low-sweep", type=int, default=0,
-                   help="kernel of the in-degree <= 64 rows (prx_options.low_sweep; 0: library default)")
     p.add_argument("--loop", default="auto", choices=("auto", "host"),
                    help="iteration loop of the Static / dynamic solves: auto (one CUDA graph) or host (kernels "
                         "visible one by one to a profiler)")
@@ -763,8 +761,8 @@ def run_ours(args):
     # the timed solves run as the library runs by default (the iteration loop
     # as one CUDA graph); the per-launch timing of the roofline comes from
     # separate solves with timing on (host-driven loop, same kernels)
-    opts = loop_opts(pg, args)(chunk_vertices=args.chunk, low_sweep=args.low_sweep)
-    topts = pg.options(timing=1, chunk_vertices=args.chunk, low_sweep=args.low_sweep)
+    opts = loop_opts(pg, args)(chunk_vertices=args.chunk)
+    topts = pg.options(timing=1, chunk_vertices=args.chunk)
     log(f"classes: vertices {cls_v} edges {cls_e}")
     for _ in range(args.warmup):
         pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr(), opts=opts)
@@ -813,7 +811,7 @@ def run_ours(args):
     if not args.no_fp32:
         ranks64 = ranks.clone()
         r32 = torch.empty_like(ranks)
-        o32 = pg.options(precision=pg.FP32_REFINE, timing=1, chunk_vertices=args.chunk, low_sweep=args.low_sweep)
+        o32 = pg.options(precision=pg.FP32_REFINE, timing=1, chunk_vertices=args.chunk)
         for _ in range(2):
             pg.solve_device(ctx, g, pg.STATIC, None, r32.data_ptr(), opts=o32)
         torch.cuda.synchronize()

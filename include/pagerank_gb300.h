@@ -125,16 +125,6 @@ typedef struct {
                                  writing ranks and result); 0: PRX_OK, as
                                  the reference returns its ranks either
                                  way [0]                                    */
-  int    low_sweep;           /* kernel of the in-degree <= 64 rows in
-                                 Static / ND sweeps and the FP64 sweeps of
-                                 PRX_FP32_REFINE: 1 one row per lane; 2..5
-                                 rows packed across a warp's lanes in equal
-                                 shares of edges (2: 128-row tiles, 8 blocks
-                                 per SM; 3: 256-row tiles, 4 per SM; 4:
-                                 256-row tiles, 8 per SM; 5: 128-row tiles,
-                                 4 per SM); 0 the library's choice (1).  Each
-                                 row is still added by one lane in source
-                                 order: results do not depend on it [0]     */
   int    hot_sources;         /* FP64 sweeps of every mode and of
                                  PRX_FP32_REFINE: the vertices of largest
                                  out-degree (at most this many, with

@@ -41,7 +41,6 @@ void prx_options_default(prx_options* o) {
   o->refine_sweeps = 0;
   o->l2_fetch_bytes = 0;
   o->require_convergence = 0;
-  o->low_sweep = 0;
   o->hot_sources = 0;
 }
 
@@ -230,7 +229,6 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
   a.st = c->st;
   a.n = g.n;
   a.mid_max = g.mid_max;
-  a.low_sweep = o.low_sweep;
   a.P = o.damping;
   a.C0 = (1 - o.damping) / (double)g.n;  // pagerankLoopCuU :679, N = order
   a.D = o.frontier_tolerance;
@@ -519,14 +517,14 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
   // Hot sources (the FP64 sweeps of every mode): a layout whose edges from
   // the highest out-degree vertices gather from a dense copy of their
   // contributions
-  const bool hot_ok = o.hot_sources >= 0 && o.low_sweep < 2;
+  const bool hot_ok = o.hot_sources >= 0;
   if (hot_ok) {
     TRY_CUDA_ST(ensure_hot(gr->g, o.hot_sources > 0 ? (uint32_t)o.hot_sources : kDefaultHotCap, c->sms,
                            c->stream));
     if (g.hot_n && (st = ensure_ch(c, g.hot_n))) return st;
   }
   const ChunkLayout *lay64 = nullptr, *lay32 = nullptr;
-  TRY_CUDA_ST(ensure_chunks(gr->g, w64, c->sms, c->stream, &lay64, o.low_sweep >= 2, hot_ok && g.hot_n > 0));
+  TRY_CUDA_ST(ensure_chunks(gr->g, w64, c->sms, c->stream, &lay64, hot_ok && g.hot_n > 0));
   if (refine) TRY_CUDA_ST(ensure_chunks(gr->g, w32, c->sms, c->stream, &lay32));
   cudaStream_t s = c->stream;
   SolveArgs a = make_args(c, g, o);
@@ -1077,7 +1075,6 @@ static int solve_common(prx_context* c, prx_graph* gr, int mode, const uint32_t*
   if (!(opt.damping > 0 && opt.damping < 1)) FAIL(PRX_EINVAL, "prx_solve: damping must be in (0, 1)");
   if (opt.l2_fetch_bytes < -1 || opt.l2_fetch_bytes > 128)
     FAIL(PRX_EINVAL, "prx_solve: l2_fetch_bytes must be in -1 .. 128");
-  if (opt.low_sweep < 0 || opt.low_sweep > 5) FAIL(PRX_EINVAL, "prx_solve: low_sweep must be in 0 .. 5");
   if (opt.hot_sources < -1) FAIL(PRX_EINVAL, "prx_solve: hot_sources must be -1, 0 or a vertex count");
   if (!ranks_out && gr->g.n) FAIL(PRX_EINVAL, "prx_solve: ranks_out is NULL");
   prx_result own;

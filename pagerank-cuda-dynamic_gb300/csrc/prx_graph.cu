@@ -555,14 +555,13 @@ cudaError_t build_default_layout_pipelined(GraphDev& g, uint32_t width, bool hot
 }
 
 cudaError_t ensure_chunks(GraphDev& g, uint32_t width, int sms, cudaStream_t s, const ChunkLayout** out,
-                          bool single, bool hot) {
+                          bool hot) {
   uint64_t& clock = g_layout_clock;
   *out = nullptr;
   if (width == 0 || g.n == 0) return cudaSuccess;
   if (hot && !g.hot_n) hot = false;
-  if (width >= g.n) {  // one chunk: the row-major CSR is the layout, or its LOW rows alone
-    const bool all_low = g.cls_begin[1] == g.n;
-    if (g.cls_begin[1] == g.cls_begin[0] || (!hot && (!single || all_low))) return cudaSuccess;
+  if (width >= g.n) {  // one chunk: the row-major CSR is the layout, unless hot sources are encoded
+    if (g.cls_begin[1] == g.cls_begin[0] || !hot) return cudaSuccess;
     width = g.n;
   }
   if (g.nseg > 1 && g.seg_shift < 5) return cudaSuccess;  // segments must start on a LOW-bitmap word

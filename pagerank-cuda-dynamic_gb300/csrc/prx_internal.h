@@ -177,12 +177,11 @@ void free_hot(GraphDev& g);
 
 // Chunk layout of `width` vertices per chunk (built on first use, cached in
 // three slots, the least recently used one rebuilt); width >= n means no
-// chunking: *out = nullptr, or with `single` a one-chunk layout of the LOW
-// rows' edges (non-LOW rows empty) when the graph has non-LOW rows.  `hot`:
-// ids of hot sources encoded (ensure_hot first; always a layout, even of
-// one chunk).
+// chunking (*out = nullptr: the in-CSR itself) unless `hot`: ids of hot
+// sources encoded (ensure_hot first), which always gives a layout, of one
+// chunk of the LOW rows' edges if need be.
 cudaError_t ensure_chunks(GraphDev& g, uint32_t width, int sms, cudaStream_t s, const ChunkLayout** out,
-                          bool single = false, bool hot = false);
+                          bool hot = false);
 void free_chunks(GraphDev& g);
 
 // Pointers a solve kernel needs.  Passed by value.
@@ -221,7 +220,6 @@ struct SolveArgs {
   uint32_t n;
   uint32_t mid_max;
   uint32_t pull_threshold;        // expand by pulling when more than this many vertices changed by > D
-  int low_sweep;                  // LOW-class sweep of Static / ND / refinement (prx_options.low_sweep)
   double C0, P, D, C;
 };
 

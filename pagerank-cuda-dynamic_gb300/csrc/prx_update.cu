@@ -240,107 +240,6 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, uint32_t v
   if (T::DYN) block_sum_u64(edges, &st->edges);
 }
 
-// ---- LOW, Static / ND / refinement FP64 sweeps: rows packed across lanes -----
-// The one-row-per-lane kernel above leaves lanes idle while the warp's
-// longest row finishes, and every row pays a masked head and tail group; on
-// GB300 (2 FP64 lanes per SM per cycle) those wasted DADD slots cost as much
-// as the useful ones.  Here a warp takes a tile of TILE consecutive rows whose
-// edges are one contiguous range of the LOW-only layout (off / edg: non-LOW
-// rows are empty), cuts that range into 32 nearly equal pieces at row
-// boundaries, and each lane adds its own run of whole rows front to back --
-// one DADD per edge, no masked adds but the first and last group of the
-// lane's run.  A row's sum starts from its carried value (earlier source
-// chunks) and goes to shared memory when the row ends; the tile's epilogue
-// then finishes all TILE rows with every lane active.  Each row is still
-// added by one lane in source order, so the sums are the reference's.
-template <int MODE, int PASS, int TILE>
-__global__ void __launch_bounds__(kThreads) k_update_low_packed(SolveArgs a, uint32_t vb, uint32_t ve,
-                                                                const uint32_t* __restrict__ off,
-                                                                const uint32_t* __restrict__ edg) {
-  using T = ModeTraits<MODE>;
-  static_assert(!T::DYN && !T::F32, "packed LOW sweep: Static / ND / refinement only");
-  constexpr bool FIRST = PASS == PASS_ONLY || PASS == PASS_FIRST;
-  constexpr bool LAST = PASS == PASS_ONLY || PASS == PASS_LAST;
-  constexpr int W = kThreads / 32;
-  __shared__ uint32_t s_off[W][TILE + 1];
-  __shared__ double s_acc[W][TILE];
-  State* st = a.st;
-  if (st->done) return;
-  const int iter = st->iter, p = data_parity<MODE>(st);
-  const double* __restrict__ c = contribs_of<MODE>(a, p);
-  const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
-  uint32_t* so = s_off[wib];
-  double* sa = s_acc[wib];
-  const uint32_t rows = ve - vb;
-  const uint32_t tiles = (rows + TILE - 1) / TILE;
-  unsigned long long emax = 0;
-  unsigned int mag = 0;
-  for (uint32_t t = blockIdx.x * W + wib; t < tiles; t += gridDim.x * W) {
-    const uint32_t r0 = t * TILE;
-    const uint32_t nr = min((uint32_t)TILE, rows - r0);
-    // offsets of the tile's rows (rows past ve: empty) and their carried sums
-    for (uint32_t i = lane; i <= (uint32_t)TILE; i += 32) so[i] = __ldg(off + r0 + min(i, nr));
-    for (uint32_t i = lane; i < (uint32_t)TILE; i += 32) sa[i] = (FIRST || i >= nr) ? 0.0 : a.acc64[vb + r0 + i];
-    __syncwarp();
-    // this lane's rows [lo, hi): those whose first edge lies in its share of
-    // the tile's edges; lo = the first row starting at or after the share
-    const uint32_t e0 = so[0], E = so[TILE] - e0;
-    const uint32_t t_lo = e0 + (uint32_t)(((uint64_t)E * lane) >> 5);
-    const uint32_t t_hi = e0 + (uint32_t)(((uint64_t)E * (lane + 1)) >> 5);
-    uint32_t lo = 0, hi = 0;
-    {
-      uint32_t a0 = 0, a1 = TILE + 1, b0 = 0, b1 = TILE + 1;  // lower bounds over so[0 .. TILE]
-      while (a0 < a1) { const uint32_t m = (a0 + a1) >> 1; if (so[m] < t_lo) a0 = m + 1; else a1 = m; }
-      while (b0 < b1) { const uint32_t m = (b0 + b1) >> 1; if (so[m] < t_hi) b0 = m + 1; else b1 = m; }
-      lo = a0;
-      hi = lane == 31 ? (uint32_t)TILE : b0;
-    }
-    const uint32_t J0 = so[min(lo, (uint32_t)TILE)], J1 = so[hi];
-    if (J0 < J1) {
-      // the row holding edge J0 (skip empty rows), its end and carried sum
-      uint32_t row = lo;
-      while (so[row + 1] <= J0) ++row;
-      uint32_t nxt = so[row + 1];
-      double acc = sa[row];
-      for (uint32_t g = J0 & ~3u; g < J1; g += 4) {
-        const uint4 u = __ldg(reinterpret_cast<const uint4*>(edg + g));
-        const uint32_t id[4] = {u.x, u.y, u.z, u.w};
-        double x[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) x[q] = (g + q >= J0 && g + q < J1) ? __ldg(c + id[q]) : 0.0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const uint32_t j = g + q;
-          if (j < J0 || j >= J1) continue;
-          if (j == nxt) {  // row ends before edge j: store it, move to the row holding j
-            sa[row] = acc;
-            do { ++row; } while (so[row + 1] <= j);
-            nxt = so[row + 1];
-            acc = sa[row];
-          }
-          acc += x[q];
-        }
-      }
-      sa[row] = acc;
-    }
-    __syncwarp();
-    // epilogue: every lane finishes (or carries) rows lane, lane + 32, ...
-    for (uint32_t i = lane; i < nr; i += 32) {
-      const uint32_t v = vb + r0 + i;
-      if (!((a.low_bm[v >> 5] >> (v & 31u)) & 1u)) continue;
-      if (LAST) {
-        bool survive, changed;
-        const unsigned long long ev = finish_vertex<MODE>(a, v, sa[i], p, survive, changed, mag);
-        emax = ev > emax ? ev : emax;
-      } else {
-        a.acc64[v] = sa[i];
-      }
-    }
-    __syncwarp();
-  }
-  if (LAST) block_max_bits(emax, &st->el_bits[iter & 1]);
-}
-
 // MID / HIGH lists: Static and ND use the graph's class lists; the dynamic
 // modes use the affected MID / HIGH vertices the LOW kernel queued.
 template <int MODE>
@@ -676,53 +575,10 @@ void launch_commit_dyn32(const SolveArgs& a, int parity, cudaStream_t s) {
   k_commit_dyn32<<<cap_grid((a.n + kThreads - 1) / kThreads, 152 * 16), kThreads, 0, s>>>(a, parity);
 }
 
-// Packed LOW sweep over rows [v0, v1) of one LOW-only CSR (off indexed from
-// v0): tile and residency from the variant (prx_options.low_sweep).
-template <int MODE, int PASS>
-static void launch_packed(const SolveArgs& a, int variant, uint32_t v0, uint32_t v1, const uint32_t* off,
-                          const uint32_t* edg, int sms, cudaStream_t s) {
-  const int tile = (variant == 2 || variant == 5) ? 128 : 256;
-  const int per_sm = (variant == 4 || variant == 2) ? 8 : 4;
-  const uint64_t tiles = ((uint64_t)(v1 - v0) + tile - 1) / tile;
-  const int grid = cap_grid((tiles + kThreads / 32 - 1) / (kThreads / 32), sms * per_sm);
-  if (tile == 128) k_update_low_packed<MODE, PASS, 128><<<grid, kThreads, 0, s>>>(a, v0, v1, off, edg);
-  else k_update_low_packed<MODE, PASS, 256><<<grid, kThreads, 0, s>>>(a, v0, v1, off, edg);
-}
-
 template <int MODE>
 static bool update_class_t(const SolveArgs& a, const GraphDev& g, int cls, const ChunkLayout* lay, int sms,
                            cudaStream_t s) {
   constexpr bool DYN = ModeTraits<MODE>::DYN;
-  if constexpr (!DYN && !ModeTraits<MODE>::F32) {
-    // Static / ND / refinement: rows packed across lanes, on a LOW-only
-    // layout (a chunk layout, or the CSR itself when every row is LOW)
-    const bool all_low = g.cls_begin[1] == g.n;
-    if (cls == LOW && a.low_sweep >= 2 && ((lay && lay->K >= 1) || all_low)) {
-      if (g.cls_begin[1] == g.cls_begin[0]) return false;
-      const size_t nseg = (lay && !lay->seg_off.empty()) ? lay->seg_off.size() : (lay ? 1 : g.nseg);
-      for (size_t q = 0; q < nseg; ++q) {
-        const uint32_t v0 = nseg == 1 ? 0 : (uint32_t)(q << g.seg_shift);
-        const uint32_t v1 = nseg == 1 ? g.n : (uint32_t)std::min<uint64_t>(g.n, ((uint64_t)q + 1) << g.seg_shift);
-        if (!lay) {  // every row LOW: the in-CSR (per segment) is the layout
-          const uint32_t* off = nseg == 1 ? g.xtoff : g.xtoff + v0 + q;
-          const uint32_t* edg = nseg == 1 ? g.xtedg : g.xtedg + g.xtpos[q];
-          launch_packed<MODE, PASS_ONLY>(a, a.low_sweep, v0, v1, off, edg, sms, s);
-          continue;
-        }
-        const uint32_t* offs = nseg == 1 ? lay->off : lay->seg_off[q];
-        const uint32_t* edg = nseg == 1 ? lay->edg : lay->seg_edg[q];
-        const size_t row = (size_t)(v1 - v0) + 1;
-        for (int k = 0; k < lay->K; ++k) {
-          const uint32_t* off = offs + k * row;
-          if (lay->K == 1) launch_packed<MODE, PASS_ONLY>(a, a.low_sweep, v0, v1, off, edg, sms, s);
-          else if (k == 0) launch_packed<MODE, PASS_FIRST>(a, a.low_sweep, v0, v1, off, edg, sms, s);
-          else if (k == lay->K - 1) launch_packed<MODE, PASS_LAST>(a, a.low_sweep, v0, v1, off, edg, sms, s);
-          else launch_packed<MODE, PASS_INNER>(a, a.low_sweep, v0, v1, off, edg, sms, s);
-        }
-      }
-      return true;
-    }
-  }
   if (cls == LOW) {
     // static: skip when the graph has no LOW vertex; dynamic: always (the
     // first pass also maintains the bitmaps)

@@ -23,7 +23,7 @@ class Options(C.Structure):
                 ("prune_tolerance", C.c_double), ("damping", C.c_double), ("max_iterations", C.c_int),
                 ("precision", C.c_int), ("loop", C.c_int), ("partition", C.c_int), ("timing", C.c_int),
                 ("expansion", C.c_int), ("chunk_vertices", C.c_uint32), ("refine_sweeps", C.c_int),
-                ("l2_fetch_bytes", C.c_int), ("require_convergence", C.c_int), ("low_sweep", C.c_int),
+                ("l2_fetch_bytes", C.c_int), ("require_convergence", C.c_int),
                 ("hot_sources", C.c_int)]
 
 

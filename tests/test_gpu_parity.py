@@ -166,37 +166,6 @@ def test_chunked_gathers_bit_exact(pg, ctx, kind, width):
 
 
 @pytest.mark.parametrize("kind", ["rmat16", "web200k", "hubs", "grid256"])
-def test_low_sweep_kernels_bit_exact(pg, ctx, kind):
-    # Static / ND / the refinement's FP64 sweeps add the in-degree <= 64 rows
-    # either one row per lane (low_sweep 1) or with rows packed across a
-    # warp's lanes in equal shares of edges (2..5, and the default 0); each
-    # row is still summed front to back by one lane, so every variant, chunk
-    # width and loop gives the oracle's ranks bit for bit
-    xoff, xedg = _synthetic(pg, kind)
-    xt = O.transpose(xoff, xedg)
-    g, _ = _graph(pg, ctx, xoff, xedg, xt)
-    want, it_w = O.solve("static", None, None, *xt)
-    q = want * (1 + 1e-3 * np.sin(np.arange(len(want))))   # a perturbed start for ND
-    nd_want, nd_it = O.solve("naive_dynamic", None, None, *xt, q=q)
-    for variant in (0, 1, 2, 3, 4, 5):
-        for width in (0, 997, 30000, 10 ** 9):
-            for loop in (pg.LOOP_AUTO, pg.LOOP_HOST):
-                o = pg.options(low_sweep=variant, chunk_vertices=width, loop=loop)
-                got, res = pg.solve(ctx, g, pg.STATIC, opts=o)
-                assert res["iterations"] == it_w, (kind, variant, width, loop)
-                np.testing.assert_array_equal(got, want, err_msg=f"{kind} variant={variant} width={width}")
-            got, res = pg.solve(ctx, g, pg.NAIVE_DYNAMIC, q=q, opts=pg.options(low_sweep=variant, chunk_vertices=width))
-            assert res["iterations"] == nd_it
-            np.testing.assert_array_equal(got, nd_want, err_msg=f"{kind} ND variant={variant} width={width}")
-            got, _ = pg.solve(ctx, g, pg.STATIC, opts=pg.options(low_sweep=variant, chunk_vertices=width,
-                                                                 precision=pg.FP32_REFINE))
-            assert np.abs(got - want).max() <= 1e-9
-    with pytest.raises(Exception):
-        pg.solve(ctx, g, pg.STATIC, opts=pg.options(low_sweep=6))
-    g.close()
-
-
-@pytest.mark.parametrize("kind", ["rmat16", "web200k", "hubs", "grid256"])
 def test_hot_sources_bit_exact(pg, ctx, kind):
     # Static / ND and the refinement's FP64 sweeps gather the contributions of
     # the highest out-degree vertices from a dense copy (hot_sources: 0 the
