@@ -76,6 +76,11 @@ def parse():
     p.add_argument("--no-offsets64", action="store_true",
                    help="skip the 64-bit-offset graph (four copies of the bench graph, 4x its edges)")
     p.add_argument("--ingest-steps", type=int, default=2)
+    p.add_argument("--tour", default=None, metavar="PARTS",
+                   help="run every hot kernel once on small graphs for a profiler and exit: comma-separated parts "
+                        "web (web-like 6M: Static, FP32 refinement, batch apply, DF-P, DF, DT), grid (1024^2: DT), "
+                        "c3 (4096^2 grid: Static, batch apply, Static, DT, DF, DF-P), "
+                        "hubs (R-MAT 18, 48 edges/vertex: MID / HIGH rows, weighted solve and adjoint, PPR)")
     p.add_argument("--detail-out", default=None,
                    help="also write the detail record (every section) to this file; it always goes to stderr")
     a = p.parse_args()
@@ -317,6 +322,69 @@ def cpu_dfp_baseline(before, after, batch, q):
             "sample": "one 1e-4|E| batch, the same graph and ranks as the GPU DF-P beside it"}
 
 
+def run_tour(args):
+    """Each hot kernel at least once, on small graphs and with the host-driven
+    loop (kernels inside a CUDA graph's conditional loop are invisible to a
+    profiler): for kernel captures, not a measurement."""
+    import numpy as np
+    import torch
+    import pagerank_gb300 as pg
+    from pagerank_gb300 import autograd as A
+    ctx = pg.Context(0)
+    host = pg.LOOP_HOST
+
+    def web():
+        xoff, xedg = pg.graphs.weblike(6_000_000, alpha=2.1, dmin=5.9, dmax=100000, local=0.7, window=4096, seed=42)
+        g = pg.Graph(ctx, *pg.graphs.transpose(xoff, xedg), xoff, xedg)
+        # two source chunks (24 MB each), as the 50M graph's two of 200 MB
+        o = pg.options(loop=host, chunk_vertices=3_000_000)
+        q, _ = pg.solve(ctx, g, pg.STATIC, opts=o)
+        pg.solve(ctx, g, pg.STATIC, opts=pg.options(loop=host, chunk_vertices=3_000_000, precision=pg.FP32_REFINE))
+        m = len(xedg)
+        b = pg.graphs.random_batch(xoff, xedg, int(2e-5 * m), int(8e-5 * m), seed=3)
+        g.apply_batch(*b)
+        for mode in (pg.PRUNE_DYNAMIC_FRONTIER, pg.DYNAMIC_FRONTIER, pg.DYNAMIC_TRAVERSAL):
+            pg.solve(ctx, g, mode, (b[0], b[1]), (b[2], b[3]), q, o)
+        g.close()
+
+    def grid(side=1024, modes=(pg.DYNAMIC_TRAVERSAL,)):
+        xoff, xedg = pg.graphs.grid(side, 0.05, seed=42)
+        g = pg.Graph(ctx, *pg.graphs.transpose(xoff, xedg), xoff, xedg)
+        q, _ = pg.solve(ctx, g, pg.STATIC, opts=pg.options(loop=host))
+        m = len(xedg)
+        b = pg.graphs.random_batch(xoff, xedg, int(2e-5 * m), int(8e-5 * m), seed=3)
+        g.apply_batch(*b)
+        for mode in modes:
+            if mode == pg.STATIC:
+                pg.solve(ctx, g, mode, opts=pg.options(loop=host))
+            else:
+                pg.solve(ctx, g, mode, (b[0], b[1]), (b[2], b[3]), q, pg.options(loop=host))
+        g.close()
+
+    def c3():
+        grid(4096, (pg.STATIC, pg.DYNAMIC_TRAVERSAL, pg.DYNAMIC_FRONTIER, pg.PRUNE_DYNAMIC_FRONTIER))
+
+    def hubs():
+        xoff, xedg = pg.graphs.rmat(18, 48, a=0.7, b=0.1, c=0.1, seed=3)
+        g = pg.Graph(ctx, *pg.graphs.transpose(xoff, xedg), xoff, xedg)
+        pg.solve(ctx, g, pg.STATIC, opts=pg.options(loop=host))
+        n = len(xoff) - 1
+        rng = np.random.default_rng(1)
+        A.set_weights(ctx, g, torch.from_numpy(rng.uniform(0.5, 2.0, len(xedg)).astype(np.float32)).cuda())
+        r, _ = A.solve_weighted(ctx, g, None, opts=pg.options(tolerance=1e-12))
+        A.adjoint(ctx, g, r, torch.from_numpy(rng.standard_normal(n)).cuda(), None, opts=pg.options(tolerance=1e-12))
+        seeds = [rng.integers(0, n, k) for k in rng.integers(1, 100, 64)]
+        pg.solve_ppr_batched(ctx, g, seeds, pg.options(tolerance=1e-9, precision=pg.FP32_REFINE, loop=host))
+        g.close()
+
+    parts = {"web": web, "grid": grid, "c3": c3, "hubs": hubs}
+    for name in args.tour.split(","):
+        parts[name]()
+    torch.cuda.synchronize()
+    ctx.close()
+    log(f"tour {args.tour}: done")
+
+
 def run_reference(args):
     """Reference arm: the reference's CPU Static PageRank (OpenMP port of
     pagerankStaticOmp; the reference's own binary cannot be built on this
@@ -479,6 +547,7 @@ def run_grid(args, pg, ctx, local):
     bp = (bt[0].data_ptr(), bt[1].data_ptr(), len(du), bt[2].data_ptr(), bt[3].data_ptr(), len(iu))
     out = torch.empty_like(q)
     res = {}
+    pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr())
     st1 = pg.solve_device(ctx, g, pg.STATIC, None, ranks.data_ptr())
     for name, mode in (("dt", pg.DYNAMIC_TRAVERSAL), ("df", pg.DYNAMIC_FRONTIER), ("dfp", pg.PRUNE_DYNAMIC_FRONTIER)):
         pg.solve_device(ctx, g, mode, q.data_ptr(), out.data_ptr(), bp)
@@ -949,7 +1018,10 @@ def main():
     else:
         import __graft_entry__
         __graft_entry__.build()
-        run_ours(args)
+        if args.tour:
+            run_tour(args)
+        else:
+            run_ours(args)
 
 
 if __name__ == "__main__":

@@ -113,6 +113,20 @@ __device__ __forceinline__ unsigned long long dbits(double x) {
   return (unsigned long long)__double_as_longlong(x);
 }
 
+// GB300 executes two FP64 lanes per SM per clock, so one warp-wide FP64
+// instruction costs as much pipe time as dozens of integer ones: the helpers
+// below keep to the FP64 operations the reference's arithmetic needs and do
+// conversions and comparisons on bit patterns.
+
+// (double)d exactly, from integer operations: d = 2^e * 1.f with e the
+// position of the leading one.
+__device__ __forceinline__ double u32_to_f64(uint32_t d) {
+  const uint32_t lz = __clz(d);  // 32 for d == 0
+  const unsigned long long frac = ((unsigned long long)d << (21 + (lz & 31))) & ((1ull << 52) - 1);
+  const unsigned long long bits = ((unsigned long long)(1054 - lz) << 52) | frac;  // 1023 + (31 - lz)
+  return d ? __longlong_as_double((long long)bits) : 0.0;
+}
+
 // a / d correctly rounded, for an integer d >= 1 and y = RN(1/d), by
 // Markstein's method (P. Markstein, "IA-64 and Elementary Functions", 2000):
 // q = RN(a*y) is within one ulp of a/d, so r = a - q*d is exact in one fma,
@@ -122,28 +136,44 @@ __device__ __forceinline__ unsigned long long dbits(double x) {
 // the IEEE division by prx_selftest.
 __device__ __forceinline__ double div_count(double a, uint32_t d, double y) {
   const double q = a * y;
-  const double r = fma(-q, (double)d, a);
+  const double r = fma(-q, u32_to_f64(d), a);
   return fma(r, y, q);
 }
 
-// RN(x / m) <= c and RN(x / m) > c for x >= 0, m >= 0 -- the comparisons of
-// a relative change with a tolerance -- decided by one multiplication unless
-// x lies within 2^-48 of c*m, where the quotient is formed as written.  Away
-// from that band the rounded quotient is on the same side of c as the exact
-// one (the product's rounding is < 2^-52 relative), so the result always
-// equals the comparison of the correctly rounded quotient, NaN (0/0)
-// included.
-__device__ __forceinline__ bool quot_le(double x, double m, double c) {
-  const double cm = c * m;
-  if (x < cm * (1.0 - 0x1p-48)) return true;
-  if (x > cm * (1.0 + 0x1p-48)) return false;
-  return x / m <= c;
+// The relative-change tests of the frontier modes, RN(x / m) <= c and
+// RN(x / m) > c with x = |a - b| and m = fmax(a, b).  For non-negative finite
+// a, b (the ranks) m is the larger bit pattern, and non-negative doubles
+// order as their bit patterns: away from a band of 64 ulps around RN(c*m)
+// the exact quotient is more than an ulp of c from c (the product's rounding
+// is one half ulp), so its rounding lies on the same side, and one FP64
+// multiplication decides.  Inside the band, or for negative, infinite or NaN
+// operands or a subnormal c*m, the quotient is formed as written.
+struct RelChange {
+  double x, m;
+  bool fast;
+};
+__device__ __forceinline__ RelChange rel_change(double a, double b) {
+  const long long ab = __double_as_longlong(a), bb = __double_as_longlong(b);
+  RelChange r;
+  r.x = fabs(a - b);
+  r.fast = (ab | bb) >= 0 && __double_as_longlong(r.x) < 0x7ff0000000000000ll;
+  r.m = r.fast ? __longlong_as_double(ab > bb ? ab : bb) : fmax(a, b);
+  return r;
 }
-__device__ __forceinline__ bool quot_gt(double x, double m, double c) {
-  const double cm = c * m;
-  if (x > cm * (1.0 + 0x1p-48)) return true;
-  if (x < cm * (1.0 - 0x1p-48)) return false;
-  return x / m > c;
+constexpr long long kRelBand = 64;
+__device__ __forceinline__ int rel_side(const RelChange& r, double c) {  // -1 below c, +1 above, 0 undecided
+  if (!r.fast) return 0;
+  const long long xb = __double_as_longlong(r.x), cb = __double_as_longlong(c * r.m);
+  if (cb < (1ll << 52)) return 0;  // c*m subnormal or zero
+  return xb < cb - kRelBand ? -1 : (xb > cb + kRelBand ? 1 : 0);
+}
+__device__ __forceinline__ bool quot_le(const RelChange& r, double c) {
+  const int side = rel_side(r, c);
+  return side ? side < 0 : r.x / r.m <= c;
+}
+__device__ __forceinline__ bool quot_gt(const RelChange& r, double c) {
+  const int side = rel_side(r, c);
+  return side ? side > 0 : r.x / r.m > c;
 }
 
 // FP32 rounds of the refinement stop once the change they predict for their
@@ -202,6 +232,50 @@ __device__ __forceinline__ T lane_row_sum(const T* __restrict__ c, const uint32_
     acc += c0;
     if (b1) acc += c1;
     if (b2) acc += c2;
+  }
+  return acc;
+}
+
+// FP64 row sums, one row per lane, for a whole warp: every lane calls it
+// (lanes with nothing to add pass s == e).  Each lane adds c[edg[j]] for j in
+// [s, e) onto acc front to back, as lane_row_sum does, but the warp issues
+// exactly L adds, L the longest row: lane_row_sum's aligned head and tail
+// groups take up to three predicated adds each, and predicated-off FP64
+// instructions cost the warp as much as live ones.  Step k reads ids
+// s+4k .. s+4k+3 out of the two aligned 16-byte groups they span (the lane's
+// offset s & 3 picks them); a lane past its row's end adds +0.0, which leaves
+// acc (a sum of non-negative terms from +0) unchanged.
+__device__ __forceinline__ double warp_row_sums(const double* __restrict__ c, const uint32_t* __restrict__ edg,
+                                                uint32_t s, uint32_t e, double acc,
+                                                const double* __restrict__ ch, bool hot) {
+  const uint32_t len = e - s;
+  const uint32_t L = __reduce_max_sync(0xffffffffu, len);
+  if (L == 0) return acc;
+  const uint32_t j0 = s & ~3u, o = s & 3u;
+  const uint4 z = make_uint4(0, 0, 0, 0);
+  uint4 g0 = len ? __ldg(reinterpret_cast<const uint4*>(edg + j0)) : z;
+  for (uint32_t t = 0; t < L; t += 4) {
+    const uint32_t jn = j0 + t + 4;
+    const uint4 g1 = jn < e ? __ldg(reinterpret_cast<const uint4*>(edg + jn)) : z;
+    // ids at s+t+i, i < 4: the 8 words of g0:g1 shifted by o
+    const bool o1 = o & 1u, o2 = o & 2u;
+    const uint32_t a0 = o1 ? g0.y : g0.x, a1 = o1 ? g0.z : g0.y, a2 = o1 ? g0.w : g0.z, a3 = o1 ? g1.x : g0.w,
+                   a4 = o1 ? g1.y : g1.x, a5 = o1 ? g1.z : g1.y;
+    const uint32_t u0 = o2 ? a2 : a0, u1 = o2 ? a3 : a1, u2 = o2 ? a4 : a2, u3 = o2 ? a5 : a3;
+    double x0 = t < len ? gather(c, ch, hot, u0) : 0.0;
+    double x1 = t + 1 < len ? gather(c, ch, hot, u1) : 0.0;
+    double x2 = t + 2 < len ? gather(c, ch, hot, u2) : 0.0;
+    const double x3 = t + 3 < len ? gather(c, ch, hot, u3) : 0.0;
+    if (t + 4 <= L) {
+      acc += x0; acc += x1; acc += x2; acc += x3;
+    } else {  // the last 1..3 adds; the trip count is the same in every lane
+      for (uint32_t r = L - t; r; --r) {
+        acc += x0;
+        x0 = x1;
+        x1 = x2;
+      }
+    }
+    g0 = g1;
   }
   return acc;
 }

@@ -226,13 +226,20 @@ __global__ void k_selftest_div(uint32_t dmax, uint32_t per, unsigned long long* 
     const double a = __longlong_as_double((long long)(((uint64_t)ex << 52) | (z & 0xFFFFFFFFFFFFFull)));
     const double y = 1.0 / (double)d;
     if (dbits(div_count(a, d, y)) != dbits(a / (double)d)) ++mine;
-    // the tolerance comparisons of a relative change, around their tie band:
-    // x = c*m*(1 + t 2^-50) for t in [-2^8, 2^8), c = 1e-6 * (1 + small)
+    if (dbits(u32_to_f64(d)) != dbits((double)d) || (i == 0 && dbits(u32_to_f64(0)) != 0)) ++mine;
+    // the tolerance comparisons of a relative change |m - b| / max(m, b)
+    // around their tie band: b = m -+ c*m*(1 + t 2^-50) for t in [-2^8, 2^8)
+    // (+-1024 ulps about c*m), c = 1e-6 * (1 + small), either argument order;
+    // every 64th case with b negated (the division path)
     const double m = a;
     const double c = 1e-6 * (1.0 + (double)(z & 0xffff) * 0x1p-20);
     const double t = (double)((int)((z >> 16) & 0x1ff) - 256);
-    const double x = c * m * (1.0 + t * 0x1p-50);
-    if (quot_le(x, m, c) != (x / m <= c) || quot_gt(x, m, c) != (x / m > c)) ++mine;
+    const double xx = c * m * (1.0 + t * 0x1p-50);
+    double b = ((z >> 25) & 1) ? m - xx : m + xx;
+    if (((z >> 27) & 63) == 0) b = -b;
+    const RelChange rc = ((z >> 26) & 1) ? rel_change(m, b) : rel_change(b, m);
+    const double q = fabs(m - b) / fmax(m, b);
+    if (quot_le(rc, c) != (q <= c) || quot_gt(rc, c) != (q > c)) ++mine;
   }
   if (mine) atomicAdd(bad, mine);
 }
@@ -613,9 +620,30 @@ cudaError_t ensure_chunks(GraphDev& g, uint32_t width, int sms, cudaStream_t s, 
 // ---- hot sources --------------------------------------------------------------
 constexpr uint32_t kDegBins = 1u << 16;  // out-degree histogram (the last bin holds every larger degree)
 
-__global__ void k_degree_hist(const uint32_t* __restrict__ xtdat, uint32_t n, uint32_t* __restrict__ hist) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
-    atomicAdd(&hist[min(xtdat[v], kDegBins - 1)], 1u);
+// Out-degrees crowd into a few bins (every vertex of a grid has 5 to 7), so
+// a warp adds each distinct degree once (__match_any_sync), and a block
+// counts the degrees below kSmallBins in shared memory before adding them to
+// the global bins.
+constexpr uint32_t kSmallBins = 1024;
+__global__ void __launch_bounds__(256) k_degree_hist(const uint32_t* __restrict__ xtdat, uint32_t n,
+                                                     uint32_t* __restrict__ hist) {
+  __shared__ uint32_t sh[kSmallBins];
+  for (uint32_t i = threadIdx.x; i < kSmallBins; i += blockDim.x) sh[i] = 0;
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u;
+  // the loop bound is the same for the whole block, so every warp stays converged for the match
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x; base < n; base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t v = base + threadIdx.x;
+    const uint32_t d = v < n ? min(xtdat[v], kDegBins - 1) : 0xffffffffu;
+    const unsigned same = __match_any_sync(0xffffffffu, d);
+    if (d != 0xffffffffu && (uint32_t)(__ffs(same) - 1) == lane) {
+      if (d < kSmallBins) atomicAdd(&sh[d], (uint32_t)__popc(same));
+      else atomicAdd(&hist[d], (uint32_t)__popc(same));
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < kSmallBins; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
 __global__ void k_hot_flags(const uint32_t* __restrict__ xtdat, uint32_t n, uint32_t t, uint32_t* __restrict__ flag) {

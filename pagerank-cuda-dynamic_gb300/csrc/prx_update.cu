@@ -47,6 +47,10 @@ template <int MODE> struct ModeTraits {
   static constexpr bool FRONTIER = DYN && BASE >= PRX_DYNAMIC_FRONTIER;
   static constexpr bool PRUNE = BASE == PRX_PRUNE_DYNAMIC_FRONTIER;
   using V = typename std::conditional<F32, float, double>::type;  // rank / contribution type
+  // resident blocks of 256 per SM the LOW kernel is compiled (register
+  // budget) and launched for: the dynamic modes' bookkeeping needs more than
+  // 32 registers a thread
+  static constexpr int LOW_BLOCKS = (DYN || F32) ? 6 : 8;
 };
 
 // Rank, contribution and carried-sum arrays of a mode: FP64 r / c / acc64,
@@ -130,10 +134,10 @@ __device__ __forceinline__ unsigned long long finish_vertex(const SolveArgs& a, 
     }
     survive = true;
     changed = false;
-    if (T::FRONTIER) {  // rel = ev / max(rv, av) compared with C and D
-      const double m = fmax(rv, av);
-      if (T::PRUNE && quot_le(ev, m, a.C)) survive = false;  // :106
-      changed = quot_gt(ev, m, a.D);                          // :107
+    if constexpr (T::FRONTIER) {  // rel = ev / max(rv, av) compared with C and D
+      const RelChange rc = rel_change(av, rv);
+      if (T::PRUNE && quot_le(rc, a.C)) survive = false;  // :106
+      changed = quot_gt(rc, a.D);                          // :107
     }
     return dbits(ev);
   }
@@ -150,10 +154,9 @@ enum Pass { PASS_ONLY = 0, PASS_FIRST = 1, PASS_INNER = 2, PASS_LAST = 3 };
 // hot: the layout encodes hot sources (the FP64 modes); their contributions
 // are gathered from a.ch[p].
 template <int MODE, int PASS>
-__global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, uint32_t vb, uint32_t ve,
-                                                         const unsigned long long* __restrict__ base,
-                                                         uint32_t shift, const uint32_t* __restrict__ off,
-                                                         const uint32_t* __restrict__ edg, bool hot) {
+__global__ void __launch_bounds__(kThreads, ModeTraits<MODE>::LOW_BLOCKS)
+    k_update_low(SolveArgs a, uint32_t vb, uint32_t ve, const unsigned long long* __restrict__ base, uint32_t shift,
+                 const uint32_t* __restrict__ off, const uint32_t* __restrict__ edg, bool hot) {
   using T = ModeTraits<MODE>;
   constexpr bool FIRST = PASS == PASS_ONLY || PASS == PASS_FIRST;
   constexpr bool LAST = PASS == PASS_ONLY || PASS == PASS_LAST;
@@ -211,9 +214,12 @@ __global__ void __launch_bounds__(kThreads) k_update_low(SolveArgs a, uint32_t v
     mine = low && (FIRST || LAST || s < e);
     bool survive = false, changed = false;
     V acc = V(0);
-    if (mine)
-      acc = lane_row_sum(c, seg_edges(edg, base, shift, v), s, e, FIRST ? V(0) : carried_of<MODE>(a)[v], ch,
-                         !T::F32 && hot);
+    if constexpr (T::F32) {
+      if (mine) acc = lane_row_sum(c, seg_edges(edg, base, shift, v), s, e, FIRST ? V(0) : carried_of<MODE>(a)[v]);
+    } else {  // the whole warp sums together
+      const V init = (mine && !FIRST) ? carried_of<MODE>(a)[v] : V(0);
+      acc = warp_row_sums(c, seg_edges(edg, base, shift, v), s, mine ? e : s, init, ch, hot);
+    }
     if (mine) {
       edges += e - s;
       if (LAST) {
@@ -585,7 +591,7 @@ static bool update_class_t(const SolveArgs& a, const GraphDev& g, int cls, const
     if (!DYN && g.cls_begin[1] == g.cls_begin[0]) return false;
     if (!lay || (lay->K <= 1 && !lay->hot)) {
       const uint64_t words = ((uint64_t)g.n + 31) / 32;
-      const int grid = cap_grid((words + 7) / 8, sms * 8);
+      const int grid = cap_grid((words + 7) / 8, sms * ModeTraits<MODE>::LOW_BLOCKS);
       k_update_low<MODE, PASS_ONLY>
           <<<grid, kThreads, 0, s>>>(a, 0, g.n, g.xtbase, g.seg_shift, g.xtoff, g.xtedg, false);
       return true;
@@ -599,7 +605,7 @@ static bool update_class_t(const SolveArgs& a, const GraphDev& g, int cls, const
       const uint32_t* offs = nseg == 1 ? lay->off : lay->seg_off[q];
       const uint32_t* edg = nseg == 1 ? lay->edg : lay->seg_edg[q];
       const size_t row = (size_t)(v1 - v0) + 1;
-      const int grid = cap_grid(((uint64_t)(v1 - v0) + 31) / 32 / 8 + 1, sms * 8);
+      const int grid = cap_grid(((uint64_t)(v1 - v0) + 31) / 32 / 8 + 1, sms * ModeTraits<MODE>::LOW_BLOCKS);
       for (int k = 0; k < lay->K; ++k) {
         const uint32_t* off = offs + k * row;
         if (lay->K == 1)
