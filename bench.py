@@ -80,6 +80,7 @@ def parse():
                    help="run every hot kernel once on small graphs for a profiler and exit: comma-separated parts "
                         "web (web-like 6M: Static, FP32 refinement, batch apply, DF-P, DF, DT), grid (1024^2: DT), "
                         "c3 (4096^2 grid: Static, batch apply, Static, DT, DF, DF-P), "
+                        "apply50m (the web-like graph of --vertices: two batch applies of 1e-4|E|), "
                         "hubs (R-MAT 18, 48 edges/vertex: MID / HIGH rows, weighted solve and adjoint, PPR)")
     p.add_argument("--detail-out", default=None,
                    help="also write the detail record (every section) to this file; it always goes to stderr")
@@ -377,7 +378,20 @@ def run_tour(args):
         pg.solve_ppr_batched(ctx, g, seeds, pg.options(tolerance=1e-9, precision=pg.FP32_REFINE, loop=host))
         g.close()
 
-    parts = {"web": web, "grid": grid, "c3": c3, "hubs": hubs}
+    def apply50m():
+        xoff, xedg = pg.graphs.weblike(args.vertices, alpha=2.1, dmin=args.dmin, dmax=100000, local=0.7,
+                                       window=4096, seed=args.seed)
+        g = pg.Graph(ctx, *pg.graphs.transpose(xoff, xedg), xoff, xedg)
+        m = len(xedg)
+        for k in range(2):
+            b = g.gen_batch(int(2e-5 * m), int(8e-5 * m), seed=3 + k)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            g.apply_batch(*b)
+            log(f"apply of {len(b[0])} deletions and {len(b[2])} insertions: {1e3 * (time.perf_counter() - t):.1f} ms")
+        g.close()
+
+    parts = {"web": web, "grid": grid, "c3": c3, "hubs": hubs, "apply50m": apply50m}
     for name in args.tour.split(","):
         parts[name]()
     torch.cuda.synchronize()

@@ -232,7 +232,10 @@ int prx_graph_download(prx_graph* g, uint32_t* xoff, uint32_t* xedg,
  * and free of duplicates -- the output of tidyBatchUpdateU
  * (inc/batch.hxx:200-208).  Same effect as applyBatchUpdateOmpU
  * (inc/batch.hxx:239-247) followed by transposeWithDegreeOmp
- * (inc/transpose.hxx:128-134).  Host pointers. */
+ * (inc/transpose.hxx:128-134).  Graphs with row segments
+ * (prx_graph_create64) keep their segments, which move to new bases; each
+ * must stay below 2^32 - 8 edges (PRX_ERANGE otherwise, graph unchanged).
+ * Host pointers. */
 int prx_graph_apply_batch(prx_graph* g,
                           const uint32_t* delu, const uint32_t* delv, uint64_t nd,
                           const uint32_t* insu, const uint32_t* insv, uint64_t ni);

@@ -1016,7 +1016,6 @@ int prx_graph_apply_batch(prx_graph* gr, const uint32_t* du, const uint32_t* dv,
   GraphDev& g = gr->g;
   prx_context* c = gr->ctx;
   if (!g.xoff) FAIL(PRX_ESTATE, "prx_graph_apply_batch: graph has no out-CSR");
-  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_graph_apply_batch: not for graphs with row segments (64-bit offsets)");
   if (ni && !iv) FAIL(PRX_EINVAL, "prx_graph_apply_batch: insertions need targets");
   int st = check_batch_ids(g.n, du, dv, nd, iu, iv, ni);
   if (st) return st;
@@ -1027,7 +1026,9 @@ int prx_graph_apply_batch(prx_graph* gr, const uint32_t* du, const uint32_t* dv,
   };
   if (!sorted_unique(du, dv, nd) || !sorted_unique(iu, iv, ni))
     FAIL(PRX_EINVAL, "prx_graph_apply_batch: batch must be sorted by (u, v) and unique (tidyBatchUpdateU)");
-  if (g.m - nd + ni > 0xffffffffull) FAIL(PRX_ERANGE, "prx_graph_apply_batch: edge count would reach 2^32");
+  if (g.nseg == 1 && g.m - nd + ni > 0xffffffffull)
+    FAIL(PRX_ERANGE, "prx_graph_apply_batch: edge count would reach 2^32 (create the graph with prx_graph_create64)");
+  if (nd + ni > kMaxVertices) FAIL(PRX_ERANGE, "prx_graph_apply_batch: batch too large");
   // The in-CSR wants the batch ordered by (v, u): the device sorts copies of
   // the (u, v)-sorted lists by v (batch_by_target).
   TRY_CUDA_ST(cudaSetDevice(c->device));
@@ -1045,6 +1046,8 @@ int prx_graph_apply_batch(prx_graph* gr, const uint32_t* du, const uint32_t* dv,
   const cudaError_t e = apply_batch_device(g, c->batch, nd, ni, c->sms, c->stream);
   if (e == cudaErrorInvalidValue)
     FAIL(PRX_EINVAL, "prx_graph_apply_batch: batch is not tidy (a deletion is missing or an insertion exists)");
+  if (e == cudaErrorInvalidConfiguration)
+    FAIL(PRX_ERANGE, "prx_graph_apply_batch: a row segment would hold 2^32 edges or more");
   TRY_CUDA_ST(e);
   drop_weights(g);  // the edges changed: weights must be set again
   return PRX_OK;

@@ -203,11 +203,27 @@ __global__ void __launch_bounds__(256) k_cls_edges(const uint32_t* __restrict__ 
   if (threadIdx.x < NCLS && acc[threadIdx.x]) atomicAdd(&out[threadIdx.x], acc[threadIdx.x]);
 }
 
+// RN(1/d) for every out-degree below kRcpTable, formed by the same divisions
+// as k_reciprocals (FP64 division is many FP64 instructions on this part, and
+// 50M vertices share a few thousand degrees).  Filled before each use on the
+// stream that reads it.
+constexpr uint32_t kRcpTable = 1u << 16;
+__device__ double g_rcp_table[kRcpTable];
+__device__ float g_rcp32_table[kRcpTable];
+
+__global__ void k_rcp_table() {
+  for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < kRcpTable; d += gridDim.x * blockDim.x) {
+    g_rcp_table[d] = 1.0 / (double)d;
+    g_rcp32_table[d] = 1.0f / (float)d;
+  }
+}
+
 __global__ void k_reciprocals(const uint32_t* __restrict__ deg, uint32_t n, double* __restrict__ rcp,
                               float* __restrict__ rcp32) {
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-    rcp[v] = 1.0 / (double)deg[v];
-    rcp32[v] = 1.0f / (float)deg[v];
+    const uint32_t d = deg[v];
+    rcp[v] = d < kRcpTable ? g_rcp_table[d] : 1.0 / (double)d;
+    rcp32[v] = d < kRcpTable ? g_rcp32_table[d] : 1.0f / (float)d;
   }
 }
 
@@ -747,7 +763,10 @@ cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
     if (e != cudaSuccess) return e;
   }
   if (n) k_low_bitmap<<<sms * 4, 256, 0, s>>>(g.xtoff, g.seg_shift, n, g.low_bm);
-  if (n) k_reciprocals<<<sms * 4, 256, 0, s>>>(g.xtdat, n, g.rcp, g.rcp32);
+  if (n) {
+    k_rcp_table<<<kRcpTable / 256, 256, 0, s>>>();
+    k_reciprocals<<<sms * 4, 256, 0, s>>>(g.xtdat, n, g.rcp, g.rcp32);
+  }
   if (!g.cls_list) {
     cudaError_t e = graph_alloc(&g.cls_list, sizeof(uint32_t) * (n ? n : 1), s);
     if (e != cudaSuccess) return e;

@@ -95,6 +95,8 @@ void ppr_free(PprWs* w) {
 struct PprArgs {
   const uint32_t* xtoff;
   const uint32_t* xtedg;
+  const unsigned long long* xtbase;  // row segments (see GraphDev); null: one segment
+  uint32_t seg_shift;
   const double* rcp;
   const float* rcp32;
   const uint32_t* toff;
@@ -134,17 +136,18 @@ __device__ __forceinline__ const typename PprType<MODE>::V2* ppr_src(const PprAr
   return reinterpret_cast<const V2*>(a.e[st->k32 & 1]);
 }
 
-// acc += row(u) / outdeg(u) over the in-edges [s, e) (lane: its two columns).
+// acc += row(u) / outdeg(u) over the in-edges [s, e) of edg (v's segment of
+// the in-CSR; lane: its two columns).
 template <int MODE>
 __device__ __forceinline__ void ppr_gather(const PprArgs& a, const typename PprType<MODE>::V2* __restrict__ src,
-                                           uint32_t s, uint32_t e, typename PprType<MODE>::V2& acc) {
+                                           const uint32_t* __restrict__ edg, uint32_t s, uint32_t e,
+                                           typename PprType<MODE>::V2& acc) {
   using S = typename PprType<MODE>::S;
   using V2 = typename PprType<MODE>::V2;
   const S* __restrict__ rc;
   if constexpr (MODE == PPR_S32) rc = a.rcp32;
   else rc = a.rcp;
   const uint32_t lane = lane_id();
-  const uint32_t* __restrict__ edg = a.xtedg;
   uint32_t j = s;
   for (; j + 4 <= e; j += 4) {
     const uint32_t u0 = __ldg(edg + j), u1 = __ldg(edg + j + 1), u2 = __ldg(edg + j + 2), u3 = __ldg(edg + j + 3);
@@ -232,12 +235,13 @@ __global__ void __launch_bounds__(256) k_ppr_low(PprArgs a) {
   unsigned int emag = 0;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < a.n; v += warps) {
-    const uint32_t s = __ldg(a.xtoff + v), e = __ldg(a.xtoff + v + 1);
+    const uint64_t iv = seg_index(v, a.seg_shift);
+    const uint32_t s = __ldg(a.xtoff + iv), e = __ldg(a.xtoff + iv + 1);
     if (e - s > a.low_max) continue;
     V2 acc;
     acc.x = 0;
     acc.y = 0;
-    ppr_gather<MODE>(a, src, s, e, acc);
+    ppr_gather<MODE>(a, src, seg_edges(a.xtedg, a.xtbase, a.seg_shift, v), s, e, acc);
     unsigned int em = 0;
     const unsigned long long d = ppr_finish<MODE>(a, st, v, acc, &em);
     dmax = d > dmax ? d : dmax;
@@ -259,13 +263,13 @@ __global__ void __launch_bounds__(kSegWarps * 32) k_ppr_seg(PprArgs a) {
   V2* part = reinterpret_cast<V2*>(a.part);
   for (uint32_t g = blockIdx.x; g < a.nseg; g += gridDim.x) {
     const uint32_t v = a.seg_v[g], s0 = a.seg_e[g];
-    const uint32_t end = min(s0 + a.seg, a.xtoff[v + 1]);
+    const uint32_t end = min(s0 + a.seg, a.xtoff[seg_index(v, a.seg_shift) + 1]);
     const uint32_t per = a.seg / kSegWarps;
     const uint32_t s = min(s0 + w * per, end), e = min(s + per, end);
     V2 acc;
     acc.x = 0;
     acc.y = 0;
-    ppr_gather<MODE>(a, src, s, e, acc);
+    ppr_gather<MODE>(a, src, seg_edges(a.xtedg, a.xtbase, a.seg_shift, v), s, e, acc);
     sh[w][lane] = acc;
     __syncthreads();
     if (w == 0) {
@@ -404,34 +408,36 @@ __global__ void k_ppr_init(PprArgs a) {
 }
 
 // Segment counts of the long vertices (ceil(indeg / seg)), then the segments.
-__global__ void k_ppr_segcount(const uint32_t* __restrict__ xtoff, const uint32_t* __restrict__ big, uint32_t nbig,
-                               uint32_t seg, uint32_t* __restrict__ cnt) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nbig; i += gridDim.x * blockDim.x) {
-    const uint32_t v = big[i];
-    cnt[i] = (xtoff[v + 1] - xtoff[v] + seg - 1) / seg;
-  }
+__global__ void k_ppr_segcount(const uint32_t* __restrict__ xtoff, uint32_t shift, const uint32_t* __restrict__ big,
+                               uint32_t nbig, uint32_t seg, uint32_t* __restrict__ cnt) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nbig; i += gridDim.x * blockDim.x)
+    cnt[i] = (row_len(xtoff, shift, big[i]) + seg - 1) / seg;
 }
 
 // Vertices of in-degree above t: flags (n + 1 entries, the last 0) for the
 // scan, then the ascending list.
-__global__ void k_ppr_bigflags(const uint32_t* __restrict__ xtoff, uint32_t n, uint32_t t, uint32_t* __restrict__ f) {
+__global__ void k_ppr_bigflags(const uint32_t* __restrict__ xtoff, uint32_t shift, uint32_t n, uint32_t t,
+                               uint32_t* __restrict__ f) {
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += gridDim.x * blockDim.x)
-    f[v] = v < n && xtoff[v + 1] - xtoff[v] > t ? 1u : 0u;
+    f[v] = v < n && row_len(xtoff, shift, v) > t ? 1u : 0u;
 }
-__global__ void k_ppr_biglist(const uint32_t* __restrict__ xtoff, uint32_t n, uint32_t t,
+__global__ void k_ppr_biglist(const uint32_t* __restrict__ xtoff, uint32_t shift, uint32_t n, uint32_t t,
                               const uint32_t* __restrict__ pos, uint32_t* __restrict__ big) {
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
-    if (xtoff[v + 1] - xtoff[v] > t) big[pos[v]] = v;
+    if (row_len(xtoff, shift, v) > t) big[pos[v]] = v;
 }
 
-__global__ void k_ppr_segfill(const uint32_t* __restrict__ xtoff, const uint32_t* __restrict__ big, uint32_t nbig,
-                              uint32_t seg, const uint32_t* __restrict__ start, uint32_t* __restrict__ seg_v,
-                              uint32_t* __restrict__ seg_e) {
+// seg_e: the segment's first in-edge, relative to v's row segment like the
+// offsets.
+__global__ void k_ppr_segfill(const uint32_t* __restrict__ xtoff, uint32_t shift, const uint32_t* __restrict__ big,
+                              uint32_t nbig, uint32_t seg, const uint32_t* __restrict__ start,
+                              uint32_t* __restrict__ seg_v, uint32_t* __restrict__ seg_e) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nbig; i += gridDim.x * blockDim.x) {
     const uint32_t v = big[i];
+    const uint32_t s0 = xtoff[seg_index(v, shift)];
     for (uint32_t g = start[i], k = 0; g < start[i + 1]; ++g, ++k) {
       seg_v[g] = v;
-      seg_e[g] = xtoff[v] + k * seg;
+      seg_e[g] = s0 + k * seg;
     }
   }
 }
@@ -517,9 +523,9 @@ static int ppr_segments(prx_context* c, const GraphDev& g, PprArgs& a) {
   } else {
     TRY_CUDA_ST(grow(&w.big, w.big_cap, 2 * ((size_t)g.n + 1)));
     uint32_t* pos = w.big + g.n + 1;
-    k_ppr_bigflags<<<grid_for((uint64_t)g.n + 1, 256, c->sms * 16), 256, 0, s>>>(g.xtoff, g.n, a.low_max, pos);
+    k_ppr_bigflags<<<grid_for((uint64_t)g.n + 1, 256, c->sms * 16), 256, 0, s>>>(g.xtoff, g.seg_shift, g.n, a.low_max, pos);
     TRY_CUDA_ST(exclusive_scan_u32(pos, g.n + 1, s));
-    k_ppr_biglist<<<grid_for(g.n, 256, c->sms * 16), 256, 0, s>>>(g.xtoff, g.n, a.low_max, pos, w.big);
+    k_ppr_biglist<<<grid_for(g.n, 256, c->sms * 16), 256, 0, s>>>(g.xtoff, g.seg_shift, g.n, a.low_max, pos, w.big);
     TRY_CUDA_ST(cudaMemcpyAsync(&nbig, pos + g.n, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
     TRY_CUDA_ST(cudaStreamSynchronize(s));
     a.big = w.big;
@@ -529,14 +535,14 @@ static int ppr_segments(prx_context* c, const GraphDev& g, PprArgs& a) {
   if (!nbig) return PRX_OK;
   TRY_CUDA_ST(grow(&w.segstart, w.segstart_cap, (size_t)nbig + 1));
   const int grid = grid_for(nbig, 256, c->sms * 4);
-  k_ppr_segcount<<<grid, 256, 0, s>>>(g.xtoff, a.big, nbig, a.seg, w.segstart);
+  k_ppr_segcount<<<grid, 256, 0, s>>>(g.xtoff, g.seg_shift, a.big, nbig, a.seg, w.segstart);
   TRY_CUDA_ST(exclusive_scan_u32(w.segstart, nbig + 1, s));
   uint32_t nseg = 0;
   TRY_CUDA_ST(cudaMemcpyAsync(&nseg, w.segstart + nbig, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   TRY_CUDA_ST(cudaStreamSynchronize(s));
   TRY_CUDA_ST(grow(&w.seg, w.seg_cap, 2 * (size_t)nseg));
   TRY_CUDA_ST(grow(&w.part, w.part_cap, (size_t)nseg * kCols));
-  k_ppr_segfill<<<grid, 256, 0, s>>>(g.xtoff, a.big, nbig, a.seg, w.segstart, w.seg, w.seg + nseg);
+  k_ppr_segfill<<<grid, 256, 0, s>>>(g.xtoff, g.seg_shift, a.big, nbig, a.seg, w.segstart, w.seg, w.seg + nseg);
   a.segstart = w.segstart;
   a.seg_v = w.seg;
   a.seg_e = w.seg + nseg;
@@ -794,7 +800,6 @@ static int ppr_common(prx_context* c, prx_graph* gr, uint32_t nvec, const uint32
   if (!(o.damping >= 0 && o.damping < 1)) FAIL(PRX_EINVAL, "prx_solve_ppr_batched: damping must be in [0, 1)");
   const GraphDev& g = gr->g;
   if (seed_off[0] != 0) FAIL(PRX_EINVAL, "prx_solve_ppr_batched: seed_off[0] must be 0");
-  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_solve_ppr_batched: not for graphs with row segments (64-bit offsets)");
   for (uint32_t k = 0; k < nvec; ++k)
     if (seed_off[k + 1] <= seed_off[k]) FAIL(PRX_EINVAL, "prx_solve_ppr_batched: every seed set must be non-empty");
   for (uint32_t i = 0; i < seed_off[nvec]; ++i)
@@ -814,6 +819,8 @@ static int ppr_common(prx_context* c, prx_graph* gr, uint32_t nvec, const uint32
   PprArgs a{};
   a.xtoff = g.xtoff;
   a.xtedg = g.xtedg;
+  a.xtbase = g.xtbase;
+  a.seg_shift = g.seg_shift;
   a.rcp = g.rcp;
   a.rcp32 = g.rcp32;
   a.x[0] = w.x[0];
@@ -878,7 +885,6 @@ int prx_solve_ppr_batched_device(prx_context* c, prx_graph* gr, uint32_t nvec, c
 int prx_autotune_ppr(prx_context* c, prx_graph* gr, prx_ppr_tune_result* out) {
   if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_autotune_ppr: bad context or graph");
   GraphDev& g = gr->g;
-  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_autotune_ppr: not for graphs with row segments (64-bit offsets)");
   prx_ppr_tune_result best{};
   if (g.n == 0) {
     if (out) *out = best;

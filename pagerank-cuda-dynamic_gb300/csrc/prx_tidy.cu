@@ -21,6 +21,7 @@
 // keys u * 2^b + v (plus v * 2^b + v for the self-loops), radix sort, unique,
 // row starts from the sorted keys; the transpose the same from v * 2^b + u.
 #include <algorithm>
+#include <vector>
 #include "prx_ctx.h"
 #include "prx_device.cuh"
 #include "prx_hash.h"
@@ -44,11 +45,29 @@ __device__ __forceinline__ uint32_t edge_position(const uint32_t* __restrict__ x
   return (lo < xoff[u + 1] && xedg[lo] == v) ? lo : 0xffffffffu;
 }
 
-// keep[i] = 1 for kept edges; key[i] = the edge's sort key.  Ids >= n (the
-// device batch generator's empty slots) are never kept.
-__global__ void k_tidy_keys(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg, uint32_t n,
+// Does the out-CSR with row segments (see GraphDev) hold edge (u, v)?
+__device__ __forceinline__ bool seg_has_edge(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg,
+                                             const unsigned long long* __restrict__ base, uint32_t shift, uint32_t u,
+                                             uint32_t v) {
+  const uint64_t k = seg_index(u, shift);
+  const uint32_t* row = seg_edges(xedg, base, shift, u);
+  uint32_t lo = xoff[k], hi = xoff[k + 1];
+  const uint32_t end = hi;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (row[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo < end && row[lo] == v;
+}
+
+// keep[i] = 1 for kept edges; key[i] = the edge's sort key: a deletion's
+// out-CSR position with pos_keys (one row segment), else u * 2^vbits + v.
+// Ids >= n (the device batch generator's empty slots) are never kept.
+__global__ void k_tidy_keys(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg,
+                            const unsigned long long* __restrict__ base, uint32_t shift, uint32_t n,
                             const uint32_t* __restrict__ u, const uint32_t* __restrict__ v, uint32_t count,
-                            int deletions, int vbits, uint32_t* __restrict__ keep,
+                            int deletions, int pos_keys, int vbits, uint32_t* __restrict__ keep,
                             unsigned long long* __restrict__ key) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
     if (u[i] >= n || v[i] >= n) {
@@ -56,13 +75,14 @@ __global__ void k_tidy_keys(const uint32_t* __restrict__ xoff, const uint32_t* _
       key[i] = 0;
       continue;
     }
-    const uint32_t p = edge_position(xoff, xedg, u[i], v[i]);
-    if (deletions) {
-      keep[i] = p != 0xffffffffu;
-      key[i] = p;
+    const unsigned long long uv = ((unsigned long long)u[i] << vbits) | v[i];
+    if (pos_keys) {
+      const uint32_t p = edge_position(xoff, xedg, u[i], v[i]);
+      keep[i] = (p != 0xffffffffu) == (deletions != 0);
+      key[i] = deletions ? p : uv;
     } else {
-      keep[i] = p == 0xffffffffu;
-      key[i] = ((unsigned long long)u[i] << vbits) | v[i];
+      keep[i] = seg_has_edge(xoff, xedg, base, shift, u[i], v[i]) == (deletions != 0);
+      key[i] = uv;
     }
   }
 }
@@ -287,16 +307,17 @@ __global__ void k_first_flags(const unsigned long long* __restrict__ key, uint32
     flag[i] = (i == 0 || key[i] != key[i - 1]) ? 1u : 0u;
 }
 
-// Decode the unique keys at pos[i] (flag[i]) into (u, v).
+// Decode the unique keys at pos[i] (flag[i]) into (u, v); pos_keys: the
+// keys are out-CSR positions.
 __global__ void k_decode(const unsigned long long* __restrict__ key, const uint32_t* __restrict__ flag,
-                         const uint32_t* __restrict__ pos, uint32_t count, int deletions, int vbits,
+                         const uint32_t* __restrict__ pos, uint32_t count, int pos_keys, int vbits,
                          const uint32_t* __restrict__ xoff, uint32_t n, const uint32_t* __restrict__ xedg,
                          uint32_t* __restrict__ ou, uint32_t* __restrict__ ov) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
     if (!flag[i]) continue;
     const unsigned long long k = key[i];
     uint32_t u, v;
-    if (deletions) {  // out-CSR position: v from the edge, u the row holding it
+    if (pos_keys) {  // out-CSR position: v from the edge, u the row holding it
       const uint32_t p = (uint32_t)k;
       v = xedg[p];
       uint32_t lo = 0, hi = n;  // last row whose start is <= p
@@ -423,23 +444,51 @@ __global__ void k_ingest_degree(const uint32_t* __restrict__ off, uint32_t n, ui
 // deletion i is the first non-self-loop edge among kDelTries uniform draws
 // (n, n when all are self-loops: dropped by the tidy); insertion i is a
 // uniform pair.
+// Edge e of the out-CSR in the compact order (the order of prx_graph_download)
+// as (u, v).  With row segments, seg holds each segment's first edge in the
+// compact order, then its position in the device array (nseg each).
+__device__ __forceinline__ void edge_at(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg, uint32_t n,
+                                        uint32_t shift, uint32_t nseg, const unsigned long long* __restrict__ seg,
+                                        uint64_t e, uint32_t& u, uint32_t& v) {
+  uint32_t k = 0, r0 = 0, rows = n;
+  uint64_t rel = e, at = 0;
+  if (nseg > 1) {
+    uint32_t lo = 0, hi = nseg - 1;  // last segment whose first edge is <= e
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (seg[mid] <= e) lo = mid;
+      else hi = mid - 1;
+    }
+    k = lo;
+    r0 = (uint32_t)((uint64_t)k << shift);
+    const uint64_t left = (uint64_t)n - r0, full = 1ull << shift;
+    rows = (uint32_t)(left < full ? left : full);
+    rel = e - seg[k];
+    at = seg[nseg + k];
+  }
+  const uint32_t* off = xoff + r0 + k;  // the segment's rows + 1 offsets
+  uint32_t lo = 0, hi = rows;           // last row whose start is <= rel
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= rel) lo = mid;
+    else hi = mid - 1;
+  }
+  u = r0 + lo;
+  v = xedg[at + rel];
+}
+
 __global__ void k_gen_deletions(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg, uint32_t n,
-                                uint64_t m, uint64_t seed, uint32_t count, uint32_t* __restrict__ du,
-                                uint32_t* __restrict__ dv) {
+                                uint64_t m, uint32_t shift, uint32_t nseg, const unsigned long long* __restrict__ seg,
+                                uint64_t seed, uint32_t count, uint32_t* __restrict__ du, uint32_t* __restrict__ dv) {
   using namespace prx_hash;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
     uint32_t ou = n, ov = n;
     for (uint64_t t = 0; t < kDelTries && m; ++t) {
       const uint64_t e = (rnd(seed, kDelStream, (uint64_t)i * kDelTries + t) >> 11) % m;
-      uint32_t lo = 0, hi = n;  // last row whose start is <= e
-      while (lo < hi) {
-        const uint32_t mid = (lo + hi + 1) >> 1;
-        if (xoff[mid] <= e) lo = mid;
-        else hi = mid - 1;
-      }
-      const uint32_t v = xedg[e];
-      if (lo == v) continue;
-      ou = lo;
+      uint32_t u, v;
+      edge_at(xoff, xedg, n, shift, nseg, seg, e, u, v);
+      if (u == v) continue;
+      ou = u;
       ov = v;
       break;
     }
@@ -475,7 +524,10 @@ static int tidy_core(prx_context* c, const GraphDev& g, TidyBufs& b, uint32_t co
   cudaStream_t s = c->stream;
   int vbits = 1;
   while (vbits < 32 && (1ull << vbits) < g.n) ++vbits;
-  const int key_bits = deletions ? 32 : std::min(64, 2 * vbits);
+  // deletions of a one-segment graph sort by their out-CSR positions (32-bit
+  // keys, fewer radix passes); every other list by u * 2^vbits + v
+  const int pos_keys = deletions && g.nseg == 1 ? 1 : 0;
+  const int key_bits = pos_keys ? 32 : std::min(64, 2 * vbits);
   const uint32_t tiles = (count + kSortTile - 1) / kSortTile;
   auto fail = [&](cudaError_t e) {
     b.release();
@@ -491,7 +543,8 @@ static int tidy_core(prx_context* c, const GraphDev& g, TidyBufs& b, uint32_t co
   if (e != cudaSuccess) return fail(e);
   const int grid = grid_of(count, c->sms);
   // 1-2. existence and keys, then compaction of the kept keys
-  k_tidy_keys<<<grid, 256, 0, s>>>(g.xoff, g.xedg, g.n, b.u, b.v, count, deletions ? 1 : 0, vbits, b.flag, b.key);
+  k_tidy_keys<<<grid, 256, 0, s>>>(g.xoff, g.xedg, g.xbase, g.seg_shift, g.n, b.u, b.v, count, deletions ? 1 : 0,
+                                   pos_keys, vbits, b.flag, b.key);
   e = cudaMemcpyAsync(b.pos, b.flag, 4ull * count, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b.pos + count, 0, 4, s);
   if (e == cudaSuccess) e = exclusive_scan_u32(b.pos, count + 1, s);
@@ -517,7 +570,7 @@ static int tidy_core(prx_context* c, const GraphDev& g, TidyBufs& b, uint32_t co
   uint32_t m3 = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&m3, b.pos + m2, 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess)
-    k_decode<<<g2, 256, 0, s>>>(src, b.flag, b.pos, m2, deletions ? 1 : 0, vbits, g.xoff, g.n, g.xedg, b.u, b.v);
+    k_decode<<<g2, 256, 0, s>>>(src, b.flag, b.pos, m2, pos_keys, vbits, g.xoff, g.n, g.xedg, b.u, b.v);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e == cudaSuccess && m3) e = cudaMemcpyAsync(ou, b.u, 4ull * m3, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && m3) e = cudaMemcpyAsync(ov, b.v, 4ull * m3, cudaMemcpyDeviceToHost, s);
@@ -678,7 +731,6 @@ int prx_graph_tidy_batch(prx_context* c, prx_graph* gr, const uint32_t* du, cons
   if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_graph_tidy_batch: bad context or graph");
   const GraphDev& g = gr->g;
   if (!g.xoff) FAIL(PRX_ESTATE, "prx_graph_tidy_batch: graph has no out-CSR");
-  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_graph_tidy_batch: not for graphs with row segments (64-bit offsets)");
   if (!out_nd || !out_ni) FAIL(PRX_EINVAL, "prx_graph_tidy_batch: NULL output length");
   if ((nd && (!du || !dv || !out_du || !out_dv)) || (ni && (!iu || !iv || !out_iu || !out_iv)))
     FAIL(PRX_EINVAL, "prx_graph_tidy_batch: NULL array with a non-zero length");
@@ -698,7 +750,6 @@ int prx_graph_gen_batch(prx_context* c, prx_graph* gr, uint64_t nd_req, uint64_t
   if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_graph_gen_batch: bad context or graph");
   const GraphDev& g = gr->g;
   if (!g.xoff) FAIL(PRX_ESTATE, "prx_graph_gen_batch: graph has no out-CSR");
-  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_graph_gen_batch: not for graphs with row segments (64-bit offsets)");
   if (!out_nd || !out_ni || (nd_req && (!out_du || !out_dv)) || (ni_req && (!out_iu || !out_iv)))
     FAIL(PRX_EINVAL, "prx_graph_gen_batch: NULL output");
   if (g.n == 0) FAIL(PRX_EINVAL, "prx_graph_gen_batch: empty graph");
@@ -709,14 +760,28 @@ int prx_graph_gen_batch(prx_context* c, prx_graph* gr, uint64_t nd_req, uint64_t
     const uint32_t count = (uint32_t)(del ? nd_req : ni_req);
     if (!count) continue;
     TidyBufs b;
+    unsigned long long* seg = nullptr;  // row segments: first edges (compact order), then device positions
     cudaError_t e = graph_alloc(&b.u, 4ull * count, c->stream);
     if (e == cudaSuccess) e = graph_alloc(&b.v, 4ull * count, c->stream);
+    if (e == cudaSuccess && del && g.nseg > 1) {
+      std::vector<unsigned long long> h(2 * (size_t)g.nseg);
+      for (uint32_t k = 0; k < g.nseg; ++k) {
+        h[k] = g.xseg0[k];
+        h[g.nseg + k] = g.xpos[k];
+      }
+      e = graph_alloc(&seg, 8 * h.size(), c->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(seg, h.data(), 8 * h.size(), cudaMemcpyHostToDevice, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // h is about to go
+    }
     if (e == cudaSuccess) {
       const int grid = grid_of(count, c->sms);
-      if (del) k_gen_deletions<<<grid, 256, 0, c->stream>>>(g.xoff, g.xedg, g.n, g.m, seed, count, b.u, b.v);
+      if (del)
+        k_gen_deletions<<<grid, 256, 0, c->stream>>>(g.xoff, g.xedg, g.n, g.m, g.seg_shift, g.nseg, seg, seed, count,
+                                                     b.u, b.v);
       else k_gen_insertions<<<grid, 256, 0, c->stream>>>(g.n, seed, count, b.u, b.v);
       e = cudaGetLastError();
     }
+    if (seg) cudaFreeAsync(seg, c->stream);
     if (e != cudaSuccess) {
       b.release();
       set_error(std::string("prx_graph_gen_batch: ") + cudaGetErrorString(e));

@@ -104,12 +104,68 @@ def test_segmented_rows_limits(pg, ctx):
     auto.apply_batch(*pg.graphs.random_batch(xoff, xedg, 5, 5, seed=1))   # plain: batches work
     auto.close()
     seg = graph64(pg, ctx, xoff, xedg, xt, 5)
-    e = np.zeros(0, np.uint32)
-    for call in (lambda: seg.apply_batch(e, e, e, e), lambda: seg.tidy_batch(e, e, e, e),
-                 lambda: seg.gen_batch(1, 1), lambda: pg.solve_ppr_batched(ctx, seg, [[0]])):
-        with pytest.raises(pg.PrxError) as err:
-            call()
-        assert err.value.status == 5   # PRX_ERANGE
+    import torch
+    from pagerank_gb300 import autograd as A
+    with pytest.raises(pg.PrxError) as err:   # edge weights: plain CSR only
+        A.set_weights(ctx, seg, torch.ones(len(xedg), dtype=torch.float32))
+    assert err.value.status == 5   # PRX_ERANGE
     seg.close()
     with pytest.raises(pg.PrxError):
         graph64(pg, ctx, xoff, xedg, xt, 33)
+
+
+def _same_graph(plain, seg):
+    a, b = plain.download(), seg.download64()
+    for x, y in zip(a, b):
+        assert np.array_equal(np.asarray(x, np.uint64), np.asarray(y, np.uint64))
+
+
+@pytest.mark.parametrize("kind,shift", [("rmat", 3), ("rmat", 5), ("rmat", 12), ("web", 4), ("web", 11),
+                                        ("grid", 7)])
+def test_segmented_batches_bit_exact(pg, ctx, kind, shift):
+    """Batch generation, tidying and application on the device keep a graph of
+    row segments identical to the plain CSR (segments move to new bases, some
+    of them not on a 32-row boundary); DF-P after the device-applied batch,
+    Static and batched PPR then give the plain CSR's bits."""
+    if kind == "rmat":
+        xoff, xedg = pg.graphs.rmat(13, 12, seed=5)
+    elif kind == "web":
+        xoff, xedg = pg.graphs.weblike(60_000, seed=5)
+    else:
+        xoff, xedg = pg.graphs.grid(120, seed=5)
+    xt = O.transpose(xoff, xedg)
+    plain = pg.Graph(ctx, *xt, xoff, xedg)
+    seg = graph64(pg, ctx, xoff, xedg, xt, shift)
+    q, _ = pg.pagerank_static(ctx, plain)
+    for step in range(2):
+        # the device generator draws the same batch from both layouts
+        b0 = plain.gen_batch(300, 900, seed=11 + step)
+        b1 = seg.gen_batch(300, 900, seed=11 + step)
+        assert all(np.array_equal(x, y) for x, y in zip(b0, b1))
+        # tidying a raw batch with repeats, missing deletions and existing insertions
+        rng = np.random.default_rng(step)
+        n = len(xoff) - 1
+        raw = (np.concatenate([b0[0], b0[0][:50], rng.integers(0, n, 40)]).astype(np.uint32),
+               np.concatenate([b0[1], b0[1][:50], rng.integers(0, n, 40)]).astype(np.uint32),
+               np.concatenate([b0[2], b0[2][:70], b0[0][:30]]).astype(np.uint32),
+               np.concatenate([b0[3], b0[3][:70], b0[1][:30]]).astype(np.uint32))
+        t0, t1 = plain.tidy_batch(*raw), seg.tidy_batch(*raw)
+        assert all(np.array_equal(x, y) for x, y in zip(t0, t1))
+        plain.apply_batch(*t0)
+        seg.apply_batch(*t0)
+        _same_graph(plain, seg)
+        for mode in ("prune_dynamic_frontier", "dynamic_frontier", "dynamic_traversal"):
+            a, ra = pg.solve(ctx, plain, pg.MODES[mode], t0[:2], t0[2:], q)
+            b, rb = pg.solve(ctx, seg, pg.MODES[mode], t0[:2], t0[2:], q)
+            assert ra["iterations"] == rb["iterations"] and np.array_equal(a, b), (kind, shift, step, mode)
+        q, rs = pg.pagerank_static(ctx, plain)
+        q1, rs1 = pg.pagerank_static(ctx, seg)
+        assert rs["iterations"] == rs1["iterations"] and np.array_equal(q, q1)
+    # batched personalized PageRank (rows above low_max in segments of seg_edges)
+    seeds = [[0], [1, 2, 3], list(range(0, len(xoff) - 1, 97))]
+    for o in (pg.options(tolerance=1e-10), pg.options(tolerance=1e-10, precision=pg.FP32_REFINE)):
+        a, ra = pg.solve_ppr_batched(ctx, plain, seeds, o)
+        b, rb = pg.solve_ppr_batched(ctx, seg, seeds, o)
+        assert ra["iterations"] == rb["iterations"] and np.array_equal(a, b)
+    plain.close()
+    seg.close()
