@@ -73,6 +73,8 @@ def parse():
     p.add_argument("--batches-per-size", type=int, default=10,
                    help="consecutive dynamic batches at each of 1e-5, 1e-4, 1e-3 |E|")
     p.add_argument("--no-ingest", action="store_true", help="skip the device graph ingest from the edge list")
+    p.add_argument("--multibatch", type=int, default=10,
+                   help="consecutive DF-P batches in one graph launch against the host loop (0: skip)")
     p.add_argument("--no-offsets64", action="store_true",
                    help="skip the 64-bit-offset graph (four copies of the bench graph, 4x its edges)")
     p.add_argument("--ingest-steps", type=int, default=2)
@@ -81,6 +83,7 @@ def parse():
                         "web (web-like 6M: Static, FP32 refinement, batch apply, DF-P, DF, DT), grid (1024^2: DT), "
                         "c3 (4096^2 grid: Static, batch apply, Static, DT, DF, DF-P), "
                         "apply50m (the web-like graph of --vertices: two batch applies of 1e-4|E|), "
+                        "multi50m (the same graph: three DF-P batches of 1e-5|E| in one graph launch), "
                         "hubs (R-MAT 18, 48 edges/vertex: MID / HIGH rows, weighted solve and adjoint, PPR)")
     p.add_argument("--detail-out", default=None,
                    help="also write the detail record (every section) to this file; it always goes to stderr")
@@ -266,7 +269,7 @@ def compact(x, digits=5):
     return x
 
 
-def summarize(fp32, dfp, dynamic, grid, ppr, adj, big, ingest, tune):
+def summarize(fp32, dfp, dynamic, grid, ppr, adj, big, ingest, tune, multi=None):
     """A few scalars per section for the stdout line (the full sections go to
     the detail record)."""
     def pick(d, *keys):
@@ -306,6 +309,10 @@ def summarize(fp32, dfp, dynamic, grid, ppr, adj, big, ingest, tune):
         out["ingest_1.9B_ms"] = statistics.median(ingest["device_ms"])
     if tune:
         out["autotune_s"] = tune.get("seconds")
+    if multi:
+        out["multibatch_dfp_1e-5_x%d" % multi["batches"]] = pick(multi, "host_loop_ms", "one_launch_ms",
+                                                                 "speedup_vs_host_loop", "graph_launches",
+                                                                 "same_bits")
     return out
 
 
@@ -383,15 +390,31 @@ def run_tour(args):
                                        window=4096, seed=args.seed)
         g = pg.Graph(ctx, *pg.graphs.transpose(xoff, xedg), xoff, xedg)
         m = len(xedg)
+        q, _ = pg.solve(ctx, g, pg.STATIC)
         for k in range(2):
             b = g.gen_batch(int(2e-5 * m), int(8e-5 * m), seed=3 + k)
             torch.cuda.synchronize()
             t = time.perf_counter()
             g.apply_batch(*b)
             log(f"apply of {len(b[0])} deletions and {len(b[2])} insertions: {1e3 * (time.perf_counter() - t):.1f} ms")
+            # the layout rebuild and a DF-P solve on the new version
+            q, _ = pg.solve(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, b[:2], b[2:], q, pg.options(loop=host))
         g.close()
 
-    parts = {"web": web, "grid": grid, "c3": c3, "hubs": hubs, "apply50m": apply50m}
+    def multi50m():
+        xoff, xedg = pg.graphs.weblike(args.vertices, alpha=2.1, dmin=args.dmin, dmax=100000, local=0.7,
+                                       window=4096, seed=args.seed)
+        xt = pg.graphs.transpose(xoff, xedg)
+        g = pg.Graph(ctx, *xt, xoff, xedg)
+        q, _ = pg.solve(ctx, g, pg.STATIC)
+        m = len(xedg)
+        cnt = int(1e-5 * m)
+        du, dv, iu, iv = pg.graphs.random_batch(xoff, xedg, 3 * (cnt // 5), 3 * (cnt - cnt // 5), seed=9)
+        batches = [(du[k::3], dv[k::3], iu[k::3], iv[k::3]) for k in range(3)]
+        pg.solve_batches(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, batches, q)
+        g.close()
+
+    parts = {"web": web, "grid": grid, "c3": c3, "hubs": hubs, "apply50m": apply50m, "multi50m": multi50m}
     for name in args.tour.split(","):
         parts[name]()
     torch.cuda.synchronize()
@@ -535,6 +558,50 @@ def run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m):
         dfp.update({"cpu_dfp_ms": cpu_dfp["ms"], "cpu_dfp_iterations": cpu_dfp["iterations"],
                     "cpu_dfp_threads": cpu_dfp["threads"], "gpu_dfp_vs_cpu_dfp": cpu_dfp["ms"] / d["ms"]})
     return {"batches": rows, "median_speedup_vs_static": summary, "tidy": tidy, "cpu_dfp": cpu_dfp}, dfp
+
+
+def run_multibatch(args, pg, ctx, local, xoff, xedg, xt, ranks, m):
+    """K consecutive DF-P batch updates of 1e-5|E| (80% insertions) on the
+    web-like graph: the host loop (prx_graph_apply_batch, then prx_solve per
+    batch) against prx_solve_batches_device (all K applies and solves in one
+    CUDA graph launch), host arrays in and out both ways; the last ranks must
+    be the same bits."""
+    import numpy as np
+    K = args.multibatch
+    cnt = int(1e-5 * m)
+    nd, ni = cnt // 5, cnt - cnt // 5
+    du, dv, iu, iv = pg.graphs.random_batch(xoff, xedg, K * nd, K * ni, seed=args.seed + 5)
+    rng = np.random.default_rng(args.seed + 6)
+    pd, pi = rng.permutation(len(du)), rng.permutation(len(iu))
+    batches = []
+    for k in range(K):
+        kd, ki = np.sort(pd[k * nd:(k + 1) * nd]), np.sort(pi[k * ni:(k + 1) * ni])
+        batches.append((du[kd], dv[kd], iu[ki], iv[ki]))
+    q0 = ranks.cpu().numpy()
+    res = {"batches": K, "batch_edges": cnt}
+    g = pg.Graph(ctx, *xt, xoff, xedg)
+
+    def host_loop():
+        q = q0
+        for b in batches:
+            g.apply_batch(*b)
+            q, _ = pg.solve(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, b[:2], b[2:], q)
+        return q
+
+    want, res["host_loop_ms"] = host_ms(host_loop)
+    g.close()
+    g = pg.Graph(ctx, *xt, xoff, xedg)
+    (last, per, _), res["one_launch_ms"] = host_ms(
+        lambda: pg.solve_batches(ctx, g, pg.PRUNE_DYNAMIC_FRONTIER, batches, q0))
+    g.close()
+    res["graph_launches"] = 1
+    res["step_ms"] = [round(r["time_ms"], 3) for r in per]
+    res["step_parts_ms"] = [[round(r[k], 3) for k in ("initialization_time_ms", "marking_time_ms",
+                                                       "computation_time_ms")] for r in per]
+    res["iterations"] = [r["iterations"] for r in per]
+    res["same_bits"] = bool(np.array_equal(last, want))
+    res["speedup_vs_host_loop"] = res["host_loop_ms"] / res["one_launch_ms"]
+    return res
 
 
 def run_grid(args, pg, ctx, local):
@@ -968,7 +1035,10 @@ def run_ours(args):
         dynamic, dfp = run_dynamic(args, pg, ctx, local, g, xoff, xedg, ranks, m)
         log(f"dfp: {dfp}")
 
-    ppr = adj = grid = ingest = big = None
+    ppr = adj = grid = ingest = big = multi = None
+    if rank == 0 and args.multibatch > 0 and not args.static_only:
+        multi = run_multibatch(args, pg, ctx, local, xoff, xedg, xt, ranks, m)
+        log(f"multibatch: {multi}")
     if rank == 0 and not args.no_offsets64 and not args.static_only:
         big = run_offsets64(args, pg, ctx, local, xt)
         log(f"offsets64: {big}")
@@ -990,7 +1060,8 @@ def run_ours(args):
     if rank == 0:
         detail = {"iterations": iters, "roofline": roofline, "e2e_steps_ms": e2e_ms, "e2e_parts": e2e_parts,
                   "h2d_only_ms": h2d_only_ms, "fp32_refine": fp32, "dfp": dfp, "dynamic": dynamic, "autotune": tune,
-                  "offsets64": big, "ingest": ingest, "grid": grid, "ppr": ppr, "adjoint": adj, "cpu_baseline": cpu}
+                  "offsets64": big, "ingest": ingest, "grid": grid, "ppr": ppr, "adjoint": adj, "multibatch": multi,
+                  "cpu_baseline": cpu}
         text = json.dumps(detail)
         log("detail: " + text)
         if args.detail_out:
@@ -1010,7 +1081,7 @@ def run_ours(args):
                        "ms_per_step": e2e_ms_max, "steps": len(e2e_ms), "statistic": "median step"},
                "roofline": {k: roofline[k] for k in keep if k in roofline},
                "clocks": clk.summary(), "cpu_baseline": cpu,
-               "summary": summarize(fp32, dfp, dynamic, grid, ppr, adj, big, ingest, tune),
+               "summary": summarize(fp32, dfp, dynamic, grid, ppr, adj, big, ingest, tune, multi),
                "detail": args.detail_out or "stderr"}
         line = json.dumps(compact(out))
         if len(line) > 4096:

@@ -260,6 +260,32 @@ int prx_solve_device(prx_context* ctx, prx_graph* g, int mode,
                      const double* q, const prx_options* o,
                      double* ranks_out, prx_result* res);
 
+/* K consecutive batch updates as ONE CUDA graph launch: for k = 0 .. K-1,
+ * apply batch k to g (as prx_graph_apply_batch does) and solve `mode`
+ * (PRX_DYNAMIC_FRONTIER or PRX_PRUNE_DYNAMIC_FRONTIER, FP64) from the
+ * previous step's ranks (q for step 0) -- the reference driver's loop over
+ * its batches (main.cu:88-147) without a host round trip between them.
+ * Batch k deletes del_u/del_v[del_off[k] .. del_off[k+1]) and inserts
+ * ins_u/ins_v[ins_off[k] .. ins_off[k+1]), each list sorted by (u, v) and
+ * tidy against the graph as the batches before it left it.  del_off and
+ * ins_off (K + 1 entries each) are HOST memory; the id arrays, q and
+ * ranks_out (n doubles: the ranks after the last step) and ranks_each
+ * (K x n doubles, row k after step k; may be NULL) are DEVICE memory.
+ * res (K entries, may be NULL): per step its iterations, marking size,
+ * edges, last change, launches, and its times from the device clock
+ * (initialization: the check, the apply and the step's layout and ranks;
+ * then marking; then computation: the iterations).  Plain
+ * graphs (prx_graph_create) only; the steps gather through a source-chunk
+ * layout rebuilt by kernels for every step and the hot sources of the graph
+ * before the batches.  A batch that is not tidy ends
+ * the sequence: PRX_EINVAL, *applied = the steps completed, and the graph
+ * and ranks_out as the last of them left them. */
+int prx_solve_batches_device(prx_context* ctx, prx_graph* g, int mode, uint32_t K,
+                             const uint64_t* del_off, const uint32_t* del_u, const uint32_t* del_v,
+                             const uint64_t* ins_off, const uint32_t* ins_u, const uint32_t* ins_v,
+                             const double* q, const prx_options* o, double* ranks_out,
+                             double* ranks_each, prx_result* res, uint32_t* applied);
+
 /* tidyBatchUpdateU (inc/batch.hxx:152-208), on the device: against graph g
  * (created with its out-CSR, before the batch is applied), keep the
  * deletions that exist and the insertions that do not, sort each list by

@@ -133,7 +133,7 @@ void* prx_context_stream(prx_context* c) { return c ? (void*)c->stream : nullptr
 }  // extern "C"
 
 // ---- workspace -------------------------------------------------------------------
-static int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
+int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
   if (c->ws_n >= n && (c->ws_dyn || !dyn)) return PRX_OK;
   const uint32_t cap = std::max(n, c->ws_n);
   const bool want_dyn = dyn || c->ws_dyn;
@@ -162,7 +162,7 @@ static int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
   return PRX_OK;
 }
 
-static int ensure_ch(prx_context* c, uint32_t hot_n) {
+int ensure_ch(prx_context* c, uint32_t hot_n) {
   if (c->ch_n >= hot_n) return PRX_OK;
   for (auto& h : c->ch) { cudaFree(h); h = nullptr; }
   c->ch_n = 0;
@@ -199,7 +199,7 @@ static int ensure_batch(prx_context* c, size_t elems) {
   return PRX_OK;
 }
 
-static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options& o) {
+SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options& o) {
   SolveArgs a;
   std::memset(&a, 0, sizeof(a));
   a.xoff = g.xoff; a.xedg = g.xedg;
@@ -239,7 +239,7 @@ static SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options&
 static bool valid_mode(int m) { return m >= PRX_STATIC && m <= PRX_PRUNE_DYNAMIC_FRONTIER; }
 
 // Initial marking of a dynamic mode on batch arrays already on the device.
-static int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint32_t* du, const uint32_t* dv,
+int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint32_t* du, const uint32_t* dv,
                        uint64_t nd, const uint32_t* iu, uint64_t ni) {
   cudaStream_t s = c->stream;
   const size_t words = ((size_t)a.n + 31) / 32;
@@ -334,13 +334,13 @@ static int launch_update_timed(prx_context* c, bool timing, int slot, F fn) {
   return PRX_OK;
 }
 
-static int enqueue_iteration(prx_context* c, const prx_graph* gr, const SolveArgs& a, int mode, bool timing,
-                             const ChunkLayout* lay) {
+int enqueue_iteration(prx_context* c, const GraphDev& g, const SolveArgs& a, int mode, bool timing,
+                      const ChunkLayout* lay) {
   cudaStream_t s = c->stream;
   for (int cls = 0; cls < NCLS; ++cls) {
     const int slot = (mode & MODE_F32) ? NCLS + cls : cls;  // FP32 sweeps are timed apart
     const int st = launch_update_timed(c, timing, slot,
-                                       [&] { return launch_update_class(a, gr->g, mode, cls, lay, c->sms, s); });
+                                       [&] { return launch_update_class(a, g, mode, cls, lay, c->sms, s); });
     if (st) return st;
   }
   // the contributions this iteration wrote (the dynamic modes' stale copies
@@ -392,7 +392,7 @@ static int run_graph_loop(prx_context* c, const prx_graph* gr, const SolveArgs& 
     cudaGraph_t body = p.conditional.phGraph_out[0];
     e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      const int st_enq = enqueue_iteration(c, gr, a, mode, false, lay);
+      const int st_enq = enqueue_iteration(c, gr->g, a, mode, false, lay);
       const int cap = (max_iter < (1 << 30) ? max_iter : (1 << 30)) + 2;
       k_loop_cond<<<1, 1, 0, s>>>(h, a.st, cap);
       per_body = c->launches - l0 + 1;
@@ -564,7 +564,7 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
       if (o.loop != PRX_LOOP_HOST && !timing) return run_graph_loop(c, gr, a, m, lay, o.max_iterations);
       for (int k = 1;; k = std::min(2 * k, 16)) {
         for (int i = 0; i < k; ++i) {
-          const int e = enqueue_iteration(c, gr, a, m, timing, lay);
+          const int e = enqueue_iteration(c, gr->g, a, m, timing, lay);
           if (e) return e;
         }
         TRY_CUDA_ST(cudaGetLastError());

@@ -169,12 +169,17 @@ struct Runs {
   const uint32_t* noff;
   const uint32_t* trow;
   uint32_t T, rows, rbase;
+  const uint32_t* Tp;  // not null: T is read here on the device (the multi-batch solve)
+  __device__ __forceinline__ void load_T() {
+    if (Tp) T = *Tp;
+  }
   __device__ __forceinline__ uint32_t first(uint32_t j) const { return j ? trow[j - 1] - rbase + 1 : 0u; }
   __device__ __forceinline__ uint32_t end(uint32_t j) const { return j < T ? trow[j] - rbase : rows; }
 };
 
 __global__ void __launch_bounds__(kThreads) k_copy_runs(Runs r, const uint32_t* __restrict__ oedg,
                                                         uint32_t* __restrict__ nedg) {
+  r.load_T();
   const uint32_t lane = lane_id();
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -214,8 +219,12 @@ __global__ void __launch_bounds__(kThreads) k_copy_runs(Runs r, const uint32_t* 
 }
 
 // The touched rows, one warp each; rows of more than kBigRow ids (old and
-// inserted) are listed in big[] for k_merge_big.
+// inserted) are listed for k_merge_big instead: entry i of big[] holds the
+// row's place in the touched list and the number of 1024-id pieces of the
+// rows listed before it, both from one 64-bit atomic (pieces in the high
+// word, rows in the low one), so the pieces are numbered in list order.
 constexpr uint32_t kBigRow = 4096;
+constexpr uint32_t kPiece = 1024;
 
 __device__ __forceinline__ RowMerge touched_merge(const Runs& r, uint32_t i, const uint32_t* oedg, uint32_t* nedg,
                                                   const uint32_t* dv, const uint32_t* dbeg, const uint32_t* dend,
@@ -225,20 +234,30 @@ __device__ __forceinline__ RowMerge touched_merge(const Runs& r, uint32_t i, con
   return row_merge(oedg, nedg, s, e - s, r.noff[row], dv, dbeg[row], dend[row], iv, ibeg[row], iend[row]);
 }
 
+__device__ __forceinline__ uint32_t merge_pieces(const RowMerge& m) {
+  return (m.len + kPiece - 1) / kPiece + (m.ni + kPiece - 1) / kPiece;
+}
+
 __global__ void __launch_bounds__(kThreads) k_merge_touched(Runs r, const uint32_t* __restrict__ oedg,
                                                             uint32_t* __restrict__ nedg, const uint32_t* dv,
                                                             const uint32_t* __restrict__ dbeg,
                                                             const uint32_t* __restrict__ dend, const uint32_t* iv,
                                                             const uint32_t* __restrict__ ibeg,
                                                             const uint32_t* __restrict__ iend, uint32_t* big,
-                                                            uint32_t* nbig) {
+                                                            unsigned long long* nbig) {
+  r.load_T();
   const uint32_t lane = lane_id();
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t i = warp; i < r.T; i += nwarps) {
     const RowMerge m = touched_merge(r, i, oedg, nedg, dv, dbeg, dend, iv, ibeg, iend);
     if (m.len + m.ni > kBigRow) {
-      if (lane == 0) big[atomicAdd(nbig, 1u)] = i;
+      if (lane == 0) {
+        const unsigned long long old = atomicAdd(nbig, ((unsigned long long)merge_pieces(m) << 32) | 1ull);
+        const uint32_t slot = (uint32_t)old;
+        big[2 * slot] = i;
+        big[2 * slot + 1] = (uint32_t)(old >> 32);
+      }
       continue;
     }
     for (uint32_t j = lane; j < m.len; j += 32) m.old_id(j);
@@ -246,7 +265,8 @@ __global__ void __launch_bounds__(kThreads) k_merge_touched(Runs r, const uint32
   }
 }
 
-// The long touched rows, each split into pieces of 1024 ids over all warps.
+// The pieces of the long touched rows, one warp each: warp p finds its row as
+// the last listed one whose first piece is at or before p.
 __global__ void __launch_bounds__(kThreads) k_merge_big(Runs r, const uint32_t* __restrict__ oedg,
                                                         uint32_t* __restrict__ nedg, const uint32_t* dv,
                                                         const uint32_t* __restrict__ dbeg,
@@ -254,24 +274,26 @@ __global__ void __launch_bounds__(kThreads) k_merge_big(Runs r, const uint32_t* 
                                                         const uint32_t* __restrict__ ibeg,
                                                         const uint32_t* __restrict__ iend,
                                                         const uint32_t* __restrict__ big,
-                                                        const uint32_t* __restrict__ nbig) {
+                                                        const unsigned long long* __restrict__ nbig) {
   const uint32_t lane = lane_id();
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  const uint32_t count = *nbig;
-  uint32_t next = 0;  // pieces of the rows before this one: spreads the first pieces of successive rows
-  for (uint32_t b = 0; b < count; ++b) {
-    const RowMerge m = touched_merge(r, big[b], oedg, nedg, dv, dbeg, dend, iv, ibeg, iend);
-    const uint32_t po = (m.len + 1023) / 1024, pieces = po + (m.ni + 1023) / 1024;
-    for (uint32_t c = (warp + nwarps - next % nwarps) % nwarps; c < pieces; c += nwarps) {
-      if (c < po) {
-        for (uint32_t j = c * 1024 + lane; j < min(m.len, (c + 1) * 1024); j += 32) m.old_id(j);
-      } else {
-        const uint32_t c2 = c - po;
-        for (uint32_t k = c2 * 1024 + lane; k < min(m.ni, (c2 + 1) * 1024); k += 32) m.ins_id(k);
-      }
+  const unsigned long long tally = *nbig;
+  const uint32_t rows = (uint32_t)tally, pieces = (uint32_t)(tally >> 32);
+  for (uint32_t p = warp; p < pieces; p += nwarps) {
+    uint32_t lo = 0, hi = rows;  // big[2*lo+1] <= p < big[2*hi+1]
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (big[2 * mid + 1] <= p) lo = mid; else hi = mid;
     }
-    next += pieces;
+    const RowMerge m = touched_merge(r, big[2 * lo], oedg, nedg, dv, dbeg, dend, iv, ibeg, iend);
+    const uint32_t c = p - big[2 * lo + 1], po = (m.len + kPiece - 1) / kPiece;
+    if (c < po) {
+      for (uint32_t j = c * kPiece + lane; j < min(m.len, (c + 1) * kPiece); j += 32) m.old_id(j);
+    } else {
+      const uint32_t c2 = c - po;
+      for (uint32_t k = c2 * kPiece + lane; k < min(m.ni, (c2 + 1) * kPiece); k += 32) m.ins_id(k);
+    }
   }
 }
 
@@ -429,11 +451,13 @@ cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd64, ui
   // and insertions, then the copy of the untouched runs and the merge of the
   // touched rows, segment by segment
   PRX_CU(graph_alloc(&ranges, sizeof(uint32_t) * 4 * (size_t)(n ? n : 1), s));
-  PRX_CU(graph_alloc(&lists, sizeof(uint32_t) * ((size_t)words + 2 + 2 * ((size_t)nd + ni) + (size_t)nseg + 2), s));
+  PRX_CU(graph_alloc(&lists, sizeof(uint32_t) * ((size_t)words + 2 + 3 * ((size_t)nd + ni) + (size_t)nseg + 4), s));
   {
     uint32_t *dbeg = ranges, *dend = dbeg + n, *ibeg = dend + n, *iend = ibeg + n;
-    uint32_t *cnt = lists, *trow = cnt + words + 2, *big = trow + nd + ni, *bounds = big + nd + ni;
-    uint32_t* nbig = bounds + nseg + 1;
+    uint32_t *cnt = lists, *trow = cnt + words + 2, *big = trow + nd + ni, *bounds = big + 2 * ((size_t)nd + ni);
+    // 8-byte aligned: the list starts at a graph allocation, and 2 + words + 3(nd + ni) + nseg + 1 is rounded up
+    unsigned long long* nbig =
+        reinterpret_cast<unsigned long long*>(lists + ((words + 2 + 3 * ((size_t)nd + ni) + nseg + 1 + 1) & ~(size_t)1));
     const uint32_t* keys[2][2] = {{du, iu}, {tdk, tik}};
     const uint32_t* vals[2][2] = {{dv, iv}, {tdv, tiv}};
     const uint32_t* ooff[2] = {g.xoff, g.xtoff};
@@ -460,10 +484,10 @@ cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd64, ui
         const uint32_t v0 = segmented ? (uint32_t)((uint64_t)k << S) : 0;
         const uint32_t v1 = segmented ? (uint32_t)std::min<uint64_t>(n, (uint64_t)v0 + (1ull << S)) : n;
         const uint64_t op = segmented ? (*opos[csr])[k] : 0, np = segmented ? pos[csr][k] : 0;
-        const Runs r{ooff[csr] + v0 + k, nof[csr] + v0 + k, trow + hb[k], hb[k + 1] - hb[k], v1 - v0, v0};
+        const Runs r{ooff[csr] + v0 + k, nof[csr] + v0 + k, trow + hb[k], hb[k + 1] - hb[k], v1 - v0, v0, nullptr};
         k_copy_runs<<<grid, kThreads, 0, s>>>(r, oedg[csr] + op, ned[csr] + np);
         if (r.T) {
-          PRX_CU(cudaMemsetAsync(nbig, 0, 4, s));
+          PRX_CU(cudaMemsetAsync(nbig, 0, 8, s));
           k_merge_touched<<<grid, kThreads, 0, s>>>(r, oedg[csr] + op, ned[csr] + np, vals[csr][0], dbeg + v0,
                                                     dend + v0, vals[csr][1], ibeg + v0, iend + v0, big, nbig);
           k_merge_big<<<grid, kThreads, 0, s>>>(r, oedg[csr] + op, ned[csr] + np, vals[csr][0], dbeg + v0, dend + v0,
@@ -495,6 +519,106 @@ done:
   graph_free({noff, ntoff, nedg, ntedg, ndat});
   graph_free({nbase, ntbase});
   return err;
+}
+
+// ---- the same apply without host synchronisation or allocation -------------
+// (captured into the multi-batch solve's CUDA graph; plain CSRs only)
+
+size_t ApplyWs::words(uint32_t n, uint32_t bmax) {
+  const size_t w = ((size_t)n + 31) / 32;
+  return 2 * (size_t)n + 2 * w + 4 * (size_t)n + (w + 2) + 3 * (size_t)bmax + 4 + scan_ws_words(n + 1) +
+         scan_ws_words((uint32_t)w + 1) + 2;
+}
+
+ApplyWs::ApplyWs(uint32_t* base, uint32_t n, uint32_t bmax) {
+  const size_t w = ((size_t)n + 31) / 32;
+  uint32_t* p = base;
+  delta = reinterpret_cast<int32_t*>(p); p += 2 * (size_t)n;
+  touched = p; p += 2 * w;
+  ranges = p; p += 4 * (size_t)n;
+  cnt = p; p += w + 2;
+  trow = p; p += bmax;
+  big = p; p += 2 * (size_t)bmax;
+  if ((p - base) & 1) ++p;  // 8-byte aligned (base is a graph allocation)
+  nbig = reinterpret_cast<unsigned long long*>(p); p += 4;
+  scan_off = p; p += scan_ws_words(n + 1);
+  scan_cnt = p;
+}
+
+cudaError_t apply_batch_graph(const CsrSet& src, const CsrSet& dst, uint32_t n, const uint32_t* b, uint32_t nd,
+                              uint32_t ni, const ApplyWs& w, int sms, cudaStream_t s) {
+  const uint32_t *du = b, *dv = b + nd, *iu = b + 2 * (size_t)nd, *iv = iu + ni;
+  const uint32_t *tdk = iv + ni, *tdv = tdk + nd, *tik = tdv + nd, *tiv = tik + ni;
+  const uint32_t words = (n + 31) / 32;
+  const int grid = sms * 8;
+  int32_t *dout = w.delta, *din = w.delta + n;
+  uint32_t *tout = w.touched, *tin = w.touched + words;
+  cudaError_t e = cudaMemsetAsync(w.delta, 0, sizeof(uint32_t) * (2 * (size_t)n + 2 * (size_t)words), s);
+  if (e != cudaSuccess) return e;
+  if (nd + ni) k_batch_deltas<<<grid, kThreads, 0, s>>>(du, dv, nd, iu, iv, ni, dout, din, tout, tin, 32, 1, nullptr);
+  k_new_degree<<<grid, kThreads, 0, s>>>(src.xoff, dout, n, 32, (uint64_t)n + 1, dst.xoff);
+  k_new_degree<<<grid, kThreads, 0, s>>>(src.xtoff, din, n, 32, (uint64_t)n + 1, dst.xtoff);
+  if ((e = exclusive_scan_u32_ws(dst.xoff, n + 1, w.scan_off, s)) != cudaSuccess) return e;
+  if ((e = exclusive_scan_u32_ws(dst.xtoff, n + 1, w.scan_off, s)) != cudaSuccess) return e;
+  uint32_t *dbeg = w.ranges, *dend = dbeg + n, *ibeg = dend + n, *iend = ibeg + n;
+  const uint32_t* keys[2][2] = {{du, iu}, {tdk, tik}};
+  const uint32_t* vals[2][2] = {{dv, iv}, {tdv, tiv}};
+  const uint32_t* ooff[2] = {src.xoff, src.xtoff};
+  const uint32_t* oedg[2] = {src.xedg, src.xtedg};
+  const uint32_t* nof[2] = {dst.xoff, dst.xtoff};
+  uint32_t* ned[2] = {dst.xedg, dst.xtedg};
+  const uint32_t* tch[2] = {tout, tin};
+  for (int csr = 0; csr < 2; ++csr) {
+    k_word_pop<<<grid, kThreads, 0, s>>>(tch[csr], words, w.cnt);
+    if ((e = exclusive_scan_u32_ws(w.cnt, words + 1, w.scan_cnt, s)) != cudaSuccess) return e;
+    k_touched_list<<<grid, kThreads, 0, s>>>(tch[csr], words, w.cnt, w.trow);
+    if ((e = cudaMemsetAsync(w.ranges, 0, sizeof(uint32_t) * 4 * (size_t)n, s)) != cudaSuccess) return e;
+    if (nd) k_batch_ranges<<<grid, kThreads, 0, s>>>(keys[csr][0], nd, dbeg, dend);
+    if (ni) k_batch_ranges<<<grid, kThreads, 0, s>>>(keys[csr][1], ni, ibeg, iend);
+    if ((e = cudaMemsetAsync(w.nbig, 0, 8, s)) != cudaSuccess) return e;
+    const Runs r{ooff[csr], nof[csr], w.trow, 0, n, 0, w.cnt + words};
+    k_copy_runs<<<grid, kThreads, 0, s>>>(r, oedg[csr], ned[csr]);
+    k_merge_touched<<<grid, kThreads, 0, s>>>(r, oedg[csr], ned[csr], vals[csr][0], dbeg, dend, vals[csr][1], ibeg,
+                                              iend, w.big, w.nbig);
+    k_merge_big<<<grid, kThreads, 0, s>>>(r, oedg[csr], ned[csr], vals[csr][0], dbeg, dend, vals[csr][1], ibeg, iend,
+                                          w.big, w.nbig);
+  }
+  k_out_degree<<<grid, kThreads, 0, s>>>(dst.xoff, 32, n, dst.xtdat);
+  return cudaGetLastError();
+}
+
+// Ids below n and each list strictly ascending in (u, v): sets err bit 8 or 4
+// otherwise.  The batch is read only if it passes (k_batch_check after it
+// reads the rows of its ids).
+__global__ void k_batch_valid(const uint32_t* b, uint32_t nd, uint32_t ni, uint32_t n, uint32_t* err) {
+  const uint32_t *du = b, *dv = b + nd, *iu = b + 2 * (size_t)nd, *iv = iu + ni;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nd + ni; i += gridDim.x * blockDim.x) {
+    const bool del = i < nd;
+    const uint32_t j = del ? i : i - nd;
+    const uint32_t* u = del ? du : iu;
+    const uint32_t* v = del ? dv : iv;
+    if (u[j] >= n || v[j] >= n) atomicOr(err, 8u);
+    else if (j > 0 && (u[j - 1] > u[j] || (u[j - 1] == u[j] && v[j - 1] >= v[j]))) atomicOr(err, 4u);
+  }
+}
+
+__global__ void k_batch_check_if_valid(const uint32_t* __restrict__ off, const uint32_t* __restrict__ edg,
+                                       const uint32_t* b, uint32_t nd, uint32_t ni, uint32_t* err) {
+  if (*err) return;  // ids out of range or lists out of order: rows must not be read
+  const uint32_t *du = b, *dv = b + nd, *iu = b + 2 * (size_t)nd, *iv = iu + ni;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nd + ni; i += gridDim.x * blockDim.x) {
+    const bool del = i < nd;
+    const uint32_t u = del ? du[i] : iu[i - nd], v = del ? dv[i] : iv[i - nd];
+    if (row_has(off, edg, nullptr, 32, u, v) != del) atomicOr(err, del ? 1u : 2u);
+  }
+}
+
+void launch_batch_check(const uint32_t* xoff, const uint32_t* xedg, uint32_t n, const uint32_t* b, uint32_t nd,
+                        uint32_t ni, uint32_t* err, int sms, cudaStream_t s) {
+  if (nd + ni) {
+    k_batch_valid<<<sms * 8, kThreads, 0, s>>>(b, nd, ni, n, err);
+    k_batch_check_if_valid<<<sms * 8, kThreads, 0, s>>>(xoff, xedg, b, nd, ni, err);
+  }
 }
 
 }  // namespace prx

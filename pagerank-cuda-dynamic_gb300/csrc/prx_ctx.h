@@ -63,6 +63,22 @@ struct prx_graph {
   GraphDev g;
 };
 
+// Solve pieces shared by prx_solve and the multi-batch solve (prx_api.cu).
+int ensure_ws(prx_context* c, uint32_t n, bool dyn);
+// The dense hot-source copies c->ch[2] for hot_n sources.
+int ensure_ch(prx_context* c, uint32_t hot_n);
+SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options& o);
+// DF / DF-P marking runs without host synchronisation; DT's closure reads
+// the control block.
+int run_marking(prx_context* c, const SolveArgs& a, int mode, const uint32_t* du, const uint32_t* dv, uint64_t nd,
+                const uint32_t* iu, uint64_t ni);
+// One iteration (update launches, expansion, k_finalize) on stream c->stream.
+int enqueue_iteration(prx_context* c, const GraphDev& g, const SolveArgs& a, int mode, bool timing,
+                      const ChunkLayout* lay);
+// Keeps a conditional WHILE node going while the solve is not done and fewer
+// than cap bodies ran (counted in st->graph_rounds).
+__global__ void k_loop_cond(cudaGraphConditionalHandle h, State* st, int cap);
+
 #define TRY_CUDA_ST(x)                                                                   \
   do {                                                                                   \
     cudaError_t e_ = (x);                                                                \

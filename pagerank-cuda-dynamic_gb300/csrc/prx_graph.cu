@@ -304,17 +304,18 @@ __global__ void k_chunk_count(const uint32_t* __restrict__ xtoff, const uint32_t
 }
 
 // Edge id as stored in a layout: a hot source's number with the flag, else
-// the id itself (hot_idx null: plain ids).
-__device__ __forceinline__ uint32_t layout_id(const uint32_t* __restrict__ hot_idx, uint32_t u) {
+// the id itself (hot_idx null: plain ids; see GraphDev::hot_idx, of a graph
+// of `words` bitmap words).
+__device__ __forceinline__ uint32_t layout_id(const uint32_t* __restrict__ hot_idx, uint32_t words, uint32_t u) {
   if (!hot_idx) return u;
-  const uint32_t h = hot_idx[u];
-  return h == kNotHot ? u : (kHotFlag | h);
+  const uint32_t w = __ldg(hot_idx + (u >> 5)), below = w & ((1u << (u & 31u)) - 1u);
+  return ((w >> (u & 31u)) & 1u) ? (kHotFlag | (__ldg(hot_idx + words + (u >> 5)) + __popc(below))) : u;
 }
 
 __global__ void k_chunk_scatter(const uint32_t* __restrict__ xtoff, const uint32_t* __restrict__ xtedg,
                                 const uint32_t* __restrict__ low_bm, uint32_t n, uint32_t width, int K,
                                 const uint32_t* __restrict__ off, uint32_t* __restrict__ edg,
-                                const uint32_t* __restrict__ hot_idx) {
+                                const uint32_t* __restrict__ hot_idx, uint32_t hot_words) {
   const size_t row = (size_t)n + 1;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     if (!((low_bm[v >> 5] >> (v & 31u)) & 1u)) continue;
@@ -323,25 +324,28 @@ __global__ void k_chunk_scatter(const uint32_t* __restrict__ xtoff, const uint32
     for (int k = 0; k < K; ++k) {
       const uint64_t hi = (uint64_t)(k + 1) * width;
       uint32_t pos = off[k * row + v];
-      while (j < e && xtedg[j] < hi) edg[pos++] = layout_id(hot_idx, xtedg[j++]);
+      while (j < e && xtedg[j] < hi) edg[pos++] = layout_id(hot_idx, hot_words, xtedg[j++]);
     }
   }
 }
 
 // Scatter for K <= kScatterK chunks, coalesced: a warp takes 32 consecutive
-// rows (lane i: row v0+i), whose edges are one contiguous range, and walks it
-// 32 edges at a time.  Each edge finds its row by a binary search over the
+// rows (lane i: row v0+i) and walks the edges of each run of consecutive LOW
+// rows among them -- one contiguous range of at most 32 x 64 edges -- 32
+// edges at a time.  Each edge finds its row by a binary search over the
 // lanes' row starts (the last row starting at or before it: empty rows are
 // skipped that way) and its destination -- chunk k's piece of the row, which
 // is a consecutive run since rows are sorted by source -- by shuffles from
-// that row's lane.  Edges of non-LOW rows are read and dropped.
+// that row's lane.  The edges of rows of other classes (a hub row can hold
+// millions) are never read.
 constexpr int kScatterK = 8;
 __global__ void __launch_bounds__(256) k_chunk_scatter_w(const uint32_t* __restrict__ xtoff,
                                                          const uint32_t* __restrict__ xtedg,
                                                          const uint32_t* __restrict__ low_bm, uint32_t n,
                                                          uint32_t width, int K, const uint32_t* __restrict__ off,
                                                          uint32_t* __restrict__ edg,
-                                                         const uint32_t* __restrict__ hot_idx, uint32_t g0 = 0,
+                                                         const uint32_t* __restrict__ hot_idx, uint32_t hot_words,
+                                                         uint32_t g0 = 0,
                                                          uint32_t g1 = 0xffffffffu, uint64_t cap = ~0ull) {
   const size_t row = (size_t)n + 1;
   const uint32_t lane = lane_id();
@@ -363,13 +367,22 @@ __global__ void __launch_bounds__(256) k_chunk_scatter_w(const uint32_t* __restr
         run += off[k * row + v + 1] - dst[k];
       }
     }
+    // runs of LOW rows [ra, rb): lanes past the group's end count as not LOW
+    const unsigned lowm = __ballot_sync(0xffffffffu, low);
+    for (unsigned rest = lowm; rest;) {
+      const uint32_t ra = __ffs(rest) - 1;
+      const unsigned above = ~rest & ~((1u << ra) - 1u);   // not LOW, at or after ra
+      const uint32_t rb = above ? (uint32_t)(__ffs(above) - 1) : 32u;
+      rest &= rb < 32 ? ~((1u << rb) - 1u) : 0u;
+      const uint32_t rs0 = __shfl_sync(0xffffffffu, s, ra);
+      const uint32_t run_end = rb < 32 ? __shfl_sync(0xffffffffu, s, rb) : end;
     // four 32-edge windows per step, their loads issued together
-    for (uint32_t base = __shfl_sync(0xffffffffu, s, 0); base < end; base += 128) {
+    for (uint32_t base = rs0; base < run_end; base += 128) {
       uint32_t uu[4];
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
         const uint32_t j = base + 32u * w + lane;
-        uu[w] = j < end ? __ldg(xtedg + j) : 0u;
+        uu[w] = j < run_end ? __ldg(xtedg + j) : 0u;
       }
 #pragma unroll
       for (int w = 0; w < 4; ++w) {
@@ -382,9 +395,12 @@ __global__ void __launch_bounds__(256) k_chunk_scatter_w(const uint32_t* __restr
         }
         const bool rlow = __shfl_sync(0xffffffffu, (int)low, r) != 0;
         const uint32_t sr = __shfl_sync(0xffffffffu, s, r);
-        const bool act = j < end && rlow;
+        const bool act = j < run_end && rlow;
         const uint32_t u = uu[w];
-        const uint32_t k = act ? u / width : 0u;
+        uint32_t k = 0;  // u's chunk: the chunk bounds at or below u (no division)
+#pragma unroll
+        for (int kk = 1; kk < kScatterK; ++kk)
+          k += (kk < K && (uint64_t)u >= (uint64_t)kk * width) ? 1u : 0u;
         uint32_t d = 0, rr = 0;
 #pragma unroll
         for (int kk = 0; kk < kScatterK; ++kk) {
@@ -397,8 +413,9 @@ __global__ void __launch_bounds__(256) k_chunk_scatter_w(const uint32_t* __restr
           }
         }
         const uint64_t at = (uint64_t)d + (j - sr - rr);
-        if (act && at < cap) edg[at] = layout_id(hot_idx, u);
+        if (act && at < cap) edg[at] = layout_id(hot_idx, hot_words, u);
       }
+    }
     }
   }
 }
@@ -416,24 +433,37 @@ void free_chunks(GraphDev& g) {
 
 // The chunk layout of one CSR of `rows` rows (offsets off[0 .. rows], edges
 // edg, LOW bitmap from its first row): counts, scan, scatter.
-static cudaError_t build_layout(const uint32_t* off, const uint32_t* edg, const uint32_t* low_bm, uint32_t rows,
-                                uint64_t low_edges, uint32_t width, int K, int sms, cudaStream_t s,
-                                uint32_t** lay_off, uint32_t** lay_edg, const uint32_t* hot_idx) {
+cudaError_t build_layout_into(const uint32_t* off, const uint32_t* edg, const uint32_t* low_bm, uint32_t rows,
+                              uint32_t width, int K, const uint32_t* hot_idx, uint32_t hot_words, uint32_t* lay_off,
+                              uint32_t* lay_edg, uint32_t* scan_ws, int sms, cudaStream_t s) {
   const size_t len = (size_t)K * ((size_t)rows + 1);
   if (len > 0xffffffffull) return cudaErrorInvalidValue;
-  cudaError_t e = graph_alloc(lay_off, sizeof(uint32_t) * len, s);
-  if (e == cudaSuccess) e = graph_alloc(lay_edg, sizeof(uint32_t) * edge_slots(low_edges), s);
-  if (e != cudaSuccess) return e;
   const int grid = sms * 8;
-  k_chunk_count<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, *lay_off);
-  e = exclusive_scan_u32(*lay_off, (uint32_t)len, s);
+  k_chunk_count<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, lay_off);
+  cudaError_t e = exclusive_scan_u32_ws(lay_off, (uint32_t)len, scan_ws, s);
   if (e == cudaSuccess) {
     if (K <= kScatterK)
-      k_chunk_scatter_w<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, *lay_off, *lay_edg, hot_idx);
+      k_chunk_scatter_w<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, lay_off, lay_edg, hot_idx, hot_words);
     else
-      k_chunk_scatter<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, *lay_off, *lay_edg, hot_idx);
+      k_chunk_scatter<<<grid, 256, 0, s>>>(off, edg, low_bm, rows, width, K, lay_off, lay_edg, hot_idx, hot_words);
     e = cudaGetLastError();
   }
+  return e;
+}
+
+static cudaError_t build_layout(const uint32_t* off, const uint32_t* edg, const uint32_t* low_bm, uint32_t rows,
+                                uint64_t low_edges, uint32_t width, int K, int sms, cudaStream_t s,
+                                uint32_t** lay_off, uint32_t** lay_edg, const uint32_t* hot_idx,
+                                uint32_t hot_words) {
+  const size_t len = (size_t)K * ((size_t)rows + 1);
+  if (len > 0xffffffffull) return cudaErrorInvalidValue;
+  uint32_t* ws = nullptr;
+  cudaError_t e = graph_alloc(lay_off, sizeof(uint32_t) * len, s);
+  if (e == cudaSuccess) e = graph_alloc(lay_edg, sizeof(uint32_t) * edge_slots(low_edges), s);
+  if (e == cudaSuccess) e = graph_alloc(&ws, sizeof(uint32_t) * scan_ws_words((uint32_t)len), s);
+  if (e == cudaSuccess)
+    e = build_layout_into(off, edg, low_bm, rows, width, K, hot_idx, hot_words, *lay_off, *lay_edg, ws, sms, s);
+  if (ws) cudaFreeAsync(ws, s);
   return e;
 }
 
@@ -551,7 +581,7 @@ cudaError_t build_default_layout_pipelined(GraphDev& g, uint32_t width, bool hot
     if (e != cudaSuccess) break;
     k_chunk_carry<<<sms * 4, 256, 0, s>>>(l->off, n, r0, r1, K, tot, p, bound);
     k_chunk_scatter_w<<<sms * 8, 256, 0, s>>>(g.xtoff, g.xtedg, g.low_bm, n, width, K, l->off, l->edg, hot_idx,
-                                              r0 >> 5, (r1 + 31) >> 5, cap);
+                                              (n + 31) >> 5, r0 >> 5, (r1 + 31) >> 5, cap);
     e = cudaGetLastError();
   }
   // every chunk must have stayed within its region (the out-degrees bound it)
@@ -605,7 +635,8 @@ cudaError_t ensure_chunks(GraphDev& g, uint32_t width, int sms, cudaStream_t s, 
   const int K = (int)((g.n + (uint64_t)width - 1) / width);
   cudaError_t e = cudaSuccess;
   if (g.nseg <= 1) {
-    e = build_layout(g.xtoff, g.xtedg, g.low_bm, g.n, g.cls_edges[LOW], width, K, sms, s, &l.off, &l.edg, hot_idx);
+    e = build_layout(g.xtoff, g.xtedg, g.low_bm, g.n, g.cls_edges[LOW], width, K, sms, s, &l.off, &l.edg, hot_idx,
+                     (g.n + 31) / 32);
   } else {
     // one layout per row segment: its rows' offsets are a plain CSR of the
     // segment's edges; sources keep their global ids, so the chunks are global
@@ -616,7 +647,7 @@ cudaError_t ensure_chunks(GraphDev& g, uint32_t width, int sms, cudaStream_t s, 
           (q + 1 < g.nseg ? g.xtseg0[q + 1] : g.m) - g.xtseg0[q];  // every edge of the segment
       uint32_t *lo = nullptr, *le = nullptr;
       e = build_layout(g.xtoff + v0 + q, g.xtedg + g.xtpos[q], g.low_bm + (v0 >> 5), rows, seg_edges_bound, width,
-                       K, sms, s, &lo, &le, hot_idx);
+                       K, sms, s, &lo, &le, hot_idx, (g.n + 31) / 32);
       l.seg_off.push_back(lo);
       l.seg_edg.push_back(le);
     }
@@ -662,19 +693,27 @@ __global__ void __launch_bounds__(256) k_degree_hist(const uint32_t* __restrict_
     if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
-__global__ void k_hot_flags(const uint32_t* __restrict__ xtdat, uint32_t n, uint32_t t, uint32_t* __restrict__ flag) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += gridDim.x * blockDim.x)
-    flag[v] = v < n && xtdat[v] >= t ? 1u : 0u;
+// The hot bitmap (out-degree >= t) and its per-word counts (rank[words] = 0
+// for the scan that turns them into counts before each word).
+__global__ void k_hot_bitmap(const uint32_t* __restrict__ xtdat, uint32_t n, uint32_t t, uint32_t* __restrict__ bm,
+                             uint32_t* __restrict__ rank) {
+  const uint32_t words = (n + 31) >> 5;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w <= words; w += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t v = (w << 5) | lane_id();
+    const unsigned b = __ballot_sync(0xffffffffu, v < n && xtdat[v] >= t);
+    if (lane_id() == 0) {
+      if (w < words) bm[w] = b;
+      rank[w] = __popc(b);
+    }
+  }
 }
 
-// flag holds the exclusive scan of the hot flags: v's number if hot
-__global__ void k_hot_index(const uint32_t* __restrict__ xtdat, uint32_t n, uint32_t t,
-                            const uint32_t* __restrict__ scan, uint32_t* __restrict__ hot_idx,
-                            uint32_t* __restrict__ hot_list) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-    const bool hot = xtdat[v] >= t;
-    hot_idx[v] = hot ? scan[v] : kNotHot;
-    if (hot) hot_list[scan[v]] = v;
+// rank holds the counts before each word: the list of hot sources in id order
+__global__ void k_hot_list(const uint32_t* __restrict__ bm, const uint32_t* __restrict__ rank, uint32_t words,
+                           uint32_t* __restrict__ hot_list) {
+  for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < words; w += gridDim.x * blockDim.x) {
+    uint32_t i = rank[w];
+    for (uint32_t b = bm[w]; b; b &= b - 1) hot_list[i++] = (w << 5) | (uint32_t)(__ffs(b) - 1);
   }
 }
 
@@ -723,19 +762,17 @@ cudaError_t ensure_hot(GraphDev& g, uint32_t cap, int sms, cudaStream_t s) {
   uint64_t count = 0;
   for (uint32_t b = t; b < kDegBins; ++b) count += h[b];
   if (count == 0 || t >= kDegBins) return cudaSuccess;
-  uint32_t* scan = nullptr;
-  e = graph_alloc(&scan, sizeof(uint32_t) * ((size_t)n + 1), s);
-  if (e == cudaSuccess) e = graph_alloc(&g.hot_idx, sizeof(uint32_t) * (size_t)n, s);
+  const uint32_t words = (n + 31) / 32;
+  e = graph_alloc(&g.hot_idx, sizeof(uint32_t) * (2 * (size_t)words + 1), s);
   if (e == cudaSuccess) e = graph_alloc(&g.hot_list, sizeof(uint32_t) * count, s);
   if (e == cudaSuccess) {
-    k_hot_flags<<<sms * 4, 256, 0, s>>>(g.xtdat, n, t, scan);
-    e = exclusive_scan_u32(scan, n + 1, s);
+    k_hot_bitmap<<<sms * 8, 256, 0, s>>>(g.xtdat, n, t, g.hot_idx, g.hot_idx + words);
+    e = exclusive_scan_u32(g.hot_idx + words, words + 1, s);
   }
   if (e == cudaSuccess) {
-    k_hot_index<<<sms * 4, 256, 0, s>>>(g.xtdat, n, t, scan, g.hot_idx, g.hot_list);
+    k_hot_list<<<sms * 4, 256, 0, s>>>(g.hot_idx, g.hot_idx + words, words, g.hot_list);
     e = cudaGetLastError();
   }
-  cudaFreeAsync(scan, s);
   if (e != cudaSuccess) {
     free_hot(g);
     return e;
@@ -762,16 +799,20 @@ cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
     cudaError_t e = graph_alloc(&g.rcp32, sizeof(float) * (n ? n : 1), s);
     if (e != cudaSuccess) return e;
   }
-  if (n) k_low_bitmap<<<sms * 4, 256, 0, s>>>(g.xtoff, g.seg_shift, n, g.low_bm);
-  if (n) {
-    k_rcp_table<<<kRcpTable / 256, 256, 0, s>>>();
-    k_reciprocals<<<sms * 4, 256, 0, s>>>(g.xtdat, n, g.rcp, g.rcp32);
-  }
+  launch_vertex_tables(g.xtoff, g.seg_shift, g.xtdat, n, g.low_bm, g.rcp, g.rcp32, sms, s);
   if (!g.cls_list) {
     cudaError_t e = graph_alloc(&g.cls_list, sizeof(uint32_t) * (n ? n : 1), s);
     if (e != cudaSuccess) return e;
   }
   return build_class_lists(g.xtoff, g.seg_shift, n, g.mid_max, g.cls_list, g.cls_begin, g.cls_edges, sms, s);
+}
+
+void launch_vertex_tables(const uint32_t* xtoff, uint32_t shift, const uint32_t* xtdat, uint32_t n, uint32_t* low_bm,
+                          double* rcp, float* rcp32, int sms, cudaStream_t s) {
+  if (!n) return;
+  k_low_bitmap<<<sms * 4, 256, 0, s>>>(xtoff, shift, n, low_bm);
+  k_rcp_table<<<kRcpTable / 256, 256, 0, s>>>();
+  k_reciprocals<<<sms * 4, 256, 0, s>>>(xtdat, n, rcp, rcp32);
 }
 
 cudaError_t build_class_lists(const uint32_t* off, uint32_t shift, uint32_t n, uint32_t mid_max, uint32_t* list,
@@ -862,16 +903,23 @@ __global__ void __launch_bounds__(256) k_scan_apply(uint32_t* __restrict__ data,
   }
 }
 
-cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t len, cudaStream_t s) {
+uint32_t scan_ws_words(uint32_t len) { return (len + kTileV - 1) / kTileV; }
+
+cudaError_t exclusive_scan_u32_ws(uint32_t* data, uint32_t len, uint32_t* sums, cudaStream_t s) {
   if (len == 0) return cudaSuccess;
-  const uint32_t ntiles = (len + kTileV - 1) / kTileV;
-  uint32_t* sums = nullptr;
-  cudaError_t e = graph_alloc(&sums, sizeof(uint32_t) * ntiles, s);
-  if (e != cudaSuccess) return e;
+  const uint32_t ntiles = scan_ws_words(len);
   k_scan_tile_sums<<<ntiles, 256, 0, s>>>(data, len, sums);
   k_scan_single<<<1, 1024, 0, s>>>(sums, ntiles);
   k_scan_apply<<<ntiles, 256, 0, s>>>(data, len, sums);
-  e = cudaGetLastError();
+  return cudaGetLastError();
+}
+
+cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t len, cudaStream_t s) {
+  if (len == 0) return cudaSuccess;
+  uint32_t* sums = nullptr;
+  cudaError_t e = graph_alloc(&sums, sizeof(uint32_t) * scan_ws_words(len), s);
+  if (e != cudaSuccess) return e;
+  e = exclusive_scan_u32_ws(data, len, sums, s);
   cudaFreeAsync(sums, s);
   return e;
 }

@@ -134,8 +134,12 @@ struct GraphDev {
   // them, out-degree at least twice the average), numbered 0 .. hot_n-1 in
   // id order.  Their contributions are copied after every sweep into a dense
   // array of hot_n values that stays in L2; edges from them are gathered
-  // there (their values are the same, so sums are unchanged).  hot_idx[v] is
-  // v's number or kNotHot; built on first use per graph version.
+  // there (their values are the same, so sums are unchanged).  hot_idx: a
+  // bitmap of the hot sources (ceil(n / 32) words), then per word the count
+  // of hot sources in the words before it, so v's number is that count plus
+  // the set bits below v in its word -- 8 bytes per 32 vertices, small
+  // enough to stay in L2 while a layout scatter looks up every edge's
+  // source.  Built on first use per graph version.
   uint32_t* hot_idx = nullptr;
   uint32_t* hot_list = nullptr;
   uint32_t hot_n = 0;
@@ -169,7 +173,6 @@ cudaError_t build_default_layout_pipelined(GraphDev& g, uint32_t width, bool hot
                                            cudaStream_t s);
 
 constexpr uint32_t kHotFlag = 0x80000000u;
-constexpr uint32_t kNotHot = 0xffffffffu;
 // The hot sources of g for a cap of `cap` vertices (0: none); graphs of 2^31
 // vertices or more get none (their ids use the flag bit).
 cudaError_t ensure_hot(GraphDev& g, uint32_t cap, int sms, cudaStream_t s);
@@ -288,6 +291,10 @@ void launch_state_reset(State* st, int max_iter, double tol, cudaStream_t s);
 
 // ---- graph construction (prx_graph.cu) ----------------------------------
 cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s);
+// The LOW-class bitmap and the reciprocal out-degrees (FP64 and FP32) of a
+// graph version, by kernels alone (build_classes runs them too).
+void launch_vertex_tables(const uint32_t* xtoff, uint32_t shift, const uint32_t* xtdat, uint32_t n, uint32_t* low_bm,
+                          double* rcp, float* rcp32, int sms, cudaStream_t s);
 // A new graph takes the picks prx_autotune made earlier in this process for a
 // graph of the same signature, if any (prx_tune.cu).
 cudaError_t tune_apply_cached(GraphDev& g, int sms, cudaStream_t s);
@@ -297,7 +304,50 @@ cudaError_t build_class_lists(const uint32_t* off, uint32_t shift, uint32_t n, u
                               uint32_t begin[NCLS + 1], uint64_t edges[NCLS], int sms, cudaStream_t s);
 // b: device array [du | dv | iu | iv | tdk | tdv | tik | tiv]; t* = batch sorted by (v, u)
 cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd, uint64_t ni, int sms, cudaStream_t s);
+// The arrays of one graph version (a plain CSR pair and the out-degrees).
+struct CsrSet {
+  uint32_t *xoff, *xedg, *xtoff, *xtedg, *xtdat;
+};
+
+// The LOW layout of `rows` rows in K source chunks of `width` vertices into
+// caller buffers: K x (rows + 1) offsets, edge ids (edge_slots of the LOW
+// edges), scan workspace of scan_ws_words(K x (rows + 1)) words; edge ids of
+// hot sources encoded when hot_idx (GraphDev::hot_idx of a graph of
+// 32 x hot_words vertices at most) is not null.  Kernels only.
+cudaError_t build_layout_into(const uint32_t* off, const uint32_t* edg, const uint32_t* low_bm, uint32_t rows,
+                              uint32_t width, int K, const uint32_t* hot_idx, uint32_t hot_words, uint32_t* lay_off,
+                              uint32_t* lay_edg, uint32_t* scan_ws, int sms, cudaStream_t s);
+
+// Workspace of apply_batch_graph for n vertices and batches of at most bmax
+// edges (deletions plus insertions), carved from words(n, bmax) words.
+struct ApplyWs {
+  int32_t* delta;
+  uint32_t *touched, *ranges, *cnt, *trow, *big, *scan_off, *scan_cnt;
+  unsigned long long* nbig;
+  static size_t words(uint32_t n, uint32_t bmax);
+  ApplyWs(uint32_t* base, uint32_t n, uint32_t bmax);
+};
+
+// Apply a tidy batch (b: [du | dv | iu | iv | tdk | tdv | tik | tiv] as for
+// apply_batch_device) to the plain CSRs src, writing dst (edge arrays large
+// enough for the new count): the kernels of apply_batch_device with every
+// count kept on the device -- no allocation and no host synchronisation, so
+// the sequence can be captured into a conditional node's body.  The batch
+// must have been checked (launch_batch_check).
+cudaError_t apply_batch_graph(const CsrSet& src, const CsrSet& dst, uint32_t n, const uint32_t* b, uint32_t nd,
+                              uint32_t ni, const ApplyWs& w, int sms, cudaStream_t s);
+// Sets bits of *err when batch b ([du | dv | iu | iv]) is not a tidy batch
+// for the plain CSR xoff / xedg of n vertices: 8 an id >= n, 4 a list not
+// strictly ascending in (u, v), then (only if neither) 1 a deletion is
+// missing, 2 an insertion exists.  A set *err on entry skips the row reads.
+void launch_batch_check(const uint32_t* xoff, const uint32_t* xedg, uint32_t n, const uint32_t* b, uint32_t nd,
+                        uint32_t ni, uint32_t* err, int sms, cudaStream_t s);
+
 cudaError_t exclusive_scan_u32(uint32_t* data, uint32_t len, cudaStream_t s);
+// The same with a caller's workspace of scan_ws_words(len) words: no
+// allocation, so it can be captured into a conditional node's body.
+uint32_t scan_ws_words(uint32_t len);
+cudaError_t exclusive_scan_u32_ws(uint32_t* data, uint32_t len, uint32_t* sums, cudaStream_t s);
 
 // Stable LSD radix sort of keys[0 .. count) on their bits [lo, hi), 8 at a
 // time, ping-ponging with tmp (both with 2 keys of slack past count: the

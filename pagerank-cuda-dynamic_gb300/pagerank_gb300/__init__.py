@@ -8,7 +8,7 @@ from ._lib import (DYNAMIC_FRONTIER, DYNAMIC_TRAVERSAL, FP32_REFINE, FP64, LOOP_
 from .api import (Context, Graph, mark_affected, options, pagerank_dynamic_frontier, pagerank_dynamic_traversal,
                   pagerank_naive_dynamic, pagerank_prune_dynamic_frontier, pagerank_static, release_cached_memory,
                   l2_fetch_granularity, graph_pool_stats, selftest_division, solve, autotune, autotune_ppr,
-                  solve_device, solve_ppr_batched, solve_ppr_batched_device)
+                  solve_device, solve_batches, solve_ppr_batched, solve_ppr_batched_device)
 from . import graphs
 
 MODES = {"static": STATIC, "naive_dynamic": NAIVE_DYNAMIC, "dynamic_traversal": DYNAMIC_TRAVERSAL,

@@ -89,7 +89,8 @@ EXPORTS = (
     "prx_release_cached_memory", "prx_graph_pool_stats", "prx_l2_fetch_granularity", "prx_graph_size",
     "prx_graph_class_stats",
     "prx_graph_download",
-    "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_mark_affected", "prx_selftest_division",
+    "prx_graph_apply_batch", "prx_solve", "prx_solve_device", "prx_solve_batches_device", "prx_mark_affected",
+    "prx_selftest_division",
     "prx_solve_ppr_batched", "prx_solve_ppr_batched_device", "prx_graph_set_weights", "prx_solve_weighted",
     "prx_adjoint", "prx_autotune", "prx_autotune_ppr", "prx_graph_tidy_batch", "prx_graph_create_from_edges",
     "prx_graph_create_from_edges_device", "prx_graph_gen_batch",
@@ -138,6 +139,8 @@ def load(build_if_missing=True):
         "prx_solve": (i32, [vp, vp, i32, vp, vp, u64, vp, vp, u64, vp, C.POINTER(Options), vp, C.POINTER(Result)]),
         "prx_solve_device": (i32, [vp, vp, i32, vp, vp, u64, vp, vp, u64, vp, C.POINTER(Options), vp,
                                    C.POINTER(Result)]),
+        "prx_solve_batches_device": (i32, [vp, vp, i32, C.c_uint32, vp, vp, vp, vp, vp, vp, vp, C.POINTER(Options),
+                                           vp, vp, vp, C.POINTER(C.c_uint32)]),
         "prx_mark_affected": (i32, [vp, vp, i32, vp, vp, u64, vp, u64, vp]),
         "prx_selftest_division": (i32, [vp, C.c_uint32, C.c_uint32, C.POINTER(u64)]),
         "prx_solve_ppr_batched": (i32, [vp, vp, C.c_uint32, vp, vp, C.POINTER(Options), vp, C.POINTER(PprResult)]),

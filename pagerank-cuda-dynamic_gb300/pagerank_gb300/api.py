@@ -42,6 +42,7 @@ class Context:
 
     def __init__(self, device=0):
         self._h = C.c_void_p()
+        self.device = device
         check(load().prx_context_create(device, C.byref(self._h)), "prx_context_create")
 
     @property
@@ -287,6 +288,43 @@ def solve_device(ctx, g, mode, q_ptr, ranks_ptr, batch_ptrs=(None, None, 0, None
     check(load().prx_solve_device(ctx.handle, g.handle, int(mode), du, dv, nd, iu, iv, ni, q_ptr,
                                   C.byref(opts or options()), ranks_ptr, C.byref(res)), "prx_solve_device")
     return res.as_dict()
+
+
+def solve_batches(ctx, g, mode, batches, q, opts=None, each=False):
+    """prx_solve_batches_device: apply and solve K consecutive batches
+    [(del_u, del_v, ins_u, ins_v), ...] as one CUDA graph launch, from ranks q
+    -> (ranks after the last batch, [result dict per batch], ranks per batch
+    float64[K, n] or None).  Host arrays in and out (copied through device
+    tensors)."""
+    import torch
+    n, _ = g.size()
+    K = len(batches)
+    dev = torch.device("cuda", ctx.device)
+    lists = [[_u32(b[i]) for b in batches] for i in range(4)]
+    del_off = np.zeros(K + 1, np.uint64)
+    ins_off = np.zeros(K + 1, np.uint64)
+    del_off[1:] = np.cumsum([len(x) for x in lists[0]])
+    ins_off[1:] = np.cumsum([len(x) for x in lists[2]])
+
+    def up(parts):
+        a = np.concatenate(parts) if parts else np.zeros(0, np.uint32)
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.int32).copy()).to(dev)
+
+    du, dv, iu, iv = (up(x) for x in lists)
+    qd = torch.from_numpy(np.ascontiguousarray(q, dtype=np.float64).copy()).to(dev)
+    out = torch.empty(max(n, 1), dtype=torch.float64, device=dev)
+    each_d = torch.empty((K, max(n, 1)), dtype=torch.float64, device=dev) if each and K else None
+    res = (Result * max(K, 1))()
+    done = C.c_uint32()
+    torch.cuda.current_stream(dev).synchronize()   # the library works on its own stream
+    st = load().prx_solve_batches_device(ctx.handle, g.handle, int(mode), K, del_off.ctypes.data,
+                                         du.data_ptr() or None, dv.data_ptr() or None, ins_off.ctypes.data,
+                                         iu.data_ptr() or None, iv.data_ptr() or None, qd.data_ptr(),
+                                         C.byref(opts or options()), out.data_ptr(),
+                                         None if each_d is None else each_d.data_ptr(), res, C.byref(done))
+    results = [res[k].as_dict() for k in range(done.value)]
+    check(st, "prx_solve_batches_device")
+    return (out.cpu().numpy()[:n], results, None if each_d is None else each_d.cpu().numpy()[:, :n])
 
 
 def release_cached_memory(device=0):
