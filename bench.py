@@ -70,6 +70,8 @@ def parse():
     p.add_argument("--adjoint-scale", type=int, default=20)
     p.add_argument("--adjoint-fd-edges", type=int, default=200, help="edges checked by finite differences")
     p.add_argument("--adjoint-batches", type=int, default=2, help="dynamic batches of 1e-4|E| after the first solve")
+    p.add_argument("--adjoint-fd-later", type=int, default=None,
+                   help="edges checked by finite differences after each batch (default: a tenth of --adjoint-fd-edges)")
     p.add_argument("--batches-per-size", type=int, default=10,
                    help="consecutive dynamic batches at each of 1e-5, 1e-4, 1e-3 |E|")
     p.add_argument("--no-ingest", action="store_true", help="skip the device graph ingest from the edge list")
@@ -739,7 +741,8 @@ def run_adjoint(args, pg, ctx, local):
         # finite differences against tightly converged forward solves
         r_t, _ = A.solve_weighted(ctx, g, None, r0=r, opts=tight)
         adj_t = A.adjoint(ctx, g, r_t, gl, None, opts=tight)["grad_w"].cpu().numpy()
-        k = args.adjoint_fd_edges if b == 0 else max(1, args.adjoint_fd_edges // 10)
+        k = args.adjoint_fd_edges if b == 0 else (args.adjoint_fd_later if args.adjoint_fd_later is not None
+                                                  else max(1, args.adjoint_fd_edges // 10))
         edges = rng.choice(m, k, replace=False)
         t0 = time.perf_counter()
         fd = A.fd_weight_gradients(ctx, g, xoff, xedg, w, r_t, gl, edges)

@@ -85,29 +85,32 @@ def fd_weight_gradients(ctx, g, xoff, xedg, weights, r, grad_r, edges, h=1e-6, t
     gl = _f64(grad_r)
     n = len(xoff) - 1
     o = options(damping=alpha, tolerance=tolerance, max_iterations=max_iterations)
+    wd = torch.from_numpy(w).to(dev)   # one device copy; each difference changes one entry in place
+    rh = r.detach().cpu().numpy() if isinstance(r, torch.Tensor) else np.asarray(r)
     out = []
     for j in edges:
         u = int(np.searchsorted(xoff, j, side="right") - 1)
         s, e = xoff[u], xoff[u + 1]
         nb = torch.from_numpy(np.asarray(xedg[s:e], np.int64)).to(dev)
         row = w[s:e].astype(np.float64)
-        ru = float(r[u])
+        ru = float(rh[u])
         diffs = []
         wj = []
         for sign in (1.0, -1.0):
-            wq = w.copy()
-            wq[j] = np.float32(w[j] + np.float32(sign * h))
-            wj.append(float(wq[j]))
+            wq_j = np.float32(w[j] + np.float32(sign * h))
+            wj.append(float(wq_j))
             rq = row.copy()
-            rq[j - s] = float(wq[j])
+            rq[j - s] = float(wq_j)
             b = alpha * ru * (rq / rq.sum() - row / row.sum())     # alpha (Pq - P)^T r, rows of u only
             t = torch.zeros(n, dtype=torch.float64, device=dev)
             t.index_add_(0, nb, torch.from_numpy(b / (1 - alpha)).to(dev))
-            set_weights(ctx, g, torch.from_numpy(wq).to(dev))
+            wd[j] = float(wq_j)
+            set_weights(ctx, g, wd)
             d, _ = solve_weighted(ctx, g, t, opts=o)
             diffs.append(float((gl * d).sum()))
+        wd[j] = float(w[j])
         out.append((diffs[0] - diffs[1]) / (wj[0] - wj[1]))
-    set_weights(ctx, g, torch.from_numpy(w).to(dev))
+    set_weights(ctx, g, wd)
     return np.array(out)
 
 
