@@ -183,11 +183,12 @@ __global__ void __launch_bounds__(kThreads) k_copy_runs(Runs r, const uint32_t* 
   const uint32_t lane = lane_id();
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  const uint32_t total = r.ooff[r.rows];
-  const uint32_t windows = (uint32_t)(((uint64_t)total + kWindow - 1) / kWindow);
+  // old positions [start, end): a CSR's offsets start at 0, a layout chunk's where its region starts
+  const uint32_t start = r.ooff[0], end = r.ooff[r.rows];
+  const uint32_t windows = (uint32_t)(((uint64_t)(end - start) + kWindow - 1) / kWindow);
   for (uint32_t wi = warp; wi < windows; wi += nwarps) {
-    const uint32_t p0 = wi * kWindow, p1 = (uint32_t)min((uint64_t)total, (uint64_t)p0 + kWindow);
-    // the last run starting at or before p0 (run 0 starts at 0)
+    const uint32_t p0 = start + wi * kWindow, p1 = (uint32_t)min((uint64_t)end, (uint64_t)p0 + kWindow);
+    // the last run starting at or before p0 (run 0 starts at `start`)
     uint32_t lo = 0, hi = r.T + 1;
     while (hi - lo > 1) {
       const uint32_t step = (hi - lo + 31) / 32, j = lo + lane * step;
@@ -297,6 +298,80 @@ __global__ void __launch_bounds__(kThreads) k_merge_big(Runs r, const uint32_t* 
   }
 }
 
+// ---- LOW layouts carried to the new version ---------------------------------
+// A cached layout (see ChunkLayout) of the old version becomes the new
+// version's without a rebuild: rows the batch did not touch keep their chunk
+// counts and segments (copied as shifted runs by k_copy_runs), touched rows
+// are counted and scattered again from the new in-CSR (a row that crossed
+// the LOW bound gains or loses its segments), with the same hot numbering.
+
+// New chunk counts (K x (n + 1), a 0 closing each chunk row): untouched rows
+// from the old offsets, touched rows from their new in-edges if still LOW.
+__global__ void k_layout_counts(const uint32_t* __restrict__ lay_off, const uint32_t* __restrict__ xtoff,
+                                const uint32_t* __restrict__ xtedg, const uint32_t* __restrict__ touched,
+                                uint32_t n, uint32_t width, int K, uint32_t* __restrict__ cnt) {
+  const size_t row = (size_t)n + 1;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += gridDim.x * blockDim.x) {
+    if (v == n) {
+      for (int k = 0; k < K; ++k) cnt[k * row + n] = 0;
+      continue;
+    }
+    if (!((touched[v >> 5] >> (v & 31u)) & 1u)) {
+      for (int k = 0; k < K; ++k) cnt[k * row + v] = lay_off[k * row + v + 1] - lay_off[k * row + v];
+      continue;
+    }
+    uint32_t j = xtoff[v];
+    const uint32_t e = xtoff[v + 1];
+    const bool low = e - j <= kLowMax;
+    for (int k = 0; k < K; ++k) {
+      const uint64_t hi = (uint64_t)(k + 1) * width;
+      const uint32_t b = j;
+      while (low && j < e && xtedg[j] < hi) ++j;
+      cnt[k * row + v] = j - b;
+    }
+  }
+}
+
+// The touched rows' segments, a thread per row (at most kLowMax ids).
+__global__ void k_layout_touched(const uint32_t* __restrict__ xtoff, const uint32_t* __restrict__ xtedg,
+                                 const uint32_t* __restrict__ trow, uint32_t T, const uint32_t* Tp, uint32_t n,
+                                 uint32_t width, int K, const uint32_t* __restrict__ off,
+                                 uint32_t* __restrict__ edg, const uint32_t* __restrict__ hot_idx,
+                                 uint32_t hot_words) {
+  const size_t row = (size_t)n + 1;
+  if (Tp) T = *Tp;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < T; i += gridDim.x * blockDim.x) {
+    const uint32_t v = trow[i];
+    uint32_t j = xtoff[v];
+    const uint32_t e = xtoff[v + 1];
+    if (e - j > kLowMax) continue;
+    for (int k = 0; k < K; ++k) {
+      const uint64_t hi = (uint64_t)(k + 1) * width;
+      uint32_t pos = off[k * row + v];
+      while (j < e && xtedg[j] < hi) edg[pos++] = layout_id(hot_idx, hot_words, xtedg[j++]);
+    }
+  }
+}
+
+cudaError_t carry_layout(const ChunkLayout& l, const uint32_t* xtoff, const uint32_t* xtedg, uint32_t n,
+                         const uint32_t* touched, const uint32_t* trow, uint32_t T, const uint32_t* Tp,
+                         const uint32_t* hot_idx, uint32_t* new_off, uint32_t* new_edg, uint32_t* scan_ws, int sms,
+                         cudaStream_t s) {
+  const size_t row = (size_t)n + 1, len = (size_t)l.K * row;
+  const int grid = sms * 8;
+  k_layout_counts<<<grid, kThreads, 0, s>>>(l.off, xtoff, xtedg, touched, n, l.width, l.K, new_off);
+  cudaError_t e = exclusive_scan_u32_ws(new_off, (uint32_t)len, scan_ws, s);
+  if (e != cudaSuccess) return e;
+  for (int k = 0; k < l.K; ++k) {
+    const Runs r{l.off + k * row, new_off + k * row, trow, T, n, 0, Tp};
+    k_copy_runs<<<grid, kThreads, 0, s>>>(r, l.edg, new_edg);
+  }
+  if (T || Tp)
+    k_layout_touched<<<grid, kThreads, 0, s>>>(xtoff, xtedg, trow, T, Tp, n, l.width, l.K, new_off, new_edg,
+                                               l.hot ? hot_idx : nullptr, (n + 31) / 32);
+  return cudaGetLastError();
+}
+
 // Per row segment k, the slice [lo, hi) of the touched list holding its rows.
 __global__ void k_list_slices(const uint32_t* __restrict__ list, uint32_t T, uint32_t n, uint32_t shift,
                               uint32_t nseg, uint32_t* __restrict__ bounds) {
@@ -390,6 +465,13 @@ cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd64, ui
   const int grid = sms * 8;
   uint32_t *scratch = nullptr, *noff = nullptr, *ntoff = nullptr, *nedg = nullptr, *ntedg = nullptr, *ndat = nullptr;
   uint32_t *ranges = nullptr, *lists = nullptr;
+  const uint32_t* in_list = nullptr;  // the in-CSR's touched rows (plain graphs)
+  uint32_t in_T = 0;
+  struct NewLayout {
+    ChunkLayout* l;
+    uint32_t *off, *edg;
+  };
+  std::vector<NewLayout> layouts_new;
   unsigned long long *nbase = nullptr, *ntbase = nullptr;
   long long* segd = nullptr;
   int32_t *dout, *din;
@@ -469,11 +551,13 @@ cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd64, ui
     std::vector<uint32_t> hb(nseg + 1);
     for (int csr = 0; csr < 2; ++csr) {
       uint32_t T = 0;
+      if (csr == 1) in_list = trow;
       k_word_pop<<<grid, kThreads, 0, s>>>(tch[csr], words, cnt);
       PRX_CU(exclusive_scan_u32(cnt, words + 1, s));
       PRX_CU(cudaMemcpyAsync(&T, cnt + words, 4, cudaMemcpyDeviceToHost, s));
       k_touched_list<<<grid, kThreads, 0, s>>>(tch[csr], words, cnt, trow);
       PRX_CU(cudaStreamSynchronize(s));  // T
+      if (csr == 1) in_T = T;
       k_list_slices<<<(nseg + 256) / 256, 256, 0, s>>>(trow, T, n, S, nseg, bounds);
       PRX_CU(cudaMemcpyAsync(hb.data(), bounds, 4 * ((size_t)nseg + 1), cudaMemcpyDeviceToHost, s));
       PRX_CU(cudaMemsetAsync(ranges, 0, sizeof(uint32_t) * 4 * (size_t)n, s));
@@ -497,8 +581,36 @@ cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd64, ui
     }
   }
   k_out_degree<<<grid, kThreads, 0, s>>>(noff, S, n, ndat);
+  // the cached LOW layouts follow the new version (plain graphs; the hot
+  // numbering is kept with them)
+  if (!segmented) {
+    const uint64_t low_edges = g.cls_edges[LOW];
+    for (auto& l : g.lay) {
+      if (!l.width || !l.off || !l.seg_off.empty()) continue;
+      const size_t len = (size_t)l.K * ((size_t)n + 1);
+      uint32_t *lo = nullptr, *le = nullptr, *ws = nullptr;
+      cudaError_t el = graph_alloc(&lo, sizeof(uint32_t) * len, s);
+      if (el == cudaSuccess) el = graph_alloc(&le, sizeof(uint32_t) * edge_slots(low_edges + ni), s);
+      if (el == cudaSuccess) el = graph_alloc(&ws, sizeof(uint32_t) * scan_ws_words((uint32_t)len), s);
+      if (el == cudaSuccess)
+        el = carry_layout(l, ntoff, ntedg, n, tin, in_list, in_T, nullptr, g.hot_idx, lo, le, ws, sms, s);
+      if (ws) cudaFreeAsync(ws, s);
+      if (el != cudaSuccess) {
+        graph_free({lo, le});
+        err = el;
+        goto done;
+      }
+      layouts_new.push_back({&l, lo, le});
+    }
+  }
   PRX_CU(cudaGetLastError());
   PRX_CU(cudaStreamSynchronize(s));
+  for (auto& x : layouts_new) {
+    graph_free({x.l->off, x.l->edg});
+    x.l->off = x.off;
+    x.l->edg = x.edg;
+  }
+  layouts_new.clear();
   graph_free({g.xoff, g.xedg, g.xtoff, g.xtedg, g.xtdat, g.xbase, g.xtbase});
   g.xoff = noff; g.xedg = nedg; g.xtoff = ntoff; g.xtedg = ntedg; g.xtdat = ndat;
   g.xbase = nbase; g.xtbase = ntbase;
@@ -510,8 +622,9 @@ cudaError_t apply_batch_device(GraphDev& g, const uint32_t* b, uint64_t nd64, ui
   }
   g.m = m2;
   g.m_cap = m2;
-  PRX_CU(build_classes(g, sms, s));
+  PRX_CU(build_classes(g, sms, s, !segmented));
 done:
+  for (auto& x : layouts_new) graph_free({x.off, x.edg});
   if (scratch) cudaFreeAsync(scratch, s);
   if (ranges) cudaFreeAsync(ranges, s);
   if (lists) cudaFreeAsync(lists, s);

@@ -191,6 +191,15 @@ __device__ __forceinline__ bool fp32_round_done(float change, float prev, float 
   return change * rate < kPredictSafety * (float)tol;
 }
 
+// Edge id as stored in a layout: a hot source's number with the flag, else
+// the id itself (hot_idx null: plain ids; see GraphDev::hot_idx, of a graph
+// of `words` bitmap words).
+__device__ __forceinline__ uint32_t layout_id(const uint32_t* __restrict__ hot_idx, uint32_t words, uint32_t u) {
+  if (!hot_idx) return u;
+  const uint32_t w = __ldg(hot_idx + (u >> 5)), below = w & ((1u << (u & 31u)) - 1u);
+  return ((w >> (u & 31u)) & 1u) ? (kHotFlag | (__ldg(hot_idx + words + (u >> 5)) + __popc(below))) : u;
+}
+
 // The contribution of edge id u: with `hot` (a layout whose hot sources are
 // encoded, kHotFlag | number) from the dense hot copy ch, else c[u].
 template <class T>

@@ -303,14 +303,6 @@ __global__ void k_chunk_count(const uint32_t* __restrict__ xtoff, const uint32_t
   }
 }
 
-// Edge id as stored in a layout: a hot source's number with the flag, else
-// the id itself (hot_idx null: plain ids; see GraphDev::hot_idx, of a graph
-// of `words` bitmap words).
-__device__ __forceinline__ uint32_t layout_id(const uint32_t* __restrict__ hot_idx, uint32_t words, uint32_t u) {
-  if (!hot_idx) return u;
-  const uint32_t w = __ldg(hot_idx + (u >> 5)), below = w & ((1u << (u & 31u)) - 1u);
-  return ((w >> (u & 31u)) & 1u) ? (kHotFlag | (__ldg(hot_idx + words + (u >> 5)) + __popc(below))) : u;
-}
 
 __global__ void k_chunk_scatter(const uint32_t* __restrict__ xtoff, const uint32_t* __restrict__ xtedg,
                                 const uint32_t* __restrict__ low_bm, uint32_t n, uint32_t width, int K,
@@ -783,10 +775,12 @@ cudaError_t ensure_hot(GraphDev& g, uint32_t cap, int sms, cudaStream_t s) {
   return cudaSuccess;
 }
 
-cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s) {
+cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s, bool keep_layouts) {
   const uint32_t n = g.n;
-  free_chunks(g);
-  free_hot(g);
+  if (!keep_layouts) {
+    free_chunks(g);
+    free_hot(g);
+  }
   if (!g.low_bm) {
     cudaError_t e = graph_alloc(&g.low_bm, sizeof(uint32_t) * (((size_t)n + 31) / 32 + 1), s);
     if (e != cudaSuccess) return e;

@@ -290,7 +290,10 @@ void launch_flags_from_bitmap(const uint32_t* bm, uint8_t* out, uint32_t n, cuda
 void launch_state_reset(State* st, int max_iter, double tol, cudaStream_t s);
 
 // ---- graph construction (prx_graph.cu) ----------------------------------
-cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s);
+// Degree classes, LOW bitmap and reciprocals of g's current arrays; the
+// cached layouts and hot sources are dropped unless keep_layouts (a batch
+// apply that carried them to the new version).
+cudaError_t build_classes(GraphDev& g, int sms, cudaStream_t s, bool keep_layouts = false);
 // The LOW-class bitmap and the reciprocal out-degrees (FP64 and FP32) of a
 // graph version, by kernels alone (build_classes runs them too).
 void launch_vertex_tables(const uint32_t* xtoff, uint32_t shift, const uint32_t* xtdat, uint32_t n, uint32_t* low_bm,
@@ -336,6 +339,17 @@ struct ApplyWs {
 // must have been checked (launch_batch_check).
 cudaError_t apply_batch_graph(const CsrSet& src, const CsrSet& dst, uint32_t n, const uint32_t* b, uint32_t nd,
                               uint32_t ni, const ApplyWs& w, int sms, cudaStream_t s);
+// The cached LOW layout l of a plain graph's previous version carried to
+// its new version (in-CSR xtoff / xtedg): untouched rows' segments copied as
+// shifted runs, the touched rows (bitmap `touched`, ascending list trow of T
+// rows, or *Tp when Tp is not null) scattered again; new_off: K x (n + 1),
+// new_edg: room for the new LOW edges, scan_ws: scan_ws_words(K x (n + 1)).
+// Kernels only.
+cudaError_t carry_layout(const ChunkLayout& l, const uint32_t* xtoff, const uint32_t* xtedg, uint32_t n,
+                         const uint32_t* touched, const uint32_t* trow, uint32_t T, const uint32_t* Tp,
+                         const uint32_t* hot_idx, uint32_t* new_off, uint32_t* new_edg, uint32_t* scan_ws, int sms,
+                         cudaStream_t s);
+
 // Sets bits of *err when batch b ([du | dv | iu | iv]) is not a tidy batch
 // for the plain CSR xoff / xedg of n vertices: 8 an id >= n, 4 a list not
 // strictly ascending in (u, v), then (only if neither) 1 a deletion is

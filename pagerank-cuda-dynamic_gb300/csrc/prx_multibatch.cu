@@ -243,11 +243,14 @@ extern "C" int prx_solve_batches_device(prx_context* c, prx_graph* gr, int mode,
   const uint32_t width = opt.chunk_vertices ? opt.chunk_vertices : g.tuned_w64 ? g.tuned_w64 : kDefaultChunk64;
   const int KC = (int)std::max<uint64_t>(1, ((uint64_t)n + width - 1) / width);
   const bool use_lay = n > 0 && (KC > 1 || (hot && g.hot_n > 0)) && (uint64_t)KC * ((uint64_t)n + 1) < 0xffffffffull;
-  uint32_t *lay_off = nullptr, *lay_edg = nullptr, *lay_ws = nullptr;
+  // two layout buffers: step k >= 1 carries step k-1's layout to its version
+  uint32_t *lay_off[2] = {nullptr, nullptr}, *lay_edg[2] = {nullptr, nullptr}, *lay_ws = nullptr;
   if (use_lay) {
     const uint32_t len = (uint32_t)((uint64_t)KC * ((uint64_t)n + 1));
-    MB_TRY(alloc((void**)&lay_off, 4 * (size_t)len));
-    MB_TRY(alloc((void**)&lay_edg, 4 * edge_slots(cap)));
+    for (int i = 0; i < 2; ++i) {
+      MB_TRY(alloc((void**)&lay_off[i], 4 * (size_t)len));
+      MB_TRY(alloc((void**)&lay_edg[i], 4 * edge_slots(cap)));
+    }
     MB_TRY(alloc((void**)&lay_ws, 4 * (size_t)scan_ws_words(len)));
   }
   uint32_t* wsbuf = nullptr;
@@ -296,10 +299,20 @@ extern "C" int prx_solve_batches_device(prx_context* c, prx_graph* gr, int mode,
           lay.width = width;
           lay.K = KC;
           lay.hot = hot && g.hot_n > 0;
-          lay.off = lay_off;
-          lay.edg = lay_edg;
-          eb = build_layout_into(dst.xtoff, dst.xtedg, low[k & 1], n, width, KC, lay.hot ? g.hot_idx : nullptr,
-                                 (n + 31) / 32, lay_off, lay_edg, lay_ws, c->sms, sb);
+          lay.off = lay_off[k & 1];
+          lay.edg = lay_edg[k & 1];
+          if (k == 0) {
+            eb = build_layout_into(dst.xtoff, dst.xtedg, low[0], n, width, KC, lay.hot ? g.hot_idx : nullptr,
+                                   (n + 31) / 32, lay.off, lay.edg, lay_ws, c->sms, sb);
+          } else {  // the in-CSR's touched rows of this apply: its bitmap, list and count in ws
+            ChunkLayout prev = lay;
+            prev.off = lay_off[(k - 1) & 1];
+            prev.edg = lay_edg[(k - 1) & 1];
+            const uint32_t words32 = (n + 31) / 32;
+            eb = carry_layout(prev, dst.xtoff, dst.xtedg, n, ws.touched + words32, ws.trow, 0, ws.cnt + words32,
+                              g.hot_idx, lay.off, lay.edg, lay_ws, c->sms, sb);
+            prev.off = prev.edg = nullptr;  // owned by the buffers above
+          }
           if (eb != cudaSuccess) return eb;
         }
         GraphDev view;  // step k's graph version
