@@ -153,6 +153,7 @@ struct GraphDev {
   double* px = nullptr;           // P_uv = w_uv / W_u in out-CSR (xedg) order
   double* pt = nullptr;           // the same in in-CSR (xtedg) order
   double* wsum = nullptr;         // W_u = sum of u's out-edge weights
+  unsigned long long* wseg = nullptr;  // row segments: each out-CSR segment's compact start (weights, dL/dw)
   uint32_t* ocls_list = nullptr;  // ids by out-degree class (rows of the out-CSR)
   uint32_t ocls_begin[NCLS + 1] = {0, 0, 0, 0};
   uint64_t ocls_edges[NCLS] = {0, 0, 0};

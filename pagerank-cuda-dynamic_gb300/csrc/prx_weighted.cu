@@ -18,6 +18,11 @@
 //
 // Rows go by length class: <= 64 one thread per row, <= 4096 one warp, else
 // one block; every sum has a fixed order, so results are deterministic.
+//
+// Graphs with row segments (64-bit offsets, see GraphDev): px / pt are laid
+// out like the edge arrays they follow (the same segment bases), and the
+// weights and dL/dw stay in the compact out-CSR order a caller uses (edge j
+// of a segment at its compact start + j).
 #include <algorithm>
 #include "prx_ctx.h"
 #include "prx_device.cuh"
@@ -28,13 +33,17 @@ void drop_weights(GraphDev& g) {
   cudaFree(g.px);
   cudaFree(g.pt);
   cudaFree(g.wsum);
+  cudaFree(g.wseg);
   g.px = g.pt = g.wsum = nullptr;
+  g.wseg = nullptr;
 }
 
 struct PullArgs {
   const uint32_t* off;            // rows to pull over
   const uint32_t* edg;
-  const double* prob;             // P of each edge of the rows
+  const double* prob;             // P of each edge of the rows (laid out like edg)
+  const unsigned long long* seg;  // row segments: the bases of edg and prob (null: one segment)
+  uint32_t shift;
   const uint32_t* list;           // row ids by class
   uint32_t begin[NCLS + 1];
   const double* base;             // b_v, or base_const when null
@@ -72,17 +81,21 @@ __global__ void __launch_bounds__(256) k_pull_low(PullArgs a) {
   for (uint32_t i = a.begin[LOW] + blockIdx.x * blockDim.x + threadIdx.x; i < a.begin[MID];
        i += gridDim.x * blockDim.x) {
     const uint32_t v = a.list[i];
-    const uint32_t s = a.off[v], e = a.off[v + 1];
+    const uint64_t iv = seg_index(v, a.shift);
+    const uint32_t s = a.off[iv], e = a.off[iv + 1];
+    const uint64_t b = a.seg ? a.seg[(uint64_t)v >> a.shift] : 0;
+    const uint32_t* __restrict__ edg = a.edg + b;
+    const double* __restrict__ prob = a.prob + b;
     double acc = 0.0;
     uint32_t j = s;
     for (; j + 2 <= e; j += 2) {
-      const uint32_t u0 = __ldg(a.edg + j), u1 = __ldg(a.edg + j + 1);
-      const double p0 = __ldg(a.prob + j), p1 = __ldg(a.prob + j + 1);
+      const uint32_t u0 = __ldg(edg + j), u1 = __ldg(edg + j + 1);
+      const double p0 = __ldg(prob + j), p1 = __ldg(prob + j + 1);
       const double x0 = __ldg(x + u0), x1 = __ldg(x + u1);
       acc = fma(p0, x0, acc);
       acc = fma(p1, x1, acc);
     }
-    if (j < e) acc = fma(__ldg(a.prob + j), __ldg(x + __ldg(a.edg + j)), acc);
+    if (j < e) acc = fma(__ldg(prob + j), __ldg(x + __ldg(edg + j)), acc);
     const unsigned long long d = pull_finish(a, v, acc);
     emax = d > emax ? d : emax;
   }
@@ -97,9 +110,13 @@ __global__ void __launch_bounds__(256) k_pull_mid(PullArgs a) {
   for (uint32_t i = a.begin[MID] + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < a.begin[HIGH];
        i += (gridDim.x * blockDim.x) >> 5) {
     const uint32_t v = a.list[i];
-    const uint32_t s = a.off[v], e = a.off[v + 1];
+    const uint64_t iv = seg_index(v, a.shift);
+    const uint32_t s = a.off[iv], e = a.off[iv + 1];
+    const uint64_t b = a.seg ? a.seg[(uint64_t)v >> a.shift] : 0;
+    const uint32_t* __restrict__ edg = a.edg + b;
+    const double* __restrict__ prob = a.prob + b;
     double acc = 0.0;
-    for (uint32_t j = s + lane; j < e; j += 32) acc = fma(__ldg(a.prob + j), __ldg(x + __ldg(a.edg + j)), acc);
+    for (uint32_t j = s + lane; j < e; j += 32) acc = fma(__ldg(prob + j), __ldg(x + __ldg(edg + j)), acc);
 #pragma unroll
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) {
@@ -117,9 +134,13 @@ __global__ void __launch_bounds__(256) k_pull_high(PullArgs a) {
   unsigned long long emax = 0;
   for (uint32_t i = a.begin[HIGH] + blockIdx.x; i < a.begin[NCLS]; i += gridDim.x) {
     const uint32_t v = a.list[i];
-    const uint32_t s = a.off[v], e = a.off[v + 1];
+    const uint64_t iv = seg_index(v, a.shift);
+    const uint32_t s = a.off[iv], e = a.off[iv + 1];
+    const uint64_t b = a.seg ? a.seg[(uint64_t)v >> a.shift] : 0;
+    const uint32_t* __restrict__ edg = a.edg + b;
+    const double* __restrict__ prob = a.prob + b;
     double acc = 0.0;
-    for (uint32_t j = s + threadIdx.x; j < e; j += 256) acc = fma(__ldg(a.prob + j), __ldg(x + __ldg(a.edg + j)), acc);
+    for (uint32_t j = s + threadIdx.x; j < e; j += 256) acc = fma(__ldg(prob + j), __ldg(x + __ldg(edg + j)), acc);
 #pragma unroll
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane_id() == 0) part[threadIdx.x >> 5] = acc;
@@ -162,17 +183,26 @@ static void pull_sweep(const PullArgs& a, int sms, cudaStream_t s, uint64_t& lau
 // Warp per source u: W_u (lane-strided partial sums folded in lane order), px,
 // and each out-edge's probability scattered to its in-CSR slot (binary search
 // of u in v's ascending in-row).  err: 1 bad weight, 2 edge missing in xt.
-__global__ void __launch_bounds__(256) k_set_weights(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg,
-                                                     const uint32_t* __restrict__ xtoff,
-                                                     const uint32_t* __restrict__ xtedg, const float* __restrict__ w,
-                                                     uint32_t n, double* __restrict__ wsum, double* __restrict__ px,
+// (Graph addressing of both CSRs: see the file comment; wseg: each out-CSR
+// segment's compact start, null for one segment.)
+struct WeightCsr {
+  const uint32_t *xoff, *xedg, *xtoff, *xtedg;
+  const unsigned long long *xbase, *xtbase, *wseg;
+  uint32_t shift;
+};
+
+__global__ void __launch_bounds__(256) k_set_weights(WeightCsr c, const float* __restrict__ w, uint32_t n,
+                                                     double* __restrict__ wsum, double* __restrict__ px,
                                                      double* __restrict__ pt, uint32_t* err) {
   const uint32_t lane = lane_id();
   for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += (gridDim.x * blockDim.x) >> 5) {
-    const uint32_t s = xoff[u], e = xoff[u + 1];
+    const uint64_t iu = seg_index(u, c.shift);
+    const uint32_t s = c.xoff[iu], e = c.xoff[iu + 1];
+    const uint64_t bu = c.xbase ? c.xbase[(uint64_t)u >> c.shift] : 0;  // device position of the row's segment
+    const uint64_t wu = c.wseg ? c.wseg[(uint64_t)u >> c.shift] : 0;    // its compact position
     double acc = 0.0;
     for (uint32_t j = s + lane; j < e; j += 32) {
-      const float x = w[j];
+      const float x = w[wu + j];
       if (!(x > 0.f) || !(x < INFINITY)) atomicOr(err, 1u);
       acc += (double)x;
     }
@@ -180,16 +210,20 @@ __global__ void __launch_bounds__(256) k_set_weights(const uint32_t* __restrict_
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) wsum[u] = acc;
     for (uint32_t j = s + lane; j < e; j += 32) {
-      const double p = (double)w[j] / acc;
-      px[j] = p;
-      const uint32_t v = xedg[j];
-      uint32_t lo = xtoff[v], hi = xtoff[v + 1];
+      const double p = (double)w[wu + j] / acc;
+      px[bu + j] = p;
+      const uint32_t v = c.xedg[bu + j];
+      const uint64_t iv = seg_index(v, c.shift);
+      const uint64_t bv = c.xtbase ? c.xtbase[(uint64_t)v >> c.shift] : 0;
+      const uint32_t* row = c.xtedg + bv;
+      uint32_t lo = c.xtoff[iv], hi = c.xtoff[iv + 1];
+      const uint32_t end = hi;
       while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (xtedg[mid] < u) lo = mid + 1;
+        if (row[mid] < u) lo = mid + 1;
         else hi = mid;
       }
-      if (lo < xtoff[v + 1] && xtedg[lo] == u) pt[lo] = p;
+      if (lo < end && row[lo] == u) pt[bv + lo] = p;
       else atomicOr(err, 2u);
     }
   }
@@ -197,14 +231,18 @@ __global__ void __launch_bounds__(256) k_set_weights(const uint32_t* __restrict_
 
 // ---- gradients -------------------------------------------------------------------
 // dL/dw_uv = (r_u / W_u) (alpha lambda_v - lambda_u + g_u), warp per source u.
-__global__ void __launch_bounds__(256) k_grad_w(const uint32_t* __restrict__ xoff, const uint32_t* __restrict__ xedg,
-                                                const double* __restrict__ wsum, const double* __restrict__ r,
-                                                const double* __restrict__ lam, const double* __restrict__ g,
-                                                double alpha, uint32_t n, double* __restrict__ out) {
+__global__ void __launch_bounds__(256) k_grad_w(WeightCsr cs, const double* __restrict__ wsum,
+                                                const double* __restrict__ r, const double* __restrict__ lam,
+                                                const double* __restrict__ g, double alpha, uint32_t n,
+                                                double* __restrict__ out) {
   const uint32_t lane = lane_id();
   for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += (gridDim.x * blockDim.x) >> 5) {
     const double f = r[u] / wsum[u], c = g[u] - lam[u];
-    for (uint32_t j = xoff[u] + lane; j < xoff[u + 1]; j += 32) out[j] = f * fma(alpha, lam[xedg[j]], c);
+    const uint64_t iu = seg_index(u, cs.shift);
+    const uint64_t bu = cs.xbase ? cs.xbase[(uint64_t)u >> cs.shift] : 0;
+    const uint64_t wu = cs.wseg ? cs.wseg[(uint64_t)u >> cs.shift] : 0;
+    for (uint32_t j = cs.xoff[iu] + lane; j < cs.xoff[iu + 1]; j += 32)
+      out[wu + j] = f * fma(alpha, lam[cs.xedg[bu + j]], c);
   }
 }
 
@@ -253,11 +291,23 @@ static int wk_grow(prx_context* c, size_t doubles) {
   return PRX_OK;
 }
 
+static WeightCsr weight_csr(const GraphDev& g) {
+  return WeightCsr{g.xoff, g.xedg, g.xtoff, g.xtedg, g.xbase, g.xtbase, g.wseg, g.seg_shift};
+}
+
+// Device slots of one CSR's edge array (its segments' positions and counts).
+static uint64_t csr_slots(const GraphDev& g, const std::vector<uint64_t>& seg0, const std::vector<uint64_t>& pos) {
+  if (g.nseg <= 1) return g.m ? g.m : 1;
+  return pos.back() + (g.m - seg0.back()) + 4;
+}
+
 static PullArgs forward_args(const GraphDev& g, const double* t, double alpha) {
   PullArgs a{};
   a.off = g.xtoff;
   a.edg = g.xtedg;
   a.prob = g.pt;
+  a.seg = g.xtbase;
+  a.shift = g.seg_shift;
   a.list = g.cls_list;
   for (int k = 0; k <= NCLS; ++k) a.begin[k] = g.cls_begin[k];
   a.base = t;
@@ -323,22 +373,26 @@ int prx_graph_set_weights(prx_context* c, prx_graph* gr, const float* w) {
   if (!c || !gr || gr->ctx != c) FAIL(PRX_EINVAL, "prx_graph_set_weights: bad context or graph");
   GraphDev& g = gr->g;
   if (!g.xoff) FAIL(PRX_ESTATE, "prx_graph_set_weights: graph has no out-CSR");
-  if (g.nseg > 1) FAIL(PRX_ERANGE, "prx_graph_set_weights: not for graphs with row segments (64-bit offsets)");
   if (!w && g.m) FAIL(PRX_EINVAL, "prx_graph_set_weights: weights are NULL");
   TRY_CUDA_ST(cudaSetDevice(c->device));
   cudaStream_t s = c->stream;
   drop_weights(g);
-  const size_t m = g.m ? g.m : 1;
-  TRY_CUDA_ST(cudaMalloc(&g.px, sizeof(double) * m));
-  TRY_CUDA_ST(cudaMalloc(&g.pt, sizeof(double) * m));
+  TRY_CUDA_ST(cudaMalloc(&g.px, sizeof(double) * csr_slots(g, g.xseg0, g.xpos)));
+  TRY_CUDA_ST(cudaMalloc(&g.pt, sizeof(double) * csr_slots(g, g.xtseg0, g.xtpos)));
   TRY_CUDA_ST(cudaMalloc(&g.wsum, sizeof(double) * (g.n ? g.n : 1)));
+  if (g.nseg > 1) {  // each out-CSR segment's compact start
+    TRY_CUDA_ST(cudaMalloc(&g.wseg, sizeof(unsigned long long) * g.nseg));
+    TRY_CUDA_ST(cudaMemcpyAsync(g.wseg, g.xseg0.data(), sizeof(unsigned long long) * g.nseg,
+                                cudaMemcpyHostToDevice, s));
+  }
   if (!g.ocls_list) TRY_CUDA_ST(cudaMalloc(&g.ocls_list, sizeof(uint32_t) * (g.n ? g.n : 1)));
   launch_state_reset(c->st, 0, 0.0, s);
   if (g.n)
-    k_set_weights<<<pull_grid((uint64_t)g.n * 32, 256, c->sms * 16), 256, 0, s>>>(
-        g.xoff, g.xedg, g.xtoff, g.xtedg, w, g.n, g.wsum, g.px, g.pt, &c->st->err);
+    k_set_weights<<<pull_grid((uint64_t)g.n * 32, 256, c->sms * 16), 256, 0, s>>>(weight_csr(g), w, g.n, g.wsum,
+                                                                                  g.px, g.pt, &c->st->err);
   TRY_CUDA_ST(cudaGetLastError());
-  const cudaError_t e = build_class_lists(g.xoff, 32, g.n, g.mid_max, g.ocls_list, g.ocls_begin, g.ocls_edges, c->sms, s);
+  const cudaError_t e = build_class_lists(g.xoff, g.seg_shift, g.n, g.mid_max, g.ocls_list, g.ocls_begin,
+                                         g.ocls_edges, c->sms, s);
   TRY_CUDA_ST(e);
   TRY_CUDA_ST(cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s));
   TRY_CUDA_ST(cudaStreamSynchronize(s));
@@ -421,6 +475,8 @@ int prx_adjoint(prx_context* c, prx_graph* gr, const double* t, const double* r,
   a.off = g.xoff;
   a.edg = g.xedg;
   a.prob = g.px;
+  a.seg = g.xbase;
+  a.shift = g.seg_shift;
   a.list = g.ocls_list;
   for (int k = 0; k <= NCLS; ++k) a.begin[k] = g.ocls_begin[k];
   a.base = gl;
@@ -440,7 +496,7 @@ int prx_adjoint(prx_context* c, prx_graph* gr, const double* t, const double* r,
   if (lambda) TRY_CUDA_ST(cudaMemcpyAsync(lambda, lam, sizeof(double) * g.n, cudaMemcpyDeviceToDevice, s));
   const int grid = pull_grid((uint64_t)g.n * 32, 256, c->sms * 16);
   if (grad_w) {
-    k_grad_w<<<grid, 256, 0, s>>>(g.xoff, g.xedg, g.wsum, r, lam, gl, alpha, g.n, grad_w);
+    k_grad_w<<<grid, 256, 0, s>>>(weight_csr(g), g.wsum, r, lam, gl, alpha, g.n, grad_w);
     c->launches += 1;
   }
   if (grad_t) {

@@ -103,15 +103,46 @@ def test_segmented_rows_limits(pg, ctx):
     assert res["iterations"] == it and np.array_equal(r, want)
     auto.apply_batch(*pg.graphs.random_batch(xoff, xedg, 5, 5, seed=1))   # plain: batches work
     auto.close()
-    seg = graph64(pg, ctx, xoff, xedg, xt, 5)
-    import torch
-    from pagerank_gb300 import autograd as A
-    with pytest.raises(pg.PrxError) as err:   # edge weights: plain CSR only
-        A.set_weights(ctx, seg, torch.ones(len(xedg), dtype=torch.float32))
-    assert err.value.status == 5   # PRX_ERANGE
-    seg.close()
     with pytest.raises(pg.PrxError):
         graph64(pg, ctx, xoff, xedg, xt, 33)
+
+
+@pytest.mark.parametrize("shift", [3, 7, 12])
+def test_segmented_weights_and_adjoint_bit_exact(pg, ctx, shift):
+    """Edge weights, the weighted solve and the adjoint (dL/dw in the caller's
+    compact out-CSR order, dL/dt, dL/dalpha) on a graph of row segments give
+    the plain CSR's bits, also after a device-applied batch."""
+    import torch
+    from pagerank_gb300 import autograd as A
+    xoff, xedg = pg.graphs.rmat(12, 16, a=0.6, b=0.15, c=0.15, seed=8)
+    xt = O.transpose(xoff, xedg)
+    plain = pg.Graph(ctx, *xt, xoff, xedg)
+    seg = graph64(pg, ctx, xoff, xedg, xt, shift)
+    rng = np.random.default_rng(shift)
+    n = len(xoff) - 1
+    gl = torch.from_numpy(rng.standard_normal(n)).cuda()
+    t = torch.from_numpy(rng.uniform(0.5, 1.5, n) / n).cuda()
+    o = pg.options(tolerance=1e-12)
+    for step in range(2):
+        m = plain.size()[1]
+        w = torch.from_numpy(rng.uniform(0.5, 2.0, m).astype(np.float32)).cuda()
+        outs = []
+        for g in (plain, seg):
+            A.set_weights(ctx, g, w)
+            r, rr = A.solve_weighted(ctx, g, t, opts=o)
+            adj = A.adjoint(ctx, g, r, gl, t, opts=o)
+            outs.append((r.cpu().numpy(), rr["iterations"], adj["grad_w"].cpu().numpy(),
+                         adj["grad_t"].cpu().numpy(), adj["grad_alpha"]))
+        a, b = outs
+        assert a[1] == b[1]
+        for x, y in zip(a, b):
+            assert np.array_equal(np.asarray(x), np.asarray(y)), (shift, step)
+        if step == 0:
+            batch = plain.gen_batch(40, 160, seed=5)
+            plain.apply_batch(*batch)
+            seg.apply_batch(*batch)
+    plain.close()
+    seg.close()
 
 
 def _same_graph(plain, seg):
