@@ -152,7 +152,7 @@ int ensure_ws(prx_context* c, uint32_t n, bool dyn) {
     TRY_CUDA_ST(cudaMalloc(&c->xb, sizeof(uint32_t) * cap));
     TRY_CUDA_ST(cudaMalloc(&c->naff, sizeof(uint32_t) * words));
     TRY_CUDA_ST(cudaMalloc(&c->ever, sizeof(uint32_t) * words));
-    TRY_CUDA_ST(cudaMalloc(&c->pf, sizeof(double) * cap));
+    TRY_CUDA_ST(cudaMalloc(&c->pf, sizeof(double) * ((size_t)cap + kPfTable)));  // + the per-degree table
     TRY_CUDA_ST(cudaMalloc(&c->xl, sizeof(uint32_t) * cap));
     for (auto& f : c->fr) TRY_CUDA_ST(cudaMalloc(&f, sizeof(uint32_t) * cap));
     for (int k = MID; k < NCLS; ++k) TRY_CUDA_ST(cudaMalloc(&c->lists[0][k], sizeof(uint32_t) * cap));
@@ -222,6 +222,7 @@ SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options& o) {
   a.rcp = g.rcp;
   a.ever = c->ever;
   a.pf = c->pf;
+  a.pf_tab = c->pf ? c->pf + c->ws_n : nullptr;
   a.acc64 = c->acc64;
   a.acc32 = c->acc32;
   // expand by pulling once more than 1/16 of the vertices changed by > D

@@ -173,6 +173,7 @@ cudaError_t build_default_layout_pipelined(GraphDev& g, uint32_t width, bool hot
                                            const uint32_t* piece_rows, const cudaEvent_t* piece_ready, int sms,
                                            cudaStream_t s);
 
+constexpr uint32_t kPfTable = 1u << 16;  // out-degrees whose DF-P factor is tabulated
 constexpr uint32_t kHotFlag = 0x80000000u;
 // The hot sources of g for a cap of `cap` vertices (0: none); graphs of 2^31
 // vertices or more get none (their ids use the flag bit).
@@ -218,6 +219,7 @@ struct SolveArgs {
   const double* rcp;              // RN(1 / outdeg)
   uint32_t* ever;                 // FP32 dynamic phase: vertices updated at least once
   double* pf;                     // DF-P: 1 / (1 - P/d) per vertex (launch_prune_factor)
+  double* pf_tab;                 // the same per out-degree d < kPfTable, formed once per solve
   double* acc64;                  // partial row sums carried between chunk passes (FP64)
   float* acc32;                   // the same for the FP32 sweeps
   State* st;

@@ -519,12 +519,24 @@ __global__ void k_init_ranks32(SolveArgs a, const double* __restrict__ q) {
 
 // The DF-P factor with the same operations as the reference's
 // (1 / (1 - P/d)) inline in the update (:104), so its bits are the same.
+// DF-P's factor depends on the out-degree alone: it is formed once per degree
+// below kPfTable (with RN(1/d) divided as rcp is, so the same bits), and the
+// vertices look it up; only larger degrees divide (an FP64 division is many
+// FP64 instructions on this part).
+__global__ void k_prune_table(SolveArgs a) {
+  for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < kPfTable; d += gridDim.x * blockDim.x)
+    a.pf_tab[d] = 1 / (1 - div_count(a.P, d, 1.0 / (double)d));
+}
+
 __global__ void k_prune_factor(SolveArgs a) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x)
-    a.pf[v] = 1 / (1 - div_count(a.P, a.xtdat[v], a.rcp[v]));
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
+    const uint32_t d = a.xtdat[v];
+    a.pf[v] = d < kPfTable ? a.pf_tab[d] : 1 / (1 - div_count(a.P, d, a.rcp[v]));
+  }
 }
 
 void launch_prune_factor(const SolveArgs& a, cudaStream_t s) {
+  k_prune_table<<<kPfTable / kThreads, kThreads, 0, s>>>(a);
   k_prune_factor<<<cap_grid((a.n + kThreads - 1) / kThreads, 152 * 16), kThreads, 0, s>>>(a);
 }
 
