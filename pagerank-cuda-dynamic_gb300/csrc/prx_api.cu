@@ -418,10 +418,87 @@ static int run_graph_loop(prx_context* c, const prx_graph* gr, const SolveArgs& 
 // FP32 refinement loop (prx_refine.cu).  *final_parity: 1 when the last FP64
 // sweep converged (its output in r[1]), 0 when the cap stopped an FP32 round
 // (the committed ranks in r[0]).
+// The same loop as one CUDA graph launch: [round 0: k_refine_round0, an FP32
+// round, commit] then WHILE (not done, under the cap) { FP64 residual sweep,
+// k_refine_finalize64, WHILE (round not ended) { FP32 sweep, k_finalize32 },
+// commit (nothing once done) }.  The answer: the last FP64 sweep's output when
+// one of them ended the solve, else the committed ranks.
+static int run_refine_graph(prx_context* c, const prx_graph* gr, const SolveArgs& a, int max_iter,
+                            const ChunkLayout* lay64, const ChunkLayout* lay32, int* final_parity, bool round0) {
+  cudaStream_t s = c->stream, s2 = nullptr, s3 = nullptr;
+  const GraphDev& g = gr->g;
+  const int cap = (max_iter < (1 << 30) ? max_iter : (1 << 30)) + 2;
+  uint64_t l32 = 0, l64 = 0, lfix = 0;  // launches per FP32 body, per FP64 body, outside the loops
+  auto fp32_body = [&](cudaStream_t sw, cudaGraphConditionalHandle h) -> cudaError_t {
+    const uint64_t l0 = c->launches;
+    for (int cls = 0; cls < NCLS; ++cls) c->launches += launch_sweep32(a, g, cls, lay32, c->sms, sw);
+    launch_finalize32(a, sw);
+    launch_refine_cond(h, a, true, cap, sw);
+    l32 = c->launches - l0 + 2;
+    return cudaGetLastError();
+  };
+  auto round_end = [&](cudaStream_t sw) {
+    launch_refine_commit(a, c->sms, sw);
+    launch_hot_copy(a, 0, c->sms, sw);
+  };
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s3, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t ec = cudaSuccess;
+    if (round0) {
+      launch_refine_round0(a, c->sms, s);
+      ec = capture_conditional(s, s2, cudaGraphCondTypeWhile, 0,
+                               [&](cudaGraphConditionalHandle h) { launch_refine_arm(h, a, true, s); }, fp32_body);
+      if (ec == cudaSuccess) round_end(s);
+    }
+    if (ec == cudaSuccess)
+      ec = capture_conditional(
+          s, s2, cudaGraphCondTypeWhile, 0, [&](cudaGraphConditionalHandle h) { launch_refine_arm(h, a, false, s); },
+          [&](cudaStream_t sb, cudaGraphConditionalHandle ho) -> cudaError_t {
+            const uint64_t l0 = c->launches;
+            for (int cls = 0; cls < NCLS; ++cls) c->launches += launch_refine_sweep64(a, g, cls, lay64, c->sms, sb);
+            launch_refine_finalize64(a, sb);
+            l64 = c->launches - l0 + 1;
+            cudaError_t eb = capture_conditional(
+                sb, s3, cudaGraphCondTypeWhile, 0,
+                [&](cudaGraphConditionalHandle h) { launch_refine_arm(h, a, true, sb); }, fp32_body);
+            if (eb != cudaSuccess) return eb;
+            round_end(sb);
+            launch_refine_cond(ho, a, false, cap, sb);
+            return cudaGetLastError();
+          });
+    const cudaError_t el = cudaGetLastError();
+    e = cudaStreamEndCapture(s, &graph);  // always leave capture mode
+    if (e == cudaSuccess) e = ec;
+    if (e == cudaSuccess) e = el;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&c->st_host[1], c->st, sizeof(State), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (s2) cudaStreamDestroy(s2);
+  if (s3) cudaStreamDestroy(s3);
+  TRY_CUDA_ST(e);
+  const State& h = c->st_host[1];
+  lfix = round0 ? 3 : 0;  // round 0, commit, hot copy
+  c->launches += lfix + (uint64_t)h.rounds * (l64 + 2) + (uint64_t)(h.iter - h.rounds) * l32;
+  // the FP64 sweep's output is the answer only when one of the outer loop's
+  // sweeps ended the solve (done may also be set on entry, by the cap)
+  *final_parity = (h.graph_rounds > 0 && h.done) ? 1 : 0;
+  return PRX_OK;
+}
+
 static int run_refine_loop(prx_context* c, const prx_graph* gr, const SolveArgs& a, bool timing, int max_iter,
-                           const ChunkLayout* lay64, const ChunkLayout* lay32, int* final_parity, bool round0) {
+                           const ChunkLayout* lay64, const ChunkLayout* lay32, int* final_parity, bool round0,
+                           bool graph) {
   cudaStream_t s = c->stream;
   int st;
+  if (graph && !timing && max_iter > 0) return run_refine_graph(c, gr, a, max_iter, lay64, lay32, final_parity, round0);
   // one round of FP32 correction sweeps until they stop, then x_b += e
   auto fp32_round = [&]() -> int {
     for (int k = 1;; k = std::min(2 * k, 16)) {
@@ -597,12 +674,16 @@ static int solve_core(prx_context* c, prx_graph* gr, int mode, const uint32_t* d
       if ((st = iterate(mode | MODE_F32, lay32))) return st;
       launch_commit_dyn32(a, c->st_host[1].iter & 1, s);
       c->launches += 1 + launch_hot_copy(a, 0, c->sms, s);
-      if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity, false))) return st;
+      if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity, false,
+                                o.loop != PRX_LOOP_HOST)))
+        return st;
     } else if (refine) {
       // Static / ND, or a dynamic mode whose marking covers most of the
       // graph: FP32 sweeps over all vertices from the initial ranks (q for
       // the dynamic modes), then the FP64 refinement
-      if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity, true))) return st;
+      if ((st = run_refine_loop(c, gr, a, timing, o.max_iterations, lay64, lay32, &final_parity, true,
+                                o.loop != PRX_LOOP_HOST)))
+        return st;
     } else if ((st = iterate(dt_all ? PRX_NAIVE_DYNAMIC : mode, lay64))) {
       return st;
     }

@@ -79,6 +79,44 @@ int enqueue_iteration(prx_context* c, const GraphDev& g, const SolveArgs& a, int
 // than cap bodies ran (counted in st->graph_rounds).
 __global__ void k_loop_cond(cudaGraphConditionalHandle h, State* st, int cap);
 
+namespace prx {
+// Inside a capture on s: a conditional node of `type` whose handle (default
+// dflt) is set by `arm` launched on s just before the node, and whose body is
+// captured on s2 by body(s2).  Leaves s depending on the node.
+template <class Arm, class Body>
+inline cudaError_t capture_conditional(cudaStream_t s, cudaStream_t s2, cudaGraphConditionalNodeType type,
+                                       unsigned dflt, Arm arm, Body body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr);
+  cudaGraphConditionalHandle h{};
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, dflt, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return e;
+  arm(h);
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* edata = nullptr;
+  size_t ndeps = 0;
+  e = cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, &edata, &ndeps);
+  cudaGraphNodeParams p{};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = type;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, deps, edata, ndeps, &p);
+  if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  if (e == cudaSuccess)
+    e = cudaStreamBeginCaptureToGraph(s2, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  const cudaError_t eb = body(s2, h);
+  cudaGraph_t captured = nullptr;
+  e = cudaStreamEndCapture(s2, &captured);  // always leave capture mode
+  return eb != cudaSuccess ? eb : e;
+}
+
+}  // namespace prx
+
 #define TRY_CUDA_ST(x)                                                                   \
   do {                                                                                   \
     cudaError_t e_ = (x);                                                                \

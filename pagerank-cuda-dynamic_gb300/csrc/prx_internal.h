@@ -259,6 +259,11 @@ constexpr uint32_t kDefaultChunk64 = (200u << 20) / sizeof(double);
 bool launch_refine_sweep64(const SolveArgs& a, const GraphDev& g, int cls, const ChunkLayout* lay, int sms,
                            cudaStream_t s);
 void launch_refine_finalize64(const SolveArgs& a, cudaStream_t s);
+// The refinement loop's conditional nodes: arm before a node, cond at the end
+// of its body (inner: the FP32 round, outer: the FP64 residual sweeps, at
+// most cap bodies).
+void launch_refine_arm(cudaGraphConditionalHandle h, const SolveArgs& a, bool inner, cudaStream_t s);
+void launch_refine_cond(cudaGraphConditionalHandle h, const SolveArgs& a, bool inner, int cap, cudaStream_t s);
 // One FP32 correction sweep of one class, and its finalize.
 bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, const ChunkLayout* lay, int sms, cudaStream_t s);
 void launch_finalize32(const SolveArgs& a, cudaStream_t s);

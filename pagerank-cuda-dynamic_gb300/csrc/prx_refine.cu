@@ -181,8 +181,10 @@ __global__ void k_refine_round0(SolveArgs a) {
   }
 }
 
-// x_b += e (FP64), c_b = x_b / outdeg.
+// x_b += e (FP64), c_b = x_b / outdeg.  Nothing once the solve is done (the
+// graph-launched loop reaches it after the FP64 sweep that converged).
 __global__ void k_refine_commit(SolveArgs a) {
+  if (a.st->done) return;
   const float* __restrict__ e = a.e[a.st->k32 & 1];
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < a.n; v += gridDim.x * blockDim.x) {
     const double x = a.r[0][v] + (double)e[v];
@@ -228,6 +230,31 @@ bool launch_sweep32(const SolveArgs& a, const GraphDev& g, int cls, const ChunkL
 }
 
 void launch_refine_finalize64(const SolveArgs& a, cudaStream_t s) { k_refine_finalize64<<<1, 1, 0, s>>>(a.st); }
+
+// Conditions of the refinement loop as one graph: the outer WHILE node runs
+// FP64 residual sweeps while the solve is not done and under the cap (its
+// bodies counted in graph_rounds, at most cap of them), the inner one the
+// FP32 sweeps of a round until k_finalize32 ends the round.
+__global__ void k_refine_arm(cudaGraphConditionalHandle h, State* st) {
+  st->graph_rounds = 0;  // the dynamic modes' FP32 phase may have counted its own loop's bodies
+  cudaGraphSetConditional(h, (!st->done && st->iter < st->max_iter) ? 1u : 0u);
+}
+__global__ void k_refine_arm_inner(cudaGraphConditionalHandle h, const State* st) {
+  cudaGraphSetConditional(h, (!st->done && !st->inner_done) ? 1u : 0u);
+}
+__global__ void k_refine_cond(cudaGraphConditionalHandle h, State* st, int cap) {
+  const int rounds = ++st->graph_rounds;
+  cudaGraphSetConditional(h, (!st->done && st->iter < st->max_iter && rounds < cap) ? 1u : 0u);
+}
+
+void launch_refine_arm(cudaGraphConditionalHandle h, const SolveArgs& a, bool inner, cudaStream_t s) {
+  if (inner) k_refine_arm_inner<<<1, 1, 0, s>>>(h, a.st);
+  else k_refine_arm<<<1, 1, 0, s>>>(h, a.st);
+}
+void launch_refine_cond(cudaGraphConditionalHandle h, const SolveArgs& a, bool inner, int cap, cudaStream_t s) {
+  if (inner) k_refine_arm_inner<<<1, 1, 0, s>>>(h, a.st);
+  else k_refine_cond<<<1, 1, 0, s>>>(h, a.st, cap);
+}
 
 void launch_finalize32(const SolveArgs& a, cudaStream_t s) { k_finalize32<<<1, 1, 0, s>>>(a.st); }
 

@@ -146,3 +146,39 @@ def test_refine_dynamic_caps_and_empty_batch(pg, ctx):
         assert np.abs(got - want).max() <= np.abs(want - conv).max() + bound(want)
     finally:
         g.close()
+
+
+@pytest.mark.parametrize("kind", ["web200k", "hubs"])
+def test_refine_graph_and_host_loops_agree(pg, ctx, kind):
+    # The refinement's rounds run as one CUDA graph launch (outer WHILE node of
+    # FP64 residual sweeps, inner WHILE node of FP32 sweeps) or from the host:
+    # the same sweeps in the same order, so the same bits, iterations and
+    # refinement rounds, also when the iteration cap ends an FP32 round
+    from test_gpu_parity import _synthetic
+    xoff, xedg = _synthetic(pg, kind)
+    m = len(xedg)
+    batch = pg.graphs.random_batch(xoff, xedg, max(1, int(2e-4 * m)), max(1, int(8e-4 * m)), seed=37)
+    du, dv, iu, iv = batch
+    q, _ = pg.pagerank_static(ctx, pg.Graph.from_out_csr(ctx, xoff, xedg))
+    yoff, yedg = pg.graphs.apply_batch(xoff, xedg, *batch)
+    yt = O.transpose(yoff, yedg)
+    g = pg.Graph(ctx, *yt, yoff, yedg)
+    try:
+        cases = [(pg.STATIC, None, 0), (pg.NAIVE_DYNAMIC, None, 0)]
+        cases += [(mode, batch, sweeps) for mode in (pg.DYNAMIC_FRONTIER, pg.PRUNE_DYNAMIC_FRONTIER)
+                  for sweeps in (1, 2)]
+        for mode, b, sweeps in cases:
+            for cap in (500, 3, 6, 9):
+                out = []
+                for loop in (pg.LOOP_GRAPH, pg.LOOP_HOST):
+                    o = pg.options(precision=pg.FP32_REFINE, loop=loop, refine_sweeps=sweeps, max_iterations=cap)
+                    if b is None:
+                        out.append(pg.solve(ctx, g, mode, q=q if mode != pg.STATIC else None, opts=o))
+                    else:
+                        out.append(pg.solve(ctx, g, mode, (du, dv), (iu, iv), q, o))
+                (a, ra), (h, rh) = out
+                assert np.array_equal(a, h), (kind, mode, sweeps, cap)
+                assert ra["iterations"] == rh["iterations"] and ra["refinements"] == rh["refinements"]
+                assert ra["last_delta"] == rh["last_delta"]
+    finally:
+        g.close()
