@@ -42,6 +42,7 @@ void prx_options_default(prx_options* o) {
   o->l2_fetch_bytes = 0;
   o->require_convergence = 0;
   o->hot_sources = 0;
+  o->int_adds = 0;
 }
 
 const char* prx_status_string(int s) {
@@ -227,6 +228,9 @@ SolveArgs make_args(prx_context* c, const GraphDev& g, const prx_options& o) {
   a.acc32 = c->acc32;
   // expand by pulling once more than 1/16 of the vertices changed by > D
   a.pull_threshold = o.expansion == 1 ? 0xffffffffu : (o.expansion == 2 ? 0u : g.n / 16);
+  // int_adds: the option, else the autotuner's pick, else the library default
+  const int ia = o.int_adds ? o.int_adds : (g.tuned_int_adds ? g.tuned_int_adds : (int)kDefaultIntAdds);
+  a.int_adds = ia > 0 ? (uint32_t)ia : 0u;
   a.st = c->st;
   a.n = g.n;
   a.mid_max = g.mid_max;
@@ -1161,6 +1165,7 @@ static int solve_common(prx_context* c, prx_graph* gr, int mode, const uint32_t*
   if (opt.l2_fetch_bytes < -1 || opt.l2_fetch_bytes > 128)
     FAIL(PRX_EINVAL, "prx_solve: l2_fetch_bytes must be in -1 .. 128");
   if (opt.hot_sources < -1) FAIL(PRX_EINVAL, "prx_solve: hot_sources must be -1, 0 or a vertex count");
+  if (opt.int_adds < -1 || opt.int_adds > 2) FAIL(PRX_EINVAL, "prx_solve: int_adds must be -1, 0, 1 or 2");
   if (!ranks_out && gr->g.n) FAIL(PRX_EINVAL, "prx_solve: ranks_out is NULL");
   prx_result own;
   if (!res) res = &own;  // the convergence check reads it

@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "prx_internal.h"
+#include "prx_softadd.h"
 
 namespace prx {
 
@@ -245,6 +246,20 @@ __device__ __forceinline__ T lane_row_sum(const T* __restrict__ c, const uint32_
   return acc;
 }
 
+// acc + x for the whole warp (all lanes converged): with `alt`, and when
+// every lane's operands are in add_nonneg_bits's range (sign clear, below
+// 2^977: a warp-uniform test), on the integer pipes; otherwise a DADD.  The
+// bits are the same either way.
+__device__ __forceinline__ double add_alt(double acc, double x, bool alt) {
+  if (alt) {
+    const uint32_t ha = (uint32_t)__double2hiint(acc), hx = (uint32_t)__double2hiint(x);
+    if (__all_sync(0xffffffffu, (ha > hx ? ha : hx) < kSoftAddHiLimit))
+      return __longlong_as_double((long long)add_nonneg_bits((uint64_t)__double_as_longlong(acc),
+                                                             (uint64_t)__double_as_longlong(x)));
+  }
+  return acc + x;
+}
+
 // FP64 row sums, one row per lane, for a whole warp: every lane calls it
 // (lanes with nothing to add pass s == e).  Each lane adds c[edg[j]] for j in
 // [s, e) onto acc front to back, as lane_row_sum does, but the warp issues
@@ -253,10 +268,12 @@ __device__ __forceinline__ T lane_row_sum(const T* __restrict__ c, const uint32_
 // instructions cost the warp as much as live ones.  Step k reads ids
 // s+4k .. s+4k+3 out of the two aligned 16-byte groups they span (the lane's
 // offset s & 3 picks them); a lane past its row's end adds +0.0, which leaves
-// acc (a sum of non-negative terms from +0) unchanged.
+// acc (a sum of non-negative terms from +0) unchanged.  int_adds (0, 1 or 2)
+// of every four adds of a full step run on the integer pipes (add_alt), so
+// the FP64 pipe, the sweep's bound, carries fewer of them.
 __device__ __forceinline__ double warp_row_sums(const double* __restrict__ c, const uint32_t* __restrict__ edg,
                                                 uint32_t s, uint32_t e, double acc,
-                                                const double* __restrict__ ch, bool hot) {
+                                                const double* __restrict__ ch, bool hot, uint32_t int_adds) {
   const uint32_t len = e - s;
   const uint32_t L = __reduce_max_sync(0xffffffffu, len);
   if (L == 0) return acc;
@@ -276,7 +293,10 @@ __device__ __forceinline__ double warp_row_sums(const double* __restrict__ c, co
     double x2 = t + 2 < len ? gather(c, ch, hot, u2) : 0.0;
     const double x3 = t + 3 < len ? gather(c, ch, hot, u3) : 0.0;
     if (t + 4 <= L) {
-      acc += x0; acc += x1; acc += x2; acc += x3;
+      acc += x0;
+      acc = add_alt(acc, x1, int_adds >= 2);
+      acc += x2;
+      acc = add_alt(acc, x3, int_adds >= 1);
     } else {  // the last 1..3 adds; the trip count is the same in every lane
       for (uint32_t r = L - t; r; --r) {
         acc += x0;

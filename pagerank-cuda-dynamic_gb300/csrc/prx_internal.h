@@ -126,6 +126,8 @@ struct GraphDev {
   uint32_t tuned_w64 = 0;         // source-chunk widths picked by prx_autotune (0: library default)
   uint32_t tuned_w32 = 0;
   int tuned_fetch = 0;            // L2 fetch granularity picked by prx_autotune (0: none)
+  int tuned_int_adds = 0;         // integer-pipe adds of the FP64 sweep picked by prx_autotune (-1 none,
+                                  // 1, 2; 0: not tuned)
   uint32_t* low_bm = nullptr;     // bitmap of the LOW class
   double* rcp = nullptr;          // RN(1 / outdeg) per vertex, for div_count
   float* rcp32 = nullptr;         // the same in FP32 (personalized PageRank sweeps)
@@ -226,6 +228,7 @@ struct SolveArgs {
   uint32_t n;
   uint32_t mid_max;
   uint32_t pull_threshold;        // expand by pulling when more than this many vertices changed by > D
+  uint32_t int_adds;              // FP64 LOW sweeps: adds of every four run on the integer pipes (0..2)
   double C0, P, D, C;
 };
 
@@ -248,6 +251,9 @@ void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s);
 // ch[p] <- the hot sources' c[p] (parity < 0: the parity the running
 // iteration wrote); false when the solve uses no hot copy.
 bool launch_hot_copy(const SolveArgs& a, int parity, int sms, cudaStream_t s);
+// Adds of every four in a full step of the FP64 LOW sweep that run on the
+// integer pipes when prx_options.int_adds is 0.
+constexpr uint32_t kDefaultIntAdds = 0;
 // Hot-source cap when prx_options.hot_sources is 0: 32 MB of FP64 values.
 constexpr uint32_t kDefaultHotCap = 4u << 20;
 // Source-chunk width of the FP64 sweeps when prx_options.chunk_vertices is 0

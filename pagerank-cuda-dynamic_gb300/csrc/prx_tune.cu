@@ -3,7 +3,10 @@
 // in the reference's 256-way order), the source-chunk widths of the FP64
 // and FP32 sweeps of the in-degree <= 64 rows, and the L2 fetch granularity
 // (how much of a line a missed gather brings in: more helps when nearby
-// contributions are read soon after, less when gathers are scattered).  No counterpart in the
+// contributions are read soon after, less when gathers are scattered), and
+// how many of every four edge additions of the FP64 sweep run on the integer
+// pipes (the FP64 pipe is the sweep's bound; the integer adder costs more
+// instructions, so the balance depends on the graph).  No counterpart in the
 // reference, which uses fixed thresholds (inc/pagerankCuda.hxx:625-638).
 //
 // Each candidate is timed by short solves on the graph itself (Static, 3
@@ -25,6 +28,7 @@ struct Pick {
   uint32_t mid_max, w64, w32;
   float ms64, ms32;
   int fetch;
+  int int_adds;  // -1 none, 1 or 2 (0: not tuned, e.g. a cache line without it)
 };
 
 std::mutex g_tune_mu;
@@ -44,7 +48,8 @@ void load_file(const char* path) {
   char line[320], key[160];
   while (fgets(line, sizeof line, f)) {
     Pick p{};
-    if (sscanf(line, "%159s %u %u %u %f %f %d", key, &p.mid_max, &p.w64, &p.w32, &p.ms64, &p.ms32, &p.fetch) >= 6)
+    if (sscanf(line, "%159s %u %u %u %f %f %d %d", key, &p.mid_max, &p.w64, &p.w32, &p.ms64, &p.ms32, &p.fetch,
+               &p.int_adds) >= 6)
       g_tune_cache[key] = p;
   }
   fclose(f);
@@ -55,20 +60,21 @@ void save_file(const char* path) {
   FILE* f = fopen(path, "w");
   if (!f) return;
   for (const auto& kv : g_tune_cache)
-    fprintf(f, "%s %u %u %u %.4f %.4f %d\n", kv.first.c_str(), kv.second.mid_max, kv.second.w64, kv.second.w32,
-            kv.second.ms64, kv.second.ms32, kv.second.fetch);
+    fprintf(f, "%s %u %u %u %.4f %.4f %d %d\n", kv.first.c_str(), kv.second.mid_max, kv.second.w64, kv.second.w32,
+            kv.second.ms64, kv.second.ms32, kv.second.fetch, kv.second.int_adds);
   fclose(f);
 }
 
 // ms per iteration of a short Static solve (best of two), or < 0 on error.
 float trial(prx_context* c, prx_graph* gr, double* ranks, int precision, uint32_t width, int* status,
-            int fetch = -1) {
+            int fetch = -1, int int_adds = 0) {
   prx_options o;
   prx_options_default(&o);
   o.max_iterations = 3;
   o.precision = precision;
   o.chunk_vertices = width;
   o.l2_fetch_bytes = fetch;
+  o.int_adds = int_adds;
   o.tolerance = 0.0;  // run all three iterations
   float best = -1.f;
   for (int rep = 0; rep < 2; ++rep) {
@@ -98,6 +104,7 @@ cudaError_t prx::tune_apply_cached(GraphDev& g, int sms, cudaStream_t s) {
   g.tuned_w64 = p.w64;
   g.tuned_w32 = p.w32;
   g.tuned_fetch = p.fetch;
+  g.tuned_int_adds = p.int_adds;
   if (p.mid_max == g.mid_max) return cudaSuccess;
   // only the MID / HIGH lists depend on the boundary (not the LOW bitmap,
   // the reciprocals or source chunks, which a new graph does not have yet)
@@ -131,13 +138,15 @@ int prx_autotune(prx_context* c, prx_graph* gr, const char* cache_path, prx_tune
     g.tuned_w64 = p.w64;
     g.tuned_w32 = p.w32;
     g.tuned_fetch = p.fetch;
-    res = {p.mid_max, p.w64, p.w32, p.ms64, p.ms32, 0, 1, p.fetch};
+    g.tuned_int_adds = p.int_adds;
+    res = {p.mid_max, p.w64, p.w32, p.ms64, p.ms32, 0, 1, p.fetch, p.int_adds};
     if (out) *out = res;
     return PRX_OK;
   }
   double* ranks = nullptr;
   TRY_CUDA_ST(cudaMalloc(&ranks, sizeof(double) * g.n));
   int st = PRX_OK, trials = 0;
+  g.tuned_int_adds = 0;  // steps 1-3 time with the library default
   // 1. MID / HIGH boundary, with the default chunk widths
   const uint32_t mids[] = {1024u, 4096u, 16384u};
   uint32_t best_mid = g.mid_max;
@@ -208,14 +217,32 @@ int prx_autotune(prx_context* c, prx_graph* gr, const char* cache_path, prx_tune
       }
     }
   }
+  // 4. integer-pipe adds of the FP64 sweep (none, one or two of every four)
+  //    with those picks, by FP64 time
+  int int_adds = -1;
+  if (!st) {
+    g.tuned_fetch = fetch;
+    float b = -1.f;
+    for (int k : {-1, 1, 2}) {
+      const float a = trial(c, gr, ranks, PRX_FP64, 0, &st, 0, k);
+      ++trials;
+      if (st) break;
+      if (b < 0 || a < b) {
+        b = a;
+        int_adds = k;
+      }
+    }
+    if (!st) ms64 = b;
+  }
   cudaFree(ranks);
   if (st) return st;
   g.tuned_w64 = w64;
   g.tuned_w32 = w32;
   g.tuned_fetch = fetch;
-  g_tune_cache[key] = {g.mid_max, w64, w32, ms64, ms32, fetch};
+  g.tuned_int_adds = int_adds;
+  g_tune_cache[key] = {g.mid_max, w64, w32, ms64, ms32, fetch, int_adds};
   save_file(cache_path);
-  res = {g.mid_max, w64, w32, ms64, ms32, trials, 0, fetch};
+  res = {g.mid_max, w64, w32, ms64, ms32, trials, 0, fetch, int_adds};
   if (out) *out = res;
   return PRX_OK;
 }

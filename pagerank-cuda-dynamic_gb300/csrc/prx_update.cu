@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(kThreads, ModeTraits<MODE>::LOW_BLOCKS)
       if (mine) acc = lane_row_sum(c, seg_edges(edg, base, shift, v), s, e, FIRST ? V(0) : carried_of<MODE>(a)[v]);
     } else {  // the whole warp sums together
       const V init = (mine && !FIRST) ? carried_of<MODE>(a)[v] : V(0);
-      acc = warp_row_sums(c, seg_edges(edg, base, shift, v), s, mine ? e : s, init, ch, hot);
+      acc = warp_row_sums(c, seg_edges(edg, base, shift, v), s, mine ? e : s, init, ch, hot, a.int_adds);
     }
     if (mine) {
       edges += e - s;

@@ -24,7 +24,7 @@ class Options(C.Structure):
                 ("precision", C.c_int), ("loop", C.c_int), ("partition", C.c_int), ("timing", C.c_int),
                 ("expansion", C.c_int), ("chunk_vertices", C.c_uint32), ("refine_sweeps", C.c_int),
                 ("l2_fetch_bytes", C.c_int), ("require_convergence", C.c_int),
-                ("hot_sources", C.c_int)]
+                ("hot_sources", C.c_int), ("int_adds", C.c_int)]
 
 
 class Result(C.Structure):
@@ -66,7 +66,7 @@ class TuneResult(C.Structure):
     """prx_tune_result (autotuner picks; no counterpart in the reference)."""
     _fields_ = [("mid_max", C.c_uint32), ("chunk_vertices64", C.c_uint32), ("chunk_vertices32", C.c_uint32),
                 ("ms_per_iteration64", C.c_float), ("ms_per_iteration32", C.c_float), ("trials", C.c_int),
-                ("cached", C.c_int), ("l2_fetch_bytes", C.c_int)]
+                ("cached", C.c_int), ("l2_fetch_bytes", C.c_int), ("int_adds", C.c_int)]
 
     as_dict = Result.as_dict
 
