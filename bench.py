@@ -311,6 +311,7 @@ def summarize(fp32, dfp, dynamic, grid, ppr, adj, big, ingest, tune, multi=None)
         out["ingest_1.9B_ms"] = statistics.median(ingest["device_ms"])
     if tune:
         out["autotune_s"] = tune.get("seconds")
+        out["autotune_int_adds"] = tune.get("int_adds")
     if multi:
         out["multibatch_dfp_1e-5_x%d" % multi["batches"]] = pick(multi, "host_loop_ms", "one_launch_ms",
                                                                  "speedup_vs_host_loop", "graph_launches",

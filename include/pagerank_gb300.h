@@ -140,9 +140,9 @@ typedef struct {
                                  on the integer pipes (a correctly rounded
                                  integer adder, the same bits as the FP64
                                  add) to unload GB300's FP64 pipe: 0 the
-                                 autotuner's pick for the graph (the library
-                                 default when untuned), -1 none, 1 or 2.
-                                 Results do not depend on it [0]            */
+                                 autotuner's pick for the graph (one when
+                                 untuned), -1 none, 1 .. 4.  Results do not
+                                 depend on it [0]                           */
 } prx_options;
 
 /* PagerankResult<V> (inc/pagerank.hxx:64-113) minus the rank vector, which
@@ -441,15 +441,15 @@ typedef struct {
   int      cached;            /* 1: picks reused for a graph of the same signature      */
   int      l2_fetch_bytes;    /* L2 fetch granularity of the solves (32, 64 or 128)     */
   int      int_adds;          /* integer-pipe adds of every four in the FP64 sweeps
-                                 (-1 none, 1 or 2; 0 from a cache line without it)   */
+                                 (-1 none, 1 .. 4; 0 from a cache line without it)   */
 } prx_tune_result;
 
 /* Times short Static solves on g (FP64 and FP32 refinement, 3 iterations
  * each, best of two) over the MID / HIGH in-degree boundary (1024, 4096,
  * 16384), the source-chunk widths (none, 200/128/64 MB of FP64
  * contributions, 96/48/24 MB of FP32 ones) and the L2 fetch granularity (32,
- * 64, 128 bytes; FP64 plus FP32 time), then prx_options.int_adds (none, 1,
- * 2; FP64 time), and keeps the fastest on g: later solves with
+ * 64, 128 bytes; FP64 plus FP32 time), then prx_options.int_adds (none,
+ * 1 .. 4; FP64 time), and keeps the fastest on g: later solves with
  * chunk_vertices = 0, l2_fetch_bytes = 0 and int_adds = 0 use them.  Results
  * do not depend on these parameters.  Picks are cached per graph signature (n, m, in-degree class
  * sizes) in the process and, when cache_path is not NULL, in that text file

@@ -1165,7 +1165,7 @@ static int solve_common(prx_context* c, prx_graph* gr, int mode, const uint32_t*
   if (opt.l2_fetch_bytes < -1 || opt.l2_fetch_bytes > 128)
     FAIL(PRX_EINVAL, "prx_solve: l2_fetch_bytes must be in -1 .. 128");
   if (opt.hot_sources < -1) FAIL(PRX_EINVAL, "prx_solve: hot_sources must be -1, 0 or a vertex count");
-  if (opt.int_adds < -1 || opt.int_adds > 2) FAIL(PRX_EINVAL, "prx_solve: int_adds must be -1, 0, 1 or 2");
+  if (opt.int_adds < -1 || opt.int_adds > 4) FAIL(PRX_EINVAL, "prx_solve: int_adds must be in -1 .. 4");
   if (!ranks_out && gr->g.n) FAIL(PRX_EINVAL, "prx_solve: ranks_out is NULL");
   prx_result own;
   if (!res) res = &own;  // the convergence check reads it

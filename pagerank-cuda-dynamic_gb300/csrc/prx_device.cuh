@@ -268,7 +268,7 @@ __device__ __forceinline__ double add_alt(double acc, double x, bool alt) {
 // instructions cost the warp as much as live ones.  Step k reads ids
 // s+4k .. s+4k+3 out of the two aligned 16-byte groups they span (the lane's
 // offset s & 3 picks them); a lane past its row's end adds +0.0, which leaves
-// acc (a sum of non-negative terms from +0) unchanged.  int_adds (0, 1 or 2)
+// acc (a sum of non-negative terms from +0) unchanged.  int_adds (0 .. 4)
 // of every four adds of a full step run on the integer pipes (add_alt), so
 // the FP64 pipe, the sweep's bound, carries fewer of them.
 __device__ __forceinline__ double warp_row_sums(const double* __restrict__ c, const uint32_t* __restrict__ edg,
@@ -293,9 +293,9 @@ __device__ __forceinline__ double warp_row_sums(const double* __restrict__ c, co
     double x2 = t + 2 < len ? gather(c, ch, hot, u2) : 0.0;
     const double x3 = t + 3 < len ? gather(c, ch, hot, u3) : 0.0;
     if (t + 4 <= L) {
-      acc += x0;
+      acc = add_alt(acc, x0, int_adds >= 4);
       acc = add_alt(acc, x1, int_adds >= 2);
-      acc += x2;
+      acc = add_alt(acc, x2, int_adds >= 3);
       acc = add_alt(acc, x3, int_adds >= 1);
     } else {  // the last 1..3 adds; the trip count is the same in every lane
       for (uint32_t r = L - t; r; --r) {

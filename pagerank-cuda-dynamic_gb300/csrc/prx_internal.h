@@ -127,7 +127,7 @@ struct GraphDev {
   uint32_t tuned_w32 = 0;
   int tuned_fetch = 0;            // L2 fetch granularity picked by prx_autotune (0: none)
   int tuned_int_adds = 0;         // integer-pipe adds of the FP64 sweep picked by prx_autotune (-1 none,
-                                  // 1, 2; 0: not tuned)
+                                  // 1 .. 4; 0: not tuned)
   uint32_t* low_bm = nullptr;     // bitmap of the LOW class
   double* rcp = nullptr;          // RN(1 / outdeg) per vertex, for div_count
   float* rcp32 = nullptr;         // the same in FP32 (personalized PageRank sweeps)
@@ -228,7 +228,7 @@ struct SolveArgs {
   uint32_t n;
   uint32_t mid_max;
   uint32_t pull_threshold;        // expand by pulling when more than this many vertices changed by > D
-  uint32_t int_adds;              // FP64 LOW sweeps: adds of every four run on the integer pipes (0..2)
+  uint32_t int_adds;              // FP64 LOW sweeps: adds of every four run on the integer pipes (0..4)
   double C0, P, D, C;
 };
 
@@ -252,8 +252,11 @@ void launch_finalize(const SolveArgs& a, int mode, cudaStream_t s);
 // iteration wrote); false when the solve uses no hot copy.
 bool launch_hot_copy(const SolveArgs& a, int parity, int sms, cudaStream_t s);
 // Adds of every four in a full step of the FP64 LOW sweep that run on the
-// integer pipes when prx_options.int_adds is 0.
-constexpr uint32_t kDefaultIntAdds = 0;
+// integer pipes when prx_options.int_adds is 0 and the graph is not tuned:
+// one.  Static measured 0.4-7% faster on the 50M web-like graph (whose sweep
+// DRAM and L1 also hold back; two or more cost more there than they save)
+// and 5% faster on the 4096^2 grid (three: 17%), DF and DF-P within 2%.
+constexpr uint32_t kDefaultIntAdds = 1;
 // Hot-source cap when prx_options.hot_sources is 0: 32 MB of FP64 values.
 constexpr uint32_t kDefaultHotCap = 4u << 20;
 // Source-chunk width of the FP64 sweeps when prx_options.chunk_vertices is 0

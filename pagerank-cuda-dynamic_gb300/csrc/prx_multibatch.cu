@@ -109,8 +109,7 @@ extern "C" int prx_solve_batches_device(prx_context* c, prx_graph* gr, int mode,
   if (o) opt = *o;
   if (opt.precision != PRX_FP64) FAIL(PRX_EINVAL, "prx_solve_batches_device: FP64 only");
   if (!(opt.damping > 0 && opt.damping < 1)) FAIL(PRX_EINVAL, "prx_solve_batches_device: damping must be in (0, 1)");
-  if (opt.int_adds < -1 || opt.int_adds > 2)
-    FAIL(PRX_EINVAL, "prx_solve_batches_device: int_adds must be -1, 0, 1 or 2");
+  if (opt.int_adds < -1 || opt.int_adds > 4) FAIL(PRX_EINVAL, "prx_solve_batches_device: int_adds must be in -1 .. 4");
   const uint32_t n = g.n;
   TRY_CUDA_ST(cudaSetDevice(c->device));
   cudaStream_t s = c->stream;

@@ -28,7 +28,7 @@ struct Pick {
   uint32_t mid_max, w64, w32;
   float ms64, ms32;
   int fetch;
-  int int_adds;  // -1 none, 1 or 2 (0: not tuned, e.g. a cache line without it)
+  int int_adds;  // -1 none, 1 .. 4 (0: not tuned, e.g. a cache line without it)
 };
 
 std::mutex g_tune_mu;
@@ -217,13 +217,13 @@ int prx_autotune(prx_context* c, prx_graph* gr, const char* cache_path, prx_tune
       }
     }
   }
-  // 4. integer-pipe adds of the FP64 sweep (none, one or two of every four)
-  //    with those picks, by FP64 time
+  // 4. integer-pipe adds of the FP64 sweep (none, or one to four of every
+  //    four) with those picks, by FP64 time
   int int_adds = -1;
   if (!st) {
     g.tuned_fetch = fetch;
     float b = -1.f;
-    for (int k : {-1, 1, 2}) {
+    for (int k : {-1, 1, 2, 3, 4}) {
       const float a = trial(c, gr, ranks, PRX_FP64, 0, &st, 0, k);
       ++trials;
       if (st) break;

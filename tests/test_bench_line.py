@@ -32,7 +32,7 @@ def _sections():
     adj = {"fd_max_rel_err": 2.737e-09, "rounds": [{"fd_edges": 1000, "adjoint_ms": 52.3}] * 21}
     big = {"ge_s": 211.7, "copy_ranks_exactly_quarter_of_single": True, "ms": 359.4}
     ingest = {"device_ms": [244.3, 226.2]}
-    tune = {"seconds": 1.104, "mid_max": 4096}
+    tune = {"seconds": 1.104, "mid_max": 4096, "int_adds": 1}
     multi = {"batches": 10, "host_loop_ms": 866.79, "one_launch_ms": 590.37, "speedup_vs_host_loop": 1.4682,
              "graph_launches": 1, "same_bits": True, "step_ms": [58.0] * 10}
     return fp32, dfp, dynamic, grid, ppr, adj, big, ingest, tune, multi

@@ -1,5 +1,5 @@
 """FP64 sweeps with part of the edge additions on the integer pipes
-(prx_options.int_adds 1 or 2): the integer adder is correctly rounded, so
+(prx_options.int_adds 1 .. 4): the integer adder is correctly rounded, so
 every mode gives the oracle's ranks and iteration counts bit for bit, with
 source chunks, hot sources, both loops and the FP32 refinement's FP64
 sweeps; operands outside its range (negative or huge ranks) fall back to the
@@ -31,7 +31,7 @@ def _synthetic(pg, kind):
     return pg.graphs.rmat(14, 48, a=0.7, b=0.1, c=0.1, seed=3)   # hubs
 
 
-@pytest.mark.parametrize("int_adds", [1, 2])
+@pytest.mark.parametrize("int_adds", [1, 2, 3, 4])
 @pytest.mark.parametrize("case", golden_cases())
 def test_golden_all_modes(pg, ctx, case, int_adds):
     z = load_golden(case)
@@ -60,7 +60,7 @@ def test_synthetic_all_modes(pg, ctx, kind):
     g.apply_batch(*batch)
     for mode in MODES:
         want, it_w = O.solve(mode, yoff, yedg, *yt, *batch, q=q)
-        for int_adds in (1, 2):
+        for int_adds in (1, 2, 3, 4):
             for width, loop in ((0, pg.LOOP_AUTO), (997, pg.LOOP_HOST)):
                 o = pg.options(int_adds=int_adds, chunk_vertices=width, loop=loop)
                 got, res = pg.solve(ctx, g, pg.MODES[mode], batch[:2], batch[2:], q, o)
@@ -70,7 +70,7 @@ def test_synthetic_all_modes(pg, ctx, kind):
     for mode in ("static", "prune_dynamic_frontier"):
         ref, r0 = pg.solve(ctx, g, pg.MODES[mode], batch[:2], batch[2:], q,
                            pg.options(int_adds=-1, precision=pg.FP32_REFINE))
-        for int_adds in (1, 2):
+        for int_adds in (1, 2, 4):
             got, r1 = pg.solve(ctx, g, pg.MODES[mode], batch[:2], batch[2:], q,
                                pg.options(int_adds=int_adds, precision=pg.FP32_REFINE))
             assert r1["iterations"] == r0["iterations"]
@@ -92,11 +92,11 @@ def test_out_of_range_operands_fall_back(pg, ctx):
         qb[::97] = bad
         for mode, ins in ((pg.NAIVE_DYNAMIC, (e, e)), (pg.DYNAMIC_FRONTIER, seed)):
             want, w = pg.solve(ctx, g, mode, (e, e), ins, qb, pg.options(max_iterations=3, int_adds=-1))
-            for int_adds in (1, 2):
+            for int_adds in (1, 2, 4):
                 got, r = pg.solve(ctx, g, mode, (e, e), ins, qb, pg.options(max_iterations=3, int_adds=int_adds))
                 assert r["iterations"] == w["iterations"]
                 assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), (bad, mode, int_adds)
-    for bad in (-2, 3):
+    for bad in (-2, 5):
         with pytest.raises(pg.PrxError):
             pg.solve(ctx, g, pg.STATIC, opts=pg.options(int_adds=bad))
     g.close()

@@ -325,7 +325,7 @@ def test_autotune_keeps_results_and_caches(pg, ctx, tmp_path):
     t2 = pg.autotune(ctx, g2)
     assert t2["cached"] == 1 and t2["trials"] == 0 and t2["mid_max"] == t["mid_max"]
     assert t["l2_fetch_bytes"] in (32, 64, 128) and t2["l2_fetch_bytes"] == t["l2_fetch_bytes"]
-    assert t["int_adds"] in (-1, 1, 2) and t2["int_adds"] == t["int_adds"]
+    assert t["int_adds"] in (-1, 1, 2, 3, 4) and t2["int_adds"] == t["int_adds"]
     lines = path.read_text().split()
     assert len(lines) >= 8 and int(lines[1]) == t["mid_max"] and int(lines[6]) == t["l2_fetch_bytes"]
     assert int(lines[7]) == t["int_adds"]
